@@ -1,0 +1,173 @@
+/*
+ * lpma.h -- C ABI of the GB300 LPMA (leveled packed memory array) engine.
+ *
+ * Drop-in boundary for the batched edge-update path of pkumod/LPMA.  Every
+ * entry point takes plain pointers and sizes, returns an lpma_status_t and
+ * never prints.  Device pointers are borrowed for the duration of the call
+ * and read only.  Calls on one handle are ordered on the stream passed in;
+ * different handles are independent.  Every call that returns a count or a
+ * host buffer synchronises with its stream before returning.
+ *
+ * Key layout (reference rpma.cuh:43-50): a 64-bit key is
+ *     src << 42 | dst << 20 | t
+ * with src, dst < num_vertices <= 0x3FFFFE and t a 20-bit timestamp.  Every
+ * vertex v owns a sentinel key v << 42 | 0x3FFFFEFFFFF that closes its row.
+ * With LPMA_KEY_PAIR32 the caller passes src << 32 | dst instead and the
+ * engine repacks it with t = 0.
+ */
+#ifndef LPMA_H
+#define LPMA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LPMA_API __attribute__((visibility("default")))
+#else
+#define LPMA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* same object as cudaStream_t; 0 is the legacy default stream */
+typedef struct CUstream_st *lpma_stream_t;
+
+typedef struct LpmaHandle LpmaHandle;
+
+typedef enum {
+    LPMA_OK = 0,
+    LPMA_ERR_INVALID_ARGUMENT = 1, /* null handle/pointer, bad config */
+    LPMA_ERR_INVALID_KEY = 2,      /* key out of range, sentinel delete, value 0xFF, expired insert */
+    LPMA_ERR_OUT_OF_MEMORY = 3,
+    LPMA_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    LPMA_ERR_CAPACITY = 5,         /* tree height would exceed LPMA_MAX_HEIGHT */
+    LPMA_ERR_INTERNAL = 6,         /* a device-side consistency check failed */
+    LPMA_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
+    LPMA_ERR_BUFFER_TOO_SMALL = 8
+} lpma_status_t;
+
+enum { LPMA_KEY_PACKED = 0, LPMA_KEY_PAIR32 = 1 };
+enum { LPMA_MAX_HEIGHT = 24 };
+
+typedef struct {
+    uint32_t segment_length;   /* slots per segment; 32 (rpma.cuh:1769) */
+    uint32_t key_format;       /* LPMA_KEY_PACKED or LPMA_KEY_PAIR32 */
+    uint32_t skip_rule;        /* 1: the reference's big-grain skip state machine (rpma.cuh:1609-1619) */
+    uint32_t reserved0;
+    double density_lower_root; /* 0.42 (rpma.cuh:77) */
+    double density_upper_root; /* 1.0 (rpma.cuh:78) */
+} LpmaConfig;
+
+typedef struct {
+    uint32_t height_before, height_after;
+    uint32_t n_ins_applied;    /* inserts of new keys */
+    uint32_t n_upserts;        /* inserts of present keys: value overwritten in place */
+    uint32_t n_del_applied;    /* deletes of present keys */
+    uint32_t n_noop;           /* absent-key deletes and in-batch duplicates */
+    uint32_t root_executed;    /* the whole-array window absorbed updates */
+    uint32_t eager_levelup;    /* a level was added after the root absorbed */
+    uint32_t overflow;         /* updates were left after the root */
+    uint32_t rebuilt;          /* full rebuild at a new height */
+    uint32_t levelup_path;     /* overflow absorbed by adding one level */
+    uint32_t fill_empty;       /* an empty segment forced a full redistribution */
+    uint64_t windows_small;    /* rebalance windows of <= 32 segments executed */
+    uint64_t windows_big;      /* larger windows (tile grain) executed */
+    uint64_t slots_rewritten;  /* slots covered by executed windows (incl. rebuild) */
+    uint64_t num_items;        /* keys stored after the call, sentinels included */
+} LpmaStats;
+
+/* defaults that reproduce the reference: 32 / 0.42 / 1.0 / skip rule on */
+LPMA_API lpma_status_t lpma_config_default(LpmaConfig *cfg);
+
+/* Replaces init_csr_rpma(RPMA&, SIZE_TYPE row_num) (rpma.cuh:1808-1824):
+ * empty height-0 array, then the num_vertices sentinel keys inserted through
+ * the update path. */
+LPMA_API lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_stream_t stream,
+                          LpmaHandle **out);
+
+/* Bulk load = one update of all edges, the pattern of test_csr.cu:49-55 and
+ * init_csr_rpma's update_rpma(row_wall) (rpma.cuh:1823).  d_vals may be NULL
+ * (every value 1, test_update_rpma.cu:72). */
+LPMA_API lpma_status_t lpma_build(LpmaHandle *h, const uint64_t *d_keys, const uint8_t *d_vals, size_t n,
+                         lpma_stream_t stream);
+
+/* Replaces bool update_rpma(RPMA&, DEV_VEC_KEY& keys, DEV_VEC_VALUE& values,
+ * DEV_VEC_KEY& edgequery, DEV_VEC_VALUE& flag, SIZE_TYPE thres)
+ * (rpma.cuh:1549-1718), extended with deletes (GPMA semantics,
+ * gpma.cuh:162-175).  The batch is a set of updates: an insert of a present
+ * key overwrites its value, a delete of an absent key is a no-op, a key
+ * both inserted and deleted in one batch ends up present.  Keys with
+ * t < thres are expired (removed at the next rebalance of their window, as
+ * in the reference); inserting a key with t < thres is rejected.  The
+ * inputs are not modified (the reference sorts them in place).  stats may
+ * be NULL; it is filled when the call returns. */
+LPMA_API lpma_status_t lpma_update(LpmaHandle *h, const uint64_t *d_ins, const uint8_t *d_ins_vals, size_t n_ins,
+                          const uint64_t *d_del, size_t n_del, uint32_t thres, lpma_stream_t stream,
+                          LpmaStats *stats);
+
+/* Same as lpma_update with host buffers: copies in, updates, fills stats.
+ * The end-to-end entry point for callers without device memory. */
+LPMA_API lpma_status_t lpma_update_host(LpmaHandle *h, const uint64_t *h_ins, const uint8_t *h_ins_vals, size_t n_ins,
+                               const uint64_t *h_del, size_t n_del, uint32_t thres, lpma_stream_t stream,
+                               LpmaStats *stats);
+
+/* Replaces to_csr_rpma(RPMA&, DEV_VEC_SIZE& row_offset, DEV_VEC_SIZE& col_index)
+ * (rpma.cuh:2249-2295).  Device arrays owned by the handle, valid until the
+ * next mutating call: row_offset has num_vertices + 1 entries with one extra
+ * slot per row for its sentinel (row length = row_offset[v+1] -
+ * row_offset[v] - 1, col_index[row_offset[v+1] - 1] == v); col_index has
+ * *nnz entries (dst for edges, src for sentinels); values has the stored
+ * value for edges and 0xFF for sentinels. */
+LPMA_API lpma_status_t lpma_csr_view(LpmaHandle *h, const uint32_t **row_offset, const uint32_t **col_index,
+                            const uint8_t **values, size_t *nnz, lpma_stream_t stream);
+
+/* Copy-out form of to_csr_rpma, which fills caller-owned vectors: writes the
+ * same three arrays into caller buffers (host or device memory; cap is the
+ * capacity of col_index and values, row_offset needs num_vertices + 1).
+ * *nnz receives the entry count.  Synchronises with the stream. */
+LPMA_API lpma_status_t lpma_to_csr(LpmaHandle *h, uint32_t *row_offset, uint32_t *col_index, uint8_t *values,
+                                   size_t cap, size_t *nnz, lpma_stream_t stream);
+
+/* Replaces get_data_rpma(RPMA&, KEY_PTR&, VALUE_PTR&) (rpma.cuh:1735-1761):
+ * every stored key (sentinels included) in sorted order into caller host
+ * buffers of capacity cap; *n receives the count.  h_vals may be NULL. */
+LPMA_API lpma_status_t lpma_export_sorted(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_vals, size_t cap, size_t *n,
+                                 lpma_stream_t stream);
+
+/* Physical layout for parity checks: the reference's level arrays laid end
+ * to end (level i at slot 32*(2^i - 1)), empty slots ~0, values of empty
+ * slots 0.  *height receives the tree height; the slot count is
+ * 32*(2^(height+1) - 1).  Also the per-vertex sentinel slots (the
+ * reference's csr_idx/csr_lane pair as one physical slot index). */
+LPMA_API lpma_status_t lpma_export_layout(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_vals, size_t cap_slots,
+                                 uint32_t *sentinel_slots, size_t cap_vertices, uint32_t *height,
+                                 lpma_stream_t stream);
+
+LPMA_API lpma_status_t lpma_info(const LpmaHandle *h, uint32_t *height, uint64_t *num_items, uint32_t *num_vertices);
+
+/* Replaces destroy_rpma (rpma.cuh:1720-1732). */
+LPMA_API lpma_status_t lpma_destroy(LpmaHandle *h);
+
+LPMA_API const char *lpma_status_string(lpma_status_t s);
+
+/* ---- synthetic workload (device generator; the same integer arithmetic
+ * as the CPU workload generator used by the tests) ---- */
+
+/* Seeded R-MAT keys src << 42 | dst << 20 with thresholds floor(p * 2^32):
+ * writes 2^scale * edge_factor raw edges into d_out (capacity cap), removes
+ * self loops and duplicates, sorts; *n_out receives the count. */
+LPMA_API lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edge_factor, uint32_t ta, uint32_t tab,
+                            uint32_t tabc, uint64_t *d_out, size_t cap, size_t *n_out, lpma_stream_t stream);
+
+/* Reorders d_keys by (mix64(seed ^ key), key). */
+LPMA_API lpma_status_t lpma_shuffle(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream);
+
+/* Number of kernels this library launched since load (a counter for benches). */
+LPMA_API uint64_t lpma_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

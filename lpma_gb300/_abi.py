@@ -1,0 +1,97 @@
+"""ctypes declarations of the C ABI in include/lpma.h.
+
+The shared library is built in-tree (lpma_gb300/_lpma.so, see build.py).  If
+it is missing, importing the package raises: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lpma.so")
+
+LPMA_OK = 0
+STATUS_NAMES = {
+    0: "LPMA_OK", 1: "LPMA_ERR_INVALID_ARGUMENT", 2: "LPMA_ERR_INVALID_KEY", 3: "LPMA_ERR_OUT_OF_MEMORY",
+    4: "LPMA_ERR_CUDA", 5: "LPMA_ERR_CAPACITY", 6: "LPMA_ERR_INTERNAL", 7: "LPMA_ERR_TIMEOUT",
+    8: "LPMA_ERR_BUFFER_TOO_SMALL",
+}
+KEY_PACKED, KEY_PAIR32 = 0, 1
+MAX_HEIGHT = 24
+
+# every entry point include/lpma.h declares
+EXPORTS = [
+    "lpma_config_default", "lpma_create", "lpma_build", "lpma_update", "lpma_update_host", "lpma_csr_view",
+    "lpma_to_csr", "lpma_export_sorted", "lpma_export_layout", "lpma_info", "lpma_destroy", "lpma_status_string",
+    "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches",
+]
+
+
+class LpmaConfig(ctypes.Structure):
+    _fields_ = [("segment_length", ctypes.c_uint32), ("key_format", ctypes.c_uint32),
+                ("skip_rule", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("density_lower_root", ctypes.c_double), ("density_upper_root", ctypes.c_double)]
+
+
+class LpmaStats(ctypes.Structure):
+    _fields_ = [("height_before", ctypes.c_uint32), ("height_after", ctypes.c_uint32),
+                ("n_ins_applied", ctypes.c_uint32), ("n_upserts", ctypes.c_uint32),
+                ("n_del_applied", ctypes.c_uint32), ("n_noop", ctypes.c_uint32),
+                ("root_executed", ctypes.c_uint32), ("eager_levelup", ctypes.c_uint32),
+                ("overflow", ctypes.c_uint32), ("rebuilt", ctypes.c_uint32),
+                ("levelup_path", ctypes.c_uint32), ("fill_empty", ctypes.c_uint32),
+                ("windows_small", ctypes.c_uint64), ("windows_big", ctypes.c_uint64),
+                ("slots_rewritten", ctypes.c_uint64), ("num_items", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class LpmaError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        super().__init__("%s: %s" % (where, STATUS_NAMES.get(status, status)))
+
+
+_lib = None
+
+
+def load():
+    """Load the engine library; raises ImportError when it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("lpma_gb300/_lpma.so is missing: build it with `python -m lpma_gb300.build` "
+                          "(or __graft_entry__.build()); the engine has no CPU fallback")
+    L = ctypes.CDLL(LIB_PATH)
+    P, SZ, U32, U64, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    sig = {
+        "lpma_config_default": [P],
+        "lpma_create": [P, U32, P, P],
+        "lpma_build": [P, P, P, SZ, P],
+        "lpma_update": [P, P, P, SZ, P, SZ, U32, P, P],
+        "lpma_update_host": [P, P, P, SZ, P, SZ, U32, P, P],
+        "lpma_csr_view": [P, P, P, P, P, P],
+        "lpma_to_csr": [P, P, P, P, SZ, P, P],
+        "lpma_export_sorted": [P, P, P, SZ, P, P],
+        "lpma_export_layout": [P, P, P, SZ, P, SZ, P, P],
+        "lpma_info": [P, P, P, P],
+        "lpma_destroy": [P],
+        "lpma_gen_rmat": [U64, U32, U32, U32, U32, U32, P, SZ, P, P],
+        "lpma_shuffle": [U64, P, SZ, P],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = I
+    L.lpma_status_string.argtypes = [I]
+    L.lpma_status_string.restype = ctypes.c_char_p
+    L.lpma_kernel_launches.argtypes = []
+    L.lpma_kernel_launches.restype = U64
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != LPMA_OK:
+        raise LpmaError(status, where)

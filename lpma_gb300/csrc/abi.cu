@@ -1,0 +1,828 @@
+// Host orchestration and the extern "C" boundary of the GB300 LPMA engine.
+//
+// One update call (reference update_rpma, rpma.cuh:1549-1718):
+//   1. pack + validate the batch (no structure change on a bad key)   [sync 1]
+//   2. radix sort, resolve + locate + membership, compaction
+//   3. count-only plan of the first level loop (skip rule on)          [sync 2]
+//   4. no overflow: execute the maximal windows once; if the root took
+//      updates, the eager level-up of rpma.cuh:1646-1653
+//      overflow (rpma.cuh:1662-1712): resize to h; h == H+1 executes the
+//      first loop, adds a level, re-locates the pending updates and runs a
+//      second plan with every level allowed, then fill_empty_segs; any
+//      other h rebuilds from the pre-batch array plus every update.
+#include <algorithm>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "kernels.cuh"
+#include "lpma.h"
+#include "prims.cuh"
+
+using namespace lpma;
+
+namespace lpma {
+uint64_t launch_count();
+}
+
+namespace {
+
+// Arrays whose size follows the tree capacity (height Hc).
+struct Cap {
+    uint32_t Hc = 0;
+    uint64_t *keys = nullptr, *keys_alt = nullptr;
+    uint8_t *vals = nullptr, *vals_alt = nullptr;
+    uint8_t *cnt = nullptr, *cnt_alt = nullptr, *cnt_live = nullptr, *srcc = nullptr, *seg_e = nullptr;
+    ulonglong2 *fl = nullptr;
+    uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
+    uint32_t *bitmap = nullptr;
+    uint32_t *scan_tmp = nullptr;
+};
+
+}  // namespace
+
+struct LpmaHandle {
+    LpmaConfig cfg{};
+    uint32_t V = 0;
+    uint32_t H = 0;
+    uint64_t total = 0;        // keys physically present
+    uint32_t min_t = 0xFFFFF;  // lower bound of the stored timestamps
+    lpma_status_t sticky = LPMA_OK;
+    Cap c;
+    uint32_t *sent = nullptr;
+    DevStatus *dst = nullptr;
+    DevStatus *hst = nullptr;   // pinned mirror
+    DevStatus *hinit = nullptr; // pinned reset template
+    // batch scratch
+    size_t bcap = 0;
+    uint64_t *bk0 = nullptr, *bk1 = nullptr;
+    uint16_t *bp0 = nullptr, *bp1 = nullptr;
+    uint8_t *kind = nullptr, *pend = nullptr;
+    uint32_t *seg = nullptr, *blk_nn = nullptr, *blk_ins = nullptr;
+    UpdList u{}, u2{};
+    Window *cand = nullptr, *wsmall = nullptr, *wbig = nullptr;
+    SortScratch sort{};
+    uint32_t *sort_err = nullptr;
+    TileJob *jobs_d = nullptr;
+    size_t jobs_cap = 0;
+    std::vector<TileJob> jobs_h;
+    std::vector<Window> big_h;
+    // host-copy staging (lpma_update_host)
+    uint64_t *stage_ins = nullptr, *stage_del = nullptr;
+    uint8_t *stage_vals = nullptr;
+    size_t stage_cap = 0;
+    // view / export
+    uint32_t *row_offset = nullptr, *col_index = nullptr;
+    uint8_t *view_vals = nullptr;
+    uint64_t *exp_keys = nullptr;
+    uint8_t *exp_vals = nullptr;
+    size_t view_cap = 0, exp_cap = 0;
+    bool view_valid = false;
+};
+
+namespace {
+
+#define CK(x)                                         \
+    do {                                              \
+        cudaError_t e_ = (x);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_);  \
+    } while (0)
+#define CKS(x)                                 \
+    do {                                       \
+        lpma_status_t s_ = (x);                \
+        if (s_ != LPMA_OK) return s_;          \
+    } while (0)
+
+lpma_status_t cuda_fail(cudaError_t e) {
+    (void)e;
+    return e == cudaErrorMemoryAllocation ? LPMA_ERR_OUT_OF_MEMORY : LPMA_ERR_CUDA;
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+uint32_t min_height(uint64_t cnt) {
+    uint32_t h = 0;
+    while (nslots_of(h) < cnt) h++;
+    return h;
+}
+
+uint64_t bitmap_words(uint32_t H) { return ((1ull << (H + 2)) + 31) / 32 + 1; }
+
+void free_cap(Cap &c) {
+    dfree(c.keys), dfree(c.keys_alt), dfree(c.vals), dfree(c.vals_alt);
+    dfree(c.cnt), dfree(c.cnt_alt), dfree(c.cnt_live), dfree(c.srcc), dfree(c.seg_e);
+    dfree(c.fl);
+    dfree(c.segP), dfree(c.q), dfree(c.qn), dfree(c.PQ), dfree(c.US), dfree(c.qi), dfree(c.qd);
+    dfree(c.bitmap), dfree(c.scan_tmp);
+    c.Hc = 0;
+}
+
+cudaError_t alloc_cap(Cap &c, uint32_t Hc) {
+    const uint64_t ns = nslots_of(Hc), nseg = nseg_of(Hc);
+    cudaError_t e;
+    c.Hc = Hc;
+#define A(p, n)                             \
+    if ((e = dalloc(&c.p, (n))) != cudaSuccess) { \
+        free_cap(c);                        \
+        return e;                           \
+    }
+    A(keys, ns) A(keys_alt, ns) A(vals, ns) A(vals_alt, ns);
+    A(cnt, nseg + 64) A(cnt_alt, nseg + 64) A(cnt_live, nseg + 64) A(srcc, nseg + 64) A(seg_e, nseg + 64);
+    A(fl, nseg);
+    A(segP, nseg + 2) A(q, nseg + 2) A(qn, nseg + 2) A(PQ, nseg + 2) A(US, nseg + 2) A(qi, nseg + 2) A(qd, nseg + 2);
+    A(bitmap, bitmap_words(Hc)) A(scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
+#undef A
+    if ((e = cudaMemset(c.cnt, 0, nseg + 64)) != cudaSuccess) return e;
+    if ((e = cudaMemset(c.cnt_live, 0, nseg + 64)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+// Grow the capacity to hold height h, keeping the current tree (prefix copy:
+// the heap layout of height H is a prefix of any larger one).
+lpma_status_t grow_to(LpmaHandle *h, uint32_t hneed, cudaStream_t s) {
+    if (hneed <= h->c.Hc) return LPMA_OK;
+    if (hneed > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
+    uint32_t Hc = std::min<uint32_t>(hneed + 1, LPMA_MAX_HEIGHT);
+    Cap n;
+    CK(alloc_cap(n, Hc));
+    Cap &o = h->c;
+    if (o.keys) {
+        CK(cudaMemcpyAsync(n.keys, o.keys, nslots_of(h->H) * 8, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.vals, o.vals, nslots_of(h->H), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.cnt, o.cnt, nseg_of(h->H), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.fl, o.fl, nseg_of(h->H) * sizeof(ulonglong2), cudaMemcpyDeviceToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    free_cap(o);
+    h->c = n;
+    return LPMA_OK;
+}
+
+lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
+    if (n <= h->bcap) return LPMA_OK;
+    size_t cap = std::max<size_t>(n, 4096);
+    cap = cap + cap / 4;
+    dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
+    dfree(h->blk_nn), dfree(h->blk_ins);
+    for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
+    dfree(h->cand), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
+    h->bcap = 0;
+    const size_t nb = cap / 256 + 4;
+    CK(dalloc(&h->bk0, cap)); CK(dalloc(&h->bk1, cap)); CK(dalloc(&h->bp0, cap)); CK(dalloc(&h->bp1, cap));
+    CK(dalloc(&h->kind, cap)); CK(dalloc(&h->pend, cap)); CK(dalloc(&h->seg, cap));
+    CK(dalloc(&h->blk_nn, nb)); CK(dalloc(&h->blk_ins, nb));
+    for (UpdList *u : {&h->u, &h->u2}) {
+        CK(dalloc(&u->key, cap)); CK(dalloc(&u->val, cap)); CK(dalloc(&u->kind, cap)); CK(dalloc(&u->seg, cap));
+        CK(dalloc(&u->ip, cap + 1));
+    }
+    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
+    h->sort.status_words = sort_status_words((uint32_t)cap);
+    CK(dalloc(&h->sort.status, h->sort.status_words));
+    h->bcap = cap;
+    return LPMA_OK;
+}
+
+lpma_status_t sync_status(LpmaHandle *h, cudaStream_t s) {
+    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    if (h->hst->error & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
+    if (h->hst->error & ERR_INTERNAL) return LPMA_ERR_INTERNAL;
+    return LPMA_OK;
+}
+
+cudaError_t reset_plan_counters(LpmaHandle *h, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&h->dst->n_cand, 0, offsetof(DevStatus, empty_found) - offsetof(DevStatus, n_cand), s);
+    if (e) return e;
+    return cudaMemsetAsync(&h->dst->slots_small, 0, 2 * sizeof(unsigned long long), s);
+}
+
+Tables make_tables(const LpmaHandle *h, uint32_t H, bool first_loop) {
+    Tables tb{};
+    uint64_t len = 32;
+    for (int i = 0; i < 32; i++) {
+        double d = h->cfg.density_lower_root * (double)len;  // recalculate_density, rpma.cuh:164
+        tb.lower[i] = (uint32_t)d;
+        len <<= 1;
+    }
+    int skip = 0;
+    for (uint32_t l = 0; l <= H + 1 && l < 32; l++) {
+        bool allowed = true;
+        if (first_loop && h->cfg.skip_rule) {
+            if (l == 4 || l == H / 3) skip = 1;  // rpma.cuh:1614-1619
+            if (l == (uint32_t)(H / 3 - 1u) || l == H + 1) skip = 0;
+            allowed = (32ull << l) <= 1024 || !skip;
+        }
+        if (allowed) tb.allowed |= 1u << l;
+    }
+    return tb;
+}
+
+bool needs_prefix(const Tables &tb, uint32_t H) {
+    for (uint32_t l = 9; l <= H; l++)
+        if ((tb.allowed >> l) & 1u) return true;
+    return false;
+}
+
+lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thres_active, uint64_t total_live,
+                       const Tables &tb, cudaStream_t s) {
+    const uint32_t H = h->H;
+    const uint64_t nseg = nseg_of(H);
+    CK(cudaMemsetAsync(h->c.bitmap, 0, bitmap_words(H) * 4, s));
+    CK(cudaMemsetAsync(h->pend, 0, std::max<size_t>(n_cap, 1), s));
+    CK(reset_plan_counters(h, s));
+    const uint8_t *cntp = thres_active ? h->c.cnt_live : h->c.cnt;
+    const bool useP = needs_prefix(tb, H);
+    if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
+    launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, H, tb, h->c.bitmap, h->cand, h->wsmall, h->wbig,
+                h->c.seg_e, h->pend, h->dst, s);
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+// Per-segment prefix arrays for the tile grain over the current geometry.
+lpma_status_t tile_prep(LpmaHandle *h, const UpdList &u, uint32_t n_list, bool thres_active, cudaStream_t s) {
+    const uint64_t nseg = nseg_of(h->H);
+    CK(cudaMemsetAsync(h->c.qi, 0, (nseg + 2) * 4, s));
+    CK(cudaMemsetAsync(h->c.qd, 0, (nseg + 2) * 4, s));
+    launch_seg_update_counts(u, n_list, h->c.qi, h->c.qd, h->dst, s);
+    launch_seg_q(h->c.cnt, thres_active ? h->c.cnt_live : nullptr, h->c.qi, h->c.qd, nseg, h->c.q, h->c.qn, h->c.srcc,
+                 s);
+    CK(scan_u32(h->c.q, h->c.PQ, (uint32_t)nseg, h->c.PQ + nseg, h->c.scan_tmp, s));
+    CK(scan_u32(h->c.qn, h->c.US, (uint32_t)nseg, h->c.US + nseg, h->c.scan_tmp, s));
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t upload_jobs(LpmaHandle *h, cudaStream_t s) {
+    if (h->jobs_h.size() > h->jobs_cap) {
+        dfree(h->jobs_d);
+        h->jobs_cap = h->jobs_h.size() * 2;
+        CK(dalloc(&h->jobs_d, h->jobs_cap));
+    }
+    CK(cudaMemcpyAsync(h->jobs_d, h->jobs_h.data(), h->jobs_h.size() * sizeof(TileJob), cudaMemcpyHostToDevice, s));
+    return LPMA_OK;
+}
+
+// Execute the planned maximal windows (status already synced).
+lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32_t thres, bool thres_active,
+                        cudaStream_t s, LpmaStats *st) {
+    const uint32_t n_small = h->hst->n_small, n_big = h->hst->n_big;
+    Geo g{h->c.keys, h->c.vals, h->H};
+    launch_exec_small(h->wsmall, n_small, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    st->windows_small += n_small;
+    st->slots_rewritten += h->hst->slots_small;
+    if (n_big) {
+        h->big_h.resize(n_big);
+        CK(cudaMemcpyAsync(h->big_h.data(), h->wbig, n_big * sizeof(Window), cudaMemcpyDeviceToHost, s));
+        CKS(tile_prep(h, u, n_list, thres_active, s));
+        CK(cudaStreamSynchronize(s));
+        std::sort(h->big_h.begin(), h->big_h.end(), [](const Window &a, const Window &b) { return a.a < b.a; });
+        h->jobs_h.clear();
+        uint32_t tiles = 0;
+        bool whole = false;
+        for (const Window &w : h->big_h) {
+            TileJob j{w.a, w.f, w.a, w.f, w.m, (w.f + 31) / 32, tiles, 0};
+            tiles += j.tiles;
+            h->jobs_h.push_back(j);
+            if (w.a == 0 && w.f == nseg_of(h->H)) whole = true;
+        }
+        CKS(upload_jobs(h, s));
+        Geo alt{h->c.keys_alt, h->c.vals_alt, h->H};
+        launch_exec_tiles(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, g, h->c.srcc, h->c.PQ, h->c.US, alt, h->c.cnt,
+                          h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        if (whole) {
+            std::swap(h->c.keys, h->c.keys_alt);
+            std::swap(h->c.vals, h->c.vals_alt);
+        } else {
+            launch_copy_segments(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, alt, g, s);
+        }
+        CK(cudaGetLastError());
+        st->windows_big += n_big;
+        st->slots_rewritten += h->hst->slots_big;
+    }
+    return LPMA_OK;
+}
+
+// Add one leaf level (alloc_or_del_levels, rpma.cuh:1396-1415): new empty
+// slots at the end of the heap layout, linear counts re-indexed.
+lpma_status_t level_up(LpmaHandle *h, cudaStream_t s) {
+    const uint32_t H = h->H;
+    CKS(grow_to(h, H + 1, s));
+    CK(cudaMemsetAsync(h->c.keys + nslots_of(H), 0xFF, (nslots_of(H + 1) - nslots_of(H)) * 8, s));
+    CK(cudaMemsetAsync(h->c.vals + nslots_of(H), 0, nslots_of(H + 1) - nslots_of(H), s));
+    CK(cudaMemsetAsync(h->c.fl + nseg_of(H), 0xFF, (nseg_of(H + 1) - nseg_of(H)) * sizeof(ulonglong2), s));
+    launch_levelup_cnt(h->c.cnt, h->c.cnt_alt, H, s);
+    std::swap(h->c.cnt, h->c.cnt_alt);
+    h->H = H + 1;
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+// Rebuild at height hh (rebuild_rpma, rpma.cuh:1417-1472): every kept key of
+// the current array plus the list's inserts, spread over the new array.
+lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_list, uint64_t m, uint32_t thres,
+                      bool thres_active, cudaStream_t s, LpmaStats *st) {
+    if (hh > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
+    const uint32_t H = h->H;
+    CKS(tile_prep(h, u, n_list, thres_active, s));
+    Cap fresh;
+    const bool grow = hh > h->c.Hc;
+    if (grow) CK(alloc_cap(fresh, std::min<uint32_t>(hh + 1, LPMA_MAX_HEIGHT)));
+    Geo src{h->c.keys, h->c.vals, H};
+    Geo dst = grow ? Geo{fresh.keys, fresh.vals, hh} : Geo{h->c.keys_alt, h->c.vals_alt, hh};
+    uint8_t *cnt_d = grow ? fresh.cnt : h->c.cnt;
+    ulonglong2 *fl_d = grow ? fresh.fl : h->c.fl;
+    const uint32_t df = (uint32_t)nseg_of(hh);
+    h->jobs_h.assign(1, TileJob{0, (uint32_t)nseg_of(H), 0, df, (uint32_t)m, (df + 31) / 32, 0, 0});
+    CKS(upload_jobs(h, s));
+    launch_exec_tiles(h->jobs_d, 1, (df + 31) / 32, src, h->c.srcc, h->c.PQ, h->c.US, dst, cnt_d, fl_d, h->sent, h->V,
+                      u, thres, h->dst, s);
+    CK(cudaGetLastError());
+    if (grow) {
+        CK(cudaStreamSynchronize(s));
+        free_cap(h->c);
+        h->c = fresh;
+    } else {
+        std::swap(h->c.keys, h->c.keys_alt);
+        std::swap(h->c.vals, h->c.vals_alt);
+        if (hh < H) CK(cudaMemsetAsync(h->c.cnt + nseg_of(hh), 0, nseg_of(H) - nseg_of(hh) + 64, s));
+    }
+    h->H = hh;
+    st->rebuilt = 1;
+    st->slots_rewritten += nslots_of(hh);
+    return LPMA_OK;
+}
+
+lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins,
+                        const uint64_t *del, size_t n_del, uint32_t thres, cudaStream_t s, LpmaStats *out,
+                        bool internal) {
+    if (h->sticky != LPMA_OK) return h->sticky;
+    LpmaStats st{};
+    st.height_before = h->H;
+    const size_t n = n_ins + n_del;
+    if ((n_ins && !ins) || (n_del && !del)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (n == 0) {
+        st.height_after = h->H;
+        st.num_items = h->total;
+        if (out) *out = st;
+        return LPMA_OK;
+    }
+    if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (thres > 0xFFFFF) return LPMA_ERR_INVALID_ARGUMENT;
+    if (min_height(h->total + n_ins) > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
+    CKS(ensure_batch(h, n));
+    h->view_valid = false;
+    const bool thres_active = thres > h->min_t;
+
+    // 1. pack + validate
+    CK(cudaMemcpyAsync(h->dst, h->hinit, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    // the engine's own sentinel keys are always in the packed layout
+    const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
+    launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
+                h->bk0, h->bp0, h->dst, s);
+    if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
+    CKS(sync_status(h, s));
+    if (h->hst->error & ERR_KEY) return LPMA_ERR_INVALID_KEY;
+    const uint64_t diff = h->hst->key_and ^ h->hst->key_or;
+    const uint32_t min_t_ins = h->hst->min_t_ins;
+    const int64_t live_before = thres_active ? (int64_t)h->hst->live_total : (int64_t)h->total;
+
+    // 2. sort, resolve + locate, compact (mutations: upserts, tombstones)
+    int which = 0;
+    CK(sort_pairs<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, diff, h->sort, &h->dst->error, s, &which));
+    const uint64_t *sk = which ? h->bk1 : h->bk0;
+    const uint16_t *sp = which ? h->bp1 : h->bp0;
+    Geo g{h->c.keys, h->c.vals, h->H};
+    launch_resolve_locate(sk, sp, (uint32_t)n, g, h->c.fl, thres, h->kind, h->seg, h->blk_nn, h->blk_ins, h->dst, s);
+    launch_compact(sk, sp, h->kind, h->seg, (uint32_t)n, h->blk_nn, h->blk_ins, h->u, h->dst, s);
+
+    // 3. plan the first loop
+    Tables tb = make_tables(h, h->H, true);
+    CKS(run_plan(h, h->u, (uint32_t)n, thres_active, (uint64_t)live_before, tb, s));
+    lpma_status_t rs = sync_status(h, s);
+    if (rs != LPMA_OK) return h->sticky = rs;
+    const uint32_t n_u = h->hst->n_u, n_new = h->hst->n_ins, n_gone = h->hst->n_del;
+    st.n_ins_applied = n_new;
+    st.n_del_applied = n_gone;
+    st.n_upserts = h->hst->n_upsert;
+    st.n_noop = h->hst->n_noop;
+    const int64_t live_after = live_before - n_gone + n_new;
+
+    lpma_status_t r = LPMA_OK;
+    if (n_u > 0 && !h->hst->ovf) {
+        const bool root = h->hst->root != 0;
+        r = exec_plan(h, h->u, (uint32_t)n, thres, thres_active, s, &st);
+        if (r == LPMA_OK && root) {
+            st.root_executed = 1;
+            if (min_height((uint64_t)live_after) + 1 > h->H) {  // eager level-up
+                r = level_up(h, s);
+                st.eager_levelup = 1;
+            }
+        }
+    } else if (n_u > 0) {
+        st.overflow = 1;
+        const uint32_t hh = min_height((uint64_t)live_after);
+        if (hh == h->H + 1) {
+            st.levelup_path = 1;
+            r = exec_plan(h, h->u, (uint32_t)n, thres, thres_active, s, &st);
+            if (r == LPMA_OK) r = level_up(h, s);
+            if (r == LPMA_OK) {
+                launch_compact_pending(h->u, h->pend, n_u, h->u2, h->blk_nn, h->blk_ins, h->dst, s);
+                r = sync_status(h, s);
+            }
+            if (r == LPMA_OK) {
+                const uint32_t n2 = h->hst->n_u, i2 = h->hst->n_ins, d2 = h->hst->n_del;
+                const int64_t live_mid = live_before - (int64_t)(n_gone - d2) + (int64_t)(n_new - i2);
+                Geo g2{h->c.keys, h->c.vals, h->H};
+                launch_relocate(h->u2, n2, g2, h->c.fl, s);
+                if (thres_active) {
+                    CK(cudaMemsetAsync(&h->dst->live_total, 0, 8, s));
+                    launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
+                }
+                Tables tb2 = make_tables(h, h->H, false);
+                r = run_plan(h, h->u2, n2, thres_active, (uint64_t)live_mid, tb2, s);
+                if (r == LPMA_OK) r = sync_status(h, s);
+                if (r == LPMA_OK && h->hst->ovf) {
+                    // the reference asserts here (rpma.cuh:1704); rebuild instead
+                    r = rebuild(h, min_height((uint64_t)live_after), h->u2, n2, (uint64_t)live_after, thres,
+                                thres_active, s, &st);
+                } else if (r == LPMA_OK) {
+                    r = exec_plan(h, h->u2, n2, thres, thres_active, s, &st);
+                    if (r == LPMA_OK && h->H > 0) {  // fill_empty_segs, rpma.cuh:1474-1530
+                        CK(cudaMemsetAsync(&h->dst->empty_found, 0, 4, s));
+                        launch_check_empty_level(h->c.cnt, h->H, h->dst, s);
+                        r = sync_status(h, s);
+                        if (r == LPMA_OK && h->hst->empty_found) {
+                            if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
+                            r = rebuild(h, h->H, h->u2, 0, (uint64_t)live_after, thres, thres_active, s, &st);
+                            st.rebuilt = 0;
+                            st.fill_empty = 1;
+                        }
+                    }
+                }
+            }
+        } else {
+            // h < H, h > H+1 (and h == H, where the reference asserts): rebuild
+            r = rebuild(h, hh, h->u, (uint32_t)n, (uint64_t)live_after, thres, thres_active, s, &st);
+        }
+    }
+    if (r != LPMA_OK) return h->sticky = r;
+    if (thres_active) {
+        CK(cudaMemsetAsync(&h->dst->cnt_total, 0, 8, s));
+        launch_sum_cnt(h->c.cnt, nseg_of(h->H), h->dst, s);
+    }
+    rs = sync_status(h, s);
+    if (rs != LPMA_OK) return h->sticky = rs;
+    h->total = thres_active ? h->hst->cnt_total : (uint64_t)live_after;
+    if (n_new && min_t_ins < h->min_t) h->min_t = min_t_ins;
+    st.height_after = h->H;
+    st.num_items = h->total;
+    if (out) *out = st;
+    return LPMA_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+lpma_status_t lpma_config_default(LpmaConfig *cfg) {
+    if (!cfg) return LPMA_ERR_INVALID_ARGUMENT;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->segment_length = 32;
+    cfg->key_format = LPMA_KEY_PACKED;
+    cfg->skip_rule = 1;
+    cfg->density_lower_root = 0.42;
+    cfg->density_upper_root = 1.0;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_destroy(LpmaHandle *h) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    free_cap(h->c);
+    dfree(h->sent), dfree(h->dst);
+    if (h->hst) cudaFreeHost(h->hst);
+    if (h->hinit) cudaFreeHost(h->hinit);
+    dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
+    dfree(h->blk_nn), dfree(h->blk_ins);
+    for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
+    dfree(h->cand), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status), dfree(h->sort.hist), dfree(h->sort.counters);
+    dfree(h->jobs_d);
+    dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
+    dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals), dfree(h->exp_keys), dfree(h->exp_vals);
+    delete h;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_stream_t stream, LpmaHandle **out) {
+    if (!out) return LPMA_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    LpmaConfig c;
+    if (cfg)
+        c = *cfg;
+    else
+        lpma_config_default(&c);
+    if (c.segment_length != 32 || c.key_format > 1 || !(c.density_lower_root >= 0.0 && c.density_lower_root <= 1.0) ||
+        c.density_upper_root != 1.0)
+        return LPMA_ERR_INVALID_ARGUMENT;
+    if (num_vertices == 0 || num_vertices > NBR_END) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    LpmaHandle *h = new LpmaHandle();
+    h->cfg = c;
+    h->V = num_vertices;
+    auto fail = [&](lpma_status_t r) {
+        lpma_destroy(h);
+        return r;
+    };
+    if (cudaMalloc(&h->dst, sizeof(DevStatus)) || cudaMallocHost(&h->hst, sizeof(DevStatus)) ||
+        cudaMallocHost(&h->hinit, sizeof(DevStatus)) || dalloc(&h->sent, num_vertices) ||
+        dalloc(&h->sort.hist, 8 * 256) || dalloc(&h->sort.counters, 16) || dalloc(&h->sort_err, 1))
+        return fail(LPMA_ERR_OUT_OF_MEMORY);
+    std::memset(h->hinit, 0, sizeof(DevStatus));
+    h->hinit->min_t_ins = 0xFFFFFFFFu;
+    h->hinit->key_and = ~0ull;
+    h->hinit->err_info[0] = 0xFFFFFFFFu;
+    if (alloc_cap(h->c, std::min<uint32_t>(min_height(num_vertices) + 1, LPMA_MAX_HEIGHT)) != cudaSuccess)
+        return fail(LPMA_ERR_OUT_OF_MEMORY);
+    // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
+    h->H = 0;
+    if (cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) || cudaMemsetAsync(h->c.vals, 0, 32, s) ||
+        cudaMemsetAsync(h->c.fl, 0xFF, sizeof(ulonglong2), s) || cudaMemsetAsync(h->sent, 0, 4ull * num_vertices, s))
+        return fail(LPMA_ERR_CUDA);
+    // the sentinels through the update path (init_csr_rpma, rpma.cuh:1819-1823)
+    uint64_t *sk = nullptr;
+    uint8_t *sv = nullptr;
+    if (dalloc(&sk, num_vertices) || dalloc(&sv, num_vertices)) return fail(LPMA_ERR_OUT_OF_MEMORY);
+    launch_sentinels(num_vertices, sk, sv, s);
+    lpma_status_t r = do_update(h, sk, sv, num_vertices, nullptr, 0, 0, s, nullptr, true);
+    cudaStreamSynchronize(s);
+    cudaFree(sk);
+    cudaFree(sv);
+    if (r != LPMA_OK) return fail(r);
+    h->min_t = 0xFFFFF;
+    *out = h;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_build(LpmaHandle *h, const uint64_t *d_keys, const uint8_t *d_vals, size_t n, lpma_stream_t stream) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    return do_update(h, d_keys, d_vals, n, nullptr, 0, 0, (cudaStream_t)stream, nullptr, false);
+}
+
+lpma_status_t lpma_update(LpmaHandle *h, const uint64_t *d_ins, const uint8_t *d_ins_vals, size_t n_ins,
+                          const uint64_t *d_del, size_t n_del, uint32_t thres, lpma_stream_t stream, LpmaStats *stats) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    return do_update(h, d_ins, d_ins_vals, n_ins, d_del, n_del, thres, (cudaStream_t)stream, stats, false);
+}
+
+lpma_status_t lpma_update_host(LpmaHandle *h, const uint64_t *h_ins, const uint8_t *h_ins_vals, size_t n_ins,
+                               const uint64_t *h_del, size_t n_del, uint32_t thres, lpma_stream_t stream,
+                               LpmaStats *stats) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if ((n_ins && !h_ins) || (n_del && !h_del)) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t need = std::max(n_ins, n_del);
+    if (need > h->stage_cap) {
+        dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
+        h->stage_cap = 0;
+        size_t cap = need + need / 4;
+        if (dalloc(&h->stage_ins, cap) || dalloc(&h->stage_del, cap) || dalloc(&h->stage_vals, cap))
+            return LPMA_ERR_OUT_OF_MEMORY;
+        h->stage_cap = cap;
+    }
+    if (n_ins && cudaMemcpyAsync(h->stage_ins, h_ins, n_ins * 8, cudaMemcpyHostToDevice, s)) return LPMA_ERR_CUDA;
+    if (n_ins && h_ins_vals && cudaMemcpyAsync(h->stage_vals, h_ins_vals, n_ins, cudaMemcpyHostToDevice, s))
+        return LPMA_ERR_CUDA;
+    if (n_del && cudaMemcpyAsync(h->stage_del, h_del, n_del * 8, cudaMemcpyHostToDevice, s)) return LPMA_ERR_CUDA;
+    return do_update(h, h->stage_ins, h_ins_vals ? h->stage_vals : nullptr, n_ins, h->stage_del, n_del, thres, s,
+                     stats, false);
+}
+
+static lpma_status_t fill_view(LpmaHandle *h, cudaStream_t s, bool csr, bool exp) {
+    const uint64_t nseg = nseg_of(h->H);
+    const size_t nnz = h->total;
+    if (csr && nnz + 1 > h->view_cap) {
+        dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals);
+        h->view_cap = 0;
+        if (dalloc(&h->row_offset, h->V + 1) || dalloc(&h->col_index, nnz + 1) || dalloc(&h->view_vals, nnz + 1))
+            return LPMA_ERR_OUT_OF_MEMORY;
+        h->view_cap = nnz + 1;
+    }
+    if (exp && nnz + 1 > h->exp_cap) {
+        dfree(h->exp_keys), dfree(h->exp_vals);
+        h->exp_cap = 0;
+        if (dalloc(&h->exp_keys, nnz + 1) || dalloc(&h->exp_vals, nnz + 1)) return LPMA_ERR_OUT_OF_MEMORY;
+        h->exp_cap = nnz + 1;
+    }
+    CK(scan_u8_to_u32(h->c.cnt, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
+    if (csr) CK(cudaMemsetAsync(h->row_offset, 0, 4ull * (h->V + 1), s));
+    Geo g{h->c.keys, h->c.vals, h->H};
+    launch_csr_fill(g, h->c.cnt, h->c.segP, csr ? h->row_offset : nullptr, csr ? h->col_index : nullptr,
+                    csr ? h->view_vals : nullptr, exp ? h->exp_keys : nullptr, exp ? h->exp_vals : nullptr, s);
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_csr_view(LpmaHandle *h, const uint32_t **row_offset, const uint32_t **col_index,
+                            const uint8_t **values, size_t *nnz, lpma_stream_t stream) {
+    if (!h || !row_offset || !col_index || !nnz) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!h->view_valid) {
+        CKS(fill_view(h, s, true, false));
+        h->view_valid = true;
+    }
+    *row_offset = h->row_offset;
+    *col_index = h->col_index;
+    if (values) *values = h->view_vals;
+    *nnz = h->total;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_to_csr(LpmaHandle *h, uint32_t *row_offset, uint32_t *col_index, uint8_t *values, size_t cap,
+                          size_t *nnz, lpma_stream_t stream) {
+    if (!h || !nnz) return LPMA_ERR_INVALID_ARGUMENT;
+    const uint32_t *ro, *ci;
+    const uint8_t *va;
+    size_t n;
+    lpma_status_t r = lpma_csr_view(h, &ro, &ci, &va, &n, stream);
+    if (r != LPMA_OK) return r;
+    *nnz = n;
+    if (!row_offset && !col_index && !values) return LPMA_OK;
+    if ((col_index || values) && cap < n) return LPMA_ERR_BUFFER_TOO_SMALL;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (row_offset) CK(cudaMemcpyAsync(row_offset, ro, 4ull * (h->V + 1), cudaMemcpyDefault, s));
+    if (col_index) CK(cudaMemcpyAsync(col_index, ci, 4 * n, cudaMemcpyDefault, s));
+    if (values) CK(cudaMemcpyAsync(values, va, n, cudaMemcpyDefault, s));
+    CK(cudaStreamSynchronize(s));
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_export_sorted(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_vals, size_t cap, size_t *n,
+                                 lpma_stream_t stream) {
+    if (!h || !n) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    *n = h->total;
+    if (!h_keys) return LPMA_OK;
+    if (cap < h->total) return LPMA_ERR_BUFFER_TOO_SMALL;
+    cudaStream_t s = (cudaStream_t)stream;
+    CKS(fill_view(h, s, false, true));
+    CK(cudaMemcpyAsync(h_keys, h->exp_keys, h->total * 8, cudaMemcpyDeviceToHost, s));
+    if (h_vals) CK(cudaMemcpyAsync(h_vals, h->exp_vals, h->total, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_export_layout(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_vals, size_t cap_slots,
+                                 uint32_t *sentinel_slots, size_t cap_vertices, uint32_t *height,
+                                 lpma_stream_t stream) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    if (height) *height = h->H;
+    const uint64_t ns = nslots_of(h->H);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h_keys) {
+        if (cap_slots < ns) return LPMA_ERR_BUFFER_TOO_SMALL;
+        CK(cudaMemcpyAsync(h_keys, h->c.keys, ns * 8, cudaMemcpyDeviceToHost, s));
+        if (h_vals) CK(cudaMemcpyAsync(h_vals, h->c.vals, ns, cudaMemcpyDeviceToHost, s));
+    }
+    if (sentinel_slots) {
+        if (cap_vertices < h->V) return LPMA_ERR_BUFFER_TOO_SMALL;
+        CK(cudaMemcpyAsync(sentinel_slots, h->sent, 4ull * h->V, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    if (h_keys && h_vals)
+        for (uint64_t i = 0; i < ns; i++)
+            if (h_keys[i] == KEY_NONE) h_vals[i] = 0;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_info(const LpmaHandle *h, uint32_t *height, uint64_t *num_items, uint32_t *num_vertices) {
+    if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (height) *height = h->H;
+    if (num_items) *num_items = h->total;
+    if (num_vertices) *num_vertices = h->V;
+    return LPMA_OK;
+}
+
+const char *lpma_status_string(lpma_status_t s) {
+    switch (s) {
+        case LPMA_OK: return "ok";
+        case LPMA_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case LPMA_ERR_INVALID_KEY: return "invalid key in batch";
+        case LPMA_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case LPMA_ERR_CUDA: return "CUDA runtime error";
+        case LPMA_ERR_CAPACITY: return "tree height limit exceeded";
+        case LPMA_ERR_INTERNAL: return "internal consistency check failed";
+        case LPMA_ERR_TIMEOUT: return "bounded device wait gave up";
+        case LPMA_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+    }
+    return "unknown status";
+}
+
+uint64_t lpma_kernel_launches(void) { return lpma::launch_count(); }
+
+lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edge_factor, uint32_t ta, uint32_t tab,
+                            uint32_t tabc, uint64_t *d_out, size_t cap, size_t *n_out, lpma_stream_t stream) {
+    if (!d_out || !n_out || scale == 0 || scale > 22) return LPMA_ERR_INVALID_ARGUMENT;
+    const uint64_t n = (1ull << scale) * edge_factor;
+    if (n >= (1ull << 30)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (cap < n) return LPMA_ERR_BUFFER_TOO_SMALL;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t *tmp = nullptr;
+    uint16_t *p0 = nullptr, *p1 = nullptr;
+    uint32_t *flags = nullptr, *pos = nullptr, *total = nullptr, *stmp = nullptr, *err = nullptr;
+    SortScratch ss;
+    ss.status_words = sort_status_words((uint32_t)n);
+    lpma_status_t r = LPMA_OK;
+    if (dalloc(&tmp, n) || dalloc(&p0, n) || dalloc(&p1, n) || dalloc(&flags, n) || dalloc(&pos, n) ||
+        dalloc(&total, 1) || dalloc(&stmp, scan_tmp_words((uint32_t)n) + 64) || dalloc(&err, 1) ||
+        dalloc(&ss.status, ss.status_words) || dalloc(&ss.hist, 8 * 256) || dalloc(&ss.counters, 16)) {
+        r = LPMA_ERR_OUT_OF_MEMORY;
+    } else {
+        cudaMemsetAsync(p0, 0, n * 2, s);
+        cudaMemsetAsync(err, 0, 4, s);
+        launch_rmat(seed, scale, n, ta, tab, tabc, d_out, s);
+        int which = 0;
+        cudaError_t e = sort_pairs<uint16_t>(d_out, p0, tmp, p1, (uint32_t)n, ~0ull, ss, err, s, &which);
+        uint64_t *sorted = which ? tmp : d_out;
+        uint64_t *other = which ? d_out : tmp;
+        if (!e) {
+            launch_unique_flags(sorted, n, flags, s);
+            e = scan_u32(flags, pos, (uint32_t)n, total, stmp, s);
+        }
+        if (!e) {
+            launch_scatter_flags(sorted, pos, flags, n, other, s);
+            if (other != d_out) e = cudaMemcpyAsync(d_out, other, n * 8, cudaMemcpyDeviceToDevice, s);
+        }
+        uint32_t tot = 0, herr = 0;
+        if (!e) e = cudaMemcpyAsync(&tot, total, 4, cudaMemcpyDeviceToHost, s);
+        if (!e) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+        if (!e) e = cudaStreamSynchronize(s);
+        if (e)
+            r = cuda_fail(e);
+        else if (herr)
+            r = LPMA_ERR_TIMEOUT;
+        *n_out = tot;
+    }
+    cudaStreamSynchronize(s);
+    dfree(tmp), dfree(p0), dfree(p1), dfree(flags), dfree(pos), dfree(total), dfree(stmp), dfree(err);
+    dfree(ss.status), dfree(ss.hist), dfree(ss.counters);
+    return r;
+}
+
+lpma_status_t lpma_shuffle(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream) {
+    if (!d_keys || n >= (1ull << 30)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (n < 2) return LPMA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t *tmp = nullptr, *hash = nullptr, *hash2 = nullptr, *pay2 = nullptr;
+    uint16_t *p0 = nullptr, *p1 = nullptr;
+    uint32_t *err = nullptr;
+    SortScratch ss;
+    ss.status_words = sort_status_words((uint32_t)n);
+    lpma_status_t r = LPMA_OK;
+    if (dalloc(&tmp, n) || dalloc(&hash, n) || dalloc(&hash2, n) || dalloc(&pay2, n) || dalloc(&p0, n) ||
+        dalloc(&p1, n) || dalloc(&err, 1) || dalloc(&ss.status, ss.status_words) || dalloc(&ss.hist, 8 * 256) ||
+        dalloc(&ss.counters, 16)) {
+        r = LPMA_ERR_OUT_OF_MEMORY;
+    } else {
+        cudaMemsetAsync(p0, 0, n * 2, s);
+        cudaMemsetAsync(err, 0, 4, s);
+        int which = 0;
+        // (hash, key) order: keys ascending, then a stable sort by hash
+        cudaError_t e = sort_pairs<uint16_t>(d_keys, p0, tmp, p1, (uint32_t)n, ~0ull, ss, err, s, &which);
+        uint64_t *sorted = which ? tmp : d_keys;
+        if (!e) {
+            launch_hash_keys(seed, sorted, hash, n, s);
+            e = sort_pairs<uint64_t>(hash, sorted, hash2, pay2, (uint32_t)n, ~0ull, ss, err, s, &which);
+        }
+        uint64_t *res = which ? pay2 : sorted;
+        if (!e && res != d_keys) e = cudaMemcpyAsync(d_keys, res, n * 8, cudaMemcpyDeviceToDevice, s);
+        uint32_t herr = 0;
+        if (!e) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+        if (!e) e = cudaStreamSynchronize(s);
+        if (e)
+            r = cuda_fail(e);
+        else if (herr)
+            r = LPMA_ERR_TIMEOUT;
+    }
+    cudaStreamSynchronize(s);
+    dfree(tmp), dfree(hash), dfree(hash2), dfree(pay2), dfree(p0), dfree(p1), dfree(err);
+    dfree(ss.status), dfree(ss.hist), dfree(ss.counters);
+    return r;
+}
+
+}  // extern "C"

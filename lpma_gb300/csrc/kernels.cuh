@@ -1,0 +1,102 @@
+// Launchers for the update-path and view kernels (definitions in update.cu
+// and view.cu).  Host orchestration lives in abi.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lpma_common.cuh"
+
+namespace lpma {
+
+struct UpdList {  // compacted, key-sorted update list
+    uint64_t *key;
+    uint8_t *val;
+    uint8_t *kind;
+    uint32_t *seg;  // linear segment located for the key
+    uint32_t *ip;   // exclusive count of inserts before each entry (n+1 entries)
+};
+
+struct Geo {  // one tree geometry in HBM
+    uint64_t *keys;
+    uint8_t *vals;
+    uint32_t H;
+};
+
+// validate + pack both input arrays into one key/payload array; payload bits
+// 0-7 = value, bit 8 = delete
+void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del,
+                 uint32_t n_del, uint32_t V, uint32_t thres, uint32_t key_format, int internal,
+                 uint64_t *keys_out, uint16_t *pay_out, DevStatus *st, cudaStream_t s);
+
+// per-segment live counts (key present and t >= thres) + their total
+void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_t *cnt_live, DevStatus *st,
+                        cudaStream_t s);
+
+// collapse duplicates, locate every key, membership test against its
+// segment, upsert/tombstone in place; per-256-block counts of kept entries
+void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t n, Geo g, const ulonglong2 *fl,
+                           uint32_t thres, uint8_t *kind, uint32_t *seg, uint32_t *blk_nn, uint32_t *blk_ins,
+                           DevStatus *st, cudaStream_t s);
+
+void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *kind, const uint32_t *seg,
+                    uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins, UpdList u, DevStatus *st, cudaStream_t s);
+
+// locate only (second loop after a level-up): u.seg from u.key
+void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s);
+
+// keep only updates flagged pending; rebuilds ip
+void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, UpdList out, uint32_t *blk_nn,
+                            uint32_t *blk_ins, DevStatus *st, cudaStream_t s);
+
+// count-only planner: per segment with updates, the first level whose
+// window passes the density test; maximal windows go to small/big lists
+void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
+                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand,
+                 Window *small, Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s);
+
+// warp-grain executor for windows of <= 32 segments, in place
+void launch_exec_small(const Window *w, uint32_t n_small, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+                       uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
+
+// per-segment counts for the tile grain: qi/qd from the update list
+void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
+                              cudaStream_t s);
+// q[s] = kept(s) + ins(s), qn[s] = ins(s) + del(s), srcc[s] = cnt[s]
+void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
+                  uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s);
+
+struct TileJob {
+    uint32_t sa, sf;  // source linear segment range
+    uint32_t da, df;  // destination linear segment range
+    uint32_t m;       // items
+    uint32_t tiles;   // ceil(df / 32)
+    uint32_t tile0;   // first tile index of this job
+    uint32_t pad;
+};
+// tile-grain executor: merge source windows with their inserts and spread
+// them over the destination geometry (another buffer)
+void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo src, const uint8_t *srcc,
+                       const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
+void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to,
+                          cudaStream_t s);
+
+// new level: cnt re-index (old s -> 2s+1), empty leaves
+void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s);
+void launch_check_empty_level(const uint8_t *cnt, uint32_t H, DevStatus *st, cudaStream_t s);
+void launch_sum_cnt(const uint8_t *cnt, uint64_t nseg, DevStatus *st, cudaStream_t s);
+
+// view
+void launch_csr_fill(Geo g, const uint8_t *cnt, const uint32_t *P, uint32_t *row_offset, uint32_t *col_index,
+                     uint8_t *values, uint64_t *export_keys, uint8_t *export_vals, cudaStream_t s);
+
+// generators
+void launch_sentinels(uint32_t V, uint64_t *keys, uint8_t *vals, cudaStream_t s);
+void launch_rmat(uint64_t seed, uint32_t scale, uint64_t n, uint32_t ta, uint32_t tab, uint32_t tabc, uint64_t *out,
+                 cudaStream_t s);
+void launch_hash_keys(uint64_t seed, const uint64_t *keys, uint64_t *hash, uint64_t n, cudaStream_t s);
+void launch_unique_flags(const uint64_t *keys, uint64_t n, uint32_t *flags, cudaStream_t s);
+void launch_scatter_flags(const uint64_t *keys, const uint32_t *pos, const uint32_t *flags, uint64_t n,
+                          uint64_t *out, cudaStream_t s);
+
+}  // namespace lpma

@@ -1,0 +1,112 @@
+// Shared definitions of the GB300 LPMA engine: key layout, segment-tree index
+// algebra, the device status block and small device utilities.
+//
+// Layout in HBM.  A tree of height H has 2^(H+1) - 1 segments of 32 slots.
+// The reference stores tree level i as its own array of 32 << i slots
+// (rpma.cuh:1396-1415); here the level arrays are laid end to end in one
+// allocation, which is heap (Eytzinger) order: segment j of level i sits at
+// heap index 2^i - 1 + pos, slots [32 j, 32 j + 32).  Adding a level appends
+// 32 << (H+1) slots and moves nothing.  The logical ("linear") order of the
+// segments is the in-order traversal: linear segment s lives at level
+// H - ctz(s+1), position (s+1) >> (ctz(s+1)+1) (GET_IDX/GET_LANE,
+// rpma.cuh:132-134).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lpma {
+
+constexpr uint64_t KEY_NONE = ~0ull;                        // rpma.cuh:38
+constexpr uint8_t VAL_TOMB = 0xFF;                          // VALUE_NONE, rpma.cuh:41 / gpma.cuh:33
+constexpr uint64_t TIME_MASK = 0x00000000000FFFFFull;       // rpma.cuh:47
+constexpr uint64_t DST_MASK = 0x000003FFFFF00000ull;        // rpma.cuh:45
+constexpr uint64_t DST_AND_TIME_MASK = 0x000003FFFFFFFFFFull;  // rpma.cuh:48
+constexpr uint64_t DST_AND_TIME_END = 0x000003FFFFEFFFFFull;   // rpma.cuh:49
+constexpr uint32_t SRC_SHIFT = 42, DST_SHIFT = 20;
+constexpr uint32_t NBR_END = 0x003FFFFEu;                   // rpma.cuh:50
+constexpr uint32_t SEG = 32;                                // rpma.cuh:1769
+constexpr uint32_t MAX_HEIGHT = 24;
+constexpr uint32_t KIND_NOP = 0, KIND_INS = 1, KIND_DEL = 2;
+constexpr uint32_t EXEC_OVF = 0xFF;                         // no window absorbed the segment
+constexpr uint32_t SMALL_WIN_SEGS = 32;                     // warp-grain windows: <= 32 segments
+
+// error bits of DevStatus::error
+constexpr uint32_t ERR_KEY = 1u, ERR_INTERNAL = 2u, ERR_TIMEOUT = 4u;
+
+__host__ __device__ inline uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+__host__ __device__ inline uint64_t nseg_of(uint32_t H) { return (2ull << H) - 1; }
+__host__ __device__ inline uint64_t nslots_of(uint32_t H) { return 32ull * nseg_of(H); }
+
+// heap index of linear segment s in a tree of height H
+__host__ __device__ inline uint64_t heap_of_linear(uint64_t s, uint32_t H) {
+    uint64_t s1 = s + 1;
+#ifdef __CUDA_ARCH__
+    uint32_t t = (uint32_t)__ffsll((long long)s1) - 1;
+#else
+    uint32_t t = (uint32_t)__builtin_ctzll(s1);
+#endif
+    uint32_t level = H - t;
+    return ((1ull << level) - 1) + (s1 >> (t + 1));
+}
+
+// linear segment of heap index j at level `level` of a tree of height H
+__host__ __device__ inline uint64_t linear_of_heap(uint64_t j, uint32_t level, uint32_t H) {
+    uint64_t pos = j - ((1ull << level) - 1);
+    return ((2 * pos + 1) << (H - level)) - 1;
+}
+
+__host__ __device__ inline bool is_sentinel(uint64_t key) {
+    return (key & DST_AND_TIME_MASK) == DST_AND_TIME_END;
+}
+
+__host__ __device__ inline bool kept_slot(uint64_t key, uint8_t val, uint32_t thres) {
+    return key != KEY_NONE && val != VAL_TOMB && (key & TIME_MASK) >= (uint64_t)thres;
+}
+
+// first destination rank of segment k when m items spread over f segments:
+// item i goes to segment floor(f*i/m) (rpma.cuh:677-679, 965-967), so
+// segment k starts at ceil(k*m/f) and its items are packed from lane 0.
+__host__ __device__ inline uint64_t first_rank(uint64_t k, uint64_t m, uint64_t f) {
+    return (k * m + f - 1) / f;
+}
+
+// Device status block, one per handle.  The host reads it at the two sync
+// points of an update call.
+struct DevStatus {
+    uint32_t error;
+    uint32_t min_t_ins;       // min timestamp over inserted keys (atomicMin)
+    unsigned long long key_and, key_or;
+    uint32_t n_u;             // compacted updates
+    uint32_t n_ins, n_del, n_upsert, n_noop;
+    uint32_t n_cand, n_small, n_big;
+    uint32_t root, ovf;
+    uint32_t empty_found;     // fill_empty_segs check
+    uint32_t pad0;
+    unsigned long long slots_small, slots_big;
+    unsigned long long live_total;   // sum of live counts (thres pass)
+    unsigned long long cnt_total;    // sum of occupancy counts (recount)
+    uint32_t err_info[4];            // first offending input index, internal-check site
+};
+
+// A rebalance window chosen by the planner (maximal executed window).
+struct Window {
+    uint32_t a;      // first linear segment
+    uint32_t f;      // segments (clipped)
+    uint32_t m;      // items after the update
+    uint32_t level;
+    uint32_t lo, hi; // range in the compacted update list
+};
+
+struct Tables {
+    uint32_t lower[32];  // trunc(0.42 * 32 * 2^i), rpma.cuh:164
+    uint32_t allowed;    // bit l: windows of level l may execute
+};
+
+__device__ inline uint32_t lanemask_lt() {
+    uint32_t r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+}  // namespace lpma

@@ -1,0 +1,440 @@
+// Radix sort and scan primitives (hand-written, sm_103a).
+//
+// Sort: LSD radix sort on 8-bit digits in the single-pass "onesweep" form
+// (Adinets & Merrill, 2022): one histogram kernel for every digit, then one
+// kernel per digit pass.  Each CTA takes a 4096-key tile in dynamic order,
+// ranks the keys of each warp with __match_any_sync, publishes its per-digit
+// tile count and resolves its global offset by decoupled look-back over the
+// tiles before it.  Every look-back wait is bounded: when a predecessor does
+// not publish within the bound, the kernel sets ERR_TIMEOUT and returns.
+// Batches of at most one tile are sorted by one CTA entirely in shared
+// memory in a single launch.
+#include <atomic>
+
+#include "lpma_common.cuh"
+#include "prims.cuh"
+
+namespace lpma {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(int k) { g_launches += (uint64_t)k; }
+uint64_t launch_count() { return g_launches.load(); }
+
+namespace {
+
+constexpr uint32_t FLAG_AGG = 1u << 30, FLAG_PREFIX = 2u << 30, VAL_MASK = (1u << 30) - 1;
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
+
+__device__ inline uint32_t ld_acquire(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ inline void st_release(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim == 256).
+__device__ inline uint32_t block_excl_scan_256(uint32_t x, uint32_t *wsum /*[8]*/, uint32_t *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < 8 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < 8) wsum[lane] = s;  // inclusive warp sums
+    }
+    __syncthreads();
+    uint32_t base = w ? wsum[w - 1] : 0;
+    if (total) *total = wsum[7];
+    uint32_t r = base + v - x;
+    __syncthreads();
+    return r;
+}
+
+// Rank the IPT keys each lane holds among the keys of its warp with the same
+// digit.  Keys of warp w are at tile positions w*32*IPT + i*32 + lane, so
+// the rank order is the input order.  whist[256] is this warp's digit
+// counter row (zeroed by the caller); on return it holds the warp's counts.
+template <int IPT>
+__device__ inline void warp_rank(const uint64_t (&k)[IPT], uint32_t valid_mask, int sh, uint32_t *whist,
+                                 uint32_t (&rank)[IPT]) {
+    const uint32_t lt = lanemask_lt();
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+        const bool valid = (valid_mask >> i) & 1u;
+        const uint32_t d = valid ? (uint32_t)((k[i] >> sh) & 0xFF) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t b = 0;
+        if (valid) b = whist[d];
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) whist[d] = b + __popc(peers);
+        __syncwarp();
+        rank[i] = b + __popc(peers & lt);
+    }
+}
+
+// ---------------------------------------------------------------- histogram
+__global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys, uint32_t n, uint32_t *hist) {
+    __shared__ uint32_t h[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
+        uint64_t k = keys[i];
+#pragma unroll
+        for (int b = 0; b < 8; b++) atomicAdd(&h[b][(k >> (8 * b)) & 0xFF], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 256; i += 256) {
+        uint32_t c = (&h[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// ---------------------------------------------------------------- one pass
+template <typename V>
+struct PassSmem {
+    uint64_t k[SORT_TILE];
+    V v[SORT_TILE];
+    uint32_t whist[8][256];
+    uint32_t gbase[256];
+    uint32_t ldig[256];
+    uint32_t wsum[8];
+    uint32_t tile;
+};
+
+template <typename V>
+__global__ void __launch_bounds__(SORT_TPB) k_pass(const uint64_t *__restrict__ ki, const V *__restrict__ vi,
+                                                   uint64_t *__restrict__ ko, V *__restrict__ vo, uint32_t n,
+                                                   int byte, const uint32_t *__restrict__ hist,
+                                                   uint32_t *status, uint32_t *counter, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PassSmem<V> &S = *reinterpret_cast<PassSmem<V> *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int sh = byte * 8;
+    if (tid == 0) S.tile = atomicAdd(counter, 1u);
+    for (int i = tid; i < 8 * 256; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
+    // global exclusive digit offsets for this pass
+    uint32_t gtotal;
+    uint32_t gdig = block_excl_scan_256(hist[byte * 256 + tid], S.wsum, &gtotal);
+    __syncthreads();
+    const uint32_t tile = S.tile;
+    const uint64_t base = (uint64_t)tile * SORT_TILE;
+    uint64_t k[SORT_IPT];
+    V v[SORT_IPT];
+    uint32_t vmask = 0;
+#pragma unroll
+    for (int i = 0; i < SORT_IPT; i++) {
+        uint64_t p = base + (uint64_t)w * 32 * SORT_IPT + i * 32 + lane;
+        if (p < n) {
+            k[i] = ki[p];
+            v[i] = vi[p];
+            vmask |= 1u << i;
+        } else {
+            k[i] = ~0ull;
+            v[i] = V(0);
+        }
+    }
+    uint32_t rank[SORT_IPT];
+    warp_rank<SORT_IPT>(k, vmask, sh, S.whist[w], rank);
+    __syncthreads();
+    // per digit (thread tid == digit): warp-exclusive offsets and tile count
+    uint32_t tcount = 0;
+#pragma unroll
+    for (int ww = 0; ww < 8; ww++) {
+        uint32_t c = S.whist[ww][tid];
+        S.whist[ww][tid] = tcount;
+        tcount += c;
+    }
+    // decoupled look-back for the exclusive prefix of this digit over tiles
+    uint32_t *my = status + (size_t)tile * 256 + tid;
+    uint32_t excl = 0;
+    if (tile == 0) {
+        st_release(my, FLAG_PREFIX | tcount);
+    } else {
+        st_release(my, FLAG_AGG | tcount);
+        int64_t p = (int64_t)tile - 1;
+        uint32_t spins = 0;
+        while (p >= 0) {
+            uint32_t s = ld_acquire(status + (size_t)p * 256 + tid);
+            uint32_t f = s & ~VAL_MASK;
+            if (f == 0) {
+                if (++spins > SPIN_LIMIT) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
+                }
+                continue;
+            }
+            excl += s & VAL_MASK;
+            if (f == FLAG_PREFIX) break;
+            --p;
+        }
+        st_release(my, FLAG_PREFIX | (excl + tcount));
+    }
+    S.gbase[tid] = gdig + excl;
+    uint32_t ldig = block_excl_scan_256(tcount, S.wsum, nullptr);
+    S.ldig[tid] = ldig;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SORT_IPT; i++) {
+        if ((vmask >> i) & 1u) {
+            uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+            uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+            S.k[pos] = k[i];
+            S.v[pos] = v[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t nvalid = (uint32_t)umin64(SORT_TILE, n - base);
+    for (uint32_t p = tid; p < nvalid; p += SORT_TPB) {
+        uint64_t kk = S.k[p];
+        uint32_t d = (uint32_t)((kk >> sh) & 0xFF);
+        uint32_t g = S.gbase[d] + (p - S.ldig[d]);
+        if (g < n) {  // only false after a timed-out look-back (error already set)
+            ko[g] = kk;
+            vo[g] = S.v[p];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- one-CTA sort
+template <typename V>
+struct SmallSmem {
+    uint64_t k[2][SORT_TILE];
+    V v[2][SORT_TILE];
+    uint32_t whist[8][256];
+    uint32_t ldig[256];
+    uint32_t wsum[8];
+};
+
+template <typename V>
+__global__ void __launch_bounds__(SORT_TPB) k_small_sort(uint64_t *keys, V *vals, uint32_t n, uint32_t byte_mask) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmallSmem<V> &S = *reinterpret_cast<SmallSmem<V> *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (uint32_t p = tid; p < n; p += SORT_TPB) {
+        S.k[0][p] = keys[p];
+        S.v[0][p] = vals[p];
+    }
+    int cur = 0;
+    for (int byte = 0; byte < 8; byte++) {
+        if (!((byte_mask >> byte) & 1u)) continue;
+        const int sh = byte * 8;
+        for (int i = tid; i < 8 * 256; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
+        __syncthreads();
+        uint64_t k[SORT_IPT];
+        V v[SORT_IPT];
+        uint32_t vmask = 0;
+#pragma unroll
+        for (int i = 0; i < SORT_IPT; i++) {
+            uint32_t p = w * 32 * SORT_IPT + i * 32 + lane;
+            if (p < n) {
+                k[i] = S.k[cur][p];
+                v[i] = S.v[cur][p];
+                vmask |= 1u << i;
+            } else {
+                k[i] = ~0ull;
+                v[i] = V(0);
+            }
+        }
+        uint32_t rank[SORT_IPT];
+        warp_rank<SORT_IPT>(k, vmask, sh, S.whist[w], rank);
+        __syncthreads();
+        uint32_t tcount = 0;
+#pragma unroll
+        for (int ww = 0; ww < 8; ww++) {
+            uint32_t c = S.whist[ww][tid];
+            S.whist[ww][tid] = tcount;
+            tcount += c;
+        }
+        uint32_t ldig = block_excl_scan_256(tcount, S.wsum, nullptr);
+        S.ldig[tid] = ldig;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < SORT_IPT; i++) {
+            if ((vmask >> i) & 1u) {
+                uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+                S.k[cur ^ 1][pos] = k[i];
+                S.v[cur ^ 1][pos] = v[i];
+            }
+        }
+        cur ^= 1;
+        __syncthreads();
+    }
+    for (uint32_t p = tid; p < n; p += SORT_TPB) {
+        keys[p] = S.k[cur][p];
+        vals[p] = S.v[cur][p];
+    }
+}
+
+// ---------------------------------------------------------------- scans
+constexpr int SCAN_TPB = 256, SCAN_IPT = 8, SCAN_TILE = SCAN_TPB * SCAN_IPT;
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_reduce(const T *__restrict__ in, uint32_t n, uint32_t *tmp) {
+    __shared__ uint32_t wsum[8];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        uint64_t p = base + (uint64_t)i * SCAN_TPB + threadIdx.x;
+        if (p < n) s += (uint32_t)in[p];
+    }
+    uint32_t tot;
+    block_excl_scan_256(s, wsum, &tot);
+    if (threadIdx.x == 0) tmp[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *tmp, uint32_t nb, uint32_t *total) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+        uint32_t i = b0 + threadIdx.x;
+        uint32_t x = i < nb ? tmp[i] : 0, v = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) ws[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t s = ws[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            ws[lane] = s;
+        }
+        __syncthreads();
+        uint32_t excl = carry + (w ? ws[w - 1] : 0) + v - x;
+        if (i < nb) tmp[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += ws[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_down(const T *__restrict__ in, uint32_t *out, uint32_t n,
+                                                       const uint32_t *tmp, uint32_t *total_single) {
+    __shared__ uint32_t wsum[8];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_IPT;
+    uint32_t x[SCAN_IPT];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        uint64_t p = base + i;
+        x[i] = p < n ? (uint32_t)in[p] : 0;
+        s += x[i];
+    }
+    uint32_t tot;
+    uint32_t off = block_excl_scan_256(s, wsum, &tot) + (tmp ? tmp[blockIdx.x] : 0);
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        uint64_t p = base + i;
+        if (p < n) out[p] = off;
+        off += x[i];
+    }
+    if (total_single && threadIdx.x == 0) *total_single = tot;
+}
+
+template <typename T>
+cudaError_t scan_impl(const T *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *tmp, cudaStream_t st) {
+    if (n == 0) {
+        if (total) return cudaMemsetAsync(total, 0, 4, st);
+        return cudaSuccess;
+    }
+    uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 1) {
+        k_scan_down<T><<<1, SCAN_TPB, 0, st>>>(in, out, n, nullptr, total);
+        note_launch();
+        return cudaGetLastError();
+    }
+    k_scan_reduce<T><<<nb, SCAN_TPB, 0, st>>>(in, n, tmp);
+    k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, total);
+    k_scan_down<T><<<nb, SCAN_TPB, 0, st>>>(in, out, n, tmp, nullptr);
+    note_launch(3);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t scan_tmp_words(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
+cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *tmp,
+                     cudaStream_t st) {
+    return scan_impl<uint32_t>(in, out, n, total, tmp, st);
+}
+cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *tmp,
+                           cudaStream_t st) {
+    return scan_impl<uint8_t>(in, out, n, total, tmp, st);
+}
+
+template <typename V>
+cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits, SortScratch &s,
+                       uint32_t *err, cudaStream_t st, int *which) {
+    *which = 0;
+    uint32_t byte_mask = 0;
+    for (int b = 0; b < 8; b++)
+        if ((diff_bits >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
+    if (n < 2 || byte_mask == 0) return cudaSuccess;
+    cudaError_t e;
+    if (n <= (uint32_t)SORT_TILE) {
+        size_t sm = sizeof(SmallSmem<V>);
+        e = cudaFuncSetAttribute(k_small_sort<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k_small_sort<V><<<1, SORT_TPB, sm, st>>>(k0, v0, n, byte_mask);
+        note_launch();
+        return cudaGetLastError();
+    }
+    uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    if (s.status_words < (size_t)tiles * 256) return cudaErrorInvalidValue;
+    if ((e = cudaMemsetAsync(s.hist, 0, 8 * 256 * sizeof(uint32_t), st))) return e;
+    if ((e = cudaMemsetAsync(s.counters, 0, 8 * sizeof(uint32_t), st))) return e;
+    uint32_t hb = tiles < 1024 ? tiles : 1024;
+    k_hist<<<hb, 256, 0, st>>>(k0, n, s.hist);
+    note_launch();
+    size_t sm = sizeof(PassSmem<V>);
+    if ((e = cudaFuncSetAttribute(k_pass<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm))) return e;
+    uint64_t *ka = k0, *kb = k1;
+    V *va = v0, *vb = v1;
+    int cur = 0;
+    for (int b = 0; b < 8; b++) {
+        if (!((byte_mask >> b) & 1u)) continue;
+        if ((e = cudaMemsetAsync(s.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), st))) return e;
+        k_pass<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, b, s.hist, s.status, s.counters + b, err);
+        note_launch();
+        uint64_t *tk = ka; ka = kb; kb = tk;
+        V *tv = va; va = vb; vb = tv;
+        cur ^= 1;
+    }
+    *which = cur;
+    return cudaGetLastError();
+}
+
+template cudaError_t sort_pairs<uint16_t>(uint64_t *, uint16_t *, uint64_t *, uint16_t *, uint32_t, uint64_t,
+                                          SortScratch &, uint32_t *, cudaStream_t, int *);
+template cudaError_t sort_pairs<uint64_t>(uint64_t *, uint64_t *, uint64_t *, uint64_t *, uint32_t, uint64_t,
+                                          SortScratch &, uint32_t *, cudaStream_t, int *);
+template cudaError_t sort_pairs<uint32_t>(uint64_t *, uint32_t *, uint64_t *, uint32_t *, uint32_t, uint64_t,
+                                          SortScratch &, uint32_t *, cudaStream_t, int *);
+
+}  // namespace lpma

@@ -1,0 +1,46 @@
+// Device-wide primitives of the engine: LSD radix sort of (u64 key, payload)
+// pairs and exclusive scans.  Hand-written for sm_103a; no CUB/Thrust.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lpma {
+
+constexpr int SORT_TPB = 256;
+constexpr int SORT_IPT = 16;
+constexpr int SORT_TILE = SORT_TPB * SORT_IPT;  // 4096 keys per tile
+
+struct SortScratch {
+    uint32_t *hist = nullptr;      // 8 x 256 global digit counts
+    uint32_t *status = nullptr;    // tiles x 256 look-back words
+    uint32_t *counters = nullptr;  // 8 dynamic tile counters + error word
+    size_t status_words = 0;
+};
+
+// Sorts n pairs by key (stable).  Only the bytes set in diff_bits are sorted
+// (bytes equal across all keys need no pass).  The result lands either in
+// (k0, v0) or in (k1, v1); *which receives 0 or 1.  err (device word, may be
+// null) gets ERR_TIMEOUT if a look-back wait gave up.
+template <typename V>
+cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits,
+                       SortScratch &s, uint32_t *err, cudaStream_t st, int *which);
+
+// Bytes of scratch status words needed for n keys.
+inline size_t sort_status_words(uint32_t n) {
+    size_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    return tiles * 256 + 1;
+}
+
+// Exclusive scan of n u32 values; out may alias in.  total (device, may be
+// null) receives the sum.  tmp needs scan_tmp_words(n) words.
+cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *tmp,
+                     cudaStream_t st);
+// same over u8 inputs (segment counts) into u32 outputs
+cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *tmp,
+                           cudaStream_t st);
+size_t scan_tmp_words(uint32_t n);
+
+// launch counter shared by every translation unit of the library
+void note_launch(int k = 1);
+
+}  // namespace lpma

@@ -1,0 +1,929 @@
+// Update-path kernels of the GB300 LPMA engine.
+//
+// One batch runs: pack/validate -> radix sort -> resolve+locate (dedup,
+// tree descent, membership, in-place upsert / tombstone) -> compaction ->
+// count-only planner -> one execution pass over the maximal windows.
+//
+// The planner replaces the reference's level loop (rpma.cuh:1611-1657),
+// which per level rebalances every candidate window, compacts the update
+// list, lifts node ids and run-length-encodes them again.  For a window W
+// at level l the reference's merge size is compacted(W) + pending(W); since
+// every sub-window executed below W absorbed exactly its own updates, this
+// equals live(W) + inserts(W) - deletes(W) whatever happened below.  So the
+// first level at which a segment's updates are absorbed is a pure function
+// of per-segment counts, and the final layout is that of the maximal
+// executed windows alone (each re-spreads its whole content), executed once.
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace lpma {
+namespace {
+
+constexpr int TPB = 256;
+constexpr int TOPL = 10;               // tree levels staged in shared memory by locate
+constexpr int TOPN = (1 << TOPL) - 1;  // 1023 heap entries = 16 KB of (first, last)
+constexpr int LSUM = 8;                // windows up to 2^8 segments sum counts directly
+
+__device__ inline uint32_t warp_sum(uint32_t v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// smallest y in [0, y0] with seg[y] >= a, given seg[y0] >= a
+__device__ inline uint32_t lb_back(const uint32_t *seg, uint32_t y, uint32_t a) {
+    uint32_t step = 1;
+    while (y > 0) {
+        uint32_t t = y > step ? y - step : 0;
+        if (seg[t] >= a) {
+            y = t;
+            step <<= 1;
+            continue;
+        }
+        uint32_t L = t + 1, R = y;
+        while (L < R) {
+            uint32_t mid = (L + R) >> 1;
+            if (seg[mid] >= a)
+                R = mid;
+            else
+                L = mid + 1;
+        }
+        return L;
+    }
+    return 0;
+}
+
+// smallest y in [y0, n] with seg[y] >= b (n if none), given seg[y0-1] < b
+__device__ inline uint32_t lb_fwd(const uint32_t *seg, uint32_t y, uint32_t n, uint64_t b) {
+    if (y >= n || seg[y] >= b) return y;
+    uint32_t low = y, step = 1;  // seg[low] < b
+    while (true) {
+        uint64_t t = (uint64_t)low + step;
+        if (t >= n) {
+            t = n;
+        } else if (seg[t] < b) {
+            low = (uint32_t)t;
+            step <<= 1;
+            continue;
+        }
+        uint32_t L = low + 1, R = (uint32_t)t;  // answer in [L, R]
+        while (L < R) {
+            uint32_t mid = (L + R) >> 1;
+            if (seg[mid] >= b)
+                R = mid;
+            else
+                L = mid + 1;
+        }
+        return L;
+    }
+}
+
+// first index in [lo, hi) whose key is >= k
+__device__ inline uint32_t lb_key(const uint64_t *key, uint32_t lo, uint32_t hi, uint64_t k) {
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (key[mid] < k)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline uint32_t lb_seg(const uint32_t *seg, uint32_t lo, uint32_t hi, uint32_t s) {
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (seg[mid] < s)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Descend the in-order segment tree (locate_leaf_kernel, rpma.cuh:281-310):
+// stop at an empty node or at a leaf; go left when key < first, right when
+// key > last, else stop.  (first, last) per heap segment; the top TOPL
+// levels come from shared memory.
+__device__ inline uint64_t descend(uint64_t key, const ulonglong2 *top, uint32_t ntop, const ulonglong2 *fl,
+                                   uint32_t H, uint32_t *level_out) {
+    uint64_t j = 0;
+    uint32_t lvl = 0;
+    while (lvl < H) {
+        ulonglong2 f = j < ntop ? top[j] : fl[j];
+        if (f.x == KEY_NONE) break;
+        if (key < f.x)
+            j = 2 * j + 1;
+        else if (key > f.y)
+            j = 2 * j + 2;
+        else
+            break;
+        ++lvl;
+    }
+    *level_out = lvl;
+    return j;
+}
+
+// ------------------------------------------------------------------ pack
+__global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, const uint8_t *__restrict__ ins_vals,
+                                              uint32_t n_ins, const uint64_t *__restrict__ del, uint32_t n_del,
+                                              uint32_t V, uint32_t thres, uint32_t key_format, int internal,
+                                              uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
+                                              DevStatus *st) {
+    const uint32_t n = n_ins + n_del;
+    unsigned long long kand = ~0ull, kor = 0;
+    uint32_t mint = 0xFFFFFFFFu, bad = 0xFFFFFFFFu;
+    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
+        uint64_t k;
+        uint16_t pay;
+        bool ok;
+        const bool is_del = i >= n_ins;
+        k = is_del ? del[i - n_ins] : ins[i];
+        bool range_ok = true;
+        if (key_format == 1) {  // src << 32 | dst
+            uint64_t s = k >> 32, d = k & 0xFFFFFFFFull;
+            range_ok = s < V && d < V;
+            k = (s << SRC_SHIFT) | (d << DST_SHIFT);
+        }
+        const uint64_t src = k >> SRC_SHIFT, dst = (k & DST_MASK) >> DST_SHIFT;
+        if (!is_del) {
+            uint8_t v = ins_vals ? ins_vals[i] : (uint8_t)1;
+            ok = range_ok && k != KEY_NONE && src < V && ((internal && is_sentinel(k)) || dst < V) && v != VAL_TOMB &&
+                 (k & TIME_MASK) >= (uint64_t)thres;
+            pay = v;
+            mint = min(mint, (uint32_t)(k & TIME_MASK));
+        } else {
+            ok = range_ok && k != KEY_NONE && src < V && dst < V;
+            pay = 0x100;
+        }
+        if (!ok) bad = min(bad, i);
+        keys_out[i] = k;
+        pay_out[i] = pay;
+        kand &= k;
+        kor |= k;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        kand &= __shfl_xor_sync(0xffffffffu, kand, o);
+        kor |= __shfl_xor_sync(0xffffffffu, kor, o);
+        mint = min(mint, __shfl_xor_sync(0xffffffffu, mint, o));
+        bad = min(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAnd(&st->key_and, kand);
+        atomicOr(&st->key_or, kor);
+        if (mint != 0xFFFFFFFFu) atomicMin(&st->min_t_ins, mint);
+        if (bad != 0xFFFFFFFFu) {
+            atomicOr(&st->error, ERR_KEY);
+            atomicMin(&st->err_info[0], bad);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ live counts
+__global__ void __launch_bounds__(TPB) k_live_counts(const uint64_t *__restrict__ keys, uint32_t H, uint32_t thres,
+                                                     uint8_t *cnt_live, DevStatus *st) {
+    const uint64_t nseg = nseg_of(H);
+    const int lane = threadIdx.x & 31;
+    uint32_t acc = 0;
+    for (uint64_t s = (blockIdx.x * (uint64_t)TPB + threadIdx.x) >> 5; s < nseg; s += (gridDim.x * (uint64_t)TPB) >> 5) {
+        uint64_t j = heap_of_linear(s, H);
+        uint64_t k = keys[32 * j + lane];
+        uint32_t c = __popc(__ballot_sync(0xffffffffu, k != KEY_NONE && (k & TIME_MASK) >= (uint64_t)thres));
+        if (lane == 0) cnt_live[s] = (uint8_t)c;
+        acc += c;
+    }
+    if (lane == 0 && acc) atomicAdd(&st->live_total, (unsigned long long)acc);
+}
+
+// ------------------------------------------------------------------ resolve + locate
+__global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restrict__ skey,
+                                                        const uint16_t *__restrict__ spay, uint32_t n, Geo g,
+                                                        const ulonglong2 *__restrict__ fl, uint32_t thres,
+                                                        uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
+                                                        uint32_t *blk_ins, DevStatus *st) {
+    __shared__ ulonglong2 top[TOPN];
+    const uint32_t H = g.H;
+    const uint32_t ntop = (uint32_t)umin64(nseg_of(H), TOPN);
+    for (uint32_t t = threadIdx.x; t < ntop; t += TPB) top[t] = fl[t];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    uint32_t kd = KIND_NOP, sg = 0, ups = 0, noop = 0;
+    if (i < n) {
+        const uint64_t key = skey[i];
+        const uint16_t p = spay[i];
+        const bool is_del = (p >> 8) & 1;
+        bool rep;
+        if (is_del)
+            rep = (i == 0 || skey[i - 1] != key);
+        else
+            rep = (i + 1 == n || skey[i + 1] != key || ((spay[i + 1] >> 8) & 1));
+        if (rep) {
+            uint32_t lvl;
+            uint64_t j = descend(key, top, ntop, fl, H, &lvl);
+            sg = (uint32_t)linear_of_heap(j, lvl, H);
+            // membership: the stop segment is sorted, NONE-padded (left packed)
+            const uint64_t *sk = g.keys + 32 * j;
+            uint32_t pos = 0;
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1)
+                if (sk[pos + step - 1] < key) pos += step;
+            const bool found = sk[pos] == key;
+            const uint64_t slot = 32 * j + pos;
+            if (!is_del) {
+                if (found) {
+                    g.vals[slot] = (uint8_t)(p & 0xFF);  // upsert (handle_del_mod, gpma.cuh:162-175)
+                    ups = 1;
+                } else {
+                    kd = KIND_INS;
+                }
+            } else {
+                if (found && (key & TIME_MASK) >= (uint64_t)thres) {
+                    g.vals[slot] = VAL_TOMB;  // tombstone until its window executes
+                    kd = KIND_DEL;
+                } else {
+                    noop = 1;
+                }
+            }
+        } else {
+            noop = 1;
+        }
+        kind[i] = (uint8_t)kd;
+        seg[i] = sg;
+    }
+    uint32_t c_nn = __syncthreads_count(kd != KIND_NOP);
+    uint32_t c_ins = __syncthreads_count(kd == KIND_INS);
+    if (threadIdx.x == 0) {
+        blk_nn[blockIdx.x] = c_nn;
+        blk_ins[blockIdx.x] = c_ins;
+    }
+    ups = warp_sum(ups);
+    noop = warp_sum(noop);
+    if ((threadIdx.x & 31) == 0) {
+        if (ups) atomicAdd(&st->n_upsert, ups);
+        if (noop) atomicAdd(&st->n_noop, noop);
+    }
+}
+
+// exclusive scans of the two block-count arrays (one CTA); totals -> status
+__global__ void __launch_bounds__(1024) k_scan_pairs(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
+                                                     DevStatus *st) {
+    __shared__ uint32_t wa[32], wb[32];
+    __shared__ uint32_t ca, cb;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) ca = cb = 0;
+    __syncthreads();
+    for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+        uint32_t i = b0 + threadIdx.x;
+        uint32_t xa = i < nb ? a[i] : 0, xb = i < nb ? b[i] : 0, va = xa, vb = xb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t ya = __shfl_up_sync(0xffffffffu, va, o), yb = __shfl_up_sync(0xffffffffu, vb, o);
+            if (lane >= o) va += ya, vb += yb;
+        }
+        if (lane == 31) wa[w] = va, wb[w] = vb;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t sa = wa[lane], sb = wb[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t ya = __shfl_up_sync(0xffffffffu, sa, o), yb = __shfl_up_sync(0xffffffffu, sb, o);
+                if (lane >= o) sa += ya, sb += yb;
+            }
+            wa[lane] = sa;
+            wb[lane] = sb;
+        }
+        __syncthreads();
+        if (i < nb) {
+            a[i] = ca + (w ? wa[w - 1] : 0) + va - xa;
+            b[i] = cb + (w ? wb[w - 1] : 0) + vb - xb;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) ca += wa[31], cb += wb[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st->n_u = ca;
+        st->n_ins = cb;
+        st->n_del = ca - cb;
+        ip[ca] = cb;
+    }
+}
+
+__device__ inline uint32_t block_excl_scan(uint32_t x, uint32_t *wsum) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < TPB / 32 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < TPB / 32) wsum[lane] = s;
+    }
+    __syncthreads();
+    uint32_t r = (w ? wsum[w - 1] : 0) + v - x;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ skey, const uint16_t *__restrict__ spay,
+                                                 const uint8_t *__restrict__ kind, const uint32_t *__restrict__ seg,
+                                                 uint32_t n, const uint32_t *blk_nn, const uint32_t *blk_ins,
+                                                 UpdList u) {
+    __shared__ uint32_t wsum[TPB / 32];
+    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    const uint32_t kd = i < n ? kind[i] : KIND_NOP;
+    // pack (kept, insert) flags into one scan word
+    const uint32_t x = (kd != KIND_NOP ? 1u : 0u) | (kd == KIND_INS ? 1u << 16 : 0u);
+    const uint32_t ex = block_excl_scan(x, wsum);
+    if (kd != KIND_NOP) {
+        const uint32_t pos = blk_nn[blockIdx.x] + (ex & 0xFFFF);
+        u.key[pos] = skey[i];
+        u.val[pos] = (uint8_t)(spay[i] & 0xFF);
+        u.kind[pos] = (uint8_t)kd;
+        u.seg[pos] = seg[i];
+        u.ip[pos] = blk_ins[blockIdx.x] + (ex >> 16);
+    }
+}
+
+// ------------------------------------------------------------------ relocate / pending
+__global__ void __launch_bounds__(TPB) k_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *__restrict__ fl) {
+    __shared__ ulonglong2 top[TOPN];
+    const uint32_t H = g.H;
+    const uint32_t ntop = (uint32_t)umin64(nseg_of(H), TOPN);
+    for (uint32_t t = threadIdx.x; t < ntop; t += TPB) top[t] = fl[t];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lvl;
+    uint64_t j = descend(u.key[i], top, ntop, fl, H, &lvl);
+    u.seg[i] = (uint32_t)linear_of_heap(j, lvl, H);
+}
+
+__global__ void __launch_bounds__(TPB) k_pending_counts(const uint8_t *__restrict__ kind, const uint8_t *__restrict__ pend,
+                                                        uint32_t n, const DevStatus *st, uint32_t *blk_nn,
+                                                        uint32_t *blk_ins) {
+    const uint32_t nu = st->n_u;
+    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    const bool keep = i < n && i < nu && pend[i];
+    uint32_t c = __syncthreads_count(keep);
+    uint32_t ci = __syncthreads_count(keep && kind[i] == KIND_INS);
+    if (threadIdx.x == 0) {
+        blk_nn[blockIdx.x] = c;
+        blk_ins[blockIdx.x] = ci;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_pending_scatter(const UpdList in, const uint8_t *__restrict__ pend, uint32_t n,
+                                                         uint32_t nu_old, const uint32_t *blk_nn,
+                                                         const uint32_t *blk_ins, UpdList out) {
+    __shared__ uint32_t wsum[TPB / 32];
+    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    const bool keep = i < n && i < nu_old && pend[i];
+    const uint32_t kd = keep ? in.kind[i] : KIND_NOP;
+    const uint32_t x = (keep ? 1u : 0u) | (kd == KIND_INS ? 1u << 16 : 0u);
+    const uint32_t ex = block_excl_scan(x, wsum);
+    if (keep) {
+        const uint32_t pos = blk_nn[blockIdx.x] + (ex & 0xFFFF);
+        out.key[pos] = in.key[i];
+        out.val[pos] = in.val[i];
+        out.kind[pos] = (uint8_t)kd;
+        out.seg[pos] = in.seg[i];
+        out.ip[pos] = blk_ins[blockIdx.x] + (ex >> 16);
+    }
+}
+
+// ------------------------------------------------------------------ planner
+__device__ inline uint32_t sum_cnt(const uint8_t *cnt, uint64_t a, uint32_t l) {
+    uint32_t s = 0;
+    if (l < 4) {
+        for (uint32_t t = 0; t < (1u << l); t++) s += cnt[a + t];
+    } else {
+        const uint4 *p = reinterpret_cast<const uint4 *>(cnt + a);
+        for (uint32_t t = 0; t < (1u << (l - 4)); t++) {
+            uint4 v = p[t];
+            s = __dp4a(v.x, 0x01010101u, s);
+            s = __dp4a(v.y, 0x01010101u, s);
+            s = __dp4a(v.z, 0x01010101u, s);
+            s = __dp4a(v.w, 0x01010101u, s);
+        }
+    }
+    return s;
+}
+
+__device__ inline uint64_t bit_of(uint32_t H, uint32_t l, uint64_t widx) {
+    return ((1ull << (H + 2)) - (1ull << (H + 2 - l))) + widx;
+}
+
+__global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
+                                              const uint32_t *__restrict__ P, int use_P, uint64_t total_live,
+                                              uint32_t H, Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
+                                              uint8_t *pend, DevStatus *st) {
+    const uint32_t nu = st->n_u;
+    const uint32_t x = blockIdx.x * TPB + threadIdx.x;
+    if (x >= nu || x >= n_cap) return;
+    const uint32_t s = u.seg[x];
+    if (x > 0 && u.seg[x - 1] == s) return;  // one thread per segment with updates
+    const uint32_t hi0 = lb_fwd(u.seg, x, nu, (uint64_t)s + 1);
+    const uint64_t nseg = nseg_of(H);
+    uint32_t lo = x, hi = hi0, e = EXEC_OVF;
+    uint64_t wa = 0, wf = 0;
+    int64_t wm = 0;
+    for (uint32_t l = 0; l <= H + 1; l++) {
+        if (!((tb.allowed >> l) & 1u)) continue;
+        const uint64_t a = ((uint64_t)s >> l) << l;
+        const uint64_t b = umin64(a + (1ull << l), nseg);
+        lo = lb_back(u.seg, lo, (uint32_t)a);
+        hi = lb_fwd(u.seg, hi, nu, b);
+        int64_t live;
+        if (l == H + 1)
+            live = (int64_t)total_live;
+        else if (l <= LSUM || !use_P)
+            live = sum_cnt(cnt, a, l);
+        else
+            live = (int64_t)P[b] - (int64_t)P[a];
+        const int64_t net = 2 * ((int64_t)u.ip[hi] - (int64_t)u.ip[lo]) - (int64_t)(hi - lo);
+        const int64_t m = live + net;
+        if (m >= (int64_t)tb.lower[l] && m <= (int64_t)(32 * (b - a))) {
+            e = l;
+            wa = a;
+            wf = b - a;
+            wm = m;
+            break;
+        }
+    }
+    seg_e[s] = (uint8_t)e;
+    if (e == EXEC_OVF) {
+        atomicOr(&st->ovf, 1u);
+        for (uint32_t y = x; y < hi0; y++) pend[y] = 1;
+        return;
+    }
+    if (e == H + 1) atomicOr(&st->root, 1u);
+    const uint64_t bit = bit_of(H, e, (uint64_t)s >> e);
+    const uint32_t mask = 1u << (bit & 31);
+    const uint32_t old = atomicOr(&bitmap[bit >> 5], mask);
+    if (!(old & mask)) {
+        const uint32_t c = atomicAdd(&st->n_cand, 1u);
+        cand[c] = Window{(uint32_t)wa, (uint32_t)wf, (uint32_t)wm, e, lo, hi};
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
+                                                  const uint32_t *__restrict__ bitmap, Window *small, Window *big,
+                                                  DevStatus *st) {
+    const uint32_t c = blockIdx.x * TPB + threadIdx.x;
+    if (c >= st->n_cand || c >= n_cap) return;
+    const Window w = cand[c];
+    for (uint32_t l = w.level + 1; l <= H + 1; l++) {
+        const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
+        if ((bitmap[bit >> 5] >> (bit & 31)) & 1u) return;  // inside a larger executed window
+    }
+    if (w.f <= SMALL_WIN_SEGS) {
+        small[atomicAdd(&st->n_small, 1u)] = w;
+        atomicAdd(&st->slots_small, 32ull * w.f);
+    } else {
+        big[atomicAdd(&st->n_big, 1u)] = w;
+        atomicAdd(&st->slots_big, 32ull * w.f);
+    }
+}
+
+// ------------------------------------------------------------------ per-segment merge
+// One warp merges one source segment (its kept slots) with the inserts that
+// located into it and stores the items whose window rank falls in
+// [R0, R1) into out[rank - R0].  Ranks start at Rs for this segment.
+// Kept slots and inserts are each sorted and the keys are distinct.
+struct SegMergeOut {
+    uint64_t *k;
+    uint8_t *v;
+};
+
+__device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals,
+                                         uint64_t j, uint32_t c, uint32_t us, uint32_t ue, uint64_t Rs, uint64_t R0,
+                                         uint64_t R1, const UpdList &u, uint32_t thres, uint64_t *kk,
+                                         SegMergeOut out) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    uint64_t key = KEY_NONE;
+    uint8_t val = 0;
+    if ((uint32_t)lane < c) {
+        key = keys[32 * j + lane];
+        val = vals[32 * j + lane];
+    }
+    const bool keep = (uint32_t)lane < c && kept_slot(key, val, thres);
+    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+    const uint32_t nk = __popc(bal), kb = __popc(bal & lt);
+    if (us == ue) {
+        if (keep) {
+            const uint64_t r = Rs + kb;
+            if (r >= R0 && r < R1) {
+                out.k[r - R0] = key;
+                out.v[r - R0] = val;
+            }
+        }
+        return nk;
+    }
+    if (keep) kk[kb] = key;
+    __syncwarp();
+    const uint32_t ip0 = u.ip[us];
+    if (keep) {
+        const uint32_t xk = lb_key(u.key, us, ue, key);
+        const uint64_t r = Rs + kb + (u.ip[xk] - ip0);
+        if (r >= R0 && r < R1) {
+            out.k[r - R0] = key;
+            out.v[r - R0] = val;
+        }
+    }
+    for (uint32_t x0 = us; x0 < ue; x0 += 32) {
+        const uint32_t x = x0 + lane;
+        if (x < ue && u.kind[x] == KIND_INS) {
+            const uint64_t y = u.key[x];
+            uint32_t L = 0, R = nk;
+            while (L < R) {
+                uint32_t mid = (L + R) >> 1;
+                if (kk[mid] < y)
+                    L = mid + 1;
+                else
+                    R = mid;
+            }
+            const uint64_t r = Rs + (u.ip[x] - ip0) + L;
+            if (r >= R0 && r < R1) {
+                out.k[r - R0] = y;
+                out.v[r - R0] = u.val[x];
+            }
+        }
+    }
+    __syncwarp();
+    return nk + (u.ip[ue] - ip0);
+}
+
+// Write destination segment k of a window spread (m items over f segments),
+// taking its items from out[first_rank(k) - R0 ...].
+__device__ inline void write_segment(uint64_t *__restrict__ dkeys, uint8_t *__restrict__ dvals, uint64_t j,
+                                     uint64_t k, uint64_t m, uint64_t f, uint64_t R0, const uint64_t *ok,
+                                     const uint8_t *ov, uint32_t *sent, uint32_t V, uint8_t *cnt_slot,
+                                     ulonglong2 *fl_slot) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t f0 = first_rank(k, m, f), f1 = first_rank(k + 1, m, f);
+    const uint32_t nk = (uint32_t)(f1 - f0);
+    uint64_t key = KEY_NONE;
+    if ((uint32_t)lane < nk) {
+        key = ok[f0 - R0 + lane];
+        dvals[32 * j + lane] = ov[f0 - R0 + lane];
+        if (is_sentinel(key)) {
+            const uint32_t row = (uint32_t)(key >> SRC_SHIFT);
+            if (row < V) sent[row] = (uint32_t)(32 * j + lane);
+        }
+    }
+    dkeys[32 * j + lane] = key;
+    if (lane == 0) {
+        *cnt_slot = (uint8_t)nk;
+        *fl_slot = nk ? make_ulonglong2(ok[f0 - R0], ok[f1 - 1 - R0]) : make_ulonglong2(KEY_NONE, KEY_NONE);
+    }
+}
+
+// ------------------------------------------------------------------ small windows
+constexpr int EXS_WARPS = 8;
+struct ExSmallSmem {
+    uint64_t outk[EXS_WARPS][1024];
+    uint8_t outv[EXS_WARPS][1024];
+    uint64_t kk[EXS_WARPS][32];
+};
+
+__global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__restrict__ wins, uint32_t n_cap, Geo g,
+                                                               uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+                                                               uint32_t V, const UpdList u, uint32_t thres,
+                                                               DevStatus *st) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ExSmallSmem &S = *reinterpret_cast<ExSmallSmem *>(smem_raw);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t nwin = min(st->n_small, n_cap);
+    SegMergeOut out{S.outk[w], S.outv[w]};
+    for (uint32_t wi = blockIdx.x * EXS_WARPS + w; wi < nwin; wi += gridDim.x * EXS_WARPS) {
+        const Window W = wins[wi];
+        // lane k < f: segment a + k
+        uint32_t c = 0, us = W.hi;
+        uint64_t j = 0;
+        if ((uint32_t)lane < W.f) {
+            const uint32_t s = W.a + lane;
+            c = cnt[s];
+            j = heap_of_linear(s, g.H);
+            us = lb_seg(u.seg, W.lo, W.hi, s);
+        }
+        uint32_t ue = __shfl_down_sync(0xffffffffu, us, 1);
+        if ((uint32_t)lane + 1 >= W.f) ue = W.hi;
+        uint64_t R = 0;
+        for (uint32_t k = 0; k < W.f; k++) {
+            const uint32_t ck = __shfl_sync(0xffffffffu, c, k);
+            const uint64_t jk = __shfl_sync(0xffffffffu, j, k);
+            const uint32_t usk = __shfl_sync(0xffffffffu, us, k);
+            const uint32_t uek = __shfl_sync(0xffffffffu, ue, k);
+            R += merge_segment(g.keys, g.vals, jk, ck, usk, uek, R, 0, 1024, u, thres, S.kk[w], out);
+        }
+        __syncwarp();
+        if (R != W.m) {
+            if (lane == 0) {
+                atomicOr(&st->error, ERR_INTERNAL);
+                st->err_info[1] = 1;
+            }
+            continue;
+        }
+        for (uint32_t k = 0; k < W.f; k++) {
+            const uint64_t jk = __shfl_sync(0xffffffffu, j, k);
+            uint8_t cn;
+            ulonglong2 f2;
+            write_segment(g.keys, g.vals, jk, k, W.m, W.f, 0, S.outk[w], S.outv[w], sent, V, &cn, &f2);
+            if (lane == 0) {
+                cnt[W.a + k] = cn;
+                fl[jk] = f2;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ tile grain
+__global__ void __launch_bounds__(TPB) k_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd,
+                                                           const DevStatus *st) {
+    const uint32_t nu = st->n_u;
+    const uint32_t x = blockIdx.x * TPB + threadIdx.x;
+    if (x >= nu || x >= n_cap) return;
+    const uint32_t s = u.seg[x];
+    if (x > 0 && u.seg[x - 1] == s) return;
+    const uint32_t hi0 = lb_fwd(u.seg, x, nu, (uint64_t)s + 1);
+    const uint32_t ins = u.ip[hi0] - u.ip[x];
+    qi[s] = ins;
+    qd[s] = (hi0 - x) - ins;
+}
+
+__global__ void __launch_bounds__(TPB) k_seg_q(const uint8_t *__restrict__ cnt, const uint8_t *__restrict__ cnt_live,
+                                               const uint32_t *__restrict__ qi, const uint32_t *__restrict__ qd,
+                                               uint64_t nseg, uint32_t *q, uint32_t *qn, uint8_t *srcc) {
+    for (uint64_t s = blockIdx.x * (uint64_t)TPB + threadIdx.x; s < nseg; s += gridDim.x * (uint64_t)TPB) {
+        const uint32_t c = cnt[s];
+        const uint32_t cl = cnt_live ? cnt_live[s] : c;
+        q[s] = cl - qd[s] + qi[s];
+        qn[s] = qi[s] + qd[s];
+        srcc[s] = (uint8_t)c;
+    }
+}
+
+struct TileSmem {
+    uint64_t outk[1056];
+    uint8_t outv[1056];
+    uint64_t kk[8][32];
+    uint32_t sbeg, send, job;
+};
+
+__global__ void __launch_bounds__(TPB) k_exec_tiles(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
+                                                    Geo src, const uint8_t *__restrict__ srcc,
+                                                    const uint32_t *__restrict__ PQ, const uint32_t *__restrict__ US,
+                                                    Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
+                                                    uint32_t V, const UpdList u, uint32_t thres, DevStatus *st) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) {
+            uint32_t L = 0, R = njobs - 1;  // last job with tile0 <= tile
+            while (L < R) {
+                uint32_t mid = (L + R + 1) >> 1;
+                if (jobs[mid].tile0 <= tile)
+                    L = mid;
+                else
+                    R = mid - 1;
+            }
+            S.job = L;
+            const TileJob J = jobs[L];
+            const uint64_t t = tile - J.tile0;
+            const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
+            const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
+            const uint32_t base = PQ[J.sa];
+            // last source segment whose first rank <= R0
+            uint32_t a = J.sa, b = J.sa + J.sf - 1;
+            while (a < b) {
+                uint32_t mid = (a + b + 1) >> 1;
+                if (PQ[mid] - base <= R0)
+                    a = mid;
+                else
+                    b = mid - 1;
+            }
+            S.sbeg = a;
+            // first source segment whose first rank >= R1
+            uint32_t c = a, d = J.sa + J.sf;
+            while (c < d) {
+                uint32_t mid = (c + d) >> 1;
+                if (PQ[mid] - base >= R1)
+                    d = mid;
+                else
+                    c = mid + 1;
+            }
+            S.send = c;
+            // the source prefix must account for exactly m items
+            if (t == 0 && PQ[J.sa + J.sf] - base != J.m) {
+                atomicOr(&st->error, ERR_INTERNAL);
+                st->err_info[1] = 2;
+            }
+        }
+        __syncthreads();
+        const TileJob J = jobs[S.job];
+        const uint64_t t = tile - J.tile0;
+        const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
+        const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
+        const uint32_t base = PQ[J.sa];
+        SegMergeOut out{S.outk, S.outv};
+        for (uint32_t s = S.sbeg + w; s < S.send; s += TPB / 32) {
+            const uint64_t j = heap_of_linear(s, src.H);
+            merge_segment(src.keys, src.vals, j, srcc[s], US[s], US[s + 1], PQ[s] - base, R0, R1, u, thres, S.kk[w],
+                          out);
+        }
+        __syncthreads();
+        for (uint64_t k = k0 + w; k < k1; k += TPB / 32) {
+            const uint64_t ds = J.da + k;
+            const uint64_t j = heap_of_linear(ds, dst.H);
+            uint8_t cn;
+            ulonglong2 f2;
+            write_segment(dst.keys, dst.vals, j, k, J.m, J.df, R0, S.outk, S.outv, sent, V, &cn, &f2);
+            if (lane == 0) {
+                cnt_d[ds] = cn;
+                fl_d[j] = f2;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_copy_segments(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
+                                                       Geo from, Geo to) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint32_t L = 0, R = njobs - 1;
+        while (L < R) {
+            uint32_t mid = (L + R + 1) >> 1;
+            if (jobs[mid].tile0 <= tile)
+                L = mid;
+            else
+                R = mid - 1;
+        }
+        const TileJob J = jobs[L];
+        const uint64_t t = tile - J.tile0;
+        const uint64_t k1 = umin64(32 * t + 32, J.df);
+        for (uint64_t k = 32 * t + w; k < k1; k += TPB / 32) {
+            const uint64_t j = heap_of_linear(J.da + k, to.H);
+            to.keys[32 * j + lane] = from.keys[32 * j + lane];
+            to.vals[32 * j + lane] = from.vals[32 * j + lane];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ levels
+__global__ void __launch_bounds__(TPB) k_levelup_cnt(const uint8_t *__restrict__ cnt_old, uint8_t *cnt_new,
+                                                     uint32_t H_old) {
+    const uint64_t nn = nseg_of(H_old + 1);
+    for (uint64_t s = blockIdx.x * (uint64_t)TPB + threadIdx.x; s < nn + 64; s += gridDim.x * (uint64_t)TPB)
+        cnt_new[s] = (s < nn && (s & 1)) ? cnt_old[s >> 1] : (uint8_t)0;
+}
+
+__global__ void __launch_bounds__(TPB) k_check_empty_level(const uint8_t *__restrict__ cnt, uint32_t H, DevStatus *st) {
+    const uint64_t nseg = nseg_of(H);
+    for (uint64_t t = blockIdx.x * (uint64_t)TPB + threadIdx.x; 4 * t + 1 < nseg; t += gridDim.x * (uint64_t)TPB)
+        if (cnt[4 * t + 1] == 0) st->empty_found = 1;
+}
+
+__global__ void __launch_bounds__(TPB) k_sum_cnt(const uint8_t *__restrict__ cnt, uint64_t nseg, DevStatus *st) {
+    uint32_t acc = 0;
+    for (uint64_t s = blockIdx.x * (uint64_t)TPB + threadIdx.x; s < nseg; s += gridDim.x * (uint64_t)TPB) acc += cnt[s];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&st->cnt_total, (unsigned long long)acc);
+}
+
+inline uint32_t grid_for(uint64_t n, uint32_t per_block, uint32_t cap = 152 * 16) {
+    uint64_t g = (n + per_block - 1) / per_block;
+    if (g == 0) g = 1;
+    return (uint32_t)(g < cap ? g : cap);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
+                 uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
+                 DevStatus *st, cudaStream_t s) {
+    k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
+                                                        keys_out, pay_out, st);
+    note_launch();
+}
+
+void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_t *cnt_live, DevStatus *st,
+                        cudaStream_t s) {
+    k_live_counts<<<grid_for(nseg_of(H), TPB / 32), TPB, 0, s>>>(keys, H, thres, cnt_live, st);
+    note_launch();
+}
+
+void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t n, Geo g, const ulonglong2 *fl,
+                           uint32_t thres, uint8_t *kind, uint32_t *seg, uint32_t *blk_nn, uint32_t *blk_ins,
+                           DevStatus *st, cudaStream_t s) {
+    const uint32_t nb = (n + TPB - 1) / TPB;
+    k_resolve_locate<<<nb, TPB, 0, s>>>(skey, spay, n, g, fl, thres, kind, seg, blk_nn, blk_ins, st);
+    note_launch();
+}
+
+void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *kind, const uint32_t *seg, uint32_t n,
+                    uint32_t *blk_nn, uint32_t *blk_ins, UpdList u, DevStatus *st, cudaStream_t s) {
+    const uint32_t nb = (n + TPB - 1) / TPB;
+    k_scan_pairs<<<1, 1024, 0, s>>>(blk_nn, blk_ins, nb, u.ip, st);
+    k_compact<<<nb, TPB, 0, s>>>(skey, spay, kind, seg, n, blk_nn, blk_ins, u);
+    note_launch(2);
+}
+
+void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s) {
+    if (!n) return;
+    k_relocate<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(u, n, g, fl);
+    note_launch();
+}
+
+void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, UpdList out, uint32_t *blk_nn,
+                            uint32_t *blk_ins, DevStatus *st, cudaStream_t s) {
+    // n = old compacted count (known on the host at this point)
+    const uint32_t nb = (n + TPB - 1) / TPB;
+    if (!nb) return;
+    k_pending_counts<<<nb, TPB, 0, s>>>(in.kind, pend, n, st, blk_nn, blk_ins);
+    k_scan_pairs<<<1, 1024, 0, s>>>(blk_nn, blk_ins, nb, out.ip, st);
+    k_pending_scatter<<<nb, TPB, 0, s>>>(in, pend, n, n, blk_nn, blk_ins, out);
+    note_launch(3);
+}
+
+void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
+                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *small,
+                 Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
+    const uint32_t nb = (n_cap + TPB - 1) / TPB;
+    if (!nb) return;
+    k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, H, tb, bitmap, cand, seg_e, pend, st);
+    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, small, big, st);
+    note_launch(2);
+}
+
+void launch_exec_small(const Window *w, uint32_t n_small, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+                       uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
+    if (!n_small) return;
+    const size_t sm = sizeof(ExSmallSmem);
+    cudaFuncSetAttribute(k_exec_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_exec_small<<<grid_for(n_small, EXS_WARPS, 152 * 8), EXS_WARPS * 32, sm, s>>>(w, n_small, g, cnt, fl, sent, V, u,
+                                                                                   thres, st);
+    note_launch();
+}
+
+void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
+                              cudaStream_t s) {
+    if (!n_cap) return;
+    k_seg_update_counts<<<(n_cap + TPB - 1) / TPB, TPB, 0, s>>>(u, n_cap, qi, qd, st);
+    note_launch();
+}
+
+void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
+                  uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s) {
+    k_seg_q<<<grid_for(nseg, TPB), TPB, 0, s>>>(cnt, cnt_live, qi, qd, nseg, q, qn, srcc);
+    note_launch();
+}
+
+void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo src, const uint8_t *srcc,
+                       const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
+    if (!ntiles) return;
+    const size_t sm = sizeof(TileSmem);
+    cudaFuncSetAttribute(k_exec_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_exec_tiles<<<grid_for(ntiles, 1, 152 * 8), TPB, sm, s>>>(jobs, njobs, ntiles, src, srcc, PQ, US, dst, cnt_d, fl_d,
+                                                               sent, V, u, thres, st);
+    note_launch();
+}
+
+void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to, cudaStream_t s) {
+    if (!ntiles) return;
+    k_copy_segments<<<grid_for(ntiles, 1, 152 * 8), TPB, 0, s>>>(jobs, njobs, ntiles, from, to);
+    note_launch();
+}
+
+void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s) {
+    k_levelup_cnt<<<grid_for(nseg_of(H_old + 1) + 64, TPB), TPB, 0, s>>>(cnt_old, cnt_new, H_old);
+    note_launch();
+}
+
+void launch_check_empty_level(const uint8_t *cnt, uint32_t H, DevStatus *st, cudaStream_t s) {
+    k_check_empty_level<<<grid_for(nseg_of(H) / 4 + 1, TPB), TPB, 0, s>>>(cnt, H, st);
+    note_launch();
+}
+
+void launch_sum_cnt(const uint8_t *cnt, uint64_t nseg, DevStatus *st, cudaStream_t s) {
+    k_sum_cnt<<<grid_for(nseg, TPB), TPB, 0, s>>>(cnt, nseg, st);
+    note_launch();
+}
+
+}  // namespace lpma

@@ -1,0 +1,110 @@
+/*
+ * CPU oracle for the LPMA batched edge-update path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests/, the smoke
+ * check and the CPU-baseline leg of bench.py load it to compute the expected
+ * layout and results.  The product (lpma_gb300) never links or calls it.
+ *
+ * Parity status: the reference (pkumod/LPMA) cannot be compiled with CUDA 13
+ * (device-side cudaDeviceSynchronize / CDP1 and the removed __shfl_down), so
+ * no reference binary exists to pin this restatement against.  It is pinned
+ * instead by the reference's own known-answer checks for this path
+ * (sorted key set, per-row adjacency with the sentinel closing each row, the
+ * index algebra, the density table and the redistribution formula), which
+ * tests/golden holds as fixtures.  The physical-layout parity of the
+ * restatement itself is "parity unpinned".
+ */
+#ifndef LPMA_ORACLE_H
+#define LPMA_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct OPma OPma;
+
+typedef struct {
+    /* what the update call did, for tests and for the byte model */
+    uint32_t height_before, height_after;
+    uint32_t n_ins_applied;     /* inserts that were new keys */
+    uint32_t n_upserts;         /* inserts whose key was present: value overwritten */
+    uint32_t n_del_applied;     /* deletes whose key was present */
+    uint32_t n_noop;            /* deletes of absent keys + in-batch duplicates */
+    uint32_t root_executed;     /* a level H+1 window absorbed updates */
+    uint32_t eager_levelup;     /* a level was added after the root absorbed */
+    uint32_t overflow;          /* updates left after the root */
+    uint32_t rebuilt;           /* full rebuild happened (resize to new height) */
+    uint32_t levelup_path;      /* overflow handled by adding one level + second loop */
+    uint32_t fill_empty;        /* fill_empty_segs redistributed the array */
+    uint64_t win_count[32];     /* executed windows per level (reference order) */
+    uint64_t win_slots[32];     /* slots covered by executed windows per level */
+} OPmaStats;
+
+/* init_csr_rpma (rpma.cuh:1808-1824): empty height-0 array, then V sentinels */
+OPma *opma_create(uint32_t num_vertices, int skip_rule);
+void opma_destroy(OPma *p);
+
+/* update_rpma (rpma.cuh:1549-1718) with delete/dedup extension.
+ * ins_vals may be NULL (value 1, as test_update_rpma.cu:72). */
+int opma_update(OPma *p, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins,
+                const uint64_t *del, size_t n_del, uint32_t thres, OPmaStats *st);
+
+uint32_t opma_height(const OPma *p);
+uint64_t opma_num_slots(const OPma *p);        /* 32 * (2^(H+1) - 1) */
+uint64_t opma_num_items(const OPma *p);        /* physically present keys */
+
+/* physical layout in heap (level-concatenated) order, as the reference's
+ * per-level arrays laid end to end; empty slots have key ~0 */
+int opma_layout(const OPma *p, uint64_t *keys, uint8_t *vals, size_t cap);
+/* sentinel slot of vertex v (physical index), the csr_idx/csr_lane pair */
+int opma_sentinel_slots(const OPma *p, uint32_t *out, size_t cap);
+
+/* get_data_rpma (rpma.cuh:1735-1761): all present keys in sorted order */
+int64_t opma_export_sorted(const OPma *p, uint64_t *keys, uint8_t *vals, size_t cap);
+
+/* to_csr_rpma (rpma.cuh:2249-2295): row_offset (V+1), col_index, values */
+int64_t opma_csr(const OPma *p, uint32_t *row_offset, uint32_t *col_index,
+                 uint8_t *values, size_t cap);
+
+/* index algebra (rpma.cuh:98-134) and thresholds (rpma.cuh:137-168), for
+ * the known-answer tests */
+uint32_t opma_get_idx(uint32_t linear, uint32_t height);
+uint32_t opma_get_lane(uint32_t linear, uint32_t idx, uint32_t height);
+uint32_t opma_get_linear_idx(uint32_t idx, uint32_t lane, uint32_t height);
+void opma_density_table(uint32_t *lower, uint32_t *upper, int n);
+/* the reference's skip state machine (rpma.cuh:1609-1619) for one height:
+ * out[level] = 1 when big-grain windows at that level are skipped */
+void opma_skip_table(uint32_t height, uint8_t *out, int n);
+/* segment count of one destination segment under even redistribution
+ * (rpma.cuh:677-679): item i -> segment floor(f*i/m) */
+void opma_redistribute_counts(uint64_t f, uint64_t m, uint32_t *counts);
+
+/* ---- synthetic workload generators (identical integer arithmetic to the
+ * device generator in lpma_gb300/csrc/gen.cu) ---- */
+uint64_t opma_mix64(uint64_t z);
+/* raw R-MAT keys (src<<42 | dst<<20), before self-loop removal/dedup */
+void opma_rmat_raw(uint64_t seed, uint32_t scale, uint64_t n_edges,
+                   uint32_t ta, uint32_t tab, uint32_t tabc, uint64_t *out);
+/* remove self loops, sort, dedup; returns the new count */
+uint64_t opma_dedup(uint64_t *keys, uint64_t n);
+/* order by (mix64(seed ^ key), key) */
+void opma_shuffle(uint64_t seed, uint64_t *keys, uint64_t n);
+
+/* ---- CPU baseline: sorted-merge CSR rebuild per batch ---- */
+typedef struct OCsr OCsr;
+OCsr *ocsr_create(uint32_t num_vertices, int threads);
+void ocsr_destroy(OCsr *c);
+int ocsr_load(OCsr *c, const uint64_t *keys, uint64_t n);
+int ocsr_insert(OCsr *c, const uint64_t *keys, uint64_t n);
+int ocsr_delete(OCsr *c, const uint64_t *keys, uint64_t n);
+uint64_t ocsr_num_edges(const OCsr *c);
+const uint64_t *ocsr_edges(const OCsr *c);
+const uint32_t *ocsr_row_offset(const OCsr *c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

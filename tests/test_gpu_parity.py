@@ -1,0 +1,232 @@
+"""GPU parity: the CUDA engine, called through the C ABI, against the CPU oracle.
+
+Bit-exact: after every batch the physical layout (keys and values of every
+slot of the reference's level arrays laid end to end), the sentinel slots
+(the reference's csr_idx/csr_lane), the height and the CSR view must equal
+the oracle's.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).cuda()
+
+
+def _dev8(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint8)).cuda()
+
+
+def assert_same(g, o, where=""):
+    gk, gv, gs, gh = g.layout()
+    ok_, ov = o.layout()
+    assert gh == o.height, "%s: height %d vs oracle %d" % (where, gh, o.height)
+    if not np.array_equal(gk, ok_):
+        bad = np.nonzero(gk != ok_)[0]
+        raise AssertionError("%s: %d key slots differ, first at %d: %x vs %x" % (where, bad.size, bad[0], gk[bad[0]],
+                                                                                ok_[bad[0]]))
+    assert np.array_equal(gv, ov), "%s: values differ" % where
+    assert np.array_equal(gs, o.sentinel_slots()), "%s: sentinel slots differ" % where
+    assert g.num_items == o.num_items(), where
+
+
+def assert_csr(g, o):
+    ro, ci, va = g.to_csr()
+    oro, oci, ova = o.csr()
+    assert np.array_equal(ro, oro)
+    assert np.array_equal(ci, oci)
+    assert np.array_equal(va, ova)
+    k, v = g.export_sorted()
+    ok_, ov = o.export_sorted()
+    assert np.array_equal(k, ok_) and np.array_equal(v, ov)
+
+
+def test_generator_and_shuffle_match_cpu(engine, oracle):
+    import torch
+    scale, ef = 14, 16
+    out = torch.empty((1 << scale) * ef, dtype=torch.int64, device="cuda")
+    n = engine.gen_rmat_device(3, scale, ef, out)
+    ref = oracle.rmat_edges(3, scale, ef)
+    got = out[:n].cpu().numpy().view(np.uint64)
+    assert n == ref.size and np.array_equal(got, ref)
+    engine.shuffle_device(9, out[:n])
+    assert np.array_equal(out[:n].cpu().numpy().view(np.uint64), oracle.shuffle(ref, 9))
+
+
+@pytest.mark.parametrize("V", [1, 5, 13, 20, 33, 52, 53, 96, 97, 200, 4096])
+def test_create_small_graphs(engine, oracle, V):
+    g = engine.Lpma(V)
+    o = oracle.OracleLpma(V)
+    assert_same(g, o, "create V=%d" % V)
+    assert_csr(g, o)
+
+
+def _stream(oracle, seed, scale, ef, batch):
+    e = oracle.shuffle(oracle.rmat_edges(seed, scale, ef), seed + 100)
+    half = e.size // 2
+    b = [(i, min(i + batch, e.size)) for i in range(half, e.size, batch)]
+    return e, half, b
+
+
+def test_config1_insert_then_delete_reverse(engine, oracle):
+    """Scale-16 R-MAT, 50% bulk, batches of 16,384 inserted then deleted in reverse."""
+    V = 1 << 16
+    e, half, batches = _stream(oracle, 1, 16, 16, 16384)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    d = _dev(e)
+    g.update(ins=d[:half])
+    o.update(ins=e[:half])
+    assert_same(g, o, "bulk")
+    for a, b in batches:
+        sg = g.update(ins=d[a:b])
+        so = o.update(ins=e[a:b])
+        assert sg["n_ins_applied"] == so["n_ins_applied"]
+        assert_same(g, o, "insert %d" % a)
+    assert_csr(g, o)
+    for a, b in reversed(batches):
+        g.update(dels=d[a:b])
+        o.update(dels=e[a:b])
+        assert_same(g, o, "delete %d" % a)
+    assert_csr(g, o)
+
+
+@pytest.mark.parametrize("batch", [1, 7, 100, 1000, 5000, 30000])
+def test_mixed_batches_scale14(engine, oracle, batch):
+    V = 1 << 14
+    e, half, batches = _stream(oracle, 5 + batch, 14, 16, batch)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    d = _dev(e)
+    g.update(ins=d[:half])
+    o.update(ins=e[:half])
+    rng = np.random.default_rng(batch)
+    stored = half
+    for i, (a, b) in enumerate(batches[:12]):
+        g.update(ins=d[a:b])
+        o.update(ins=e[a:b])
+        assert_same(g, o, "ins %d" % i)
+        # delete a random sample of what is stored, plus some absent keys
+        k = rng.choice(stored, size=min(b - a, stored), replace=False)
+        dels = np.concatenate([e[k], e[-3:]])
+        g.update(dels=_dev(dels))
+        o.update(dels=dels)
+        assert_same(g, o, "del %d" % i)
+    assert_csr(g, o)
+
+
+def test_bulk_then_heavy_deletes_halving(engine, oracle):
+    V = 1 << 13
+    e = oracle.shuffle(oracle.rmat_edges(21, 13, 16), 4)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    g.update(ins=_dev(e))
+    o.update(ins=e)
+    heights = [o.height]
+    for i in range(0, int(e.size * 0.95), 4096):
+        g.update(dels=_dev(e[i:i + 4096]))
+        o.update(dels=e[i:i + 4096])
+        assert_same(g, o, "del %d" % i)
+        heights.append(o.height)
+    assert heights[-1] < heights[0]
+    assert_csr(g, o)
+
+
+def test_batch_semantics(engine, oracle):
+    """Duplicates, upserts, insert+delete of one key, absent deletes, values."""
+    V = 1 << 10
+    e = oracle.shuffle(oracle.rmat_edges(8, 10, 8), 2)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    vals = (np.arange(e.size) % 200 + 1).astype(np.uint8)
+    g.update(ins=_dev(e[:3000]), ins_vals=_dev8(vals[:3000]))
+    o.update(ins=e[:3000], ins_vals=vals[:3000])
+    assert_same(g, o, "bulk")
+    ins = np.concatenate([e[2990:3100], e[3000:3050], e[100:120]])  # dups + upserts
+    iv = (np.arange(ins.size) % 250 + 2).astype(np.uint8)
+    dels = np.concatenate([e[50:70], e[3100:3110], e[110:115]])      # present, absent, also inserted
+    sg = g.update(ins=_dev(ins), ins_vals=_dev8(iv), dels=_dev(dels))
+    so = o.update(ins=ins, ins_vals=iv, dels=dels)
+    for k in ("n_ins_applied", "n_upserts", "n_del_applied", "n_noop"):
+        assert sg[k] == so[k], k
+    assert_same(g, o, "mixed")
+    assert_csr(g, o)
+    # empty batch
+    g.update()
+    assert_same(g, o, "empty")
+
+
+def test_invalid_keys_rejected_without_change(engine, oracle):
+    from lpma_gb300 import LpmaError
+    V = 1 << 10
+    e = oracle.shuffle(oracle.rmat_edges(8, 10, 8), 2)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    g.update(ins=_dev(e[:2000]))
+    o.update(ins=e[:2000])
+    bad = [
+        dict(ins=np.array([(1 << 64) - 1], np.uint64)),                       # KEY_NONE
+        dict(ins=np.array([(V + 5) << 42], np.uint64)),                       # src out of range
+        dict(ins=np.array([(3 << 42) | ((V + 1) << 20)], np.uint64)),         # dst out of range
+        dict(dels=np.array([(7 << 42) + 0x000003FFFFEFFFFF], np.uint64)),      # sentinel delete
+        dict(ins=e[2000:2001], ins_vals=np.array([0xFF], np.uint8)),          # tombstone value
+    ]
+    for kw in bad:
+        dkw = {k: (_dev8(v) if k == "ins_vals" else _dev(v)) for k, v in kw.items()}
+        with pytest.raises(LpmaError):
+            g.update(**dkw)
+        assert_same(g, o, "after rejected %s" % list(kw))
+
+
+def test_host_entry_point_and_pair32(engine, oracle):
+    V = 1 << 12
+    e = oracle.shuffle(oracle.rmat_edges(4, 12, 8), 3)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    g.update(ins=e[:5000])          # numpy -> lpma_update_host
+    o.update(ins=e[:5000])
+    assert_same(g, o, "host path")
+    cfg = engine.default_config(key_format=1)
+    g2 = engine.Lpma(V, config=cfg)
+    pairs = ((e >> np.uint64(42)) << np.uint64(32)) | ((e >> np.uint64(20)) & np.uint64(0x3FFFFF))
+    g2.update(ins=_dev(pairs[:5000]))
+    k1, _ = g.export_sorted()
+    k2, _ = g2.export_sorted()
+    assert np.array_equal(k1, k2)
+
+
+def test_timestamp_expiry(engine, oracle):
+    V = 1 << 10
+    e = oracle.shuffle(oracle.rmat_edges(6, 10, 16), 8)
+    t = (np.arange(e.size) // 500).astype(np.uint64) + np.uint64(1)
+    keys = e | t
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    for i in range(0, keys.size, 500):
+        thres = max(0, int(t[i]) - 4)
+        g.update(ins=_dev(keys[i:i + 500]), thres=thres)
+        o.update(ins=keys[i:i + 500], thres=thres)
+        assert_same(g, o, "ts batch %d" % i)
+    assert_csr(g, o)
+
+
+@pytest.mark.parametrize("batch", [1024, 10240, 102400])
+def test_scale18_stream(engine, oracle, batch):
+    """Larger tree: root rebalances, eager level-ups and rebuilds along the stream."""
+    V = 1 << 18
+    e, half, batches = _stream(oracle, 31, 18, 16, batch)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    d = _dev(e)
+    g.update(ins=d[:half])
+    o.update(ins=e[:half])
+    assert_same(g, o, "bulk")
+    events = set()
+    for i, (a, b) in enumerate(batches[:6]):
+        s1 = g.update(ins=d[a:b])
+        o.update(ins=e[a:b])
+        assert_same(g, o, "ins %d" % i)
+        s2 = g.update(dels=d[a:(a + b) // 2])
+        o.update(dels=e[a:(a + b) // 2])
+        assert_same(g, o, "del %d" % i)
+        for s in (s1, s2):
+            for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path", "fill_empty"):
+                if s[k]:
+                    events.add(k)
+    assert_csr(g, o)
