@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Benchmark of the LPMA batched edge-update path on one GB300.
+
+Workload (the reference metric's configuration): directed R-MAT, scale 21
+(2,097,152 vertices), edge factor 16, (a,b,c,d) = (.57,.19,.19,.05), seeded;
+self loops and duplicates removed; shuffled; 50% bulk-loaded.  A step is one
+update call of B edges (B = 1,048,576 by default), alternately an insert
+batch drawn from the unloaded edges and a delete batch drawn from the stored
+ones (uniform: the bulk is a shuffled sample); deleted edges return to the
+insert pool.  The same stream at batch sizes 1K/10K/100K is reported under
+"per_batch_size".  Inputs are generated on the device and stay resident in
+HBM; the PMA working set (0.3-0.6 GB) is larger than the 129 MB L2, so no L2
+flush is done between steps.
+
+--impl reference runs the CPU baseline (sorted-merge CSR rebuild per batch on
+the host cores, the reference's CPU path) on the same workload and metric.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "updated edges/s vs batch size on 1 GB300 (bit-exact); served p50/p99 batch latency"
+WORKLOAD = "rmat-s21-ef16 stream, 50% bulk, alternating insert/delete batches"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=1 << 20)
+    ap.add_argument("--scale", type=int, default=21)
+    ap.add_argument("--ef", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--sweep", default="1024,10240,102400")
+    ap.add_argument("--sweep-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = [n for i, n in enumerate(names) if any(s[3 + i].lower() == "active" for s in self.samples)]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+class Stream:
+    """Insert/delete batches over the cyclic sequences (U ++ S) and (S ++ U)."""
+
+    def __init__(self, ins_seq, del_seq):
+        self.ins_seq, self.del_seq = ins_seq, del_seq
+        self.ci = self.cd = 0
+        self.n = ins_seq.shape[0]
+
+    def next(self, kind, B):
+        if kind == "ins":
+            a = self.ci
+            self.ci += B
+            seq = self.ins_seq
+        else:
+            a = self.cd
+            self.cd += B
+            seq = self.del_seq
+        if a + B > self.n:
+            raise RuntimeError("edge stream exhausted; use fewer steps")
+        return seq[a:a + B]
+
+
+def build_workload(args, device):
+    import torch
+    import lpma_gb300 as L
+    n_raw = (1 << args.scale) * args.ef
+    raw = torch.empty(n_raw, dtype=torch.int64, device=device)
+    n = L.gen_rmat_device(args.seed, args.scale, args.ef, raw)
+    e = raw[:n]
+    L.shuffle_device(args.seed + 1000, e)
+    half = n // 2
+    S, U = e[:half], e[half:]
+    ins_seq = torch.cat([U, S])
+    del_seq = torch.cat([S, U])
+    return e, S, ins_seq, del_seq
+
+
+def gpu_arm(args, rank, world):
+    import torch
+    import lpma_gb300 as L
+    device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(device)
+    V = 1 << args.scale
+    e, S, ins_seq, del_seq = build_workload(args, device)
+    g = L.Lpma(V)
+    g.build(S)
+    st = Stream(ins_seq, del_seq)
+    kinds = ["ins", "del"]
+    stream = torch.cuda.current_stream()
+
+    def run(B, steps):
+        for i in range(steps):
+            batch = st.next(kinds[i % 2], B)
+            g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+
+    # per-batch-size sweep (1K, 10K, 100K): same stream, 20 steps each
+    sweep = {}
+    for B in [int(x) for x in args.sweep.split(",") if x]:
+        run(B, 2)
+        torch.cuda.synchronize()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweep_steps + 1)]
+        evs[0].record(stream)
+        for i in range(args.sweep_steps):
+            batch = st.next(kinds[i % 2], B)
+            g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize()
+        lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.sweep_steps)]
+        tot = sum(lat) / 1e3
+        sweep[str(B)] = {"edges_per_s": B * args.sweep_steps / tot, "p50_ms": float(np.percentile(lat, 50)),
+                         "p99_ms": float(np.percentile(lat, 99))}
+
+    # main: W warmup + K timed steps at B
+    B = args.batch
+    clk = Clocks(device.index).__enter__()
+    time.sleep(0.3)
+    for i in range(args.warmup):
+        batch = st.next(kinds[i % 2], B)
+        g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.kernel_launches()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    stats = []
+    if True:
+        t0 = time.perf_counter()
+        evs[0].record(stream)
+        for i in range(args.steps):
+            batch = st.next(kinds[(args.warmup + i) % 2], B)
+            s = g.update(ins=batch) if (args.warmup + i) % 2 == 0 else g.update(dels=batch)
+            stats.append(s)
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    time.sleep(0.25)
+    clk.__exit__()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = L.kernel_launches() - launches0
+    lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    t = evs[0].elapsed_time(evs[-1]) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=device)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+
+    # roofline: per-kernel CUDA events over K more steps of the same stream
+    L.profile_enable(True)
+    pstats = []
+    prof_steps = min(args.steps, 10)
+    for i in range(prof_steps):
+        k = (args.warmup + args.steps + i) % 2
+        batch = st.next(kinds[k], B)
+        pstats.append(g.update(ins=batch) if k == 0 else g.update(dels=batch))
+    torch.cuda.synchronize()
+    prof = L.profile_report()
+    L.profile_enable(False)
+
+    # end to end through the host entry point: pinned host batch -> lpma_update_host
+    e2e_steps = min(args.steps, 10)
+    host_batches = []
+    for i in range(e2e_steps):
+        k = (args.warmup + args.steps + prof_steps + i) % 2
+        b = st.next(kinds[k], B)
+        hb = torch.empty(B, dtype=torch.int64, pin_memory=True)
+        hb.copy_(b)
+        host_batches.append((k, hb.numpy().view(np.uint64)))
+    torch.cuda.synchronize()
+    e2e_stats = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t_e0 = time.perf_counter()
+    for k, hb in host_batches:
+        e2e_stats.append(g.update(ins=hb) if k == 0 else g.update(dels=hb))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = max(ev0.elapsed_time(ev1) / 1e3, time.perf_counter() - t_e0)
+    h2d = sum(s["h2d_bytes"] for s in e2e_stats) / len(e2e_stats)
+    d2h = sum(s["d2h_bytes"] for s in e2e_stats) / len(e2e_stats)
+    info = g.info()
+    res = {"t": t, "lat": lat, "wall": wall, "launches": launches, "clocks": clk.summary(), "stats": stats,
+           "pstats": pstats, "prof": prof, "sweep": sweep, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
+           "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"]}
+    host_edges = None
+    if rank == 0 and not args.no_cpu_baseline:
+        host_edges = (e.cpu().numpy().view(np.uint64), int(S.shape[0]))
+    g.close()
+    return res, host_edges
+
+
+def roofline(res, B, peak, peak_kind):
+    prof = res["prof"]
+    if not prof:
+        return None
+    name = max(prof, key=lambda k: prof[k][1])
+    cnt, ms = prof[name]
+    pst = res["pstats"]
+    # algorithmic bytes per launch of the dominant kernel
+    if name == "exec_small":
+        units = sum(s["slots_small"] for s in pst) / cnt
+        per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
+    elif name == "exec_tiles":
+        units = sum(s["slots_rewritten"] - s["slots_small"] for s in pst) / cnt
+        per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
+    elif name == "sort_pass":
+        units = B
+        per_unit, unit_name = 20, "key (8 B key + 2 B payload, read and written)"
+    elif name == "resolve_locate":
+        units = B
+        per_unit, unit_name = 15, "key (8 B key + 2 B payload read, 1 B kind + 4 B segment written)"
+    else:
+        units, per_unit, unit_name = B, 8, "key"
+    alg = units * per_unit
+    avg_s = ms / cnt / 1e3
+    achieved = alg / avg_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if os.path.exists(tf):
+        for line in open(tf):
+            p = line.split()
+            if len(p) >= 3 and p[0] == name:
+                traffic = float(p[1]) * (units / float(p[2]) if float(p[2]) else 1.0)
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "bytes_per_launch": alg, "per_unit_bytes": per_unit, "unit_desc": unit_name,
+            "launches": cnt, "avg_launch_us": avg_s * 1e6,
+            "kernel_share": {k: round(v[1] / sum(x[1] for x in prof.values()), 4) for k, v in prof.items()},
+            "kernel_ms_per_step": {k: round(v[1] / len(pst), 4) for k, v in prof.items()}}
+
+
+def cpu_baseline(host_edges, B, steps, threads):
+    from oracle import pyoracle as O
+    edges, half = host_edges
+    S, U = edges[:half], edges[half:]
+    ins_seq = np.concatenate([U, S])
+    del_seq = np.concatenate([S, U])
+    V = int((edges.max() >> np.uint64(42)) + 1) if edges.size else 1
+    c = O.CsrBaseline(max(V, 1 << 21), threads=threads)
+    t0 = time.perf_counter()
+    c.load(S)
+    t_load = time.perf_counter() - t0
+    lat = []
+    for i in range(steps):
+        b = (ins_seq if i % 2 == 0 else del_seq)[(i // 2) * B:(i // 2 + 1) * B]
+        t0 = time.perf_counter()
+        (c.insert if i % 2 == 0 else c.delete)(b)
+        lat.append(time.perf_counter() - t0)
+    c.close()
+    return {"value": B * steps / sum(lat), "lat": lat, "load_s": t_load}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    peak, peak_kind = peaks()
+    res, host_edges = gpu_arm(args, rank, world)
+    B = args.batch
+    value = B * args.steps * world / res["t"]
+    out = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["t"] * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded device R-MAT)",
+        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.ef, "batch": B,
+                   "edges": res["n_edges"], "bulk": res["n_edges"] // 2, "height": res["height"],
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "PMA working set > 129 MB L2, no flush", "timing": "CUDA events on the update stream"},
+        "batch_latency_ms": {"p50": float(np.percentile(res["lat"], 50)), "p99": float(np.percentile(res["lat"], 99))},
+        "per_batch_size": dict(res["sweep"], **{str(B): {
+            "edges_per_s": B * args.steps / res["t"], "p50_ms": float(np.percentile(res["lat"], 50)),
+            "p99_ms": float(np.percentile(res["lat"], 99))}}),
+        "roofline": roofline(res, B, peak, peak_kind),
+        "e2e": {"value": B * res["e2e_steps"] * world / res["t_e2e"], "unit": "edges/s", "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"], "entry": "lpma_update_host (pinned host batch)"},
+        "gpu_launches": res["launches"],
+        "clocks": res["clocks"],
+    }
+    s = res["stats"]
+    out["events"] = {k: sum(x[k] for x in s) for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path",
+                                                       "fill_empty")}
+    out["slots_rewritten_per_step"] = sum(x["slots_rewritten"] for x in s) / len(s)
+    alg = 16 * B + 18 * out["slots_rewritten_per_step"]
+    out["batch_hbm"] = {"alg_bytes_per_step": alg, "achieved_GBps": alg / (res["t"] / args.steps) / 1e9,
+                        "frac": alg / (res["t"] / args.steps) / 1e9 / peak}
+    if rank == 0 and host_edges is not None:
+        threads = os.cpu_count() or 1
+        cb = cpu_baseline(host_edges, B, args.cpu_steps, threads)
+        out["cpu_baseline"] = {"value": cb["value"], "unit": "edges/s", "cores": threads, "kind": "port",
+                               "sample": "%d alternating insert/delete batches of %d edges on the scale-%d stream "
+                                         "(sorted-merge CSR rebuild per batch, oracle/lpma_oracle.c)"
+                                         % (args.cpu_steps, B, args.scale)}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_arm(args, rank, world):
+    """The reference's CPU path for this workload on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import torch
+    import lpma_gb300 as L  # only to generate the identical edge stream on the device
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    n_raw = (1 << args.scale) * args.ef
+    raw = torch.empty(n_raw, dtype=torch.int64, device="cuda")
+    n = L.gen_rmat_device(args.seed, args.scale, args.ef, raw)
+    e = raw[:n]
+    L.shuffle_device(args.seed + 1000, e)
+    edges = e.cpu().numpy().view(np.uint64)
+    threads = os.cpu_count() or 1
+    B = args.batch
+    steps = args.steps
+    cb = cpu_baseline((edges, n // 2), B, steps, threads)
+    out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "edges/s", "n_gpus": world,
+           "steps": steps, "warmup": args.warmup, "ms_per_step": sum(cb["lat"]) * 1e3 / steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+           "data": "synthetic (seeded R-MAT)",
+           "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.ef, "batch": B, "edges": n},
+           "cpu_baseline": {"value": cb["value"], "unit": "edges/s", "cores": threads, "kind": "port",
+                            "sample": "%d alternating insert/delete batches of %d edges (sorted-merge CSR rebuild "
+                                      "per batch; the reference GPU build does not compile under CUDA 13)"
+                                      % (steps, B)},
+           "e2e": {"value": cb["value"], "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -75,7 +75,10 @@ typedef struct {
     uint64_t windows_small;    /* rebalance windows of <= 32 segments executed */
     uint64_t windows_big;      /* larger windows (tile grain) executed */
     uint64_t slots_rewritten;  /* slots covered by executed windows (incl. rebuild) */
+    uint64_t slots_small;      /* of which in windows of <= 32 segments */
     uint64_t num_items;        /* keys stored after the call, sentinels included */
+    uint64_t h2d_bytes;        /* host->device bytes the call copied (inputs, control) */
+    uint64_t d2h_bytes;        /* device->host bytes the call copied (status blocks) */
 } LpmaStats;
 
 /* defaults that reproduce the reference: 32 / 0.42 / 1.0 / skip rule on */
@@ -163,6 +166,13 @@ LPMA_API lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edg
 
 /* Reorders d_keys by (mix64(seed ^ key), key). */
 LPMA_API lpma_status_t lpma_shuffle(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream);
+
+/* Per-kernel timing for profiling: while enabled, each kernel launch is
+ * bracketed by CUDA events on its stream.  lpma_prof_report writes one line
+ * "name launches total_ms" per kernel name into buf, clears the record and
+ * returns the full report length. */
+LPMA_API lpma_status_t lpma_prof_enable(int on);
+LPMA_API size_t lpma_prof_report(char *buf, size_t cap);
 
 /* Number of kernels this library launched since load (a counter for benches). */
 LPMA_API uint64_t lpma_kernel_launches(void);

@@ -22,7 +22,7 @@ MAX_HEIGHT = 24
 EXPORTS = [
     "lpma_config_default", "lpma_create", "lpma_build", "lpma_update", "lpma_update_host", "lpma_csr_view",
     "lpma_to_csr", "lpma_export_sorted", "lpma_export_layout", "lpma_info", "lpma_destroy", "lpma_status_string",
-    "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches",
+    "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches", "lpma_prof_enable", "lpma_prof_report",
 ]
 
 
@@ -40,7 +40,9 @@ class LpmaStats(ctypes.Structure):
                 ("overflow", ctypes.c_uint32), ("rebuilt", ctypes.c_uint32),
                 ("levelup_path", ctypes.c_uint32), ("fill_empty", ctypes.c_uint32),
                 ("windows_small", ctypes.c_uint64), ("windows_big", ctypes.c_uint64),
-                ("slots_rewritten", ctypes.c_uint64), ("num_items", ctypes.c_uint64)]
+                ("slots_rewritten", ctypes.c_uint64), ("slots_small", ctypes.c_uint64),
+                ("num_items", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -86,6 +88,10 @@ def load():
         f.restype = I
     L.lpma_status_string.argtypes = [I]
     L.lpma_status_string.restype = ctypes.c_char_p
+    L.lpma_prof_enable.argtypes = [I]
+    L.lpma_prof_enable.restype = I
+    L.lpma_prof_report.argtypes = [ctypes.c_char_p, SZ]
+    L.lpma_prof_report.restype = SZ
     L.lpma_kernel_launches.argtypes = []
     L.lpma_kernel_launches.restype = U64
     _lib = L

@@ -24,6 +24,8 @@ using namespace lpma;
 
 namespace lpma {
 uint64_t launch_count();
+void prof_enable(int on);
+size_t prof_report(char *buf, size_t cap);
 }
 
 namespace {
@@ -38,6 +40,7 @@ struct Cap {
     uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
     uint32_t *bitmap = nullptr;
     uint32_t *scan_tmp = nullptr;
+    uint2 *tile_bounds = nullptr;  // per destination tile of 32 segments
 };
 
 }  // namespace
@@ -61,7 +64,7 @@ struct LpmaHandle {
     uint8_t *kind = nullptr, *pend = nullptr;
     uint32_t *seg = nullptr, *blk_nn = nullptr, *blk_ins = nullptr;
     UpdList u{}, u2{};
-    Window *cand = nullptr, *wsmall = nullptr, *wbig = nullptr;
+    Window *cand = nullptr, *wsingle = nullptr, *wsmall = nullptr, *wbig = nullptr;
     SortScratch sort{};
     uint32_t *sort_err = nullptr;
     TileJob *jobs_d = nullptr;
@@ -79,6 +82,8 @@ struct LpmaHandle {
     uint8_t *exp_vals = nullptr;
     size_t view_cap = 0, exp_cap = 0;
     bool view_valid = false;
+    uint64_t h2d = 0, d2h = 0;  // bytes copied by the current call
+    bool host_staged = false;    // h2d already holds the staged input bytes
 };
 
 namespace {
@@ -124,7 +129,7 @@ void free_cap(Cap &c) {
     dfree(c.cnt), dfree(c.cnt_alt), dfree(c.cnt_live), dfree(c.srcc), dfree(c.seg_e);
     dfree(c.fl);
     dfree(c.segP), dfree(c.q), dfree(c.qn), dfree(c.PQ), dfree(c.US), dfree(c.qi), dfree(c.qd);
-    dfree(c.bitmap), dfree(c.scan_tmp);
+    dfree(c.bitmap), dfree(c.scan_tmp), dfree(c.tile_bounds);
     c.Hc = 0;
 }
 
@@ -142,6 +147,7 @@ cudaError_t alloc_cap(Cap &c, uint32_t Hc) {
     A(fl, nseg);
     A(segP, nseg + 2) A(q, nseg + 2) A(qn, nseg + 2) A(PQ, nseg + 2) A(US, nseg + 2) A(qi, nseg + 2) A(qd, nseg + 2);
     A(bitmap, bitmap_words(Hc)) A(scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
+    A(tile_bounds, nseg / 16 + 4);  // tiles of 32 segments, windows rounded up
 #undef A
     if ((e = cudaMemset(c.cnt, 0, nseg + 64)) != cudaSuccess) return e;
     if ((e = cudaMemset(c.cnt_live, 0, nseg + 64)) != cudaSuccess) return e;
@@ -176,7 +182,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
     dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
     dfree(h->blk_nn), dfree(h->blk_ins);
     for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
+    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
     h->bcap = 0;
     const size_t nb = cap / 256 + 4;
     CK(dalloc(&h->bk0, cap)); CK(dalloc(&h->bk1, cap)); CK(dalloc(&h->bp0, cap)); CK(dalloc(&h->bp1, cap));
@@ -186,7 +192,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
         CK(dalloc(&u->key, cap)); CK(dalloc(&u->val, cap)); CK(dalloc(&u->kind, cap)); CK(dalloc(&u->seg, cap));
         CK(dalloc(&u->ip, cap + 1));
     }
-    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
+    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsingle, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
     h->sort.status_words = sort_status_words((uint32_t)cap);
     CK(dalloc(&h->sort.status, h->sort.status_words));
     h->bcap = cap;
@@ -195,6 +201,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
 
 lpma_status_t sync_status(LpmaHandle *h, cudaStream_t s) {
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    h->d2h += sizeof(DevStatus);
     CK(cudaStreamSynchronize(s));
     CK(cudaGetLastError());
     if (h->hst->error & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
@@ -245,8 +252,8 @@ lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thr
     const uint8_t *cntp = thres_active ? h->c.cnt_live : h->c.cnt;
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
-    launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, H, tb, h->c.bitmap, h->cand, h->wsmall, h->wbig,
-                h->c.seg_e, h->pend, h->dst, s);
+    launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, H, tb, h->c.bitmap, h->cand, h->wsingle,
+                h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
     CK(cudaGetLastError());
     return LPMA_OK;
 }
@@ -272,20 +279,24 @@ lpma_status_t upload_jobs(LpmaHandle *h, cudaStream_t s) {
         CK(dalloc(&h->jobs_d, h->jobs_cap));
     }
     CK(cudaMemcpyAsync(h->jobs_d, h->jobs_h.data(), h->jobs_h.size() * sizeof(TileJob), cudaMemcpyHostToDevice, s));
+    h->h2d += h->jobs_h.size() * sizeof(TileJob);
     return LPMA_OK;
 }
 
 // Execute the planned maximal windows (status already synced).
 lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32_t thres, bool thres_active,
                         cudaStream_t s, LpmaStats *st) {
-    const uint32_t n_small = h->hst->n_small, n_big = h->hst->n_big;
+    const uint32_t n_single = h->hst->n_single, n_small = h->hst->n_small, n_big = h->hst->n_big;
     Geo g{h->c.keys, h->c.vals, h->H};
-    launch_exec_small(h->wsmall, n_small, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-    st->windows_small += n_small;
+    launch_exec_small(h->wsingle, n_single, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    launch_exec_small(h->wsmall, n_small, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    st->windows_small += n_single + n_small;
     st->slots_rewritten += h->hst->slots_small;
+    st->slots_small += h->hst->slots_small;
     if (n_big) {
         h->big_h.resize(n_big);
         CK(cudaMemcpyAsync(h->big_h.data(), h->wbig, n_big * sizeof(Window), cudaMemcpyDeviceToHost, s));
+        h->d2h += n_big * sizeof(Window);
         CKS(tile_prep(h, u, n_list, thres_active, s));
         CK(cudaStreamSynchronize(s));
         std::sort(h->big_h.begin(), h->big_h.end(), [](const Window &a, const Window &b) { return a.a < b.a; });
@@ -300,8 +311,8 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
         }
         CKS(upload_jobs(h, s));
         Geo alt{h->c.keys_alt, h->c.vals_alt, h->H};
-        launch_exec_tiles(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, g, h->c.srcc, h->c.PQ, h->c.US, alt, h->c.cnt,
-                          h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        launch_exec_tiles(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, h->c.tile_bounds, g, h->c.srcc, h->c.PQ,
+                          h->c.US, alt, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
         if (whole) {
             std::swap(h->c.keys, h->c.keys_alt);
             std::swap(h->c.vals, h->c.vals_alt);
@@ -347,8 +358,9 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     const uint32_t df = (uint32_t)nseg_of(hh);
     h->jobs_h.assign(1, TileJob{0, (uint32_t)nseg_of(H), 0, df, (uint32_t)m, (df + 31) / 32, 0, 0});
     CKS(upload_jobs(h, s));
-    launch_exec_tiles(h->jobs_d, 1, (df + 31) / 32, src, h->c.srcc, h->c.PQ, h->c.US, dst, cnt_d, fl_d, h->sent, h->V,
-                      u, thres, h->dst, s);
+    uint2 *bounds = grow ? fresh.tile_bounds : h->c.tile_bounds;
+    launch_exec_tiles(h->jobs_d, 1, (df + 31) / 32, bounds, src, h->c.srcc, h->c.PQ, h->c.US, dst, cnt_d, fl_d,
+                      h->sent, h->V, u, thres, h->dst, s);
     CK(cudaGetLastError());
     if (grow) {
         CK(cudaStreamSynchronize(s));
@@ -369,6 +381,9 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
                         const uint64_t *del, size_t n_del, uint32_t thres, cudaStream_t s, LpmaStats *out,
                         bool internal) {
     if (h->sticky != LPMA_OK) return h->sticky;
+    if (!internal && !h->host_staged) h->h2d = 0;
+    h->host_staged = false;
+    h->d2h = 0;
     LpmaStats st{};
     st.height_before = h->H;
     const size_t n = n_ins + n_del;
@@ -388,6 +403,7 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
 
     // 1. pack + validate
     CK(cudaMemcpyAsync(h->dst, h->hinit, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    h->h2d += sizeof(DevStatus);
     // the engine's own sentinel keys are always in the packed layout
     const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
     launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
@@ -489,6 +505,8 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     if (n_new && min_t_ins < h->min_t) h->min_t = min_t_ins;
     st.height_after = h->H;
     st.num_items = h->total;
+    st.h2d_bytes = h->h2d;
+    st.d2h_bytes = h->d2h;
     if (out) *out = st;
     return LPMA_OK;
 }
@@ -519,7 +537,8 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
     dfree(h->blk_nn), dfree(h->blk_ins);
     for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status), dfree(h->sort.hist), dfree(h->sort.counters);
+    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status), dfree(h->sort.hist),
+        dfree(h->sort.counters);
     dfree(h->jobs_d);
     dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
     dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals), dfree(h->exp_keys), dfree(h->exp_vals);
@@ -607,6 +626,8 @@ lpma_status_t lpma_update_host(LpmaHandle *h, const uint64_t *h_ins, const uint8
     if (n_ins && h_ins_vals && cudaMemcpyAsync(h->stage_vals, h_ins_vals, n_ins, cudaMemcpyHostToDevice, s))
         return LPMA_ERR_CUDA;
     if (n_del && cudaMemcpyAsync(h->stage_del, h_del, n_del * 8, cudaMemcpyHostToDevice, s)) return LPMA_ERR_CUDA;
+    h->h2d = n_ins * 8 + (h_ins_vals ? n_ins : 0) + n_del * 8;
+    h->host_staged = true;
     return do_update(h, h->stage_ins, h_ins_vals ? h->stage_vals : nullptr, n_ins, h->stage_del, n_del, thres, s,
                      stats, false);
 }
@@ -734,6 +755,13 @@ const char *lpma_status_string(lpma_status_t s) {
 }
 
 uint64_t lpma_kernel_launches(void) { return lpma::launch_count(); }
+
+lpma_status_t lpma_prof_enable(int on) {
+    lpma::prof_enable(on);
+    return LPMA_OK;
+}
+
+size_t lpma_prof_report(char *buf, size_t cap) { return lpma::prof_report(buf, cap); }
 
 lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edge_factor, uint32_t ta, uint32_t tab,
                             uint32_t tabc, uint64_t *d_out, size_t cap, size_t *n_out, lpma_stream_t stream) {

@@ -51,12 +51,13 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 // count-only planner: per segment with updates, the first level whose
 // window passes the density test; maximal windows go to small/big lists
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
-                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand,
+                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *single,
                  Window *small, Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s);
 
-// warp-grain executor for windows of <= 32 segments, in place
-void launch_exec_small(const Window *w, uint32_t n_small, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
-                       uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
+// warp-grain executor for windows of <= 32 segments, in place; single != 0
+// takes the single-segment list (count in DevStatus::n_single)
+void launch_exec_small(const Window *w, uint32_t n_cap, int single, Geo g, uint8_t *cnt, ulonglong2 *fl,
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
 
 // per-segment counts for the tile grain: qi/qd from the update list
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
@@ -75,9 +76,10 @@ struct TileJob {
 };
 // tile-grain executor: merge source windows with their inserts and spread
 // them over the destination geometry (another buffer)
-void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo src, const uint8_t *srcc,
-                       const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
+void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, uint2 *bounds, Geo src,
+                       const uint8_t *srcc, const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d,
+                       ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
+                       cudaStream_t s);
 void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to,
                           cudaStream_t s);
 

@@ -79,10 +79,9 @@ struct DevStatus {
     unsigned long long key_and, key_or;
     uint32_t n_u;             // compacted updates
     uint32_t n_ins, n_del, n_upsert, n_noop;
-    uint32_t n_cand, n_small, n_big;
+    uint32_t n_cand, n_single, n_small, n_big;
     uint32_t root, ovf;
     uint32_t empty_found;     // fill_empty_segs check
-    uint32_t pad0;
     unsigned long long slots_small, slots_big;
     unsigned long long live_total;   // sum of live counts (thres pass)
     unsigned long long cnt_total;    // sum of occupancy counts (recount)

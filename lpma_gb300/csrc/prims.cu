@@ -10,6 +10,11 @@
 // Batches of at most one tile are sorted by one CTA entirely in shared
 // memory in a single launch.
 #include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "lpma_common.cuh"
 #include "prims.cuh"
@@ -19,6 +24,85 @@ namespace lpma {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(int k) { g_launches += (uint64_t)k; }
 uint64_t launch_count() { return g_launches.load(); }
+
+struct ProfRec {
+    const char *name;
+    cudaEvent_t a, b;
+};
+static std::vector<ProfRec> g_prof;
+static std::vector<cudaEvent_t> g_event_pool;
+static bool g_prof_on = false;
+static std::mutex g_prof_mu;
+
+static cudaEvent_t pool_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+bool prof_enabled() { return g_prof_on; }
+
+ProfScope::ProfScope(const char *name, cudaStream_t st) : idx(-1), s(st) {
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRec r{name, pool_event(), pool_event()};
+    cudaEventRecord(r.a, s);
+    g_prof.push_back(r);
+    idx = (int)g_prof.size() - 1;
+}
+ProfScope::~ProfScope() {
+    if (idx < 0) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEventRecord(g_prof[idx].b, s);
+}
+
+void prof_enable(int on) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_on = on != 0;
+}
+
+// "name launches total_ms" per kernel name, in order of first appearance;
+// clears the record.  Synchronises with the recorded events.
+size_t prof_report(char *buf, size_t cap) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::vector<std::string> names;
+    std::vector<double> tot;
+    std::vector<long> cnt;
+    for (ProfRec &r : g_prof) {
+        cudaEventSynchronize(r.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        size_t k = 0;
+        while (k < names.size() && names[k] != r.name) k++;
+        if (k == names.size()) {
+            names.push_back(r.name);
+            tot.push_back(0.0);
+            cnt.push_back(0);
+        }
+        tot[k] += ms;
+        cnt[k] += 1;
+        g_event_pool.push_back(r.a);
+        g_event_pool.push_back(r.b);
+    }
+    g_prof.clear();
+    std::string out;
+    char line[256];
+    for (size_t k = 0; k < names.size(); k++) {
+        snprintf(line, sizeof(line), "%s %ld %.6f\n", names[k].c_str(), cnt[k], tot[k]);
+        out += line;
+    }
+    if (buf && cap) {
+        size_t n = out.size() < cap - 1 ? out.size() : cap - 1;
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return out.size();
+}
 
 namespace {
 
@@ -164,21 +248,33 @@ __global__ void __launch_bounds__(SORT_TPB) k_pass(const uint64_t *__restrict__ 
         st_release(my, FLAG_PREFIX | tcount);
     } else {
         st_release(my, FLAG_AGG | tcount);
+        // look back over the predecessors LB at a time (independent loads in
+        // flight): every tile is resident at once, so chains of AGG entries
+        // are long unless they are read in parallel
+        constexpr int LB = 16;
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
-        while (p >= 0) {
-            uint32_t s = ld_acquire(status + (size_t)p * 256 + tid);
-            uint32_t f = s & ~VAL_MASK;
-            if (f == 0) {
-                if (++spins > SPIN_LIMIT) {
-                    atomicOr(err, ERR_TIMEOUT);
+        bool done = false;
+        while (p >= 0 && !done) {
+            uint32_t s[LB];
+#pragma unroll
+            for (int k = 0; k < LB; k++) s[k] = p - k >= 0 ? ld_acquire(status + (size_t)(p - k) * 256 + tid) : FLAG_PREFIX;
+            int k = 0;
+            for (; k < LB; k++) {
+                const uint32_t f = s[k] & ~VAL_MASK;
+                if (f == 0) break;  // not published yet: poll again from here
+                excl += s[k] & VAL_MASK;
+                if (f == FLAG_PREFIX) {
+                    done = true;
                     break;
                 }
-                continue;
             }
-            excl += s & VAL_MASK;
-            if (f == FLAG_PREFIX) break;
-            --p;
+            if (done) break;
+            p -= k;
+            if (k < LB && ++spins > SPIN_LIMIT) {
+                atomicOr(err, ERR_TIMEOUT);
+                break;
+            }
         }
         st_release(my, FLAG_PREFIX | (excl + tcount));
     }
@@ -363,6 +459,7 @@ cudaError_t scan_impl(const T *in, uint32_t *out, uint32_t n, uint32_t *total, u
         return cudaSuccess;
     }
     uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    ProfScope ps("scan", st);
     if (nb == 1) {
         k_scan_down<T><<<1, SCAN_TPB, 0, st>>>(in, out, n, nullptr, total);
         note_launch();
@@ -401,6 +498,7 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
         size_t sm = sizeof(SmallSmem<V>);
         e = cudaFuncSetAttribute(k_small_sort<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
+        ProfScope ps("sort_small", st);
         k_small_sort<V><<<1, SORT_TPB, sm, st>>>(k0, v0, n, byte_mask);
         note_launch();
         return cudaGetLastError();
@@ -410,7 +508,10 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
     if ((e = cudaMemsetAsync(s.hist, 0, 8 * 256 * sizeof(uint32_t), st))) return e;
     if ((e = cudaMemsetAsync(s.counters, 0, 8 * sizeof(uint32_t), st))) return e;
     uint32_t hb = tiles < 1024 ? tiles : 1024;
-    k_hist<<<hb, 256, 0, st>>>(k0, n, s.hist);
+    {
+        ProfScope ps("sort_hist", st);
+        k_hist<<<hb, 256, 0, st>>>(k0, n, s.hist);
+    }
     note_launch();
     size_t sm = sizeof(PassSmem<V>);
     if ((e = cudaFuncSetAttribute(k_pass<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm))) return e;
@@ -420,7 +521,10 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
     for (int b = 0; b < 8; b++) {
         if (!((byte_mask >> b) & 1u)) continue;
         if ((e = cudaMemsetAsync(s.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), st))) return e;
-        k_pass<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, b, s.hist, s.status, s.counters + b, err);
+        {
+            ProfScope ps("sort_pass", st);
+            k_pass<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, b, s.hist, s.status, s.counters + b, err);
+        }
         note_launch();
         uint64_t *tk = ka; ka = kb; kb = tk;
         V *tv = va; va = vb; vb = tv;

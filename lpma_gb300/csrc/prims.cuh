@@ -43,4 +43,14 @@ size_t scan_tmp_words(uint32_t n);
 // launch counter shared by every translation unit of the library
 void note_launch(int k = 1);
 
+// Optional per-kernel timing: when enabled, every launcher brackets its
+// launch with CUDA events on the launching stream.
+struct ProfScope {
+    ProfScope(const char *name, cudaStream_t s);
+    ~ProfScope();
+    int idx;
+    cudaStream_t s;
+};
+bool prof_enabled();
+
 }  // namespace lpma

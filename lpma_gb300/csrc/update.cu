@@ -169,7 +169,19 @@ __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, 
         mint = min(mint, __shfl_xor_sync(0xffffffffu, mint, o));
         bad = min(bad, __shfl_xor_sync(0xffffffffu, bad, o));
     }
-    if ((threadIdx.x & 31) == 0) {
+    // one set of atomics per block: the status words are single addresses
+    __shared__ unsigned long long s_and[TPB / 32], s_or[TPB / 32];
+    __shared__ uint32_t s_min[TPB / 32], s_bad[TPB / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) s_and[w] = kand, s_or[w] = kor, s_min[w] = mint, s_bad[w] = bad;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < TPB / 32; i++) {
+            kand &= s_and[i];
+            kor |= s_or[i];
+            mint = min(mint, s_min[i]);
+            bad = min(bad, s_bad[i]);
+        }
         atomicAnd(&st->key_and, kand);
         atomicOr(&st->key_or, kor);
         if (mint != 0xFFFFFFFFu) atomicMin(&st->min_t_ins, mint);
@@ -428,71 +440,116 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
                                               const uint32_t *__restrict__ P, int use_P, uint64_t total_live,
                                               uint32_t H, Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
                                               uint8_t *pend, DevStatus *st) {
+    __shared__ uint32_t wsum[TPB / 32];
+    __shared__ uint32_t base_s;
     const uint32_t nu = st->n_u;
     const uint32_t x = blockIdx.x * TPB + threadIdx.x;
-    if (x >= nu || x >= n_cap) return;
-    const uint32_t s = u.seg[x];
-    if (x > 0 && u.seg[x - 1] == s) return;  // one thread per segment with updates
-    const uint32_t hi0 = lb_fwd(u.seg, x, nu, (uint64_t)s + 1);
-    const uint64_t nseg = nseg_of(H);
-    uint32_t lo = x, hi = hi0, e = EXEC_OVF;
+    uint32_t s = 0;
+    bool lead = false;
+    if (x < nu && x < n_cap) {
+        s = u.seg[x];
+        lead = (x == 0 || u.seg[x - 1] != s);  // one thread per segment with updates
+    }
+    uint32_t e = EXEC_OVF, lo = x, hi = x;
     uint64_t wa = 0, wf = 0;
     int64_t wm = 0;
-    for (uint32_t l = 0; l <= H + 1; l++) {
-        if (!((tb.allowed >> l) & 1u)) continue;
-        const uint64_t a = ((uint64_t)s >> l) << l;
-        const uint64_t b = umin64(a + (1ull << l), nseg);
-        lo = lb_back(u.seg, lo, (uint32_t)a);
-        hi = lb_fwd(u.seg, hi, nu, b);
-        int64_t live;
-        if (l == H + 1)
-            live = (int64_t)total_live;
-        else if (l <= LSUM || !use_P)
-            live = sum_cnt(cnt, a, l);
-        else
-            live = (int64_t)P[b] - (int64_t)P[a];
-        const int64_t net = 2 * ((int64_t)u.ip[hi] - (int64_t)u.ip[lo]) - (int64_t)(hi - lo);
-        const int64_t m = live + net;
-        if (m >= (int64_t)tb.lower[l] && m <= (int64_t)(32 * (b - a))) {
-            e = l;
-            wa = a;
-            wf = b - a;
-            wm = m;
-            break;
+    bool own = false;
+    if (lead) {
+        const uint32_t hi0 = lb_fwd(u.seg, x, nu, (uint64_t)s + 1);
+        const uint64_t nseg = nseg_of(H);
+        hi = hi0;
+        for (uint32_t l = 0; l <= H + 1; l++) {
+            if (!((tb.allowed >> l) & 1u)) continue;
+            const uint64_t a = ((uint64_t)s >> l) << l;
+            const uint64_t b = umin64(a + (1ull << l), nseg);
+            lo = lb_back(u.seg, lo, (uint32_t)a);
+            hi = lb_fwd(u.seg, hi, nu, b);
+            int64_t live;
+            if (l == H + 1)
+                live = (int64_t)total_live;
+            else if (l <= LSUM || !use_P)
+                live = sum_cnt(cnt, a, l);
+            else
+                live = (int64_t)P[b] - (int64_t)P[a];
+            const int64_t net = 2 * ((int64_t)u.ip[hi] - (int64_t)u.ip[lo]) - (int64_t)(hi - lo);
+            const int64_t m = live + net;
+            if (m >= (int64_t)tb.lower[l] && m <= (int64_t)(32 * (b - a))) {
+                e = l;
+                wa = a;
+                wf = b - a;
+                wm = m;
+                break;
+            }
+        }
+        seg_e[s] = (uint8_t)e;
+        if (e == EXEC_OVF) {
+            for (uint32_t y = x; y < hi0; y++) pend[y] = 1;
+        } else {
+            const uint64_t bit = bit_of(H, e, (uint64_t)s >> e);
+            const uint32_t mask = 1u << (bit & 31);
+            own = !(atomicOr(&bitmap[bit >> 5], mask) & mask);
         }
     }
-    seg_e[s] = (uint8_t)e;
-    if (e == EXEC_OVF) {
-        atomicOr(&st->ovf, 1u);
-        for (uint32_t y = x; y < hi0; y++) pend[y] = 1;
-        return;
+    const int any_ovf = __syncthreads_or(lead && e == EXEC_OVF);
+    const int any_root = __syncthreads_or(lead && e == H + 1);
+    if (threadIdx.x == 0) {
+        if (any_ovf) atomicOr(&st->ovf, 1u);
+        if (any_root) atomicOr(&st->root, 1u);
     }
-    if (e == H + 1) atomicOr(&st->root, 1u);
-    const uint64_t bit = bit_of(H, e, (uint64_t)s >> e);
-    const uint32_t mask = 1u << (bit & 31);
-    const uint32_t old = atomicOr(&bitmap[bit >> 5], mask);
-    if (!(old & mask)) {
-        const uint32_t c = atomicAdd(&st->n_cand, 1u);
-        cand[c] = Window{(uint32_t)wa, (uint32_t)wf, (uint32_t)wm, e, lo, hi};
-    }
+    // block-aggregated append of the windows this block owns
+    const uint32_t ex = block_excl_scan(own ? 1u : 0u, wsum);
+    if (threadIdx.x == TPB - 1) base_s = atomicAdd(&st->n_cand, ex + (own ? 1u : 0u));
+    __syncthreads();
+    if (own) cand[base_s + ex] = Window{(uint32_t)wa, (uint32_t)wf, (uint32_t)wm, e, lo, hi};
 }
 
+// Keep the candidates not inside a larger executed window; sort them into
+// single-segment, small (<= 32 segments) and big lists.
 __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
-                                                  const uint32_t *__restrict__ bitmap, Window *small, Window *big,
-                                                  DevStatus *st) {
+                                                  const uint32_t *__restrict__ bitmap, Window *single, Window *small,
+                                                  Window *big, DevStatus *st) {
+    __shared__ uint32_t wsum[TPB / 32];
+    __shared__ uint32_t base_s[3];
+    __shared__ unsigned long long sl[2][TPB / 32];
     const uint32_t c = blockIdx.x * TPB + threadIdx.x;
-    if (c >= st->n_cand || c >= n_cap) return;
-    const Window w = cand[c];
-    for (uint32_t l = w.level + 1; l <= H + 1; l++) {
-        const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
-        if ((bitmap[bit >> 5] >> (bit & 31)) & 1u) return;  // inside a larger executed window
+    uint32_t cls = 3;
+    Window w{};
+    if (c < st->n_cand && c < n_cap) {
+        w = cand[c];
+        cls = w.f == 1 ? 0 : (w.f <= SMALL_WIN_SEGS ? 1 : 2);
+        for (uint32_t l = w.level + 1; l <= H + 1; l++) {
+            const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
+            if ((bitmap[bit >> 5] >> (bit & 31)) & 1u) {  // inside a larger executed window
+                cls = 3;
+                break;
+            }
+        }
     }
-    if (w.f <= SMALL_WIN_SEGS) {
-        small[atomicAdd(&st->n_small, 1u)] = w;
-        atomicAdd(&st->slots_small, 32ull * w.f);
-    } else {
-        big[atomicAdd(&st->n_big, 1u)] = w;
-        atomicAdd(&st->slots_big, 32ull * w.f);
+    const uint32_t packed = cls < 3 ? 1u << (10 * cls) : 0u;
+    const uint32_t ex = block_excl_scan(packed, wsum);
+    unsigned long long s_small = cls <= 1 ? 32ull * w.f : 0, s_big = cls == 2 ? 32ull * w.f : 0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        s_small += __shfl_xor_sync(0xffffffffu, s_small, o);
+        s_big += __shfl_xor_sync(0xffffffffu, s_big, o);
+    }
+    if ((threadIdx.x & 31) == 0) sl[0][threadIdx.x >> 5] = s_small, sl[1][threadIdx.x >> 5] = s_big;
+    if (threadIdx.x == TPB - 1) {
+        const uint32_t tot = ex + packed;
+        base_s[0] = atomicAdd(&st->n_single, tot & 1023u);
+        base_s[1] = atomicAdd(&st->n_small, (tot >> 10) & 1023u);
+        base_s[2] = atomicAdd(&st->n_big, tot >> 20);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = 0, b = 0;
+        for (int i = 0; i < TPB / 32; i++) a += sl[0][i], b += sl[1][i];
+        if (a) atomicAdd(&st->slots_small, a);
+        if (b) atomicAdd(&st->slots_big, b);
+    }
+    if (cls < 3) {
+        const uint32_t idx = base_s[cls] + ((ex >> (10 * cls)) & 1023u);
+        (cls == 0 ? single : cls == 1 ? small : big)[idx] = w;
     }
 }
 
@@ -512,12 +569,10 @@ __device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, cons
                                          SegMergeOut out) {
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
-    uint64_t key = KEY_NONE;
-    uint8_t val = 0;
-    if ((uint32_t)lane < c) {
-        key = keys[32 * j + lane];
-        val = vals[32 * j + lane];
-    }
+    // all 32 slots in one 256-byte access, issued without waiting for the
+    // count (slots at or past the count are empty: segments are left-packed)
+    const uint64_t key = keys[32 * j + lane];
+    const uint8_t val = vals[32 * j + lane];
     const bool keep = (uint32_t)lane < c && kept_slot(key, val, thres);
     const uint32_t bal = __ballot_sync(0xffffffffu, keep);
     const uint32_t nk = __popc(bal), kb = __popc(bal & lt);
@@ -534,6 +589,7 @@ __device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, cons
     if (keep) kk[kb] = key;
     __syncwarp();
     const uint32_t ip0 = u.ip[us];
+    const uint32_t total = nk + (u.ip[ue] - ip0);
     if (keep) {
         const uint32_t xk = lb_key(u.key, us, ue, key);
         const uint64_t r = Rs + kb + (u.ip[xk] - ip0);
@@ -542,9 +598,46 @@ __device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, cons
             out.v[r - R0] = val;
         }
     }
-    for (uint32_t x0 = us; x0 < ue; x0 += 32) {
+    // Update entries whose merged rank falls in [R0, R1): the rank of entry x
+    // is Rs + (inserts before x) + (kept keys below key[x]), monotone in x,
+    // so the range is found by binary search (a segment can carry millions
+    // of inserts when a bulk load lands in a near-empty tree).
+    uint32_t x_lo = us, x_hi = ue;
+    if (Rs < R0 || Rs + total > R1) {
+        auto rank_at = [&](uint32_t x) -> uint64_t {
+            const uint64_t y = u.key[x];
+            uint32_t L = 0, R = nk;
+            while (L < R) {
+                uint32_t mid = (L + R) >> 1;
+                if (kk[mid] < y)
+                    L = mid + 1;
+                else
+                    R = mid;
+            }
+            return Rs + (u.ip[x] - ip0) + L;
+        };
+        uint32_t a = us, b = ue;
+        while (a < b) {
+            uint32_t mid = (a + b) >> 1;
+            if (rank_at(mid) < R0)
+                a = mid + 1;
+            else
+                b = mid;
+        }
+        x_lo = a;
+        b = ue;
+        while (a < b) {
+            uint32_t mid = (a + b) >> 1;
+            if (rank_at(mid) < R1)
+                a = mid + 1;
+            else
+                b = mid;
+        }
+        x_hi = a;
+    }
+    for (uint32_t x0 = x_lo; x0 < x_hi; x0 += 32) {
         const uint32_t x = x0 + lane;
-        if (x < ue && u.kind[x] == KIND_INS) {
+        if (x < x_hi && u.kind[x] == KIND_INS) {
             const uint64_t y = u.key[x];
             uint32_t L = 0, R = nk;
             while (L < R) {
@@ -562,7 +655,7 @@ __device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, cons
         }
     }
     __syncwarp();
-    return nk + (u.ip[ue] - ip0);
+    return total;
 }
 
 // Write destination segment k of a window spread (m items over f segments),
@@ -591,21 +684,28 @@ __device__ inline void write_segment(uint64_t *__restrict__ dkeys, uint8_t *__re
 }
 
 // ------------------------------------------------------------------ small windows
+// One warp per window of <= 32 segments, in place: every source slot of the
+// window is read (into registers / shared memory) before any is written.
+// OUTCAP = 32 serves single-segment windows with 0.5 KB of shared memory
+// per warp (full occupancy); OUTCAP = 1024 serves windows of 2..32 segments.
 constexpr int EXS_WARPS = 8;
+template <int OUTCAP>
 struct ExSmallSmem {
-    uint64_t outk[EXS_WARPS][1024];
-    uint8_t outv[EXS_WARPS][1024];
+    uint64_t outk[EXS_WARPS][OUTCAP];
+    uint8_t outv[EXS_WARPS][OUTCAP];
     uint64_t kk[EXS_WARPS][32];
 };
 
-__global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__restrict__ wins, uint32_t n_cap, Geo g,
-                                                               uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+template <int OUTCAP>
+__global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__restrict__ wins,
+                                                               const uint32_t *__restrict__ n_win, uint32_t n_cap,
+                                                               Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
                                                                uint32_t V, const UpdList u, uint32_t thres,
                                                                DevStatus *st) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ExSmallSmem &S = *reinterpret_cast<ExSmallSmem *>(smem_raw);
+    ExSmallSmem<OUTCAP> &S = *reinterpret_cast<ExSmallSmem<OUTCAP> *>(smem_raw);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t nwin = min(st->n_small, n_cap);
+    const uint32_t nwin = min(*n_win, n_cap);
     SegMergeOut out{S.outk[w], S.outv[w]};
     for (uint32_t wi = blockIdx.x * EXS_WARPS + w; wi < nwin; wi += gridDim.x * EXS_WARPS) {
         const Window W = wins[wi];
@@ -616,7 +716,7 @@ __global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__r
             const uint32_t s = W.a + lane;
             c = cnt[s];
             j = heap_of_linear(s, g.H);
-            us = lb_seg(u.seg, W.lo, W.hi, s);
+            us = W.f == 1 ? W.lo : lb_seg(u.seg, W.lo, W.hi, s);
         }
         uint32_t ue = __shfl_down_sync(0xffffffffu, us, 1);
         if ((uint32_t)lane + 1 >= W.f) ue = W.hi;
@@ -626,10 +726,10 @@ __global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__r
             const uint64_t jk = __shfl_sync(0xffffffffu, j, k);
             const uint32_t usk = __shfl_sync(0xffffffffu, us, k);
             const uint32_t uek = __shfl_sync(0xffffffffu, ue, k);
-            R += merge_segment(g.keys, g.vals, jk, ck, usk, uek, R, 0, 1024, u, thres, S.kk[w], out);
+            R += merge_segment(g.keys, g.vals, jk, ck, usk, uek, R, 0, OUTCAP, u, thres, S.kk[w], out);
         }
         __syncwarp();
-        if (R != W.m) {
+        if (R != W.m || W.m > (uint32_t)OUTCAP) {
             if (lane == 0) {
                 atomicOr(&st->error, ERR_INTERNAL);
                 st->err_info[1] = 1;
@@ -644,6 +744,142 @@ __global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__r
             if (lane == 0) {
                 cnt[W.a + k] = cn;
                 fl[jk] = f2;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ single-segment windows
+// The level-0 windows (one segment, about 94% of the executed windows) get a
+// group of 8 lanes each, so a warp keeps 4 windows in flight.  Lane gl of a
+// group moves slots 4gl..4gl+3 with two 16-byte key loads/stores and one
+// 4-byte value load/store.  Merged ranks come from group shuffles; the
+// re-packed segment is staged in 288 bytes of shared memory per group.
+constexpr int ES_TPB = 256;
+constexpr int ES_GROUPS = ES_TPB / 8;
+
+__global__ void __launch_bounds__(ES_TPB) k_exec_single(const Window *__restrict__ wins,
+                                                        const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
+                                                        uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
+                                                        const UpdList u, uint32_t thres, DevStatus *st) {
+    __shared__ __align__(16) uint64_t sk[ES_GROUPS][32];
+    __shared__ __align__(16) uint8_t sv[ES_GROUPS][32];
+    const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
+    const uint32_t nwin = min(*n_win, n_cap);
+    for (uint32_t wi = blockIdx.x * ES_GROUPS + grp; __any_sync(0xffffffffu, wi < nwin); wi += gridDim.x * ES_GROUPS) {
+        const bool active = wi < nwin;
+        Window W{};
+        if (active) W = wins[wi];
+        const uint64_t j = active ? heap_of_linear(W.a, g.H) : 0;
+        uint64_t k[4];
+        uint8_t v[4];
+        uint32_t kmask = 0;
+        if (active) {
+            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+            const ulonglong2 a = kp[0], b = kp[1];
+            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
+            k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                v[q] = (uint8_t)(v4 >> (8 * q));
+                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) k[q] = KEY_NONE, v[q] = 0;
+        }
+        // exclusive prefix of kept counts across the group
+        const uint32_t nl = __popc(kmask);
+        uint32_t incl = nl;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 8);
+            if (gl >= o) incl += y;
+        }
+        const uint32_t kbase = incl - nl;
+        const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
+        // updates of the window, 8 per round
+        const uint32_t lo = W.lo, hi = active ? W.hi : W.lo;
+        const uint32_t ip0 = active ? u.ip[lo] : 0;
+        const uint32_t nins = active ? u.ip[hi] - ip0 : 0;
+        uint32_t ins_less[4] = {0, 0, 0, 0};
+        const uint32_t rounds = __reduce_max_sync(0xffffffffu, (hi - lo + 7) / 8);
+        for (uint32_t r = 0; r < rounds; r++) {
+            const uint32_t x = lo + 8 * r + gl;
+            const bool has = x < hi;
+            uint64_t yk = KEY_NONE;
+            bool yins = false;
+            uint8_t yv = 0;
+            uint32_t yip = 0;
+            if (has) {
+                yk = u.key[x];
+                yins = u.kind[x] == KIND_INS;
+                yv = u.val[x];
+                yip = u.ip[x];
+            }
+            uint32_t my_below = 0;
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const uint64_t bk = __shfl_sync(0xffffffffu, yk, t, 8);
+                const bool bins = __shfl_sync(0xffffffffu, yins, t, 8);
+                uint32_t below = 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const bool kq = (kmask >> q) & 1u;
+                    if (bins && kq && bk < k[q]) ins_less[q]++;
+                    below += (kq && k[q] < bk) ? 1u : 0u;
+                }
+                below += __shfl_xor_sync(0xffffffffu, below, 1, 8);
+                below += __shfl_xor_sync(0xffffffffu, below, 2, 8);
+                below += __shfl_xor_sync(0xffffffffu, below, 4, 8);
+                if (gl == t) my_below = below;
+            }
+            if (yins) {
+                const uint32_t rk = (yip - ip0) + my_below;
+                if (rk < 32) {
+                    sk[grp][rk] = yk;
+                    sv[grp][rk] = yv;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if ((kmask >> q) & 1u) {
+                const uint32_t rk = kbase + __popc(kmask & ((1u << q) - 1)) + ins_less[q];
+                if (rk < 32) {
+                    sk[grp][rk] = k[q];
+                    sv[grp][rk] = v[q];
+                }
+            }
+        }
+        __syncwarp();
+        const uint32_t m = nk + nins;
+        const bool ok = active && m == W.m && m <= 32;
+        if (active && !ok && gl == 0) {
+            atomicOr(&st->error, ERR_INTERNAL);
+            st->err_info[1] = 3;
+        }
+        if (ok) {
+            uint64_t o[4];
+            uint32_t ov = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t slot = 4 * gl + q;
+                o[q] = slot < m ? sk[grp][slot] : KEY_NONE;
+                ov |= (slot < m ? (uint32_t)sv[grp][slot] : 0u) << (8 * q);
+                if (slot < m && is_sentinel(o[q])) {
+                    const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
+                    if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                }
+            }
+            ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+            kp[0] = make_ulonglong2(o[0], o[1]);
+            kp[1] = make_ulonglong2(o[2], o[3]);
+            *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ov;
+            if (gl == 0) {
+                cnt[W.a] = (uint8_t)m;
+                fl[j] = m ? make_ulonglong2(sk[grp][0], sk[grp][m - 1]) : make_ulonglong2(KEY_NONE, KEY_NONE);
             }
         }
         __syncwarp();
@@ -676,71 +912,79 @@ __global__ void __launch_bounds__(TPB) k_seg_q(const uint8_t *__restrict__ cnt, 
     }
 }
 
+// Per destination tile: the source segments whose merged ranks overlap the
+// tile's rank range (binary searches over the window prefix PQ), one thread
+// per tile so that the tile kernel starts with its bounds in hand.
+__device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_t tile) {
+    uint32_t L = 0, R = njobs - 1;  // last job with tile0 <= tile
+    while (L < R) {
+        uint32_t mid = (L + R + 1) >> 1;
+        if (jobs[mid].tile0 <= tile)
+            L = mid;
+        else
+            R = mid - 1;
+    }
+    return L;
+}
+
+__global__ void __launch_bounds__(TPB) k_tile_bounds(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
+                                                     const uint32_t *__restrict__ PQ, uint2 *bounds, DevStatus *st) {
+    const uint32_t tile = blockIdx.x * TPB + threadIdx.x;
+    if (tile >= ntiles) return;
+    const uint32_t jb = find_job(jobs, njobs, tile);
+    const TileJob J = jobs[jb];
+    const uint64_t t = tile - J.tile0;
+    const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
+    const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
+    const uint32_t base = PQ[J.sa];
+    uint32_t a = J.sa, b = J.sa + J.sf - 1;  // last source segment whose first rank <= R0
+    while (a < b) {
+        uint32_t mid = (a + b + 1) >> 1;
+        if (PQ[mid] - base <= R0)
+            a = mid;
+        else
+            b = mid - 1;
+    }
+    uint32_t c = a, d = J.sa + J.sf;  // first source segment whose first rank >= R1
+    while (c < d) {
+        uint32_t mid = (c + d) >> 1;
+        if (PQ[mid] - base >= R1)
+            d = mid;
+        else
+            c = mid + 1;
+    }
+    bounds[tile] = make_uint2(a, c);
+    // the source prefix must account for exactly m items
+    if (t == 0 && PQ[J.sa + J.sf] - base != J.m) {
+        atomicOr(&st->error, ERR_INTERNAL);
+        st->err_info[1] = 2;
+    }
+}
+
 struct TileSmem {
     uint64_t outk[1056];
     uint8_t outv[1056];
     uint64_t kk[8][32];
-    uint32_t sbeg, send, job;
 };
 
 __global__ void __launch_bounds__(TPB) k_exec_tiles(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
-                                                    Geo src, const uint8_t *__restrict__ srcc,
-                                                    const uint32_t *__restrict__ PQ, const uint32_t *__restrict__ US,
-                                                    Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
-                                                    uint32_t V, const UpdList u, uint32_t thres, DevStatus *st) {
+                                                    const uint2 *__restrict__ bounds, Geo src,
+                                                    const uint8_t *__restrict__ srcc, const uint32_t *__restrict__ PQ,
+                                                    const uint32_t *__restrict__ US, Geo dst, uint8_t *cnt_d,
+                                                    ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u,
+                                                    uint32_t thres) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (threadIdx.x == 0) {
-            uint32_t L = 0, R = njobs - 1;  // last job with tile0 <= tile
-            while (L < R) {
-                uint32_t mid = (L + R + 1) >> 1;
-                if (jobs[mid].tile0 <= tile)
-                    L = mid;
-                else
-                    R = mid - 1;
-            }
-            S.job = L;
-            const TileJob J = jobs[L];
-            const uint64_t t = tile - J.tile0;
-            const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
-            const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
-            const uint32_t base = PQ[J.sa];
-            // last source segment whose first rank <= R0
-            uint32_t a = J.sa, b = J.sa + J.sf - 1;
-            while (a < b) {
-                uint32_t mid = (a + b + 1) >> 1;
-                if (PQ[mid] - base <= R0)
-                    a = mid;
-                else
-                    b = mid - 1;
-            }
-            S.sbeg = a;
-            // first source segment whose first rank >= R1
-            uint32_t c = a, d = J.sa + J.sf;
-            while (c < d) {
-                uint32_t mid = (c + d) >> 1;
-                if (PQ[mid] - base >= R1)
-                    d = mid;
-                else
-                    c = mid + 1;
-            }
-            S.send = c;
-            // the source prefix must account for exactly m items
-            if (t == 0 && PQ[J.sa + J.sf] - base != J.m) {
-                atomicOr(&st->error, ERR_INTERNAL);
-                st->err_info[1] = 2;
-            }
-        }
-        __syncthreads();
-        const TileJob J = jobs[S.job];
+        const TileJob J = jobs[find_job(jobs, njobs, tile)];
+        const uint2 bd = bounds[tile];
         const uint64_t t = tile - J.tile0;
         const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
         const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
         const uint32_t base = PQ[J.sa];
         SegMergeOut out{S.outk, S.outv};
-        for (uint32_t s = S.sbeg + w; s < S.send; s += TPB / 32) {
+        for (uint32_t s = bd.x + w; s < bd.y; s += TPB / 32) {
             const uint64_t j = heap_of_linear(s, src.H);
             merge_segment(src.keys, src.vals, j, srcc[s], US[s], US[s + 1], PQ[s] - base, R0, R1, u, thres, S.kk[w],
                           out);
@@ -765,15 +1009,7 @@ __global__ void __launch_bounds__(TPB) k_copy_segments(const TileJob *__restrict
                                                        Geo from, Geo to) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        uint32_t L = 0, R = njobs - 1;
-        while (L < R) {
-            uint32_t mid = (L + R + 1) >> 1;
-            if (jobs[mid].tile0 <= tile)
-                L = mid;
-            else
-                R = mid - 1;
-        }
-        const TileJob J = jobs[L];
+        const TileJob J = jobs[find_job(jobs, njobs, tile)];
         const uint64_t t = tile - J.tile0;
         const uint64_t k1 = umin64(32 * t + 32, J.df);
         for (uint64_t k = 32 * t + w; k < k1; k += TPB / 32) {
@@ -817,6 +1053,7 @@ inline uint32_t grid_for(uint64_t n, uint32_t per_block, uint32_t cap = 152 * 16
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
                  DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("pack", s);
     k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
                                                         keys_out, pay_out, st);
     note_launch();
@@ -824,6 +1061,7 @@ void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, c
 
 void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_t *cnt_live, DevStatus *st,
                         cudaStream_t s) {
+    ProfScope ps_("live_counts", s);
     k_live_counts<<<grid_for(nseg_of(H), TPB / 32), TPB, 0, s>>>(keys, H, thres, cnt_live, st);
     note_launch();
 }
@@ -831,6 +1069,7 @@ void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_
 void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t n, Geo g, const ulonglong2 *fl,
                            uint32_t thres, uint8_t *kind, uint32_t *seg, uint32_t *blk_nn, uint32_t *blk_ins,
                            DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("resolve_locate", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
     k_resolve_locate<<<nb, TPB, 0, s>>>(skey, spay, n, g, fl, thres, kind, seg, blk_nn, blk_ins, st);
     note_launch();
@@ -838,6 +1077,7 @@ void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t 
 
 void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *kind, const uint32_t *seg, uint32_t n,
                     uint32_t *blk_nn, uint32_t *blk_ins, UpdList u, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("compact", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
     k_scan_pairs<<<1, 1024, 0, s>>>(blk_nn, blk_ins, nb, u.ip, st);
     k_compact<<<nb, TPB, 0, s>>>(skey, spay, kind, seg, n, blk_nn, blk_ins, u);
@@ -845,6 +1085,7 @@ void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *k
 }
 
 void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s) {
+    ProfScope ps_("relocate", s);
     if (!n) return;
     k_relocate<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(u, n, g, fl);
     note_launch();
@@ -852,6 +1093,7 @@ void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStr
 
 void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, UpdList out, uint32_t *blk_nn,
                             uint32_t *blk_ins, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("compact_pending", s);
     // n = old compacted count (known on the host at this point)
     const uint32_t nb = (n + TPB - 1) / TPB;
     if (!nb) return;
@@ -862,27 +1104,35 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 }
 
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
-                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *small,
-                 Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
+                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *single,
+                 Window *small, Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
     k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, H, tb, bitmap, cand, seg_e, pend, st);
-    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, small, big, st);
+    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, single, small, big, st);
     note_launch(2);
 }
 
-void launch_exec_small(const Window *w, uint32_t n_small, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
-                       uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
-    if (!n_small) return;
-    const size_t sm = sizeof(ExSmallSmem);
-    cudaFuncSetAttribute(k_exec_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_exec_small<<<grid_for(n_small, EXS_WARPS, 152 * 8), EXS_WARPS * 32, sm, s>>>(w, n_small, g, cnt, fl, sent, V, u,
-                                                                                   thres, st);
+void launch_exec_small(const Window *w, uint32_t n_cap, int single, Geo g, uint8_t *cnt, ulonglong2 *fl,
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_(single ? "exec_single" : "exec_small", s);
+    if (!n_cap) return;
+    if (single) {
+        k_exec_single<<<grid_for(n_cap, ES_GROUPS, 152 * 8), ES_TPB, 0, s>>>(w, &st->n_single, n_cap, g, cnt, fl, sent,
+                                                                         V, u, thres, st);
+    } else {
+        const size_t sm = sizeof(ExSmallSmem<1024>);
+        cudaFuncSetAttribute(k_exec_small<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_exec_small<1024><<<grid_for(n_cap, EXS_WARPS, 152 * 8), EXS_WARPS * 32, sm, s>>>(
+            w, &st->n_small, n_cap, g, cnt, fl, sent, V, u, thres, st);
+    }
     note_launch();
 }
 
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
                               cudaStream_t s) {
+    ProfScope ps_("seg_counts", s);
     if (!n_cap) return;
     k_seg_update_counts<<<(n_cap + TPB - 1) / TPB, TPB, 0, s>>>(u, n_cap, qi, qd, st);
     note_launch();
@@ -890,38 +1140,46 @@ void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uin
 
 void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
                   uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s) {
+    ProfScope ps_("seg_q", s);
     k_seg_q<<<grid_for(nseg, TPB), TPB, 0, s>>>(cnt, cnt_live, qi, qd, nseg, q, qn, srcc);
     note_launch();
 }
 
-void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo src, const uint8_t *srcc,
-                       const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
+void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, uint2 *bounds, Geo src,
+                       const uint8_t *srcc, const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d,
+                       ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
+                       cudaStream_t s) {
+    ProfScope ps_("exec_tiles", s);
     if (!ntiles) return;
+    k_tile_bounds<<<(ntiles + TPB - 1) / TPB, TPB, 0, s>>>(jobs, njobs, ntiles, PQ, bounds, st);
     const size_t sm = sizeof(TileSmem);
     cudaFuncSetAttribute(k_exec_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_exec_tiles<<<grid_for(ntiles, 1, 152 * 8), TPB, sm, s>>>(jobs, njobs, ntiles, src, srcc, PQ, US, dst, cnt_d, fl_d,
-                                                               sent, V, u, thres, st);
-    note_launch();
+    k_exec_tiles<<<grid_for(ntiles, 1, 152 * 8), TPB, sm, s>>>(jobs, njobs, ntiles, bounds, src, srcc, PQ, US, dst,
+                                                               cnt_d, fl_d, sent, V, u, thres);
+    note_launch(2);
 }
 
 void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to, cudaStream_t s) {
+    ProfScope ps_("copy_segments", s);
     if (!ntiles) return;
     k_copy_segments<<<grid_for(ntiles, 1, 152 * 8), TPB, 0, s>>>(jobs, njobs, ntiles, from, to);
     note_launch();
 }
 
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s) {
+    ProfScope ps_("levelup_cnt", s);
     k_levelup_cnt<<<grid_for(nseg_of(H_old + 1) + 64, TPB), TPB, 0, s>>>(cnt_old, cnt_new, H_old);
     note_launch();
 }
 
 void launch_check_empty_level(const uint8_t *cnt, uint32_t H, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("check_empty", s);
     k_check_empty_level<<<grid_for(nseg_of(H) / 4 + 1, TPB), TPB, 0, s>>>(cnt, H, st);
     note_launch();
 }
 
 void launch_sum_cnt(const uint8_t *cnt, uint64_t nseg, DevStatus *st, cudaStream_t s) {
+    ProfScope ps_("sum_cnt", s);
     k_sum_cnt<<<grid_for(nseg, TPB), TPB, 0, s>>>(cnt, nseg, st);
     note_launch();
 }

@@ -98,18 +98,21 @@ inline uint32_t grid_for(uint64_t n, uint32_t per_block, uint32_t cap = 152 * 16
 
 void launch_csr_fill(Geo g, const uint8_t *cnt, const uint32_t *P, uint32_t *row_offset, uint32_t *col_index,
                      uint8_t *values, uint64_t *export_keys, uint8_t *export_vals, cudaStream_t s) {
+    ProfScope ps_("csr_fill", s);
     k_csr_fill<<<grid_for(nseg_of(g.H), TPB / 32), TPB, 0, s>>>(g, cnt, P, row_offset, col_index, values, export_keys,
                                                                 export_vals);
     note_launch();
 }
 
 void launch_sentinels(uint32_t V, uint64_t *keys, uint8_t *vals, cudaStream_t s) {
+    ProfScope ps_("sentinels", s);
     k_sentinels<<<grid_for(V, TPB), TPB, 0, s>>>(V, keys, vals);
     note_launch();
 }
 
 void launch_rmat(uint64_t seed, uint32_t scale, uint64_t n, uint32_t ta, uint32_t tab, uint32_t tabc, uint64_t *out,
                  cudaStream_t s) {
+    ProfScope ps_("gen_rmat", s);
     uint64_t s0 = seed;
     // same seeding as the CPU generator: s0 = mix64(seed)
     s0 += 0x9E3779B97F4A7C15ull;
@@ -121,17 +124,20 @@ void launch_rmat(uint64_t seed, uint32_t scale, uint64_t n, uint32_t ta, uint32_
 }
 
 void launch_hash_keys(uint64_t seed, const uint64_t *keys, uint64_t *hash, uint64_t n, cudaStream_t s) {
+    ProfScope ps_("hash_keys", s);
     k_hash_keys<<<grid_for(n, TPB), TPB, 0, s>>>(seed, keys, hash, n);
     note_launch();
 }
 
 void launch_unique_flags(const uint64_t *keys, uint64_t n, uint32_t *flags, cudaStream_t s) {
+    ProfScope ps_("unique_flags", s);
     k_unique_flags<<<grid_for(n, TPB), TPB, 0, s>>>(keys, n, flags);
     note_launch();
 }
 
 void launch_scatter_flags(const uint64_t *keys, const uint32_t *pos, const uint32_t *flags, uint64_t n, uint64_t *out,
                           cudaStream_t s) {
+    ProfScope ps_("scatter_flags", s);
     k_scatter_flags<<<grid_for(n, TPB), TPB, 0, s>>>(keys, pos, flags, n, out);
     note_launch();
 }

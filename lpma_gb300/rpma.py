@@ -228,5 +228,22 @@ def kernel_launches():
     return _abi.load().lpma_kernel_launches()
 
 
+def profile_enable(on=True):
+    _abi.load().lpma_prof_enable(1 if on else 0)
+
+
+def profile_report():
+    """{kernel name: (launches, total ms)} since the last report (synchronises)."""
+    L = _abi.load()
+    buf = ctypes.create_string_buffer(1 << 16)
+    L.lpma_prof_report(buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out
+
+
 __all__ = ["Lpma", "LpmaError", "default_config", "init_csr_rpma", "update_rpma", "to_csr_rpma", "get_data_rpma",
-           "destroy_rpma", "pack_key", "sentinel_key", "gen_rmat_device", "shuffle_device", "kernel_launches"]
+           "destroy_rpma", "pack_key", "sentinel_key", "gen_rmat_device", "shuffle_device", "kernel_launches",
+           "profile_enable", "profile_report"]
