@@ -267,15 +267,21 @@ def roofline(res, B, peak, peak_kind):
     cnt, ms = prof[name]
     pst = res["pstats"]
     # algorithmic bytes per launch of the dominant kernel
-    if name == "exec_small":
-        units = sum(s["slots_small"] for s in pst) / cnt
+    if name == "exec_single":
+        units = sum(32 * s["windows_single"] for s in pst) / cnt
+        per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
+    elif name == "exec_small":
+        units = sum(s["slots_small"] - 32 * s["windows_single"] for s in pst) / cnt
         per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
     elif name == "exec_tiles":
         units = sum(s["slots_rewritten"] - s["slots_small"] for s in pst) / cnt
         per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
-    elif name == "sort_pass":
+    elif name in ("sort_pass", "sort_downsweep"):
         units = B
         per_unit, unit_name = 20, "key (8 B key + 2 B payload, read and written)"
+    elif name == "sort_upsweep":
+        units = B
+        per_unit, unit_name = 8, "key (8 B read)"
     elif name == "resolve_locate":
         units = B
         per_unit, unit_name = 15, "key (8 B key + 2 B payload read, 1 B kind + 4 B segment written)"

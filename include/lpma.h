@@ -72,7 +72,8 @@ typedef struct {
     uint32_t rebuilt;          /* full rebuild at a new height */
     uint32_t levelup_path;     /* overflow absorbed by adding one level */
     uint32_t fill_empty;       /* an empty segment forced a full redistribution */
-    uint64_t windows_small;    /* rebalance windows of <= 32 segments executed */
+    uint64_t windows_single;   /* single-segment rebalance windows executed */
+    uint64_t windows_small;    /* rebalance windows of <= 32 segments executed (incl. single) */
     uint64_t windows_big;      /* larger windows (tile grain) executed */
     uint64_t slots_rewritten;  /* slots covered by executed windows (incl. rebuild) */
     uint64_t slots_small;      /* of which in windows of <= 32 segments */

@@ -39,7 +39,8 @@ class LpmaStats(ctypes.Structure):
                 ("root_executed", ctypes.c_uint32), ("eager_levelup", ctypes.c_uint32),
                 ("overflow", ctypes.c_uint32), ("rebuilt", ctypes.c_uint32),
                 ("levelup_path", ctypes.c_uint32), ("fill_empty", ctypes.c_uint32),
-                ("windows_small", ctypes.c_uint64), ("windows_big", ctypes.c_uint64),
+                ("windows_single", ctypes.c_uint64), ("windows_small", ctypes.c_uint64),
+                ("windows_big", ctypes.c_uint64),
                 ("slots_rewritten", ctypes.c_uint64), ("slots_small", ctypes.c_uint64),
                 ("num_items", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]

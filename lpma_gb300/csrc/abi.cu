@@ -290,6 +290,7 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
     Geo g{h->c.keys, h->c.vals, h->H};
     launch_exec_small(h->wsingle, n_single, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
     launch_exec_small(h->wsmall, n_small, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    st->windows_single += n_single;
     st->windows_small += n_single + n_small;
     st->slots_rewritten += h->hst->slots_small;
     st->slots_small += h->hst->slots_small;

@@ -1,14 +1,13 @@
 // Radix sort and scan primitives (hand-written, sm_103a).
 //
-// Sort: LSD radix sort on 8-bit digits in the single-pass "onesweep" form
-// (Adinets & Merrill, 2022): one histogram kernel for every digit, then one
-// kernel per digit pass.  Each CTA takes a 4096-key tile in dynamic order,
-// ranks the keys of each warp with __match_any_sync, publishes its per-digit
-// tile count and resolves its global offset by decoupled look-back over the
-// tiles before it.  Every look-back wait is bounded: when a predecessor does
-// not publish within the bound, the kernel sets ERR_TIMEOUT and returns.
-// Batches of at most one tile are sorted by one CTA entirely in shared
-// memory in a single launch.
+// Sort: LSD radix sort on 8-bit digits, reduce-then-scan per digit pass:
+// k_upsweep counts the digits of every 2048-key tile, k_dscan turns the
+// (digit, tile) counts into exclusive global offsets (digit-major, one warp
+// per digit, digit bases from a histogram of all eight digits taken once
+// per sort), k_downsweep ranks each tile's keys stably with
+// __match_any_sync and scatters them.  No CTA waits on another.  Bytes that
+// are equal across all keys are skipped.  Batches of at most one tile are
+// sorted by one CTA in shared memory in a single launch.
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -106,18 +105,6 @@ size_t prof_report(char *buf, size_t cap) {
 
 namespace {
 
-constexpr uint32_t FLAG_AGG = 1u << 30, FLAG_PREFIX = 2u << 30, VAL_MASK = (1u << 30) - 1;
-constexpr uint32_t SPIN_LIMIT = 1u << 24;
-
-__device__ inline uint32_t ld_acquire(const uint32_t *p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ inline void st_release(uint32_t *p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // Block-wide exclusive scan of one value per thread (blockDim == 256).
 __device__ inline uint32_t block_excl_scan_256(uint32_t x, uint32_t *wsum /*[8]*/, uint32_t *total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -175,7 +162,7 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys,
     for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
-        uint64_t k = keys[i];
+        const uint64_t k = keys[i];
 #pragma unroll
         for (int b = 0; b < 8; b++) atomicAdd(&h[b][(k >> (8 * b)) & 0xFF], 1u);
     }
@@ -187,6 +174,47 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys,
 }
 
 // ---------------------------------------------------------------- one pass
+__global__ void __launch_bounds__(SORT_TPB) k_upsweep(const uint64_t *__restrict__ keys, uint32_t n, int sh,
+                                                      uint32_t *counts, uint32_t T) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+#pragma unroll
+    for (int i = 0; i < SORT_IPT; i++) {
+        const uint64_t p = base + (uint64_t)i * SORT_TPB + threadIdx.x;
+        if (p < n) atomicAdd(&h[(keys[p] >> sh) & 0xFF], 1u);
+    }
+    __syncthreads();
+    counts[(size_t)threadIdx.x * T + blockIdx.x] = h[threadIdx.x];
+}
+
+// one warp per digit: offs[d][t] = base(d) + sum of counts[d][t' < t]
+__global__ void __launch_bounds__(256) k_dscan(const uint32_t *__restrict__ counts, uint32_t T,
+                                               const uint32_t *__restrict__ hist, uint32_t *offs) {
+    __shared__ uint32_t gd[256];
+    __shared__ uint32_t wsum[8];
+    gd[threadIdx.x] = block_excl_scan_256(hist[threadIdx.x], wsum, nullptr);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint32_t d = blockIdx.x * 8 + (threadIdx.x >> 5);
+    uint32_t run = gd[d];
+    const uint32_t *c = counts + (size_t)d * T;
+    uint32_t *o = offs + (size_t)d * T;
+    for (uint32_t t0 = 0; t0 < T; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        const uint32_t x = t < T ? c[t] : 0;
+        uint32_t v = x;
+#pragma unroll
+        for (int k = 1; k < 32; k <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, k);
+            if (lane >= k) v += y;
+        }
+        if (t < T) o[t] = run + v - x;
+        run += __shfl_sync(0xffffffffu, v, 31);
+    }
+}
+
 template <typename V>
 struct PassSmem {
     uint64_t k[SORT_TILE];
@@ -195,32 +223,26 @@ struct PassSmem {
     uint32_t gbase[256];
     uint32_t ldig[256];
     uint32_t wsum[8];
-    uint32_t tile;
 };
 
 template <typename V>
-__global__ void __launch_bounds__(SORT_TPB) k_pass(const uint64_t *__restrict__ ki, const V *__restrict__ vi,
-                                                   uint64_t *__restrict__ ko, V *__restrict__ vo, uint32_t n,
-                                                   int byte, const uint32_t *__restrict__ hist,
-                                                   uint32_t *status, uint32_t *counter, uint32_t *err) {
+__global__ void __launch_bounds__(SORT_TPB) k_downsweep(const uint64_t *__restrict__ ki, const V *__restrict__ vi,
+                                                        uint64_t *__restrict__ ko, V *__restrict__ vo, uint32_t n,
+                                                        int sh, const uint32_t *__restrict__ offs, uint32_t T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem<V> &S = *reinterpret_cast<PassSmem<V> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int sh = byte * 8;
-    if (tid == 0) S.tile = atomicAdd(counter, 1u);
+    const uint32_t tile = blockIdx.x;
     for (int i = tid; i < 8 * 256; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
-    // global exclusive digit offsets for this pass
-    uint32_t gtotal;
-    uint32_t gdig = block_excl_scan_256(hist[byte * 256 + tid], S.wsum, &gtotal);
+    S.gbase[tid] = offs[(size_t)tid * T + tile];
     __syncthreads();
-    const uint32_t tile = S.tile;
     const uint64_t base = (uint64_t)tile * SORT_TILE;
     uint64_t k[SORT_IPT];
     V v[SORT_IPT];
     uint32_t vmask = 0;
 #pragma unroll
     for (int i = 0; i < SORT_IPT; i++) {
-        uint64_t p = base + (uint64_t)w * 32 * SORT_IPT + i * 32 + lane;
+        const uint64_t p = base + (uint64_t)w * 32 * SORT_IPT + i * 32 + lane;
         if (p < n) {
             k[i] = ki[p];
             v[i] = vi[p];
@@ -237,56 +259,17 @@ __global__ void __launch_bounds__(SORT_TPB) k_pass(const uint64_t *__restrict__ 
     uint32_t tcount = 0;
 #pragma unroll
     for (int ww = 0; ww < 8; ww++) {
-        uint32_t c = S.whist[ww][tid];
+        const uint32_t c = S.whist[ww][tid];
         S.whist[ww][tid] = tcount;
         tcount += c;
     }
-    // decoupled look-back for the exclusive prefix of this digit over tiles
-    uint32_t *my = status + (size_t)tile * 256 + tid;
-    uint32_t excl = 0;
-    if (tile == 0) {
-        st_release(my, FLAG_PREFIX | tcount);
-    } else {
-        st_release(my, FLAG_AGG | tcount);
-        // look back over the predecessors LB at a time (independent loads in
-        // flight): every tile is resident at once, so chains of AGG entries
-        // are long unless they are read in parallel
-        constexpr int LB = 16;
-        int64_t p = (int64_t)tile - 1;
-        uint32_t spins = 0;
-        bool done = false;
-        while (p >= 0 && !done) {
-            uint32_t s[LB];
-#pragma unroll
-            for (int k = 0; k < LB; k++) s[k] = p - k >= 0 ? ld_acquire(status + (size_t)(p - k) * 256 + tid) : FLAG_PREFIX;
-            int k = 0;
-            for (; k < LB; k++) {
-                const uint32_t f = s[k] & ~VAL_MASK;
-                if (f == 0) break;  // not published yet: poll again from here
-                excl += s[k] & VAL_MASK;
-                if (f == FLAG_PREFIX) {
-                    done = true;
-                    break;
-                }
-            }
-            if (done) break;
-            p -= k;
-            if (k < LB && ++spins > SPIN_LIMIT) {
-                atomicOr(err, ERR_TIMEOUT);
-                break;
-            }
-        }
-        st_release(my, FLAG_PREFIX | (excl + tcount));
-    }
-    S.gbase[tid] = gdig + excl;
-    uint32_t ldig = block_excl_scan_256(tcount, S.wsum, nullptr);
-    S.ldig[tid] = ldig;
+    S.ldig[tid] = block_excl_scan_256(tcount, S.wsum, nullptr);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < SORT_IPT; i++) {
         if ((vmask >> i) & 1u) {
-            uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
-            uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+            const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+            const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
             S.k[pos] = k[i];
             S.v[pos] = v[i];
         }
@@ -294,13 +277,11 @@ __global__ void __launch_bounds__(SORT_TPB) k_pass(const uint64_t *__restrict__ 
     __syncthreads();
     const uint32_t nvalid = (uint32_t)umin64(SORT_TILE, n - base);
     for (uint32_t p = tid; p < nvalid; p += SORT_TPB) {
-        uint64_t kk = S.k[p];
-        uint32_t d = (uint32_t)((kk >> sh) & 0xFF);
-        uint32_t g = S.gbase[d] + (p - S.ldig[d]);
-        if (g < n) {  // only false after a timed-out look-back (error already set)
-            ko[g] = kk;
-            vo[g] = S.v[p];
-        }
+        const uint64_t kk = S.k[p];
+        const uint32_t d = (uint32_t)((kk >> sh) & 0xFF);
+        const uint32_t g = S.gbase[d] + (p - S.ldig[d]);
+        ko[g] = kk;
+        vo[g] = S.v[p];
     }
 }
 
@@ -503,29 +484,36 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
         note_launch();
         return cudaGetLastError();
     }
-    uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
-    if (s.status_words < (size_t)tiles * 256) return cudaErrorInvalidValue;
+    const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    if (s.status_words < 2 * (size_t)tiles * 256) return cudaErrorInvalidValue;
+    uint32_t *counts = s.status, *offs = s.status + (size_t)tiles * 256;
     if ((e = cudaMemsetAsync(s.hist, 0, 8 * 256 * sizeof(uint32_t), st))) return e;
-    if ((e = cudaMemsetAsync(s.counters, 0, 8 * sizeof(uint32_t), st))) return e;
-    uint32_t hb = tiles < 1024 ? tiles : 1024;
+    const uint32_t hb = tiles < 1024 ? tiles : 1024;
     {
         ProfScope ps("sort_hist", st);
         k_hist<<<hb, 256, 0, st>>>(k0, n, s.hist);
     }
     note_launch();
-    size_t sm = sizeof(PassSmem<V>);
-    if ((e = cudaFuncSetAttribute(k_pass<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm))) return e;
+    const size_t sm = sizeof(PassSmem<V>);
+    if ((e = cudaFuncSetAttribute(k_downsweep<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm))) return e;
     uint64_t *ka = k0, *kb = k1;
     V *va = v0, *vb = v1;
     int cur = 0;
     for (int b = 0; b < 8; b++) {
         if (!((byte_mask >> b) & 1u)) continue;
-        if ((e = cudaMemsetAsync(s.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), st))) return e;
         {
-            ProfScope ps("sort_pass", st);
-            k_pass<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, b, s.hist, s.status, s.counters + b, err);
+            ProfScope ps("sort_upsweep", st);
+            k_upsweep<<<tiles, SORT_TPB, 0, st>>>(ka, n, 8 * b, counts, tiles);
         }
-        note_launch();
+        {
+            ProfScope ps("sort_dscan", st);
+            k_dscan<<<32, 256, 0, st>>>(counts, tiles, s.hist + 256 * b, offs);
+        }
+        {
+            ProfScope ps("sort_downsweep", st);
+            k_downsweep<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, 8 * b, offs, tiles);
+        }
+        note_launch(3);
         uint64_t *tk = ka; ka = kb; kb = tk;
         V *tv = va; va = vb; vb = tv;
         cur ^= 1;

@@ -7,20 +7,20 @@
 namespace lpma {
 
 constexpr int SORT_TPB = 256;
-constexpr int SORT_IPT = 16;
-constexpr int SORT_TILE = SORT_TPB * SORT_IPT;  // 4096 keys per tile
+constexpr int SORT_IPT = 8;
+constexpr int SORT_TILE = SORT_TPB * SORT_IPT;  // 2048 keys per tile
 
 struct SortScratch {
     uint32_t *hist = nullptr;      // 8 x 256 global digit counts
-    uint32_t *status = nullptr;    // tiles x 256 look-back words
-    uint32_t *counters = nullptr;  // 8 dynamic tile counters + error word
+    uint32_t *status = nullptr;    // (digit, tile) counts and offsets of one pass
+    uint32_t *counters = nullptr;  // unused by the reduce-then-scan passes
     size_t status_words = 0;
 };
 
 // Sorts n pairs by key (stable).  Only the bytes set in diff_bits are sorted
 // (bytes equal across all keys need no pass).  The result lands either in
-// (k0, v0) or in (k1, v1); *which receives 0 or 1.  err (device word, may be
-// null) gets ERR_TIMEOUT if a look-back wait gave up.
+// (k0, v0) or in (k1, v1); *which receives 0 or 1.  err is kept for the
+// interface (no kernel of the sort waits on another CTA).
 template <typename V>
 cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits,
                        SortScratch &s, uint32_t *err, cudaStream_t st, int *which);
@@ -28,7 +28,7 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
 // Bytes of scratch status words needed for n keys.
 inline size_t sort_status_words(uint32_t n) {
     size_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
-    return tiles * 256 + 1;
+    return 2 * tiles * 256 + 2;  // per-pass (digit, tile) counts and offsets
 }
 
 // Exclusive scan of n u32 values; out may alias in.  total (device, may be

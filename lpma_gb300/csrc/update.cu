@@ -214,60 +214,66 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
                                                         const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
                                                         uint32_t *blk_ins, DevStatus *st) {
+    // persistent grid: the top TOPL levels are staged once per CTA and the
+    // CTA walks 256-entry chunks; chunk c writes its counts to blk_*[c]
     __shared__ ulonglong2 top[TOPN];
     const uint32_t H = g.H;
     const uint32_t ntop = (uint32_t)umin64(nseg_of(H), TOPN);
     for (uint32_t t = threadIdx.x; t < ntop; t += TPB) top[t] = fl[t];
     __syncthreads();
-    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
-    uint32_t kd = KIND_NOP, sg = 0, ups = 0, noop = 0;
-    if (i < n) {
-        const uint64_t key = skey[i];
-        const uint16_t p = spay[i];
-        const bool is_del = (p >> 8) & 1;
-        bool rep;
-        if (is_del)
-            rep = (i == 0 || skey[i - 1] != key);
-        else
-            rep = (i + 1 == n || skey[i + 1] != key || ((spay[i + 1] >> 8) & 1));
-        if (rep) {
-            uint32_t lvl;
-            uint64_t j = descend(key, top, ntop, fl, H, &lvl);
-            sg = (uint32_t)linear_of_heap(j, lvl, H);
-            // membership: the stop segment is sorted, NONE-padded (left packed)
-            const uint64_t *sk = g.keys + 32 * j;
-            uint32_t pos = 0;
+    const uint32_t nchunks = (n + TPB - 1) / TPB;
+    uint32_t ups = 0, noop = 0;
+    for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+        const uint32_t i = chunk * TPB + threadIdx.x;
+        uint32_t kd = KIND_NOP, sg = 0;
+        if (i < n) {
+            const uint64_t key = skey[i];
+            const uint16_t p = spay[i];
+            const bool is_del = (p >> 8) & 1;
+            bool rep;
+            if (is_del)
+                rep = (i == 0 || skey[i - 1] != key);
+            else
+                rep = (i + 1 == n || skey[i + 1] != key || ((spay[i + 1] >> 8) & 1));
+            if (rep) {
+                uint32_t lvl;
+                const uint64_t j = descend(key, top, ntop, fl, H, &lvl);
+                sg = (uint32_t)linear_of_heap(j, lvl, H);
+                // membership: the stop segment is sorted, NONE-padded (left packed)
+                const uint64_t *sk = g.keys + 32 * j;
+                uint32_t pos = 0;
 #pragma unroll
-            for (uint32_t step = 16; step; step >>= 1)
-                if (sk[pos + step - 1] < key) pos += step;
-            const bool found = sk[pos] == key;
-            const uint64_t slot = 32 * j + pos;
-            if (!is_del) {
-                if (found) {
-                    g.vals[slot] = (uint8_t)(p & 0xFF);  // upsert (handle_del_mod, gpma.cuh:162-175)
-                    ups = 1;
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (sk[pos + step - 1] < key) pos += step;
+                const bool found = sk[pos] == key;
+                const uint64_t slot = 32 * j + pos;
+                if (!is_del) {
+                    if (found) {
+                        g.vals[slot] = (uint8_t)(p & 0xFF);  // upsert (handle_del_mod, gpma.cuh:162-175)
+                        ups++;
+                    } else {
+                        kd = KIND_INS;
+                    }
                 } else {
-                    kd = KIND_INS;
+                    if (found && (key & TIME_MASK) >= (uint64_t)thres) {
+                        g.vals[slot] = VAL_TOMB;  // tombstone until its window executes
+                        kd = KIND_DEL;
+                    } else {
+                        noop++;
+                    }
                 }
             } else {
-                if (found && (key & TIME_MASK) >= (uint64_t)thres) {
-                    g.vals[slot] = VAL_TOMB;  // tombstone until its window executes
-                    kd = KIND_DEL;
-                } else {
-                    noop = 1;
-                }
+                noop++;
             }
-        } else {
-            noop = 1;
+            kind[i] = (uint8_t)kd;
+            seg[i] = sg;
         }
-        kind[i] = (uint8_t)kd;
-        seg[i] = sg;
-    }
-    uint32_t c_nn = __syncthreads_count(kd != KIND_NOP);
-    uint32_t c_ins = __syncthreads_count(kd == KIND_INS);
-    if (threadIdx.x == 0) {
-        blk_nn[blockIdx.x] = c_nn;
-        blk_ins[blockIdx.x] = c_ins;
+        const uint32_t c_nn = __syncthreads_count(kd != KIND_NOP);
+        const uint32_t c_ins = __syncthreads_count(kd == KIND_INS);
+        if (threadIdx.x == 0) {
+            blk_nn[chunk] = c_nn;
+            blk_ins[chunk] = c_ins;
+        }
     }
     ups = warp_sum(ups);
     noop = warp_sum(noop);
@@ -492,9 +498,19 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
     }
     const int any_ovf = __syncthreads_or(lead && e == EXEC_OVF);
     const int any_root = __syncthreads_or(lead && e == H + 1);
+    // levels with an executed window, for the maximality test
+    uint32_t lv = (lead && e != EXEC_OVF) ? 1u << e : 0u;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) lv |= __shfl_xor_sync(0xffffffffu, lv, o);
+    __shared__ uint32_t s_lv;
+    if (threadIdx.x == 0) s_lv = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && lv) atomicOr(&s_lv, lv);
+    __syncthreads();
     if (threadIdx.x == 0) {
         if (any_ovf) atomicOr(&st->ovf, 1u);
         if (any_root) atomicOr(&st->root, 1u);
+        if (s_lv) atomicOr(&st->exec_levels, s_lv);
     }
     // block-aggregated append of the windows this block owns
     const uint32_t ex = block_excl_scan(own ? 1u : 0u, wsum);
@@ -517,13 +533,17 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
     if (c < st->n_cand && c < n_cap) {
         w = cand[c];
         cls = w.f == 1 ? 0 : (w.f <= SMALL_WIN_SEGS ? 1 : 2);
+        // inside a larger executed window?  The ancestor words are loaded
+        // without an early exit so that the loads are in flight together.
+        uint32_t hit = 0;
+        const uint32_t lv = st->exec_levels;
+#pragma unroll 4
         for (uint32_t l = w.level + 1; l <= H + 1; l++) {
+            if (!((lv >> l) & 1u)) continue;  // no window of that level executes
             const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
-            if ((bitmap[bit >> 5] >> (bit & 31)) & 1u) {  // inside a larger executed window
-                cls = 3;
-                break;
-            }
+            hit |= (bitmap[bit >> 5] >> (bit & 31)) & 1u;
         }
+        if (hit) cls = 3;
     }
     const uint32_t packed = cls < 3 ? 1u << (10 * cls) : 0u;
     const uint32_t ex = block_excl_scan(packed, wsum);
@@ -754,40 +774,59 @@ __global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__r
 // The level-0 windows (one segment, about 94% of the executed windows) get a
 // group of 8 lanes each, so a warp keeps 4 windows in flight.  Lane gl of a
 // group moves slots 4gl..4gl+3 with two 16-byte key loads/stores and one
-// 4-byte value load/store.  Merged ranks come from group shuffles; the
-// re-packed segment is staged in 288 bytes of shared memory per group.
+// 4-byte value load/store.  Merged ranks come from binary searches over the
+// window's kept keys and insert keys staged in shared memory; the re-packed
+// segment is staged there too (800 bytes per group).
 constexpr int ES_TPB = 256;
 constexpr int ES_GROUPS = ES_TPB / 8;
 
-__global__ void __launch_bounds__(ES_TPB) k_exec_single(const Window *__restrict__ wins,
+__global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restrict__ wins,
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
                                                         const UpdList u, uint32_t thres, DevStatus *st) {
     __shared__ __align__(16) uint64_t sk[ES_GROUPS][32];
     __shared__ __align__(16) uint8_t sv[ES_GROUPS][32];
+    __shared__ uint64_t kk[ES_GROUPS][32];  // kept keys of the window, compacted
+    __shared__ uint64_t ik[ES_GROUPS][32];  // insert keys of the window
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
-    for (uint32_t wi = blockIdx.x * ES_GROUPS + grp; __any_sync(0xffffffffu, wi < nwin); wi += gridDim.x * ES_GROUPS) {
+    const uint32_t stride = gridDim.x * ES_GROUPS;
+    // software pipeline: the next window's record, segment slots and update
+    // bounds are loaded while the current one is merged
+    uint32_t wi = blockIdx.x * ES_GROUPS + grp;
+    Window Wn{};
+    ulonglong2 na = make_ulonglong2(KEY_NONE, KEY_NONE), nb = na;
+    uint32_t nv4 = 0, nip0 = 0, nip1 = 0;
+    if (wi < nwin) {
+        Wn = wins[wi];
+        const uint64_t jn = heap_of_linear(Wn.a, g.H);
+        const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
+        na = kp[0], nb = kp[1];
+        nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
+        nip0 = u.ip[Wn.lo], nip1 = u.ip[Wn.hi];
+    }
+    for (; __any_sync(0xffffffffu, wi < nwin); wi += stride) {
         const bool active = wi < nwin;
-        Window W{};
-        if (active) W = wins[wi];
+        const Window W = Wn;
+        const ulonglong2 a = na, b = nb;
+        const uint32_t v4 = nv4, ip0c = nip0, ip1c = nip1;
+        if (wi + stride < nwin) {
+            Wn = wins[wi + stride];
+            const uint64_t jn = heap_of_linear(Wn.a, g.H);
+            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
+            na = kp[0], nb = kp[1];
+            nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
+            nip0 = u.ip[Wn.lo], nip1 = u.ip[Wn.hi];
+        }
         const uint64_t j = active ? heap_of_linear(W.a, g.H) : 0;
         uint64_t k[4];
         uint8_t v[4];
         uint32_t kmask = 0;
-        if (active) {
-            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
-            const ulonglong2 a = kp[0], b = kp[1];
-            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
-            k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+        k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                v[q] = (uint8_t)(v4 >> (8 * q));
-                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < 4; q++) k[q] = KEY_NONE, v[q] = 0;
+        for (int q = 0; q < 4; q++) {
+            v[q] = (uint8_t)(v4 >> (8 * q));
+            if (active && kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
         }
         // exclusive prefix of kept counts across the group
         const uint32_t nl = __popc(kmask);
@@ -799,54 +838,51 @@ __global__ void __launch_bounds__(ES_TPB) k_exec_single(const Window *__restrict
         }
         const uint32_t kbase = incl - nl;
         const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
-        // updates of the window, 8 per round
+        // kept keys, compacted and sorted, for the insert ranks
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if ((kmask >> q) & 1u) kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
+        __syncwarp();
+        // updates of the window, 8 per round (usually one round): an insert's
+        // rank is (inserts before it) + (kept keys below it)
         const uint32_t lo = W.lo, hi = active ? W.hi : W.lo;
-        const uint32_t ip0 = active ? u.ip[lo] : 0;
-        const uint32_t nins = active ? u.ip[hi] - ip0 : 0;
-        uint32_t ins_less[4] = {0, 0, 0, 0};
+        const uint32_t ip0 = active ? ip0c : 0;
+        const uint32_t nins = active ? ip1c - ip0 : 0;
         const uint32_t rounds = __reduce_max_sync(0xffffffffu, (hi - lo + 7) / 8);
         for (uint32_t r = 0; r < rounds; r++) {
             const uint32_t x = lo + 8 * r + gl;
-            const bool has = x < hi;
-            uint64_t yk = KEY_NONE;
-            bool yins = false;
-            uint8_t yv = 0;
-            uint32_t yip = 0;
-            if (has) {
-                yk = u.key[x];
-                yins = u.kind[x] == KIND_INS;
-                yv = u.val[x];
-                yip = u.ip[x];
-            }
-            uint32_t my_below = 0;
-#pragma unroll
-            for (int t = 0; t < 8; t++) {
-                const uint64_t bk = __shfl_sync(0xffffffffu, yk, t, 8);
-                const bool bins = __shfl_sync(0xffffffffu, yins, t, 8);
-                uint32_t below = 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const bool kq = (kmask >> q) & 1u;
-                    if (bins && kq && bk < k[q]) ins_less[q]++;
-                    below += (kq && k[q] < bk) ? 1u : 0u;
+            if (x < hi && u.kind[x] == KIND_INS) {
+                const uint64_t yk = u.key[x];
+                const uint32_t ri = u.ip[x] - ip0;
+                uint32_t L = 0, R = nk;
+                while (L < R) {
+                    const uint32_t mid = (L + R) >> 1;
+                    if (kk[grp][mid] < yk)
+                        L = mid + 1;
+                    else
+                        R = mid;
                 }
-                below += __shfl_xor_sync(0xffffffffu, below, 1, 8);
-                below += __shfl_xor_sync(0xffffffffu, below, 2, 8);
-                below += __shfl_xor_sync(0xffffffffu, below, 4, 8);
-                if (gl == t) my_below = below;
-            }
-            if (yins) {
-                const uint32_t rk = (yip - ip0) + my_below;
-                if (rk < 32) {
-                    sk[grp][rk] = yk;
-                    sv[grp][rk] = yv;
+                if (ri < 32) ik[grp][ri] = yk;
+                if (ri + L < 32) {
+                    sk[grp][ri + L] = yk;
+                    sv[grp][ri + L] = u.val[x];
                 }
             }
         }
+        __syncwarp();
+        // a kept key's rank is (kept keys before it) + (inserts below it)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if ((kmask >> q) & 1u) {
-                const uint32_t rk = kbase + __popc(kmask & ((1u << q) - 1)) + ins_less[q];
+                uint32_t L = 0, R = nins < 32 ? nins : 32;
+                while (L < R) {
+                    const uint32_t mid = (L + R) >> 1;
+                    if (ik[grp][mid] < k[q])
+                        L = mid + 1;
+                    else
+                        R = mid;
+                }
+                const uint32_t rk = kbase + __popc(kmask & ((1u << q) - 1)) + L;
                 if (rk < 32) {
                     sk[grp][rk] = k[q];
                     sv[grp][rk] = v[q];
@@ -1071,7 +1107,8 @@ void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t 
                            DevStatus *st, cudaStream_t s) {
     ProfScope ps_("resolve_locate", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
-    k_resolve_locate<<<nb, TPB, 0, s>>>(skey, spay, n, g, fl, thres, kind, seg, blk_nn, blk_ins, st);
+    k_resolve_locate<<<nb < 152 * 8 ? nb : 152 * 8, TPB, 0, s>>>(skey, spay, n, g, fl, thres, kind, seg, blk_nn,
+                                                                 blk_ins, st);
     note_launch();
 }
 
