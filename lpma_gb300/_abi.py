@@ -48,6 +48,9 @@ class LpmaStats(ctypes.Structure):
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
+    def __getitem__(self, name):
+        return getattr(self, name)
+
 
 class LpmaError(RuntimeError):
     def __init__(self, status, where=""):

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -40,7 +41,18 @@ struct Cap {
     uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
     uint32_t *bitmap = nullptr;
     uint32_t *scan_tmp = nullptr;
-    uint2 *tile_bounds = nullptr;  // per destination tile of 32 segments
+};
+
+// Replays of the front as a CUDA graph, one per batch shape and buffer set.
+// Only the pack kernel's input pointers change between replays.
+struct FrontGraph {
+    uint64_t key[12];
+    uint64_t stamp;
+    uint64_t launches;  // kernels in the graph, for the launch counter
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    cudaGraphNode_t pack;
+    cudaKernelNodeParams pack_params;
 };
 
 }  // namespace
@@ -83,6 +95,9 @@ struct LpmaHandle {
     size_t view_cap = 0, exp_cap = 0;
     bool view_valid = false;
     uint64_t h2d = 0, d2h = 0;  // bytes copied by the current call
+    cudaStream_t cap_stream = nullptr;  // private stream for graph capture
+    std::vector<FrontGraph> graphs;
+    uint64_t graph_clock = 0;
     bool host_staged = false;    // h2d already holds the staged input bytes
 };
 
@@ -129,7 +144,7 @@ void free_cap(Cap &c) {
     dfree(c.cnt), dfree(c.cnt_alt), dfree(c.cnt_live), dfree(c.srcc), dfree(c.seg_e);
     dfree(c.fl);
     dfree(c.segP), dfree(c.q), dfree(c.qn), dfree(c.PQ), dfree(c.US), dfree(c.qi), dfree(c.qd);
-    dfree(c.bitmap), dfree(c.scan_tmp), dfree(c.tile_bounds);
+    dfree(c.bitmap), dfree(c.scan_tmp);
     c.Hc = 0;
 }
 
@@ -147,7 +162,6 @@ cudaError_t alloc_cap(Cap &c, uint32_t Hc) {
     A(fl, nseg);
     A(segP, nseg + 2) A(q, nseg + 2) A(qn, nseg + 2) A(PQ, nseg + 2) A(US, nseg + 2) A(qi, nseg + 2) A(qd, nseg + 2);
     A(bitmap, bitmap_words(Hc)) A(scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
-    A(tile_bounds, nseg / 16 + 4);  // tiles of 32 segments, windows rounded up
 #undef A
     if ((e = cudaMemset(c.cnt, 0, nseg + 64)) != cudaSuccess) return e;
     if ((e = cudaMemset(c.cnt_live, 0, nseg + 64)) != cudaSuccess) return e;
@@ -204,8 +218,9 @@ lpma_status_t sync_status(LpmaHandle *h, cudaStream_t s) {
     h->d2h += sizeof(DevStatus);
     CK(cudaStreamSynchronize(s));
     CK(cudaGetLastError());
-    if (h->hst->error & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
-    if (h->hst->error & ERR_INTERNAL) return LPMA_ERR_INTERNAL;
+    const uint32_t e = h->hst->error | h->hst->sticky;
+    if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
+    if (e & ERR_INTERNAL) return LPMA_ERR_INTERNAL;
     return LPMA_OK;
 }
 
@@ -243,7 +258,7 @@ bool needs_prefix(const Tables &tb, uint32_t H) {
 }
 
 lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thres_active, uint64_t total_live,
-                       const Tables &tb, cudaStream_t s) {
+                       const Tables &tb, cudaStream_t s, const unsigned long long *total_live_dev = nullptr) {
     const uint32_t H = h->H;
     const uint64_t nseg = nseg_of(H);
     CK(cudaMemsetAsync(h->c.bitmap, 0, bitmap_words(H) * 4, s));
@@ -252,8 +267,8 @@ lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thr
     const uint8_t *cntp = thres_active ? h->c.cnt_live : h->c.cnt;
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
-    launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, H, tb, h->c.bitmap, h->cand, h->wsingle,
-                h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
+    launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, total_live_dev, H, tb, h->c.bitmap, h->cand,
+                h->wsingle, h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
     CK(cudaGetLastError());
     return LPMA_OK;
 }
@@ -303,23 +318,13 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
         std::sort(h->big_h.begin(), h->big_h.end(), [](const Window &a, const Window &b) { return a.a < b.a; });
         h->jobs_h.clear();
         uint32_t tiles = 0;
-        bool whole = false;
         for (const Window &w : h->big_h) {
-            TileJob j{w.a, w.f, w.a, w.f, w.m, (w.f + 31) / 32, tiles, 0};
-            tiles += j.tiles;
-            h->jobs_h.push_back(j);
-            if (w.a == 0 && w.f == nseg_of(h->H)) whole = true;
+            h->jobs_h.push_back(TileJob{w.a, w.f, w.a, w.f, w.m, tiles, tiles, 0});
+            tiles += (w.f + 31) / 32;
         }
         CKS(upload_jobs(h, s));
-        Geo alt{h->c.keys_alt, h->c.vals_alt, h->H};
-        launch_exec_tiles(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, h->c.tile_bounds, g, h->c.srcc, h->c.PQ,
-                          h->c.US, alt, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-        if (whole) {
-            std::swap(h->c.keys, h->c.keys_alt);
-            std::swap(h->c.vals, h->c.vals_alt);
-        } else {
-            launch_copy_segments(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, alt, g, s);
-        }
+        launch_exec_big(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, tiles, g, h->c.PQ, h->c.US, u, thres,
+                        h->c.keys_alt, h->c.vals_alt, g, h->c.cnt, h->c.fl, h->sent, h->V, h->dst, s);
         CK(cudaGetLastError());
         st->windows_big += n_big;
         st->slots_rewritten += h->hst->slots_big;
@@ -352,29 +357,156 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     Cap fresh;
     const bool grow = hh > h->c.Hc;
     if (grow) CK(alloc_cap(fresh, std::min<uint32_t>(hh + 1, LPMA_MAX_HEIGHT)));
+    // gather into the alternate buffer, spread into the main buffer (of the
+    // new capacity when the tree outgrows the current one)
     Geo src{h->c.keys, h->c.vals, H};
-    Geo dst = grow ? Geo{fresh.keys, fresh.vals, hh} : Geo{h->c.keys_alt, h->c.vals_alt, hh};
+    Geo dst = grow ? Geo{fresh.keys, fresh.vals, hh} : Geo{h->c.keys, h->c.vals, hh};
+    uint64_t *Mk = grow ? fresh.keys_alt : h->c.keys_alt;
+    uint8_t *Mv = grow ? fresh.vals_alt : h->c.vals_alt;
     uint8_t *cnt_d = grow ? fresh.cnt : h->c.cnt;
     ulonglong2 *fl_d = grow ? fresh.fl : h->c.fl;
-    const uint32_t df = (uint32_t)nseg_of(hh);
-    h->jobs_h.assign(1, TileJob{0, (uint32_t)nseg_of(H), 0, df, (uint32_t)m, (df + 31) / 32, 0, 0});
+    const uint32_t sf = (uint32_t)nseg_of(H), df = (uint32_t)nseg_of(hh);
+    h->jobs_h.assign(1, TileJob{0, sf, 0, df, (uint32_t)m, 0, 0, 0});
     CKS(upload_jobs(h, s));
-    uint2 *bounds = grow ? fresh.tile_bounds : h->c.tile_bounds;
-    launch_exec_tiles(h->jobs_d, 1, (df + 31) / 32, bounds, src, h->c.srcc, h->c.PQ, h->c.US, dst, cnt_d, fl_d,
-                      h->sent, h->V, u, thres, h->dst, s);
+    launch_exec_big(h->jobs_d, 1, (sf + 31) / 32, (df + 31) / 32, src, h->c.PQ, h->c.US, u, thres, Mk, Mv, dst, cnt_d,
+                    fl_d, h->sent, h->V, h->dst, s);
     CK(cudaGetLastError());
     if (grow) {
         CK(cudaStreamSynchronize(s));
         free_cap(h->c);
         h->c = fresh;
-    } else {
-        std::swap(h->c.keys, h->c.keys_alt);
-        std::swap(h->c.vals, h->c.vals_alt);
-        if (hh < H) CK(cudaMemsetAsync(h->c.cnt + nseg_of(hh), 0, nseg_of(H) - nseg_of(hh) + 64, s));
+    } else if (hh < H) {
+        CK(cudaMemsetAsync(h->c.cnt + nseg_of(hh), 0, nseg_of(H) - nseg_of(hh) + 64, s));
     }
     h->H = hh;
     st->rebuilt = 1;
     st->slots_rewritten += nslots_of(hh);
+    return LPMA_OK;
+}
+
+// Everything of an update call up to the host round trip: status reset,
+// pack, sort, resolve + locate, compaction, plan and the status read-back.
+lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, const uint8_t *ins_vals,
+                            size_t n_ins, const uint64_t *del, size_t n_del, uint32_t thres, bool thres_active,
+                            bool internal) {
+    const size_t n = n_ins + n_del;
+    CK(cudaMemcpyAsync(h->dst, h->hinit, offsetof(DevStatus, sticky), cudaMemcpyHostToDevice, s));
+    // the engine's own sentinel keys are always in the packed layout
+    const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
+    launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
+                h->bk0, h->bp0, h->dst, s);
+    if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
+    // sort (digit bytes decided on the device), resolve + locate, compact
+    const SortMask mask{&h->dst->key_and, 0xFFu};
+    CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s));
+    Geo g{h->c.keys, h->c.vals, h->H};
+    launch_resolve_locate(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, g, h->c.fl, thres, h->kind, h->seg,
+                          h->blk_nn, h->blk_ins, h->dst, s);
+    launch_compact(h->bk0, h->bp0, h->bk1, h->bp1, mask, h->kind, h->seg, (uint32_t)n, h->blk_nn, h->blk_ins, h->u,
+                   h->dst, s);
+    // plan the first loop
+    Tables tb = make_tables(h, h->H, true);
+    CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
+                 thres_active ? &h->dst->live_total : &h->dst->total_items));
+    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    return LPMA_OK;
+}
+
+bool graphs_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("LPMA_NO_GRAPH");
+        on = (e && e[0] == '1') ? 0 : 1;
+    }
+    return on == 1;
+}
+
+lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins,
+                        const uint64_t *del, size_t n_del, uint32_t thres, bool thres_active, bool internal) {
+    const size_t n = n_ins + n_del;
+    h->h2d += offsetof(DevStatus, sticky);
+    h->d2h += sizeof(DevStatus);
+    // the stored-key count reaches the planner through the status reset copy,
+    // so that it is not a kernel argument of a cached graph
+    h->hinit->total_items = h->total;
+    if (internal || prof_enabled() || !graphs_enabled()) {
+        CKS(enqueue_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
+    } else {
+        const uint64_t key[12] = {n_ins, n_del, h->H, thres, (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1),
+                                  (uint64_t)h->c.keys, (uint64_t)h->c.vals, (uint64_t)h->c.cnt, (uint64_t)h->c.fl,
+                                  (uint64_t)h->bk0, (uint64_t)h->c.cnt_live, (uint64_t)h->c.bitmap};
+        FrontGraph *fg = nullptr;
+        for (FrontGraph &f : h->graphs)
+            if (!memcmp(f.key, key, sizeof(key))) fg = &f;
+        if (!fg) {
+            if (h->graphs.size() >= 16) {
+                auto lru = std::min_element(h->graphs.begin(), h->graphs.end(),
+                                            [](const FrontGraph &a, const FrontGraph &b) { return a.stamp < b.stamp; });
+                cudaGraphExecDestroy(lru->exec);
+                cudaGraphDestroy(lru->graph);
+                h->graphs.erase(lru);
+            }
+            FrontGraph f{};
+            memcpy(f.key, key, sizeof(key));
+            const uint64_t l0 = launch_count();
+            CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+            lpma_status_t r = enqueue_front(h, h->cap_stream, ins, ins_vals, n_ins, del, n_del, thres, thres_active,
+                                            internal);
+            cudaGraph_t gr = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &gr);
+            if (r != LPMA_OK) return r;
+            CK(ce);
+            f.graph = gr;
+            f.launches = launch_count() - l0;
+            CK(cudaGraphInstantiate(&f.exec, gr, 0));
+            size_t nn = 0;
+            CK(cudaGraphGetNodes(gr, nullptr, &nn));
+            std::vector<cudaGraphNode_t> nodes(nn);
+            CK(cudaGraphGetNodes(gr, nodes.data(), &nn));
+            for (cudaGraphNode_t nd : nodes) {
+                cudaGraphNodeType t;
+                CK(cudaGraphNodeGetType(nd, &t));
+                if (t != cudaGraphNodeTypeKernel) continue;
+                cudaKernelNodeParams kp;
+                CK(cudaGraphKernelNodeGetParams(nd, &kp));
+                if (kp.func == pack_kernel_fn()) {
+                    f.pack = nd;
+                    f.pack_params = kp;
+                }
+            }
+            if (!f.pack) return LPMA_ERR_INTERNAL;
+            h->graphs.push_back(f);
+            fg = &h->graphs.back();
+            note_launch(-(int)f.launches);  // counted again on each replay
+        }
+        fg->stamp = ++h->graph_clock;
+        // k_pack(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st)
+        const uint64_t *a_ins = ins, *a_del = del;
+        const uint8_t *a_vals = ins_vals;
+        uint32_t a_nins = (uint32_t)n_ins, a_ndel = (uint32_t)n_del, a_V = h->V, a_thres = thres,
+                 a_fmt = h->cfg.key_format;
+        int a_internal = 0;
+        uint64_t *a_ko = h->bk0;
+        uint16_t *a_po = h->bp0;
+        DevStatus *a_st = h->dst;
+        void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st};
+        cudaKernelNodeParams kp = fg->pack_params;
+        kp.kernelParams = args;
+        kp.extra = nullptr;
+        CK(cudaGraphExecKernelNodeSetParams(fg->exec, fg->pack, &kp));
+        CK(cudaGraphLaunch(fg->exec, s));
+        note_launch((int)fg->launches);
+    }
+    (void)n;
+    return LPMA_OK;
+}
+
+lpma_status_t wait_front(LpmaHandle *h, cudaStream_t s) {
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    const uint32_t e = h->hst->error | h->hst->sticky;
+    if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
+    if (e & ERR_INTERNAL) return LPMA_ERR_INTERNAL;
     return LPMA_OK;
 }
 
@@ -402,34 +534,15 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     h->view_valid = false;
     const bool thres_active = thres > h->min_t;
 
-    // 1. pack + validate
-    CK(cudaMemcpyAsync(h->dst, h->hinit, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-    h->h2d += sizeof(DevStatus);
-    // the engine's own sentinel keys are always in the packed layout
-    const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
-    launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
-                h->bk0, h->bp0, h->dst, s);
-    if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
-    CKS(sync_status(h, s));
+    // pack, sort, resolve + locate, compact, plan (one CUDA graph when the
+    // batch shape repeats), then the one host round trip of the common path;
+    // a rejected batch turns every kernel after k_pack into a no-op
+    CKS(run_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
+    lpma_status_t rs = wait_front(h, s);
+    if (rs != LPMA_OK) return h->sticky = rs;
     if (h->hst->error & ERR_KEY) return LPMA_ERR_INVALID_KEY;
-    const uint64_t diff = h->hst->key_and ^ h->hst->key_or;
     const uint32_t min_t_ins = h->hst->min_t_ins;
     const int64_t live_before = thres_active ? (int64_t)h->hst->live_total : (int64_t)h->total;
-
-    // 2. sort, resolve + locate, compact (mutations: upserts, tombstones)
-    int which = 0;
-    CK(sort_pairs<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, diff, h->sort, &h->dst->error, s, &which));
-    const uint64_t *sk = which ? h->bk1 : h->bk0;
-    const uint16_t *sp = which ? h->bp1 : h->bp0;
-    Geo g{h->c.keys, h->c.vals, h->H};
-    launch_resolve_locate(sk, sp, (uint32_t)n, g, h->c.fl, thres, h->kind, h->seg, h->blk_nn, h->blk_ins, h->dst, s);
-    launch_compact(sk, sp, h->kind, h->seg, (uint32_t)n, h->blk_nn, h->blk_ins, h->u, h->dst, s);
-
-    // 3. plan the first loop
-    Tables tb = make_tables(h, h->H, true);
-    CKS(run_plan(h, h->u, (uint32_t)n, thres_active, (uint64_t)live_before, tb, s));
-    lpma_status_t rs = sync_status(h, s);
-    if (rs != LPMA_OK) return h->sticky = rs;
     const uint32_t n_u = h->hst->n_u, n_new = h->hst->n_ins, n_gone = h->hst->n_del;
     st.n_ins_applied = n_new;
     st.n_del_applied = n_gone;
@@ -497,11 +610,13 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     }
     if (r != LPMA_OK) return h->sticky = r;
     if (thres_active) {
+        // executed windows dropped expired keys: recount what is stored
         CK(cudaMemsetAsync(&h->dst->cnt_total, 0, 8, s));
         launch_sum_cnt(h->c.cnt, nseg_of(h->H), h->dst, s);
+        rs = sync_status(h, s);
+        if (rs != LPMA_OK) return h->sticky = rs;
     }
-    rs = sync_status(h, s);
-    if (rs != LPMA_OK) return h->sticky = rs;
+    // the common path returns here while the executors run on the stream
     h->total = thres_active ? h->hst->cnt_total : (uint64_t)live_after;
     if (n_new && min_t_ins < h->min_t) h->min_t = min_t_ins;
     st.height_after = h->H;
@@ -531,6 +646,12 @@ lpma_status_t lpma_config_default(LpmaConfig *cfg) {
 lpma_status_t lpma_destroy(LpmaHandle *h) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
+    for (FrontGraph &f : h->graphs) {
+        cudaGraphExecDestroy(f.exec);
+        cudaGraphDestroy(f.graph);
+    }
+    h->graphs.clear();
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     free_cap(h->c);
     dfree(h->sent), dfree(h->dst);
     if (h->hst) cudaFreeHost(h->hst);
@@ -579,7 +700,10 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         return fail(LPMA_ERR_OUT_OF_MEMORY);
     // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
     h->H = 0;
-    if (cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) || cudaMemsetAsync(h->c.vals, 0, 32, s) ||
+    if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) || sort_prepare())
+        return fail(LPMA_ERR_CUDA);
+    if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), s) || cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) ||
+        cudaMemsetAsync(h->c.vals, 0, 32, s) ||
         cudaMemsetAsync(h->c.fl, 0xFF, sizeof(ulonglong2), s) || cudaMemsetAsync(h->sent, 0, 4ull * num_vertices, s))
         return fail(LPMA_ERR_CUDA);
     // the sentinels through the update path (init_csr_rpma, rpma.cuh:1819-1823)

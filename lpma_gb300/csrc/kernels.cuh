@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "lpma_common.cuh"
+#include "prims.cuh"
 
 namespace lpma {
 
@@ -28,18 +29,23 @@ void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, c
                  uint32_t n_del, uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                  uint64_t *keys_out, uint16_t *pay_out, DevStatus *st, cudaStream_t s);
 
+// the pack kernel's entry (graph replays update its input pointers)
+const void *pack_kernel_fn();
+
 // per-segment live counts (key present and t >= thres) + their total
 void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_t *cnt_live, DevStatus *st,
                         cudaStream_t s);
 
 // collapse duplicates, locate every key, membership test against its
 // segment, upsert/tombstone in place; per-256-block counts of kept entries
-void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t n, Geo g, const ulonglong2 *fl,
-                           uint32_t thres, uint8_t *kind, uint32_t *seg, uint32_t *blk_nn, uint32_t *blk_ins,
-                           DevStatus *st, cudaStream_t s);
+// The sorted batch is (k0, p0) or (k1, p1), as sort_pairs_dev left it.
+void launch_resolve_locate(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, uint32_t n,
+                           SortMask mask, Geo g, const ulonglong2 *fl, uint32_t thres, uint8_t *kind, uint32_t *seg,
+                           uint32_t *blk_nn, uint32_t *blk_ins, DevStatus *st, cudaStream_t s);
 
-void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *kind, const uint32_t *seg,
-                    uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins, UpdList u, DevStatus *st, cudaStream_t s);
+void launch_compact(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, SortMask mask,
+                    const uint8_t *kind, const uint32_t *seg, uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins,
+                    UpdList u, DevStatus *st, cudaStream_t s);
 
 // locate only (second loop after a level-up): u.seg from u.key
 void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s);
@@ -51,8 +57,9 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 // count-only planner: per segment with updates, the first level whose
 // window passes the density test; maximal windows go to small/big lists
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
-                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *single,
-                 Window *small, Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s);
+                 uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
+                 uint32_t *bitmap, Window *cand, Window *single, Window *small, Window *big, uint8_t *seg_e,
+                 uint8_t *pend, DevStatus *st, cudaStream_t s);
 
 // warp-grain executor for windows of <= 32 segments, in place; single != 0
 // takes the single-segment list (count in DevStatus::n_single)
@@ -66,22 +73,20 @@ void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uin
 void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
                   uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s);
 
-struct TileJob {
+struct TileJob {      // one window of more than 32 segments, or a rebuild
     uint32_t sa, sf;  // source linear segment range
     uint32_t da, df;  // destination linear segment range
     uint32_t m;       // items
-    uint32_t tiles;   // ceil(df / 32)
-    uint32_t tile0;   // first tile index of this job
+    uint32_t stile0;  // first 32-segment source tile of this job
+    uint32_t dtile0;  // first 32-segment destination tile of this job
     uint32_t pad;
 };
-// tile-grain executor: merge source windows with their inserts and spread
-// them over the destination geometry (another buffer)
-void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, uint2 *bounds, Geo src,
-                       const uint8_t *srcc, const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d,
-                       ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
-                       cudaStream_t s);
-void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to,
-                          cudaStream_t s);
+// big windows and rebuilds: gather the merged items into M (rank order),
+// then spread them over the destination geometry
+void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
+                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t thres, uint64_t *Mk,
+                     uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
+                     DevStatus *st, cudaStream_t s);
 
 // new level: cnt re-index (old s -> 2s+1), empty leaves
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s);

@@ -86,7 +86,11 @@ struct DevStatus {
     unsigned long long slots_small, slots_big;
     unsigned long long live_total;   // sum of live counts (thres pass)
     unsigned long long cnt_total;    // sum of occupancy counts (recount)
+    unsigned long long total_items;  // keys stored before the call (set by the host)
     uint32_t err_info[4];            // first offending input index, internal-check site
+    // Not reset per call (the reset copies the fields above only): the
+    // executors set ERR_INTERNAL here after the call may have returned.
+    uint32_t sticky;
 };
 
 // A rebalance window chosen by the planner (maximal executed window).

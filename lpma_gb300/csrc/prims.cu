@@ -174,8 +174,13 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys,
 }
 
 // ---------------------------------------------------------------- one pass
-__global__ void __launch_bounds__(SORT_TPB) k_upsweep(const uint64_t *__restrict__ keys, uint32_t n, int sh,
-                                                      uint32_t *counts, uint32_t T) {
+__global__ void __launch_bounds__(SORT_TPB) k_upsweep(const uint64_t *__restrict__ k0, const uint64_t *__restrict__ k1,
+                                                      uint32_t n, int byte, SortMask mask, uint32_t *counts,
+                                                      uint32_t T) {
+    const uint32_t act = active_bytes(mask);
+    if (!((act >> byte) & 1u)) return;
+    const uint64_t *keys = (__popc(act & ((1u << byte) - 1)) & 1) ? k1 : k0;
+    const int sh = 8 * byte;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -191,7 +196,9 @@ __global__ void __launch_bounds__(SORT_TPB) k_upsweep(const uint64_t *__restrict
 
 // one warp per digit: offs[d][t] = base(d) + sum of counts[d][t' < t]
 __global__ void __launch_bounds__(256) k_dscan(const uint32_t *__restrict__ counts, uint32_t T,
-                                               const uint32_t *__restrict__ hist, uint32_t *offs) {
+                                               const uint32_t *__restrict__ hist, uint32_t *offs, int byte,
+                                               SortMask mask) {
+    if (!((active_bytes(mask) >> byte) & 1u)) return;
     __shared__ uint32_t gd[256];
     __shared__ uint32_t wsum[8];
     gd[threadIdx.x] = block_excl_scan_256(hist[threadIdx.x], wsum, nullptr);
@@ -226,9 +233,16 @@ struct PassSmem {
 };
 
 template <typename V>
-__global__ void __launch_bounds__(SORT_TPB) k_downsweep(const uint64_t *__restrict__ ki, const V *__restrict__ vi,
-                                                        uint64_t *__restrict__ ko, V *__restrict__ vo, uint32_t n,
-                                                        int sh, const uint32_t *__restrict__ offs, uint32_t T) {
+__global__ void __launch_bounds__(SORT_TPB) k_downsweep(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, int byte,
+                                                        SortMask mask, const uint32_t *__restrict__ offs, uint32_t T) {
+    const uint32_t act = active_bytes(mask);
+    if (!((act >> byte) & 1u)) return;
+    const bool odd = __popc(act & ((1u << byte) - 1)) & 1;
+    const uint64_t *__restrict__ ki = odd ? k1 : k0;
+    const V *__restrict__ vi = odd ? v1 : v0;
+    uint64_t *__restrict__ ko = odd ? k0 : k1;
+    V *__restrict__ vo = odd ? v0 : v1;
+    const int sh = 8 * byte;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem<V> &S = *reinterpret_cast<PassSmem<V> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -296,7 +310,8 @@ struct SmallSmem {
 };
 
 template <typename V>
-__global__ void __launch_bounds__(SORT_TPB) k_small_sort(uint64_t *keys, V *vals, uint32_t n, uint32_t byte_mask) {
+__global__ void __launch_bounds__(SORT_TPB) k_small_sort(uint64_t *keys, V *vals, uint32_t n, SortMask mask) {
+    const uint32_t byte_mask = active_bytes(mask);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallSmem<V> &S = *reinterpret_cast<SmallSmem<V> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -467,20 +482,14 @@ cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_
 }
 
 template <typename V>
-cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits, SortScratch &s,
-                       uint32_t *err, cudaStream_t st, int *which) {
-    *which = 0;
-    uint32_t byte_mask = 0;
-    for (int b = 0; b < 8; b++)
-        if ((diff_bits >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
-    if (n < 2 || byte_mask == 0) return cudaSuccess;
+static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
+                             cudaStream_t st) {
+    if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
     if (n <= (uint32_t)SORT_TILE) {
-        size_t sm = sizeof(SmallSmem<V>);
-        e = cudaFuncSetAttribute(k_small_sort<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
+        const size_t sm = sizeof(SmallSmem<V>);
         ProfScope ps("sort_small", st);
-        k_small_sort<V><<<1, SORT_TPB, sm, st>>>(k0, v0, n, byte_mask);
+        k_small_sort<V><<<1, SORT_TPB, sm, st>>>(k0, v0, n, mask);
         note_launch();
         return cudaGetLastError();
     }
@@ -495,33 +504,68 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
     }
     note_launch();
     const size_t sm = sizeof(PassSmem<V>);
-    if ((e = cudaFuncSetAttribute(k_downsweep<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm))) return e;
-    uint64_t *ka = k0, *kb = k1;
-    V *va = v0, *vb = v1;
-    int cur = 0;
     for (int b = 0; b < 8; b++) {
-        if (!((byte_mask >> b) & 1u)) continue;
+        if (!((mask.host_mask >> b) & 1u)) continue;
         {
             ProfScope ps("sort_upsweep", st);
-            k_upsweep<<<tiles, SORT_TPB, 0, st>>>(ka, n, 8 * b, counts, tiles);
+            k_upsweep<<<tiles, SORT_TPB, 0, st>>>(k0, k1, n, b, mask, counts, tiles);
         }
         {
             ProfScope ps("sort_dscan", st);
-            k_dscan<<<32, 256, 0, st>>>(counts, tiles, s.hist + 256 * b, offs);
+            k_dscan<<<32, 256, 0, st>>>(counts, tiles, s.hist + 256 * b, offs, b, mask);
         }
         {
             ProfScope ps("sort_downsweep", st);
-            k_downsweep<V><<<tiles, SORT_TPB, sm, st>>>(ka, va, kb, vb, n, 8 * b, offs, tiles);
+            k_downsweep<V><<<tiles, SORT_TPB, sm, st>>>(k0, v0, k1, v1, n, b, mask, offs, tiles);
         }
         note_launch(3);
-        uint64_t *tk = ka; ka = kb; kb = tk;
-        V *tv = va; va = vb; vb = tv;
-        cur ^= 1;
     }
-    *which = cur;
     return cudaGetLastError();
 }
 
+// Shared-memory opt-ins of the sort kernels, set once outside any stream
+// capture.
+cudaError_t sort_prepare() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_small_sort<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(SmallSmem<uint16_t>))))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_small_sort<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(SmallSmem<uint64_t>))))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_downsweep<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(PassSmem<uint16_t>))))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_downsweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(PassSmem<uint64_t>))))
+        return e;
+    done = true;
+    return cudaSuccess;
+}
+
+template <typename V>
+cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits, SortScratch &s,
+                       uint32_t *err, cudaStream_t st, int *which) {
+    (void)err;
+    uint32_t byte_mask = 0;
+    for (int b = 0; b < 8; b++)
+        if ((diff_bits >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
+    *which = (n > (uint32_t)SORT_TILE) ? (__builtin_popcount(byte_mask) & 1) : 0;
+    cudaError_t e = sort_prepare();
+    if (e != cudaSuccess) return e;
+    return sort_impl<V>(k0, v0, k1, v1, n, SortMask{nullptr, byte_mask}, s, st);
+}
+
+template <typename V>
+cudaError_t sort_pairs_dev(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
+                           cudaStream_t st) {
+    return sort_impl<V>(k0, v0, k1, v1, n, mask, s, st);
+}
+
+template cudaError_t sort_pairs_dev<uint16_t>(uint64_t *, uint16_t *, uint64_t *, uint16_t *, uint32_t, SortMask,
+                                              SortScratch &, cudaStream_t);
 template cudaError_t sort_pairs<uint16_t>(uint64_t *, uint16_t *, uint64_t *, uint16_t *, uint32_t, uint64_t,
                                           SortScratch &, uint32_t *, cudaStream_t, int *);
 template cudaError_t sort_pairs<uint64_t>(uint64_t *, uint64_t *, uint64_t *, uint64_t *, uint32_t, uint64_t,

@@ -17,6 +17,39 @@ struct SortScratch {
     size_t status_words = 0;
 };
 
+// Digit bytes to sort: host_mask, intersected (when andor is set) with the
+// bytes where the device words andor[0] (AND of all keys) and andor[1] (OR
+// of all keys) differ.
+struct SortMask {
+    const unsigned long long *andor;
+    uint32_t host_mask;
+};
+
+// Which digit bytes a sort pass must handle: either fixed by the host, or
+// read from the device (bytes where the keys' AND and OR differ, restricted
+// to the host mask) so that no host round trip is needed before the sort.
+__device__ inline uint32_t active_bytes(SortMask m) {
+    if (!m.andor) return m.host_mask;
+    const uint64_t d = m.andor[0] ^ m.andor[1];
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < 8; b++)
+        if ((d >> (8 * b)) & 0xFF) r |= 1u << b;
+    return r & m.host_mask;
+}
+
+// true when sort_pairs_dev left its result in the second buffer pair
+__device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
+    return n > (uint32_t)SORT_TILE && (__popc(active_bytes(m)) & 1);
+}
+
+// Device-decided variant: the result lands in (k1, v1) when n > SORT_TILE
+// and the number of active bytes is odd, else in (k0, v0); kernels that
+// consume it compute the same parity (sort_result_odd).
+template <typename V>
+cudaError_t sort_pairs_dev(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
+                           cudaStream_t st);
+
 // Sorts n pairs by key (stable).  Only the bytes set in diff_bits are sorted
 // (bytes equal across all keys need no pass).  The result lands either in
 // (k0, v0) or in (k1, v1); *which receives 0 or 1.  err is kept for the
@@ -30,6 +63,9 @@ inline size_t sort_status_words(uint32_t n) {
     size_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
     return 2 * tiles * 256 + 2;  // per-pass (digit, tile) counts and offsets
 }
+
+// One-time kernel attribute setup (outside stream capture).
+cudaError_t sort_prepare();
 
 // Exclusive scan of n u32 values; out may alias in.  total (device, may be
 // null) receives the sum.  tmp needs scan_tmp_words(n) words.

@@ -209,11 +209,18 @@ __global__ void __launch_bounds__(TPB) k_live_counts(const uint64_t *__restrict_
 }
 
 // ------------------------------------------------------------------ resolve + locate
-__global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restrict__ skey,
-                                                        const uint16_t *__restrict__ spay, uint32_t n, Geo g,
-                                                        const ulonglong2 *__restrict__ fl, uint32_t thres,
+__global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restrict__ k0,
+                                                        const uint16_t *__restrict__ p0,
+                                                        const uint64_t *__restrict__ k1,
+                                                        const uint16_t *__restrict__ p1, uint32_t n, SortMask mask,
+                                                        Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
                                                         uint32_t *blk_ins, DevStatus *st) {
+    const bool odd = sort_result_odd(mask, n);
+    const uint64_t *__restrict__ skey = odd ? k1 : k0;
+    const uint16_t *__restrict__ spay = odd ? p1 : p0;
+    // a rejected batch (validation in k_pack) changes nothing
+    const bool rejected = (st->error & ERR_KEY) != 0;
     // persistent grid: the top TOPL levels are staged once per CTA and the
     // CTA walks 256-entry chunks; chunk c writes its counts to blk_*[c]
     __shared__ ulonglong2 top[TOPN];
@@ -226,7 +233,7 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
     for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
         const uint32_t i = chunk * TPB + threadIdx.x;
         uint32_t kd = KIND_NOP, sg = 0;
-        if (i < n) {
+        if (i < n && !rejected) {
             const uint64_t key = skey[i];
             const uint16_t p = spay[i];
             const bool is_del = (p >> 8) & 1;
@@ -265,6 +272,8 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
             } else {
                 noop++;
             }
+        }
+        if (i < n) {
             kind[i] = (uint8_t)kd;
             seg[i] = sg;
         }
@@ -353,10 +362,14 @@ __device__ inline uint32_t block_excl_scan(uint32_t x, uint32_t *wsum) {
     return r;
 }
 
-__global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ skey, const uint16_t *__restrict__ spay,
-                                                 const uint8_t *__restrict__ kind, const uint32_t *__restrict__ seg,
-                                                 uint32_t n, const uint32_t *blk_nn, const uint32_t *blk_ins,
-                                                 UpdList u) {
+__global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
+                                                 const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
+                                                 SortMask mask, const uint8_t *__restrict__ kind,
+                                                 const uint32_t *__restrict__ seg, uint32_t n,
+                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u) {
+    const bool odd = sort_result_odd(mask, n);
+    const uint64_t *__restrict__ skey = odd ? k1 : k0;
+    const uint16_t *__restrict__ spay = odd ? p1 : p0;
     __shared__ uint32_t wsum[TPB / 32];
     const uint32_t i = blockIdx.x * TPB + threadIdx.x;
     const uint32_t kd = i < n ? kind[i] : KIND_NOP;
@@ -443,9 +456,11 @@ __device__ inline uint64_t bit_of(uint32_t H, uint32_t l, uint64_t widx) {
 }
 
 __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
-                                              const uint32_t *__restrict__ P, int use_P, uint64_t total_live,
-                                              uint32_t H, Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
+                                              const uint32_t *__restrict__ P, int use_P, uint64_t total_live_host,
+                                              const unsigned long long *__restrict__ total_live_dev, uint32_t H,
+                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
                                               uint8_t *pend, DevStatus *st) {
+    const uint64_t total_live = total_live_dev ? *total_live_dev : total_live_host;
     __shared__ uint32_t wsum[TPB / 32];
     __shared__ uint32_t base_s;
     const uint32_t nu = st->n_u;
@@ -751,7 +766,7 @@ __global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__r
         __syncwarp();
         if (R != W.m || W.m > (uint32_t)OUTCAP) {
             if (lane == 0) {
-                atomicOr(&st->error, ERR_INTERNAL);
+                atomicOr(&st->sticky, ERR_INTERNAL);
                 st->err_info[1] = 1;
             }
             continue;
@@ -893,7 +908,7 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restr
         const uint32_t m = nk + nins;
         const bool ok = active && m == W.m && m <= 32;
         if (active && !ok && gl == 0) {
-            atomicOr(&st->error, ERR_INTERNAL);
+            atomicOr(&st->sticky, ERR_INTERNAL);
             st->err_info[1] = 3;
         }
         if (ok) {
@@ -948,14 +963,19 @@ __global__ void __launch_bounds__(TPB) k_seg_q(const uint8_t *__restrict__ cnt, 
     }
 }
 
-// Per destination tile: the source segments whose merged ranks overlap the
-// tile's rank range (binary searches over the window prefix PQ), one thread
-// per tile so that the tile kernel starts with its bounds in hand.
-__device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_t tile) {
-    uint32_t L = 0, R = njobs - 1;  // last job with tile0 <= tile
+// Windows larger than 32 segments (root, level >= 6, rebuild) run in two
+// fully parallel phases.  Gather: one 8-lane group per source segment merges
+// its kept slots with the inserts located into it and writes them, in
+// window rank order, to a contiguous sequence M (the alternate buffer) at
+// PQ[s] + rank.  Spread: one 8-lane group per destination segment takes its
+// items [first_rank(k), first_rank(k+1)) from M.  Every source slot is read
+// before any destination slot is written (two launches), so the windows are
+// rewritten in place.
+__device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_t tile, bool dst) {
+    uint32_t L = 0, R = njobs - 1;  // last job whose first tile <= tile
     while (L < R) {
-        uint32_t mid = (L + R + 1) >> 1;
-        if (jobs[mid].tile0 <= tile)
+        const uint32_t mid = (L + R + 1) >> 1;
+        if ((dst ? jobs[mid].dtile0 : jobs[mid].stile0) <= tile)
             L = mid;
         else
             R = mid - 1;
@@ -963,95 +983,127 @@ __device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_
     return L;
 }
 
-__global__ void __launch_bounds__(TPB) k_tile_bounds(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
-                                                     const uint32_t *__restrict__ PQ, uint2 *bounds, DevStatus *st) {
-    const uint32_t tile = blockIdx.x * TPB + threadIdx.x;
-    if (tile >= ntiles) return;
-    const uint32_t jb = find_job(jobs, njobs, tile);
-    const TileJob J = jobs[jb];
-    const uint64_t t = tile - J.tile0;
-    const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
-    const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
-    const uint32_t base = PQ[J.sa];
-    uint32_t a = J.sa, b = J.sa + J.sf - 1;  // last source segment whose first rank <= R0
-    while (a < b) {
-        uint32_t mid = (a + b + 1) >> 1;
-        if (PQ[mid] - base <= R0)
-            a = mid;
-        else
-            b = mid - 1;
-    }
-    uint32_t c = a, d = J.sa + J.sf;  // first source segment whose first rank >= R1
-    while (c < d) {
-        uint32_t mid = (c + d) >> 1;
-        if (PQ[mid] - base >= R1)
-            d = mid;
-        else
-            c = mid + 1;
-    }
-    bounds[tile] = make_uint2(a, c);
-    // the source prefix must account for exactly m items
-    if (t == 0 && PQ[J.sa + J.sf] - base != J.m) {
-        atomicOr(&st->error, ERR_INTERNAL);
-        st->err_info[1] = 2;
-    }
-}
+constexpr int GT_TPB = 256;             // 32 groups of 8 lanes: one 32-segment tile per CTA
+constexpr int GT_GROUPS = GT_TPB / 8;
 
-struct TileSmem {
-    uint64_t outk[1056];
-    uint8_t outv[1056];
-    uint64_t kk[8][32];
-};
-
-__global__ void __launch_bounds__(TPB) k_exec_tiles(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
-                                                    const uint2 *__restrict__ bounds, Geo src,
-                                                    const uint8_t *__restrict__ srcc, const uint32_t *__restrict__ PQ,
-                                                    const uint32_t *__restrict__ US, Geo dst, uint8_t *cnt_d,
-                                                    ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u,
-                                                    uint32_t thres) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
+                                                   Geo src, const uint32_t *__restrict__ PQ,
+                                                   const uint32_t *__restrict__ US, const UpdList u, uint32_t thres,
+                                                   uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv) {
+    __shared__ uint64_t kk[GT_GROUPS][32];
+    const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const TileJob J = jobs[find_job(jobs, njobs, tile)];
-        const uint2 bd = bounds[tile];
-        const uint64_t t = tile - J.tile0;
-        const uint64_t k0 = 32 * t, k1 = umin64(32 * t + 32, J.df);
-        const uint64_t R0 = first_rank(k0, J.m, J.df), R1 = first_rank(k1, J.m, J.df);
-        const uint32_t base = PQ[J.sa];
-        SegMergeOut out{S.outk, S.outv};
-        for (uint32_t s = bd.x + w; s < bd.y; s += TPB / 32) {
+        const TileJob J = jobs[find_job(jobs, njobs, tile, false)];
+        const uint32_t s = J.sa + 32 * (tile - J.stile0) + grp;
+        const bool active = s < J.sa + J.sf;
+        uint64_t k[4] = {KEY_NONE, KEY_NONE, KEY_NONE, KEY_NONE};
+        uint8_t v[4] = {0, 0, 0, 0};
+        uint32_t kmask = 0, us = 0, ue = 0;
+        uint64_t base = 0;
+        if (active) {
             const uint64_t j = heap_of_linear(s, src.H);
-            merge_segment(src.keys, src.vals, j, srcc[s], US[s], US[s + 1], PQ[s] - base, R0, R1, u, thres, S.kk[w],
-                          out);
+            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(src.keys + 32 * j + 4 * gl);
+            const ulonglong2 a = kp[0], b = kp[1];
+            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(src.vals + 32 * j + 4 * gl);
+            k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                v[q] = (uint8_t)(v4 >> (8 * q));
+                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
+            }
+            us = US[s];
+            ue = US[s + 1];
+            base = PQ[s];
         }
-        __syncthreads();
-        for (uint64_t k = k0 + w; k < k1; k += TPB / 32) {
-            const uint64_t ds = J.da + k;
-            const uint64_t j = heap_of_linear(ds, dst.H);
-            uint8_t cn;
-            ulonglong2 f2;
-            write_segment(dst.keys, dst.vals, j, k, J.m, J.df, R0, S.outk, S.outv, sent, V, &cn, &f2);
-            if (lane == 0) {
-                cnt_d[ds] = cn;
-                fl_d[j] = f2;
+        const uint32_t nl = __popc(kmask);
+        uint32_t incl = nl;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 8);
+            if (gl >= o) incl += y;
+        }
+        const uint32_t kbase = incl - nl;
+        const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if ((kmask >> q) & 1u) kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
+        __syncwarp();
+        const uint32_t ip0 = active ? u.ip[us] : 0;
+        // kept slots: rank = kept before + inserts of this segment below the key
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if ((kmask >> q) & 1u) {
+                uint32_t below = 0;
+                if (ue > us) below = u.ip[lb_key(u.key, us, ue, k[q])] - ip0;
+                const uint64_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
+                Mk[r] = k[q];
+                Mv[r] = v[q];
             }
         }
-        __syncthreads();
+        // inserts: rank = inserts before + kept keys below
+        const uint32_t rounds = __reduce_max_sync(0xffffffffu, (ue - us + 7) / 8);
+        for (uint32_t rd = 0; rd < rounds; rd++) {
+            const uint32_t x = us + 8 * rd + gl;
+            if (x < ue && u.kind[x] == KIND_INS) {
+                const uint64_t y = u.key[x];
+                uint32_t L = 0, R = nk;
+                while (L < R) {
+                    const uint32_t mid = (L + R) >> 1;
+                    if (kk[grp][mid] < y)
+                        L = mid + 1;
+                    else
+                        R = mid;
+                }
+                const uint64_t r = base + (u.ip[x] - ip0) + L;
+                Mk[r] = y;
+                Mv[r] = u.val[x];
+            }
+        }
+        __syncwarp();
     }
 }
 
-__global__ void __launch_bounds__(TPB) k_copy_segments(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
-                                                       Geo from, Geo to) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
+                                                   Geo dst, const uint64_t *__restrict__ Mk,
+                                                   const uint8_t *__restrict__ Mv, const uint32_t *__restrict__ PQ,
+                                                   uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
+                                                   DevStatus *st) {
+    const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const TileJob J = jobs[find_job(jobs, njobs, tile)];
-        const uint64_t t = tile - J.tile0;
-        const uint64_t k1 = umin64(32 * t + 32, J.df);
-        for (uint64_t k = 32 * t + w; k < k1; k += TPB / 32) {
-            const uint64_t j = heap_of_linear(J.da + k, to.H);
-            to.keys[32 * j + lane] = from.keys[32 * j + lane];
-            to.vals[32 * j + lane] = from.vals[32 * j + lane];
+        const TileJob J = jobs[find_job(jobs, njobs, tile, true)];
+        const uint64_t k = 32ull * (tile - J.dtile0) + grp;
+        if (k >= J.df) continue;
+        const uint64_t mb = PQ[J.sa];
+        if (k == 0 && gl == 0 && PQ[J.sa + J.sf] - mb != J.m) {  // the gather must account for m items
+            atomicOr(&st->sticky, ERR_INTERNAL);
+            st->err_info[1] = 2;
+        }
+        const uint64_t ds = J.da + k;
+        const uint64_t j = heap_of_linear(ds, dst.H);
+        const uint64_t f0 = first_rank(k, J.m, J.df), f1 = first_rank(k + 1, J.m, J.df);
+        const uint32_t nk = (uint32_t)(f1 - f0);
+        uint64_t o[4];
+        uint32_t ov = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t slot = 4 * gl + q;
+            o[q] = KEY_NONE;
+            if (slot < nk) {
+                o[q] = Mk[mb + f0 + slot];
+                ov |= (uint32_t)Mv[mb + f0 + slot] << (8 * q);
+                if (is_sentinel(o[q])) {
+                    const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
+                    if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                }
+            }
+        }
+        ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(dst.keys + 32 * j + 4 * gl);
+        kp[0] = make_ulonglong2(o[0], o[1]);
+        kp[1] = make_ulonglong2(o[2], o[3]);
+        *reinterpret_cast<uint32_t *>(dst.vals + 32 * j + 4 * gl) = ov;
+        if (gl == 0) {
+            cnt_d[ds] = (uint8_t)nk;
+            fl_d[j] = nk ? make_ulonglong2(Mk[mb + f0], Mk[mb + f1 - 1]) : make_ulonglong2(KEY_NONE, KEY_NONE);
         }
     }
 }
@@ -1086,6 +1138,8 @@ inline uint32_t grid_for(uint64_t n, uint32_t per_block, uint32_t cap = 152 * 16
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
+const void *pack_kernel_fn() { return reinterpret_cast<const void *>(&k_pack); }
+
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
                  DevStatus *st, cudaStream_t s) {
@@ -1102,22 +1156,23 @@ void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_
     note_launch();
 }
 
-void launch_resolve_locate(const uint64_t *skey, const uint16_t *spay, uint32_t n, Geo g, const ulonglong2 *fl,
-                           uint32_t thres, uint8_t *kind, uint32_t *seg, uint32_t *blk_nn, uint32_t *blk_ins,
-                           DevStatus *st, cudaStream_t s) {
+void launch_resolve_locate(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, uint32_t n,
+                           SortMask mask, Geo g, const ulonglong2 *fl, uint32_t thres, uint8_t *kind, uint32_t *seg,
+                           uint32_t *blk_nn, uint32_t *blk_ins, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("resolve_locate", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
-    k_resolve_locate<<<nb < 152 * 8 ? nb : 152 * 8, TPB, 0, s>>>(skey, spay, n, g, fl, thres, kind, seg, blk_nn,
-                                                                 blk_ins, st);
+    k_resolve_locate<<<nb < 152 * 8 ? nb : 152 * 8, TPB, 0, s>>>(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg,
+                                                                 blk_nn, blk_ins, st);
     note_launch();
 }
 
-void launch_compact(const uint64_t *skey, const uint16_t *spay, const uint8_t *kind, const uint32_t *seg, uint32_t n,
-                    uint32_t *blk_nn, uint32_t *blk_ins, UpdList u, DevStatus *st, cudaStream_t s) {
+void launch_compact(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, SortMask mask,
+                    const uint8_t *kind, const uint32_t *seg, uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins,
+                    UpdList u, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("compact", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
     k_scan_pairs<<<1, 1024, 0, s>>>(blk_nn, blk_ins, nb, u.ip, st);
-    k_compact<<<nb, TPB, 0, s>>>(skey, spay, kind, seg, n, blk_nn, blk_ins, u);
+    k_compact<<<nb, TPB, 0, s>>>(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u);
     note_launch(2);
 }
 
@@ -1141,12 +1196,14 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 }
 
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
-                 uint64_t total_live, uint32_t H, const Tables &tb, uint32_t *bitmap, Window *cand, Window *single,
-                 Window *small, Window *big, uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
+                 uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
+                 uint32_t *bitmap, Window *cand, Window *single, Window *small, Window *big, uint8_t *seg_e,
+                 uint8_t *pend, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
-    k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, H, tb, bitmap, cand, seg_e, pend, st);
+    k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap, cand, seg_e, pend,
+                              st);
     k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, single, small, big, st);
     note_launch(2);
 }
@@ -1182,25 +1239,21 @@ void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *q
     note_launch();
 }
 
-void launch_exec_tiles(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, uint2 *bounds, Geo src,
-                       const uint8_t *srcc, const uint32_t *PQ, const uint32_t *US, Geo dst, uint8_t *cnt_d,
-                       ulonglong2 *fl_d, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
-                       cudaStream_t s) {
-    ProfScope ps_("exec_tiles", s);
-    if (!ntiles) return;
-    k_tile_bounds<<<(ntiles + TPB - 1) / TPB, TPB, 0, s>>>(jobs, njobs, ntiles, PQ, bounds, st);
-    const size_t sm = sizeof(TileSmem);
-    cudaFuncSetAttribute(k_exec_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_exec_tiles<<<grid_for(ntiles, 1, 152 * 8), TPB, sm, s>>>(jobs, njobs, ntiles, bounds, src, srcc, PQ, US, dst,
-                                                               cnt_d, fl_d, sent, V, u, thres);
+void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
+                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t thres, uint64_t *Mk,
+                     uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
+                     DevStatus *st, cudaStream_t s) {
+    if (!njobs) return;
+    {
+        ProfScope ps_("exec_gather", s);
+        k_gather<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv);
+    }
+    {
+        ProfScope ps_("exec_spread", s);
+        k_spread<<<grid_for(dtiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, dtiles, dst, Mk, Mv, PQ, cnt_d, fl_d,
+                                                                 sent, V, st);
+    }
     note_launch(2);
-}
-
-void launch_copy_segments(const TileJob *jobs, uint32_t njobs, uint32_t ntiles, Geo from, Geo to, cudaStream_t s) {
-    ProfScope ps_("copy_segments", s);
-    if (!ntiles) return;
-    k_copy_segments<<<grid_for(ntiles, 1, 152 * 8), TPB, 0, s>>>(jobs, njobs, ntiles, from, to);
-    note_launch();
 }
 
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s) {

@@ -38,14 +38,20 @@ def default_config(**kw):
     return cfg
 
 
+_torch = None
+
+
 def _stream_ptr(stream):
+    global _torch
     if stream is None:
-        try:
-            import torch
-            if torch.cuda.is_available():
-                return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        except ImportError:
-            pass
+        if _torch is None:
+            try:
+                import torch
+                _torch = torch if torch.cuda.is_available() else False
+            except ImportError:
+                _torch = False
+        if _torch:
+            return _torch.cuda.current_stream().cuda_stream
         return None
     if isinstance(stream, int):
         return ctypes.c_void_p(stream)
@@ -56,17 +62,21 @@ def _is_cuda_tensor(x):
     return hasattr(x, "is_cuda") and x.is_cuda
 
 
-_SAME_BITS = {"uint64": ("uint64", "int64"), "uint8": ("uint8", "int8")}
+_SAME_BITS = {"uint64": ("torch.uint64", "torch.int64"), "uint8": ("torch.uint8", "torch.int8")}
+_OK_DTYPES = {}
 
 
 def _dev(x, dtype_name):
     if x is None:
         return None, 0
-    if repr(x.dtype).split(".")[-1] not in _SAME_BITS[dtype_name]:
+    ok = _OK_DTYPES.get((x.dtype, dtype_name))
+    if ok is None:
+        ok = _OK_DTYPES[(x.dtype, dtype_name)] = str(x.dtype) in _SAME_BITS[dtype_name]
+    if not ok:
         raise TypeError("expected a torch.%s tensor, got %s" % (dtype_name, x.dtype))
     if not x.is_contiguous():
         raise ValueError("device inputs must be contiguous")
-    return ctypes.c_void_p(x.data_ptr()), x.numel()
+    return x.data_ptr(), x.numel()
 
 
 def _host(x, dtype):
@@ -95,14 +105,14 @@ class Lpma:
         return self.update(ins=keys, ins_vals=values)
 
     def update(self, ins=None, ins_vals=None, dels=None, thres=0):
-        """update_rpma with deletes; returns the call's LpmaStats as a dict."""
+        """update_rpma with deletes; returns the call's LpmaStats (indexable like a dict)."""
         st = LpmaStats()
         sp = _stream_ptr(self.stream)
         if _is_cuda_tensor(ins) or _is_cuda_tensor(dels):
             pi, ni = _dev(ins, "uint64") if ins is not None else (None, 0)
             pv, _ = _dev(ins_vals, "uint8") if ins_vals is not None else (None, 0)
             pd, nd = _dev(dels, "uint64") if dels is not None else (None, 0)
-            rc = self._L.lpma_update(self._h, pi, pv, ni, pd, nd, int(thres), sp, ctypes.byref(st))
+            rc = self._L.lpma_update(self._h, pi, pv, ni, pd, nd, thres, sp, ctypes.byref(st))
         else:
             ai, pi, ni = _host(ins, np.uint64)
             av, pv, _ = _host(ins_vals, np.uint8)
@@ -110,7 +120,7 @@ class Lpma:
             rc = self._L.lpma_update_host(self._h, pi, pv, ni, pd, nd, int(thres), sp, ctypes.byref(st))
             del ai, av, ad
         check(rc, "lpma_update")
-        return st.as_dict()
+        return st
 
     # -------------------------------------------------------------- views
     def info(self):
