@@ -52,6 +52,22 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(t, device=None):
+    """Slowest rank's time (torch.distributed; NCCL on GPUs, gloo on CPU)."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(t)
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_seed(seed, rank):
+    """Replicas only: each rank updates its own graph from its own stream."""
+    return seed + 7919 * rank
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -130,14 +146,14 @@ class Stream:
         return seq[a:a + B]
 
 
-def build_workload(args, device):
+def build_workload(args, device, seed):
     import torch
     import lpma_gb300 as L
     n_raw = (1 << args.scale) * args.ef
     raw = torch.empty(n_raw, dtype=torch.int64, device=device)
-    n = L.gen_rmat_device(args.seed, args.scale, args.ef, raw)
+    n = L.gen_rmat_device(seed, args.scale, args.ef, raw)
     e = raw[:n]
-    L.shuffle_device(args.seed + 1000, e)
+    L.shuffle_device(seed + 1000, e)
     half = n // 2
     S, U = e[:half], e[half:]
     ins_seq = torch.cat([U, S])
@@ -151,7 +167,7 @@ def gpu_arm(args, rank, world):
     device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(device)
     V = 1 << args.scale
-    e, S, ins_seq, del_seq = build_workload(args, device)
+    e, S, ins_seq, del_seq = build_workload(args, device, replica_seed(args.seed, rank))
     g = L.Lpma(V)
     g.build(S)
     st = Stream(ins_seq, del_seq)
@@ -209,11 +225,7 @@ def gpu_arm(args, rank, world):
         torch.distributed.barrier()
     launches = L.kernel_launches() - launches0
     lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
-    t = evs[0].elapsed_time(evs[-1]) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], device=device)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(evs[0].elapsed_time(evs[-1]) / 1e3, device)
 
     # roofline: per-kernel CUDA events over K more steps of the same stream
     L.profile_enable(True)
@@ -361,6 +373,7 @@ def main():
     out["events"] = {k: sum(x[k] for x in s) for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path",
                                                        "fill_empty")}
     out["slots_rewritten_per_step"] = sum(x["slots_rewritten"] for x in s) / len(s)
+    out["single_windows_per_step"] = sum(x["windows_single"] for x in s) / len(s)
     alg = 16 * B + 18 * out["slots_rewritten_per_step"]
     out["batch_hbm"] = {"alg_bytes_per_step": alg, "achieved_GBps": alg / (res["t"] / args.steps) / 1e9,
                         "frac": alg / (res["t"] / args.steps) / 1e9 / peak}

@@ -76,7 +76,7 @@ struct LpmaHandle {
     uint8_t *kind = nullptr, *pend = nullptr;
     uint32_t *seg = nullptr, *blk_nn = nullptr, *blk_ins = nullptr;
     UpdList u{}, u2{};
-    Window *cand = nullptr, *wsingle = nullptr, *wsmall = nullptr, *wbig = nullptr;
+    Window *cand = nullptr, *wsingle = nullptr, *wsmall4 = nullptr, *wsmall = nullptr, *wbig = nullptr;
     SortScratch sort{};
     uint32_t *sort_err = nullptr;
     TileJob *jobs_d = nullptr;
@@ -196,7 +196,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
     dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
     dfree(h->blk_nn), dfree(h->blk_ins);
     for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
+    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall4), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
     h->bcap = 0;
     const size_t nb = cap / 256 + 4;
     CK(dalloc(&h->bk0, cap)); CK(dalloc(&h->bk1, cap)); CK(dalloc(&h->bp0, cap)); CK(dalloc(&h->bp1, cap));
@@ -206,7 +206,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
         CK(dalloc(&u->key, cap)); CK(dalloc(&u->val, cap)); CK(dalloc(&u->kind, cap)); CK(dalloc(&u->seg, cap));
         CK(dalloc(&u->ip, cap + 1));
     }
-    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsingle, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
+    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsingle, cap)); CK(dalloc(&h->wsmall4, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
     h->sort.status_words = sort_status_words((uint32_t)cap);
     CK(dalloc(&h->sort.status, h->sort.status_words));
     h->bcap = cap;
@@ -262,13 +262,12 @@ lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thr
     const uint32_t H = h->H;
     const uint64_t nseg = nseg_of(H);
     CK(cudaMemsetAsync(h->c.bitmap, 0, bitmap_words(H) * 4, s));
-    CK(cudaMemsetAsync(h->pend, 0, std::max<size_t>(n_cap, 1), s));
     CK(reset_plan_counters(h, s));
     const uint8_t *cntp = thres_active ? h->c.cnt_live : h->c.cnt;
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
     launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, total_live_dev, H, tb, h->c.bitmap, h->cand,
-                h->wsingle, h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
+                h->wsingle, h->wsmall4, h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
     CK(cudaGetLastError());
     return LPMA_OK;
 }
@@ -301,12 +300,14 @@ lpma_status_t upload_jobs(LpmaHandle *h, cudaStream_t s) {
 // Execute the planned maximal windows (status already synced).
 lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32_t thres, bool thres_active,
                         cudaStream_t s, LpmaStats *st) {
-    const uint32_t n_single = h->hst->n_single, n_small = h->hst->n_small, n_big = h->hst->n_big;
+    const uint32_t n_single = h->hst->n_single, n_small4 = h->hst->n_small4, n_small = h->hst->n_small,
+                   n_big = h->hst->n_big;
     Geo g{h->c.keys, h->c.vals, h->H};
-    launch_exec_small(h->wsingle, n_single, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-    launch_exec_small(h->wsmall, n_small, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    launch_exec_small(h->wsingle, n_single, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    launch_exec_small(h->wsmall4, n_small4, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    launch_exec_small(h->wsmall, n_small, 2, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
     st->windows_single += n_single;
-    st->windows_small += n_single + n_small;
+    st->windows_small += n_single + n_small4 + n_small;
     st->slots_rewritten += h->hst->slots_small;
     st->slots_small += h->hst->slots_small;
     if (n_big) {
@@ -323,8 +324,9 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
             tiles += (w.f + 31) / 32;
         }
         CKS(upload_jobs(h, s));
-        launch_exec_big(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, tiles, g, h->c.PQ, h->c.US, u, thres,
-                        h->c.keys_alt, h->c.vals_alt, g, h->c.cnt, h->c.fl, h->sent, h->V, h->dst, s);
+        launch_exec_big(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, tiles, g, h->c.PQ, h->c.US, u, n_list,
+                        thres_active ? thres : 0, h->c.keys_alt, h->c.vals_alt, g, h->c.cnt, h->c.fl, h->sent, h->V,
+                        h->dst, s);
         CK(cudaGetLastError());
         st->windows_big += n_big;
         st->slots_rewritten += h->hst->slots_big;
@@ -368,8 +370,8 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     const uint32_t sf = (uint32_t)nseg_of(H), df = (uint32_t)nseg_of(hh);
     h->jobs_h.assign(1, TileJob{0, sf, 0, df, (uint32_t)m, 0, 0, 0});
     CKS(upload_jobs(h, s));
-    launch_exec_big(h->jobs_d, 1, (sf + 31) / 32, (df + 31) / 32, src, h->c.PQ, h->c.US, u, thres, Mk, Mv, dst, cnt_d,
-                    fl_d, h->sent, h->V, h->dst, s);
+    launch_exec_big(h->jobs_d, 1, (sf + 31) / 32, (df + 31) / 32, src, h->c.PQ, h->c.US, u, n_list,
+                    thres_active ? thres : 0, Mk, Mv, dst, cnt_d, fl_d, h->sent, h->V, h->dst, s);
     CK(cudaGetLastError());
     if (grow) {
         CK(cudaStreamSynchronize(s));
@@ -659,7 +661,8 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
     dfree(h->blk_nn), dfree(h->blk_ins);
     for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status), dfree(h->sort.hist),
+    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall4), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status),
+        dfree(h->sort.hist),
         dfree(h->sort.counters);
     dfree(h->jobs_d);
     dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);

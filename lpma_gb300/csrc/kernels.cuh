@@ -58,12 +58,13 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 // window passes the density test; maximal windows go to small/big lists
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
-                 uint32_t *bitmap, Window *cand, Window *single, Window *small, Window *big, uint8_t *seg_e,
-                 uint8_t *pend, DevStatus *st, cudaStream_t s);
+                 uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
+                 uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s);
 
-// warp-grain executor for windows of <= 32 segments, in place; single != 0
-// takes the single-segment list (count in DevStatus::n_single)
-void launch_exec_small(const Window *w, uint32_t n_cap, int single, Geo g, uint8_t *cnt, ulonglong2 *fl,
+// in-place executors for windows of <= 32 segments: kind 0 the
+// single-segment list (DevStatus::n_single), 1 windows of 2..4 segments
+// (n_small4), 2 windows of 5..32 segments (n_small)
+void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
                        uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
 
 // per-segment counts for the tile grain: qi/qd from the update list
@@ -84,9 +85,9 @@ struct TileJob {      // one window of more than 32 segments, or a rebuild
 // big windows and rebuilds: gather the merged items into M (rank order),
 // then spread them over the destination geometry
 void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
-                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t thres, uint64_t *Mk,
-                     uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
-                     DevStatus *st, cudaStream_t s);
+                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t n_upd, uint32_t thres,
+                     uint64_t *Mk, uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
+                     uint32_t V, DevStatus *st, cudaStream_t s);
 
 // new level: cnt re-index (old s -> 2s+1), empty leaves
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s);

@@ -79,7 +79,7 @@ struct DevStatus {
     unsigned long long key_and, key_or;
     uint32_t n_u;             // compacted updates
     uint32_t n_ins, n_del, n_upsert, n_noop;
-    uint32_t n_cand, n_single, n_small, n_big;
+    uint32_t n_cand, n_single, n_small4, n_small, n_big;
     uint32_t root, ovf;
     uint32_t exec_levels;     // bit l: some window of level l executes
     uint32_t empty_found;     // fill_empty_segs check

@@ -503,9 +503,7 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
             }
         }
         seg_e[s] = (uint8_t)e;
-        if (e == EXEC_OVF) {
-            for (uint32_t y = x; y < hi0; y++) pend[y] = 1;
-        } else {
+        if (e != EXEC_OVF) {
             const uint64_t bit = bit_of(H, e, (uint64_t)s >> e);
             const uint32_t mask = 1u << (bit & 31);
             own = !(atomicOr(&bitmap[bit >> 5], mask) & mask);
@@ -537,17 +535,24 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
 // Keep the candidates not inside a larger executed window; sort them into
 // single-segment, small (<= 32 segments) and big lists.
 __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
-                                                  const uint32_t *__restrict__ bitmap, Window *single, Window *small,
-                                                  Window *big, DevStatus *st) {
+                                                  const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
+                                                  Window *small, Window *big, const UpdList u,
+                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
+    // updates of segments that no window absorbed stay pending (overflow)
+    {
+        const uint32_t x = blockIdx.x * TPB + threadIdx.x;
+        if (x < st->n_u && x < n_cap) pend[x] = seg_e[u.seg[x]] == EXEC_OVF;
+    }
     __shared__ uint32_t wsum[TPB / 32];
-    __shared__ uint32_t base_s[3];
+    __shared__ uint32_t base_s[4];
     __shared__ unsigned long long sl[2][TPB / 32];
     const uint32_t c = blockIdx.x * TPB + threadIdx.x;
-    uint32_t cls = 3;
+    // classes: 0 single segment, 1 two to four, 2 five to 32, 3 larger, 4 none
+    uint32_t cls = 4;
     Window w{};
     if (c < st->n_cand && c < n_cap) {
         w = cand[c];
-        cls = w.f == 1 ? 0 : (w.f <= SMALL_WIN_SEGS ? 1 : 2);
+        cls = w.f == 1 ? 0 : (w.f <= 4 ? 1 : (w.f <= SMALL_WIN_SEGS ? 2 : 3));
         // inside a larger executed window?  The ancestor words are loaded
         // without an early exit so that the loads are in flight together.
         uint32_t hit = 0;
@@ -558,11 +563,13 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
             const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
             hit |= (bitmap[bit >> 5] >> (bit & 31)) & 1u;
         }
-        if (hit) cls = 3;
+        if (hit) cls = 4;
     }
-    const uint32_t packed = cls < 3 ? 1u << (10 * cls) : 0u;
-    const uint32_t ex = block_excl_scan(packed, wsum);
-    unsigned long long s_small = cls <= 1 ? 32ull * w.f : 0, s_big = cls == 2 ? 32ull * w.f : 0;
+    const uint32_t pa = cls < 2 ? 1u << (16 * cls) : 0u;
+    const uint32_t pb = (cls == 2 || cls == 3) ? 1u << (16 * (cls - 2)) : 0u;
+    const uint32_t exa = block_excl_scan(pa, wsum);
+    const uint32_t exb = block_excl_scan(pb, wsum);
+    unsigned long long s_small = cls <= 2 ? 32ull * w.f : 0, s_big = cls == 3 ? 32ull * w.f : 0;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         s_small += __shfl_xor_sync(0xffffffffu, s_small, o);
@@ -570,10 +577,11 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
     }
     if ((threadIdx.x & 31) == 0) sl[0][threadIdx.x >> 5] = s_small, sl[1][threadIdx.x >> 5] = s_big;
     if (threadIdx.x == TPB - 1) {
-        const uint32_t tot = ex + packed;
-        base_s[0] = atomicAdd(&st->n_single, tot & 1023u);
-        base_s[1] = atomicAdd(&st->n_small, (tot >> 10) & 1023u);
-        base_s[2] = atomicAdd(&st->n_big, tot >> 20);
+        const uint32_t ta = exa + pa, tb = exb + pb;
+        base_s[0] = atomicAdd(&st->n_single, ta & 0xFFFFu);
+        base_s[1] = atomicAdd(&st->n_small4, ta >> 16);
+        base_s[2] = atomicAdd(&st->n_small, tb & 0xFFFFu);
+        base_s[3] = atomicAdd(&st->n_big, tb >> 16);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -582,206 +590,163 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
         if (a) atomicAdd(&st->slots_small, a);
         if (b) atomicAdd(&st->slots_big, b);
     }
-    if (cls < 3) {
-        const uint32_t idx = base_s[cls] + ((ex >> (10 * cls)) & 1023u);
-        (cls == 0 ? single : cls == 1 ? small : big)[idx] = w;
+    if (cls < 4) {
+        const uint32_t ex = cls < 2 ? exa : exb;
+        const uint32_t idx = base_s[cls] + ((ex >> (16 * (cls & 1))) & 0xFFFFu);
+        (cls == 0 ? single : cls == 1 ? small4 : cls == 2 ? small : big)[idx] = w;
     }
 }
 
-// ------------------------------------------------------------------ per-segment merge
-// One warp merges one source segment (its kept slots) with the inserts that
-// located into it and stores the items whose window rank falls in
-// [R0, R1) into out[rank - R0].  Ranks start at Rs for this segment.
-// Kept slots and inserts are each sorted and the keys are distinct.
-struct SegMergeOut {
-    uint64_t *k;
-    uint8_t *v;
+// ------------------------------------------------------------------ multi-segment windows
+// A unit of G groups of 8 lanes rewrites one window of 2..G segments in
+// shared memory: group g loads segment a+g (16-byte loads, 4 slots a lane),
+// the unit scans the per-segment item counts, every group places its kept
+// slots and inserts at their window ranks, then group g writes destination
+// segment g.  G = 4 makes a unit of one warp (windows of 2..4 segments),
+// G = 32 a unit of the whole CTA (5..32 segments).  In place: the unit reads
+// every slot of its window before it writes any.
+constexpr int EM_TPB = 256;
+
+template <int G>
+struct MultiSmem {
+    uint64_t outk[32 / G][32 * G];
+    uint8_t outv[32 / G][32 * G];
+    uint64_t kk[32][32];
+    uint32_t q[32];
+    uint32_t base[32];
 };
 
-__device__ inline uint32_t merge_segment(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals,
-                                         uint64_t j, uint32_t c, uint32_t us, uint32_t ue, uint64_t Rs, uint64_t R0,
-                                         uint64_t R1, const UpdList &u, uint32_t thres, uint64_t *kk,
-                                         SegMergeOut out) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t lt = lanemask_lt();
-    // all 32 slots in one 256-byte access, issued without waiting for the
-    // count (slots at or past the count are empty: segments are left-packed)
-    const uint64_t key = keys[32 * j + lane];
-    const uint8_t val = vals[32 * j + lane];
-    const bool keep = (uint32_t)lane < c && kept_slot(key, val, thres);
-    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-    const uint32_t nk = __popc(bal), kb = __popc(bal & lt);
-    if (us == ue) {
-        if (keep) {
-            const uint64_t r = Rs + kb;
-            if (r >= R0 && r < R1) {
-                out.k[r - R0] = key;
-                out.v[r - R0] = val;
-            }
-        }
-        return nk;
-    }
-    if (keep) kk[kb] = key;
-    __syncwarp();
-    const uint32_t ip0 = u.ip[us];
-    const uint32_t total = nk + (u.ip[ue] - ip0);
-    if (keep) {
-        const uint32_t xk = lb_key(u.key, us, ue, key);
-        const uint64_t r = Rs + kb + (u.ip[xk] - ip0);
-        if (r >= R0 && r < R1) {
-            out.k[r - R0] = key;
-            out.v[r - R0] = val;
-        }
-    }
-    // Update entries whose merged rank falls in [R0, R1): the rank of entry x
-    // is Rs + (inserts before x) + (kept keys below key[x]), monotone in x,
-    // so the range is found by binary search (a segment can carry millions
-    // of inserts when a bulk load lands in a near-empty tree).
-    uint32_t x_lo = us, x_hi = ue;
-    if (Rs < R0 || Rs + total > R1) {
-        auto rank_at = [&](uint32_t x) -> uint64_t {
-            const uint64_t y = u.key[x];
-            uint32_t L = 0, R = nk;
-            while (L < R) {
-                uint32_t mid = (L + R) >> 1;
-                if (kk[mid] < y)
-                    L = mid + 1;
-                else
-                    R = mid;
-            }
-            return Rs + (u.ip[x] - ip0) + L;
-        };
-        uint32_t a = us, b = ue;
-        while (a < b) {
-            uint32_t mid = (a + b) >> 1;
-            if (rank_at(mid) < R0)
-                a = mid + 1;
-            else
-                b = mid;
-        }
-        x_lo = a;
-        b = ue;
-        while (a < b) {
-            uint32_t mid = (a + b) >> 1;
-            if (rank_at(mid) < R1)
-                a = mid + 1;
-            else
-                b = mid;
-        }
-        x_hi = a;
-    }
-    for (uint32_t x0 = x_lo; x0 < x_hi; x0 += 32) {
-        const uint32_t x = x0 + lane;
-        if (x < x_hi && u.kind[x] == KIND_INS) {
-            const uint64_t y = u.key[x];
-            uint32_t L = 0, R = nk;
-            while (L < R) {
-                uint32_t mid = (L + R) >> 1;
-                if (kk[mid] < y)
-                    L = mid + 1;
-                else
-                    R = mid;
-            }
-            const uint64_t r = Rs + (u.ip[x] - ip0) + L;
-            if (r >= R0 && r < R1) {
-                out.k[r - R0] = y;
-                out.v[r - R0] = u.val[x];
-            }
-        }
-    }
-    __syncwarp();
-    return total;
-}
-
-// Write destination segment k of a window spread (m items over f segments),
-// taking its items from out[first_rank(k) - R0 ...].
-__device__ inline void write_segment(uint64_t *__restrict__ dkeys, uint8_t *__restrict__ dvals, uint64_t j,
-                                     uint64_t k, uint64_t m, uint64_t f, uint64_t R0, const uint64_t *ok,
-                                     const uint8_t *ov, uint32_t *sent, uint32_t V, uint8_t *cnt_slot,
-                                     ulonglong2 *fl_slot) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t f0 = first_rank(k, m, f), f1 = first_rank(k + 1, m, f);
-    const uint32_t nk = (uint32_t)(f1 - f0);
-    uint64_t key = KEY_NONE;
-    if ((uint32_t)lane < nk) {
-        key = ok[f0 - R0 + lane];
-        dvals[32 * j + lane] = ov[f0 - R0 + lane];
-        if (is_sentinel(key)) {
-            const uint32_t row = (uint32_t)(key >> SRC_SHIFT);
-            if (row < V) sent[row] = (uint32_t)(32 * j + lane);
-        }
-    }
-    dkeys[32 * j + lane] = key;
-    if (lane == 0) {
-        *cnt_slot = (uint8_t)nk;
-        *fl_slot = nk ? make_ulonglong2(ok[f0 - R0], ok[f1 - 1 - R0]) : make_ulonglong2(KEY_NONE, KEY_NONE);
-    }
-}
-
-// ------------------------------------------------------------------ small windows
-// One warp per window of <= 32 segments, in place: every source slot of the
-// window is read (into registers / shared memory) before any is written.
-// OUTCAP = 32 serves single-segment windows with 0.5 KB of shared memory
-// per warp (full occupancy); OUTCAP = 1024 serves windows of 2..32 segments.
-constexpr int EXS_WARPS = 8;
-template <int OUTCAP>
-struct ExSmallSmem {
-    uint64_t outk[EXS_WARPS][OUTCAP];
-    uint8_t outv[EXS_WARPS][OUTCAP];
-    uint64_t kk[EXS_WARPS][32];
-};
-
-template <int OUTCAP>
-__global__ void __launch_bounds__(EXS_WARPS * 32) k_exec_small(const Window *__restrict__ wins,
-                                                               const uint32_t *__restrict__ n_win, uint32_t n_cap,
-                                                               Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
-                                                               uint32_t V, const UpdList u, uint32_t thres,
-                                                               DevStatus *st) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    ExSmallSmem<OUTCAP> &S = *reinterpret_cast<ExSmallSmem<OUTCAP> *>(smem_raw);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t nwin = min(*n_win, n_cap);
-    SegMergeOut out{S.outk[w], S.outv[w]};
-    for (uint32_t wi = blockIdx.x * EXS_WARPS + w; wi < nwin; wi += gridDim.x * EXS_WARPS) {
-        const Window W = wins[wi];
-        // lane k < f: segment a + k
-        uint32_t c = 0, us = W.hi;
-        uint64_t j = 0;
-        if ((uint32_t)lane < W.f) {
-            const uint32_t s = W.a + lane;
-            c = cnt[s];
-            j = heap_of_linear(s, g.H);
-            us = W.f == 1 ? W.lo : lb_seg(u.seg, W.lo, W.hi, s);
-        }
-        uint32_t ue = __shfl_down_sync(0xffffffffu, us, 1);
-        if ((uint32_t)lane + 1 >= W.f) ue = W.hi;
-        uint64_t R = 0;
-        for (uint32_t k = 0; k < W.f; k++) {
-            const uint32_t ck = __shfl_sync(0xffffffffu, c, k);
-            const uint64_t jk = __shfl_sync(0xffffffffu, j, k);
-            const uint32_t usk = __shfl_sync(0xffffffffu, us, k);
-            const uint32_t uek = __shfl_sync(0xffffffffu, ue, k);
-            R += merge_segment(g.keys, g.vals, jk, ck, usk, uek, R, 0, OUTCAP, u, thres, S.kk[w], out);
-        }
+template <int G>
+__device__ inline void unit_sync() {
+    if (G == 32)
+        __syncthreads();
+    else
         __syncwarp();
-        if (R != W.m || W.m > (uint32_t)OUTCAP) {
-            if (lane == 0) {
+}
+
+template <int G>
+__global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
+                                                       uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
+                                                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
+                                                       DevStatus *st) {
+    __shared__ MultiSmem<G> S;
+    constexpr int UNITS = 32 / G;
+    const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
+    const int unit = grp / G, ug = grp % G;
+    const uint32_t nwin = min(*n_win, n_cap);
+    for (uint32_t wi = blockIdx.x * UNITS + unit; wi < nwin; wi += gridDim.x * UNITS) {
+        const Window W = wins[wi];
+        const bool active = (uint32_t)ug < W.f;
+        const uint32_t s = W.a + ug;
+        uint64_t k[4] = {KEY_NONE, KEY_NONE, KEY_NONE, KEY_NONE};
+        uint8_t v[4] = {0, 0, 0, 0};
+        uint32_t kmask = 0, us = W.hi, ue = W.hi;
+        uint64_t j = 0;
+        if (active) {
+            j = heap_of_linear(s, g.H);
+            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+            const ulonglong2 a = kp[0], b = kp[1];
+            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
+            k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                v[q] = (uint8_t)(v4 >> (8 * q));
+                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
+            }
+            us = lb_seg(u.seg, W.lo, W.hi, s);
+            ue = lb_seg(u.seg, us, W.hi, s + 1);
+        }
+        const uint32_t nl = __popc(kmask);
+        uint32_t incl = nl;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 8);
+            if (gl >= o) incl += y;
+        }
+        const uint32_t kbase = incl - nl;
+        const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if ((kmask >> q) & 1u) S.kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
+        const uint32_t ip0 = u.ip[us];
+        const uint32_t nins = u.ip[ue] - ip0;
+        if (gl == 0) S.q[grp] = active ? nk + nins : 0;
+        unit_sync<G>();
+        if (gl == 0) {
+            uint32_t b = 0;
+            for (int t = 0; t < ug; t++) b += S.q[unit * G + t];
+            S.base[grp] = b;
+        }
+        unit_sync<G>();
+        const uint32_t base = S.base[grp];
+        uint64_t *outk = S.outk[unit];
+        uint8_t *outv = S.outv[unit];
+        // kept slots: rank = kept before + inserts of the segment below the key
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if ((kmask >> q) & 1u) {
+                const uint32_t below = ue > us ? u.ip[lb_key(u.key, us, ue, k[q])] - ip0 : 0;
+                const uint32_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
+                if (r < 32 * G) {
+                    outk[r] = k[q];
+                    outv[r] = v[q];
+                }
+            }
+        }
+        // inserts: rank = inserts before + kept keys below
+        for (uint32_t x = us + gl; x < ue; x += 8) {
+            if (u.kind[x] != KIND_INS) continue;
+            const uint64_t y = u.key[x];
+            uint32_t L = 0, R = nk;
+            while (L < R) {
+                const uint32_t mid = (L + R) >> 1;
+                if (S.kk[grp][mid] < y)
+                    L = mid + 1;
+                else
+                    R = mid;
+            }
+            const uint32_t r = base + (u.ip[x] - ip0) + L;
+            if (r < 32 * G) {
+                outk[r] = y;
+                outv[r] = u.val[x];
+            }
+        }
+        unit_sync<G>();
+        const uint32_t total = S.base[unit * G + W.f - 1] + S.q[unit * G + W.f - 1];
+        if (total != W.m || W.m > 32u * W.f) {
+            if (ug == 0 && gl == 0) {
                 atomicOr(&st->sticky, ERR_INTERNAL);
                 st->err_info[1] = 1;
             }
-            continue;
-        }
-        for (uint32_t k = 0; k < W.f; k++) {
-            const uint64_t jk = __shfl_sync(0xffffffffu, j, k);
-            uint8_t cn;
-            ulonglong2 f2;
-            write_segment(g.keys, g.vals, jk, k, W.m, W.f, 0, S.outk[w], S.outv[w], sent, V, &cn, &f2);
-            if (lane == 0) {
-                cnt[W.a + k] = cn;
-                fl[jk] = f2;
+        } else if (active) {
+            // destination segment ug of the even spread
+            const uint64_t f0 = first_rank(ug, W.m, W.f), f1 = first_rank(ug + 1, W.m, W.f);
+            const uint32_t cnk = (uint32_t)(f1 - f0);
+            uint64_t o[4];
+            uint32_t ov = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t slot = 4 * gl + q;
+                o[q] = KEY_NONE;
+                if (slot < cnk) {
+                    o[q] = outk[f0 + slot];
+                    ov |= (uint32_t)outv[f0 + slot] << (8 * q);
+                    if (is_sentinel(o[q])) {
+                        const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
+                        if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                    }
+                }
+            }
+            ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+            kp[0] = make_ulonglong2(o[0], o[1]);
+            kp[1] = make_ulonglong2(o[2], o[3]);
+            *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ov;
+            if (gl == 0) {
+                cnt[s] = (uint8_t)cnk;
+                fl[j] = cnk ? make_ulonglong2(outk[f0], outk[f1 - 1]) : make_ulonglong2(KEY_NONE, KEY_NONE);
             }
         }
-        __syncwarp();
+        unit_sync<G>();
     }
 }
 
@@ -983,14 +948,12 @@ __device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_
     return L;
 }
 
-constexpr int GT_TPB = 256;             // 32 groups of 8 lanes: one 32-segment tile per CTA
-constexpr int GT_GROUPS = GT_TPB / 8;
+constexpr int GT_TPB = 256;  // 32 groups of 8 lanes: one 32-segment tile per CTA
 
 __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
                                                    Geo src, const uint32_t *__restrict__ PQ,
                                                    const uint32_t *__restrict__ US, const UpdList u, uint32_t thres,
                                                    uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv) {
-    __shared__ uint64_t kk[GT_GROUPS][32];
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const TileJob J = jobs[find_job(jobs, njobs, tile, false)];
@@ -1023,11 +986,6 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
             if (gl >= o) incl += y;
         }
         const uint32_t kbase = incl - nl;
-        const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if ((kmask >> q) & 1u) kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
-        __syncwarp();
         const uint32_t ip0 = active ? u.ip[us] : 0;
         // kept slots: rank = kept before + inserts of this segment below the key
 #pragma unroll
@@ -1040,26 +998,52 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
                 Mv[r] = v[q];
             }
         }
-        // inserts: rank = inserts before + kept keys below
-        const uint32_t rounds = __reduce_max_sync(0xffffffffu, (ue - us + 7) / 8);
-        for (uint32_t rd = 0; rd < rounds; rd++) {
-            const uint32_t x = us + 8 * rd + gl;
-            if (x < ue && u.kind[x] == KIND_INS) {
-                const uint64_t y = u.key[x];
-                uint32_t L = 0, R = nk;
-                while (L < R) {
-                    const uint32_t mid = (L + R) >> 1;
-                    if (kk[grp][mid] < y)
-                        L = mid + 1;
-                    else
-                        R = mid;
-                }
-                const uint64_t r = base + (u.ip[x] - ip0) + L;
-                Mk[r] = y;
-                Mv[r] = u.val[x];
-            }
-        }
         __syncwarp();
+    }
+}
+
+// The inserts of big windows, one thread each (a segment may carry millions
+// of them when a bulk load lands in a near-empty tree): rank = segment base
+// + inserts of the segment before it + kept slots of the segment below it.
+// Slots below it that are not kept are the tombstones of the segment's
+// deletes before it in the sorted update list, plus expired keys.
+__global__ void __launch_bounds__(TPB) k_gather_ins(const TileJob *__restrict__ jobs, uint32_t njobs, Geo src,
+                                                    const uint32_t *__restrict__ PQ,
+                                                    const uint32_t *__restrict__ US, const UpdList u,
+                                                    const DevStatus *st, uint32_t n_cap, uint32_t thres,
+                                                    uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv) {
+    const uint32_t nu = min(st->n_u, n_cap);
+    for (uint32_t x = blockIdx.x * TPB + threadIdx.x; x < nu; x += gridDim.x * TPB) {
+        if (u.kind[x] != KIND_INS) continue;
+        const uint32_t s = u.seg[x];
+        uint32_t L = 0, R = njobs - 1;  // last job starting at or before s
+        while (L < R) {
+            const uint32_t mid = (L + R + 1) >> 1;
+            if (jobs[mid].sa <= s)
+                L = mid;
+            else
+                R = mid - 1;
+        }
+        if (s < jobs[L].sa || s >= jobs[L].sa + jobs[L].sf) continue;  // a small window took it
+        const uint64_t y = u.key[x];
+        const uint32_t us = US[s];
+        const uint32_t ri = u.ip[x] - u.ip[us];
+        const uint32_t tomb_below = (x - us) - ri;
+        const uint64_t *sk = src.keys + 32 * heap_of_linear(s, src.H);
+        uint32_t pos = 0;  // slots below y (the segment is sorted, NONE-padded)
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1)
+            if (sk[pos + step - 1] < y) pos += step;
+        if (sk[pos] < y) pos++;
+        uint32_t expired_below = 0;
+        if (thres) {
+            const uint8_t *sv = src.vals + (sk - src.keys);
+            for (uint32_t t = 0; t < pos; t++)
+                expired_below += (sv[t] != VAL_TOMB && (sk[t] & TIME_MASK) < (uint64_t)thres) ? 1u : 0u;
+        }
+        const uint64_t r = (uint64_t)PQ[s] + ri + (pos - tomb_below - expired_below);
+        Mk[r] = y;
+        Mv[r] = u.val[x];
     }
 }
 
@@ -1197,29 +1181,32 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
-                 uint32_t *bitmap, Window *cand, Window *single, Window *small, Window *big, uint8_t *seg_e,
-                 uint8_t *pend, DevStatus *st, cudaStream_t s) {
+                 uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
+                 uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
     k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap, cand, seg_e, pend,
                               st);
-    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, single, small, big, st);
+    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend, st);
     note_launch(2);
 }
 
-void launch_exec_small(const Window *w, uint32_t n_cap, int single, Geo g, uint8_t *cnt, ulonglong2 *fl,
+void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
                        uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
-    ProfScope ps_(single ? "exec_single" : "exec_small", s);
     if (!n_cap) return;
-    if (single) {
+    if (kind == 0) {
+        ProfScope ps_("exec_single", s);
         k_exec_single<<<grid_for(n_cap, ES_GROUPS, 152 * 8), ES_TPB, 0, s>>>(w, &st->n_single, n_cap, g, cnt, fl, sent,
                                                                          V, u, thres, st);
+    } else if (kind == 1) {
+        ProfScope ps_("exec_small4", s);
+        k_exec_multi<4><<<grid_for(n_cap, 8, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small4, n_cap, g, cnt, fl, sent, V, u,
+                                                                       thres, st);
     } else {
-        const size_t sm = sizeof(ExSmallSmem<1024>);
-        cudaFuncSetAttribute(k_exec_small<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_exec_small<1024><<<grid_for(n_cap, EXS_WARPS, 152 * 8), EXS_WARPS * 32, sm, s>>>(
-            w, &st->n_small, n_cap, g, cnt, fl, sent, V, u, thres, st);
+        ProfScope ps_("exec_small32", s);
+        k_exec_multi<32><<<grid_for(n_cap, 1, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small, n_cap, g, cnt, fl, sent, V, u,
+                                                                        thres, st);
     }
     note_launch();
 }
@@ -1240,20 +1227,22 @@ void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *q
 }
 
 void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
-                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t thres, uint64_t *Mk,
-                     uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
-                     DevStatus *st, cudaStream_t s) {
+                     const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t n_upd, uint32_t thres,
+                     uint64_t *Mk, uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
+                     uint32_t V, DevStatus *st, cudaStream_t s) {
     if (!njobs) return;
     {
         ProfScope ps_("exec_gather", s);
         k_gather<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv);
+        if (n_upd)
+            k_gather_ins<<<grid_for(n_upd, TPB), TPB, 0, s>>>(jobs, njobs, src, PQ, US, u, st, n_upd, thres, Mk, Mv);
     }
     {
         ProfScope ps_("exec_spread", s);
         k_spread<<<grid_for(dtiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, dtiles, dst, Mk, Mv, PQ, cnt_d, fl_d,
                                                                  sent, V, st);
     }
-    note_launch(2);
+    note_launch(n_upd ? 3 : 2);
 }
 
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s) {
