@@ -1,9 +1,12 @@
 // Host orchestration and the extern "C" boundary of the GB300 LPMA engine.
 //
 // One update call (reference update_rpma, rpma.cuh:1549-1718):
-//   1. pack + validate the batch (no structure change on a bad key)   [sync 1]
+//   1. pack + validate the batch (a bad key turns the rest of the front
+//      into a no-op, so the structure does not change)
 //   2. radix sort, resolve + locate + membership, compaction
-//   3. count-only plan of the first level loop (skip rule on)          [sync 2]
+//   3. count-only plan of the first level loop (skip rule on); steps 1-3
+//      replay as one CUDA graph, then the host reads the status block
+//      (the one synchronisation of a call without overflow)
 //   4. no overflow: execute the maximal windows once; if the root took
 //      updates, the eager level-up of rpma.cuh:1646-1653
 //      overflow (rpma.cuh:1662-1712): resize to h; h == H+1 executes the
