@@ -45,7 +45,8 @@ typedef enum {
     LPMA_ERR_CAPACITY = 5,         /* tree height would exceed LPMA_MAX_HEIGHT */
     LPMA_ERR_INTERNAL = 6,         /* a device-side consistency check failed */
     LPMA_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
-    LPMA_ERR_BUFFER_TOO_SMALL = 8
+    LPMA_ERR_BUFFER_TOO_SMALL = 8,
+    LPMA_ERR_SCRATCH_LIMIT = 9     /* n above the fixed scratch of lpma_shuffle_static */
 } lpma_status_t;
 
 enum { LPMA_KEY_PACKED = 0, LPMA_KEY_PAIR32 = 1 };
@@ -167,6 +168,36 @@ LPMA_API lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edg
 
 /* Reorders d_keys by (mix64(seed ^ key), key). */
 LPMA_API lpma_status_t lpma_shuffle(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream);
+
+/* ---- shuffle without allocation (no counterpart in the reference) ----
+ *
+ * Same result as lpma_shuffle, bit for bit, for n <= LPMA_SHUFFLE_STATIC_MAX_KEYS,
+ * but it allocates nothing: no cudaMalloc, no cudaFree, no allocating
+ * library call.  It is meant for callers that must not allocate or free
+ * device memory while they run -- a serving loop that has handed the whole
+ * HBM budget to resident graphs and cannot risk an out-of-memory failure in
+ * mid-request, or a latency-critical path where cudaFree's implicit device
+ * synchronisation would stall every stream.
+ *
+ * Its scratch is one fixed device array inside the library,
+ * LPMA_SHUFFLE_STATIC_SCRATCH_BYTES long (about 2.5 MB), enough for
+ * LPMA_SHUFFLE_STATIC_MAX_KEYS keys.  A larger n returns
+ * LPMA_ERR_SCRATCH_LIMIT before anything is launched, with d_keys untouched.
+ * No part of the scratch has to hold zeros on entry: the call clears what it
+ * counts in and writes every other byte before reading it.
+ *
+ * The first call on each device does a one-time set-up with that device
+ * current (it looks up the array's device address and sets kernel
+ * attributes); make that first call before any stream capture begins.
+ *
+ * Every call in the process shares the one array per device, so calls whose
+ * GPU work overlaps -- on different streams, or from different threads --
+ * race on it and give wrong results.  Issue them on one stream, or order
+ * them.  The call is asynchronous on `stream`.  While per-kernel profiling
+ * (lpma_prof_enable) is on, the profiler creates CUDA events for this call's
+ * launches too; keep it off where nothing may be allocated. */
+enum { LPMA_SHUFFLE_STATIC_MAX_KEYS = 65536, LPMA_SHUFFLE_STATIC_SCRATCH_BYTES = 2621440 };
+LPMA_API lpma_status_t lpma_shuffle_static(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream);
 
 /* Per-kernel timing for profiling: while enabled, each kernel launch is
  * bracketed by CUDA events on its stream.  lpma_prof_report writes one line

@@ -881,6 +881,7 @@ const char *lpma_status_string(lpma_status_t s) {
         case LPMA_ERR_INTERNAL: return "internal consistency check failed";
         case LPMA_ERR_TIMEOUT: return "bounded device wait gave up";
         case LPMA_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+        case LPMA_ERR_SCRATCH_LIMIT: return "n exceeds the fixed scratch of this entry point";
     }
     return "unknown status";
 }
