@@ -288,6 +288,9 @@ def roofline(res, B, peak, peak_kind):
     elif name == "exec_tiles":
         units = sum(s["slots_rewritten"] - s["slots_small"] for s in pst) / cnt
         per_unit, unit_name = 18, "window slot (8 B key + 1 B value, read and written)"
+    elif name == "sort_coop":
+        units = sum(B * s["sort_passes"] for s in pst) / cnt
+        per_unit, unit_name = 20, "key per digit pass (8 B key + 2 B payload, read and written)"
     elif name in ("sort_pass", "sort_downsweep"):
         units = B
         per_unit, unit_name = 20, "key (8 B key + 2 B payload, read and written)"

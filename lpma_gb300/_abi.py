@@ -45,7 +45,8 @@ class LpmaStats(ctypes.Structure):
                 ("windows_big", ctypes.c_uint64),
                 ("slots_rewritten", ctypes.c_uint64), ("slots_small", ctypes.c_uint64),
                 ("num_items", ctypes.c_uint64),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("sort_passes", ctypes.c_uint32), ("reserved1", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -328,8 +328,8 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
         }
         CKS(upload_jobs(h, s));
         launch_exec_big(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, tiles, g, h->c.PQ, h->c.US, u, n_list,
-                        thres_active ? thres : 0, h->c.keys_alt, h->c.vals_alt, g, h->c.cnt, h->c.fl, h->sent, h->V,
-                        h->dst, s);
+                        thres_active ? thres : 0, h->c.keys_alt, h->c.vals_alt, nslots_of(h->c.Hc), g, h->c.cnt,
+                        h->c.fl, h->sent, h->V, h->dst, s);
         CK(cudaGetLastError());
         st->windows_big += n_big;
         st->slots_rewritten += h->hst->slots_big;
@@ -373,8 +373,9 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     const uint32_t sf = (uint32_t)nseg_of(H), df = (uint32_t)nseg_of(hh);
     h->jobs_h.assign(1, TileJob{0, sf, 0, df, (uint32_t)m, 0, 0, 0});
     CKS(upload_jobs(h, s));
+    const uint64_t m_cap = nslots_of(grow ? fresh.Hc : h->c.Hc);
     launch_exec_big(h->jobs_d, 1, (sf + 31) / 32, (df + 31) / 32, src, h->c.PQ, h->c.US, u, n_list,
-                    thres_active ? thres : 0, Mk, Mv, dst, cnt_d, fl_d, h->sent, h->V, h->dst, s);
+                    thres_active ? thres : 0, Mk, Mv, m_cap, dst, cnt_d, fl_d, h->sent, h->V, h->dst, s);
     CK(cudaGetLastError());
     if (grow) {
         CK(cudaStreamSynchronize(s));
@@ -544,8 +545,15 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     // a rejected batch turns every kernel after k_pack into a no-op
     CKS(run_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
     lpma_status_t rs = wait_front(h, s);
+    // a sort that gave up a bounded wait turned the front into a no-op:
+    // nothing changed, so the handle stays usable
+    if (rs == LPMA_ERR_TIMEOUT && h->hst->sticky == 0) return rs;
     if (rs != LPMA_OK) return h->sticky = rs;
     if (h->hst->error & ERR_KEY) return LPMA_ERR_INVALID_KEY;
+    {
+        const uint64_t diff = h->hst->key_and ^ h->hst->key_or;
+        for (int b = 0; b < 8; b++) st.sort_passes += ((diff >> (8 * b)) & 0xFF) ? 1u : 0u;
+    }
     const uint32_t min_t_ins = h->hst->min_t_ins;
     const int64_t live_before = thres_active ? (int64_t)h->hst->live_total : (int64_t)h->total;
     const uint32_t n_u = h->hst->n_u, n_new = h->hst->n_ins, n_gone = h->hst->n_del;
@@ -698,6 +706,9 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         cudaMallocHost(&h->hinit, sizeof(DevStatus)) || dalloc(&h->sent, num_vertices) ||
         dalloc(&h->sort.hist, 8 * 256) || dalloc(&h->sort.counters, 16) || dalloc(&h->sort_err, 1))
         return fail(LPMA_ERR_OUT_OF_MEMORY);
+    // batches up to coop_sort_max_keys() sort in one cooperative launch
+    h->sort.bar = h->sort.counters;
+    h->sort.err = &h->dst->error;
     std::memset(h->hinit, 0, sizeof(DevStatus));
     h->hinit->min_t_ins = 0xFFFFFFFFu;
     h->hinit->key_and = ~0ull;

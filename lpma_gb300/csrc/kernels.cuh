@@ -86,8 +86,8 @@ struct TileJob {      // one window of more than 32 segments, or a rebuild
 // then spread them over the destination geometry
 void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
                      const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t n_upd, uint32_t thres,
-                     uint64_t *Mk, uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
-                     uint32_t V, DevStatus *st, cudaStream_t s);
+                     uint64_t *Mk, uint8_t *Mv, uint64_t m_cap, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
+                     uint32_t *sent, uint32_t V, DevStatus *st, cudaStream_t s);
 
 // new level: cnt re-index (old s -> 2s+1), empty leaves
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s);

@@ -21,9 +21,8 @@ namespace {
 constexpr size_t MAXN = LPMA_SHUFFLE_STATIC_MAX_KEYS;
 constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Radix-sort status words for MAXN keys: per pass, one count and one offset
-// per (tile, digit), plus two spare words.
-constexpr size_t STATUS_WORDS = 2 * ((MAXN + SORT_TILE - 1) / SORT_TILE) * 256 + 2;
+// Radix-sort status words for MAXN keys (counts and offsets per tile and digit).
+constexpr size_t STATUS_WORDS = sort_status_words((uint32_t)MAXN);
 
 // Layout of the scratch array; every piece starts on a 256-byte boundary.
 constexpr size_t OFF_TMP = 0;                                   // u64 keys, second buffer of sort 1

@@ -8,6 +8,7 @@
 // __match_any_sync and scatters them.  No CTA waits on another.  Bytes that
 // are equal across all keys are skipped.  Batches of at most one tile are
 // sorted by one CTA in shared memory in a single launch.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -137,23 +138,34 @@ __device__ inline uint32_t block_excl_scan_256(uint32_t x, uint32_t *wsum /*[8]*
 // digit.  Keys of warp w are at tile positions w*32*IPT + i*32 + lane, so
 // the rank order is the input order.  whist[256] is this warp's digit
 // counter row (zeroed by the caller); on return it holds the warp's counts.
+// The lanes that share a digit are found with eight ballots (one per digit
+// bit), which issue far faster than a match instruction; the lowest of them
+// adds the group's size to the warp's counter and shares the old value.
+// Counter updates of one warp land in program order, so ranks are stable.
 template <int IPT>
 __device__ inline void warp_rank(const uint64_t (&k)[IPT], uint32_t valid_mask, int sh, uint32_t *whist,
-                                 uint32_t (&rank)[IPT]) {
+                                 uint32_t (&rank)[IPT], int rounds = IPT) {
     const uint32_t lt = lanemask_lt();
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int i = 0; i < IPT; i++) {
+        if (i >= rounds) break;  // warp-uniform: no valid key in rounds >= rounds
         const bool valid = (valid_mask >> i) & 1u;
-        const uint32_t d = valid ? (uint32_t)((k[i] >> sh) & 0xFF) : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
-        uint32_t b = 0;
-        if (valid) b = whist[d];
-        __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) whist[d] = b + __popc(peers);
-        __syncwarp();
-        rank[i] = b + __popc(peers & lt);
+        const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+        uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? bal : ~bal;
+        }
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&whist[d], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader & 31);
+        rank[i] = base + __popc(peers & lt);
     }
+    __syncwarp();
 }
 
 // ---------------------------------------------------------------- histogram
@@ -296,6 +308,212 @@ __global__ void __launch_bounds__(SORT_TPB) k_downsweep(uint64_t *k0, V *v0, uin
         const uint32_t g = S.gbase[d] + (p - S.ldig[d]);
         ko[g] = kk;
         vo[g] = S.v[p];
+    }
+}
+
+// ---------------------------------------------------------------- cooperative sort
+// All digit passes of one sort in one cooperative launch: CTA t owns tile t
+// (COOP_TILE keys) in every pass.  A pass is: load the tile, rank it by the
+// pass digit, publish the tile's digit counts; grid barrier; CTAs scan the
+// count columns (one digit each); grid barrier; every CTA adds its column
+// offsets to the global digit bases, reorders its tile through shared
+// memory and writes it out; grid barrier before the next pass reads.  The
+// three grid barriers replace the reduce-then-scan sort's three launches
+// per digit and its separate histogram pass.  Every barrier wait is bounded:
+// after BAR_SPIN_LIMIT polls the CTA records ERR_TIMEOUT and goes on, so
+// the kernel always ends.
+
+constexpr uint32_t BAR_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t target, uint32_t *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        uint32_t it = 0;
+        while (ld_acquire_gpu(bar) < target) {
+            if (++it > BAR_SPIN_LIMIT) {
+                if (err) atomicOr(err, ERR_TIMEOUT);
+                break;
+            }
+            if (it > 64) __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+template <typename V>
+struct CoopSmem {
+    uint64_t k[COOP_TILE];
+    V v[COOP_TILE];
+    uint32_t whist[8][256];
+    uint32_t gbase[256];
+    uint32_t ldig[256];
+    uint32_t wsum[8];
+};
+
+template <typename V>
+__device__ __forceinline__ V ld_cg(const V *p) {
+    return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ uint16_t ld_cg<uint16_t>(const uint16_t *p) {
+    return (uint16_t)__ldcg(reinterpret_cast<const unsigned short *>(p));
+}
+
+// Tile t is keys [t * tile_len, min(n, (t+1) * tile_len)), tile_len <=
+// COOP_TILE; warp w of a tile takes a contiguous run of ceil(tile_len / 8)
+// of them.  counts is [256][G] (digit-major, for the column scans), offs
+// [G][256] (tile-major, one row per CTA), totals [256].
+template <typename V>
+__global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n,
+                                                           uint32_t tile_len, SortMask mask, uint32_t *counts,
+                                                           uint32_t *offs, uint32_t *totals, uint32_t *bar,
+                                                           uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CoopSmem<V> &S = *reinterpret_cast<CoopSmem<V> *>(smem_raw);
+    const uint32_t G = gridDim.x, tile = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t act = active_bytes(mask);
+    const uint64_t base = (uint64_t)tile * tile_len;
+    const uint32_t nvalid = (uint32_t)umin64(tile_len, n - base);
+    const uint32_t pw = (tile_len + 7) / 8;  // keys per warp
+    const uint32_t wbeg = (uint32_t)umin64((uint64_t)w * pw, nvalid), wend = (uint32_t)umin64(wbeg + pw, nvalid);
+    const int rounds = (int)((wend - wbeg + 31) / 32);
+    uint32_t target = 0;
+    int pass = 0;
+    for (int byte = 0; byte < 8; byte++) {
+        if (!((act >> byte) & 1u)) continue;
+        const int sh = 8 * byte;
+        const bool odd = pass & 1;
+        const uint64_t *ki = odd ? k1 : k0;
+        const V *vi = odd ? v1 : v0;
+        uint64_t *ko = odd ? k0 : k1;
+        V *vo = odd ? v0 : v1;
+        for (int i = tid; i < 8 * 256; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
+        __syncthreads();
+        // keys written by other CTAs in the previous pass: load through L2
+        uint64_t k[COOP_IPT];
+        V v[COOP_IPT];
+        uint32_t vmask = 0;
+#pragma unroll
+        for (int i = 0; i < COOP_IPT; i++) {
+            const uint32_t q = wbeg + i * 32 + lane;
+            if (q < wend) {
+                k[i] = __ldcg(ki + base + q);
+                v[i] = ld_cg<V>(vi + base + q);
+                vmask |= 1u << i;
+            } else {
+                k[i] = ~0ull;
+                v[i] = V(0);
+            }
+        }
+        uint32_t rank[COOP_IPT];
+        warp_rank<COOP_IPT>(k, vmask, sh, S.whist[w], rank, rounds);
+        __syncthreads();
+        uint32_t tcount = 0;
+#pragma unroll
+        for (int ww = 0; ww < 8; ww++) {
+            const uint32_t c = S.whist[ww][tid];
+            S.whist[ww][tid] = tcount;
+            tcount += c;
+        }
+        counts[(size_t)tid * G + tile] = tcount;
+        S.ldig[tid] = block_excl_scan_256(tcount, S.wsum, nullptr);
+        target += G;
+        grid_barrier(bar, target, err);
+        // column scans: offs[d][t] = sum of counts[d][t' < t], totals[d].
+        // Groups of S threads (S = G rounded up to a power of two) scan one
+        // column each, so the 256 columns take one or two rounds of the grid
+        // whatever G is (G <= 512; above 256 a thread takes two entries).
+        if (G > 256) {
+            // thread tid takes the adjacent entries 2 tid and 2 tid + 1
+            const uint32_t i0 = 2 * (uint32_t)tid, i1 = i0 + 1;
+            for (uint32_t d = tile; d < 256; d += G) {
+                const uint32_t *c = counts + (size_t)d * G;
+                const uint32_t x0 = i0 < G ? __ldcg(c + i0) : 0u;
+                const uint32_t x1 = i1 < G ? __ldcg(c + i1) : 0u;
+                uint32_t tot = 0;
+                const uint32_t e = block_excl_scan_256(x0 + x1, S.wsum, &tot);
+                if (i0 < G) offs[(size_t)i0 * 256 + d] = e;
+                if (i1 < G) offs[(size_t)i1 * 256 + d] = e + x0;
+                if (tid == 0) totals[d] = tot;
+            }
+        } else {
+            const uint32_t Sg = G <= 1 ? 1u : 1u << (32 - __clz(G - 1));  // power of two >= G
+            const uint32_t per = 256 / Sg, grp = tid / Sg, t = tid % Sg;
+            for (uint32_t d0 = tile * per; d0 < 256; d0 += G * per) {
+                const uint32_t d = d0 + grp;
+                const bool live = d < 256 && t < G;
+                const uint32_t x = live ? __ldcg(counts + (size_t)d * G + t) : 0u;
+                uint32_t v = x, tot;
+                if (Sg <= 32) {
+                    for (uint32_t o = 1; o < Sg; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o, Sg);
+                        if (t >= o) v += y;
+                    }
+                    tot = __shfl_sync(0xffffffffu, v, Sg - 1, Sg);
+                } else {
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+                        if (lane >= o) v += y;
+                    }
+                    if (lane == 31) S.wsum[w] = v;
+                    __syncthreads();
+                    const int wpg = (int)(Sg / 32), w0 = w - w % wpg;
+                    uint32_t pre = 0;
+                    tot = 0;
+                    for (int ww = w0; ww < w0 + wpg; ww++) {
+                        if (ww < w) pre += S.wsum[ww];
+                        tot += S.wsum[ww];
+                    }
+                    v += pre;
+                    __syncthreads();
+                }
+                if (live) offs[(size_t)t * 256 + d] = v - x;
+                if (d < 256 && t == 0) totals[d] = tot;
+            }
+        }
+        target += G;
+        grid_barrier(bar, target, err);
+        {
+            const uint32_t T = __ldcg(totals + tid);
+            const uint32_t o = __ldcg(offs + (size_t)tile * 256 + tid);
+            const uint32_t gb = block_excl_scan_256(T, S.wsum, nullptr);
+            S.gbase[tid] = gb + o;
+        }
+#pragma unroll
+        for (int i = 0; i < COOP_IPT; i++) {
+            if ((vmask >> i) & 1u) {
+                const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+                S.k[pos] = k[i];
+                S.v[pos] = v[i];
+            }
+        }
+        __syncthreads();
+        for (uint32_t p = tid; p < nvalid; p += SORT_TPB) {
+            const uint64_t kk = S.k[p];
+            const uint32_t d = (uint32_t)((kk >> sh) & 0xFF);
+            const uint32_t g = S.gbase[d] + (p - S.ldig[d]);
+            if (g < n) {  // always, unless a barrier wait gave up
+                ko[g] = kk;
+                vo[g] = S.v[p];
+            }
+        }
+        pass++;
+        if (act >> (byte + 1)) {
+            target += G;
+            grid_barrier(bar, target, err);
+        }
     }
 }
 
@@ -481,11 +699,36 @@ cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_
     return scan_impl<uint8_t>(in, out, n, total, tmp, st);
 }
 
+uint32_t g_coop_max_ctas[3];  // resident CTAs of k_coop_sort<u16/u32/u64>, set by sort_prepare
+
+template <typename V>
+constexpr int coop_slot() {
+    return sizeof(V) == 2 ? 0 : (sizeof(V) == 4 ? 1 : 2);
+}
+
 template <typename V>
 static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
                              cudaStream_t st) {
     if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
+    // cooperative sort: tiles of at least COOP_MIN_TILE keys, spread over
+    // every resident CTA slot so that the SMs carry equal work
+    const uint32_t maxG = g_coop_max_ctas[coop_slot<V>()] < 512u ? g_coop_max_ctas[coop_slot<V>()] : 512u;
+    const uint32_t tile_len = maxG ? std::max<uint32_t>(COOP_MIN_TILE, (n + maxG - 1) / maxG) : 0u;
+    const uint32_t G = tile_len ? (n + tile_len - 1) / tile_len : 0u;
+    if (s.bar && n > (uint32_t)SORT_TILE && tile_len && tile_len <= (uint32_t)COOP_TILE && G <= maxG &&
+        s.status_words >= 512 * (size_t)G + 256) {
+        if ((e = cudaMemsetAsync(s.bar, 0, sizeof(uint32_t), st))) return e;
+        uint32_t *counts = s.status, *offs = s.status + 256 * (size_t)G, *totals = s.status + 512 * (size_t)G;
+        uint32_t *bar = s.bar, *err = s.err;
+        uint32_t tl = tile_len;
+        void *args[] = {&k0, &v0, &k1, &v1, &n, &tl, &mask, &counts, &offs, &totals, &bar, &err};
+        ProfScope ps("sort_coop", st);
+        e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V>, dim3(G), dim3(SORT_TPB), args,
+                                        sizeof(CoopSmem<V>), st);
+        note_launch();
+        return e;
+    }
     if (n <= (uint32_t)SORT_TILE) {
         const size_t sm = sizeof(SmallSmem<V>);
         ProfScope ps("sort_small", st);
@@ -525,6 +768,11 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
 
 // Shared-memory opt-ins of the sort kernels, set once outside any stream
 // capture.
+uint32_t coop_sort_max_keys() {
+    const uint32_t g = g_coop_max_ctas[0] < 512u ? g_coop_max_ctas[0] : 512u;
+    return g * (uint32_t)COOP_TILE;
+}
+
 cudaError_t sort_prepare() {
     static bool done = false;
     if (done) return cudaSuccess;
@@ -541,6 +789,26 @@ cudaError_t sort_prepare() {
     if ((e = cudaFuncSetAttribute(k_downsweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(PassSmem<uint64_t>))))
         return e;
+    {
+        int dev = 0, sms = 0, per[3] = {0, 0, 0};
+        if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+            return e;
+        if ((e = cudaFuncSetAttribute(k_coop_sort<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint16_t>))) ||
+            (e = cudaFuncSetAttribute(k_coop_sort<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint32_t>))) ||
+            (e = cudaFuncSetAttribute(k_coop_sort<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint64_t>))))
+            return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_coop_sort<uint16_t>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint16_t>))) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_coop_sort<uint32_t>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint32_t>))) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_coop_sort<uint64_t>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint64_t>))))
+            return e;
+        for (int i = 0; i < 3; i++) g_coop_max_ctas[i] = (uint32_t)(per[i] * sms);
+    }
     done = true;
     return cudaSuccess;
 }

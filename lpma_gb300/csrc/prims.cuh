@@ -15,6 +15,11 @@ struct SortScratch {
     uint32_t *status = nullptr;    // (digit, tile) counts and offsets of one pass
     uint32_t *counters = nullptr;  // unused by the reduce-then-scan passes
     size_t status_words = 0;
+    // Set both to sort batches of up to coop_sort_max_keys() keys in one
+    // cooperative launch: bar is a barrier counter word (cleared by the
+    // sort), err receives ERR_TIMEOUT if a bounded barrier wait gives up.
+    uint32_t *bar = nullptr;
+    uint32_t *err = nullptr;
 };
 
 // Digit bytes to sort: host_mask, intersected (when andor is set) with the
@@ -58,14 +63,27 @@ template <typename V>
 cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uint64_t diff_bits,
                        SortScratch &s, uint32_t *err, cudaStream_t st, int *which);
 
-// Bytes of scratch status words needed for n keys.
-inline size_t sort_status_words(uint32_t n) {
-    size_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
-    return 2 * tiles * 256 + 2;  // per-pass (digit, tile) counts and offsets
+// Status words needed for n keys: per-pass (digit, tile) counts and
+// offsets of the reduce-then-scan passes (tiles of SORT_TILE keys), or of
+// the cooperative sort (tiles of at least COOP_MIN_TILE keys, plus 256
+// digit totals), whichever is larger.
+constexpr int COOP_MIN_TILE = 1024;
+constexpr size_t sort_status_words(uint32_t n) {
+    return (2 * (((size_t)n + SORT_TILE - 1) / SORT_TILE) * 256 + 2) >
+                   (512 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 256)
+               ? (2 * (((size_t)n + SORT_TILE - 1) / SORT_TILE) * 256 + 2)
+               : (512 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 256);
 }
 
 // One-time kernel attribute setup (outside stream capture).
 cudaError_t sort_prepare();
+
+// Keys per tile of the cooperative sort, and the largest batch it takes on
+// this device (tiles that can be resident at once x tile); valid after
+// sort_prepare().
+constexpr int COOP_IPT = 16;
+constexpr int COOP_TILE = SORT_TPB * COOP_IPT;  // 4096 keys per CTA
+uint32_t coop_sort_max_keys();
 
 // Exclusive scan of n u32 values; out may alias in.  total (device, may be
 // null) receives the sum.  tmp needs scan_tmp_words(n) words.

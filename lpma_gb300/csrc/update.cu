@@ -219,8 +219,9 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
     const bool odd = sort_result_odd(mask, n);
     const uint64_t *__restrict__ skey = odd ? k1 : k0;
     const uint16_t *__restrict__ spay = odd ? p1 : p0;
-    // a rejected batch (validation in k_pack) changes nothing
-    const bool rejected = (st->error & ERR_KEY) != 0;
+    // a rejected batch (validation in k_pack), or one whose sort gave up a
+    // bounded wait, changes nothing
+    const bool rejected = (st->error & (ERR_KEY | ERR_TIMEOUT)) != 0;
     // persistent grid: the top TOPL levels are staged once per CTA and the
     // CTA walks 256-entry chunks; chunk c writes its counts to blk_*[c]
     __shared__ ulonglong2 top[TOPN];
@@ -953,7 +954,8 @@ constexpr int GT_TPB = 256;  // 32 groups of 8 lanes: one 32-segment tile per CT
 __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
                                                    Geo src, const uint32_t *__restrict__ PQ,
                                                    const uint32_t *__restrict__ US, const UpdList u, uint32_t thres,
-                                                   uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv) {
+                                                   uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv, uint64_t m_cap,
+                                                   DevStatus *st) {
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const TileJob J = jobs[find_job(jobs, njobs, tile, false)];
@@ -994,8 +996,13 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
                 uint32_t below = 0;
                 if (ue > us) below = u.ip[lb_key(u.key, us, ue, k[q])] - ip0;
                 const uint64_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
-                Mk[r] = k[q];
-                Mv[r] = v[q];
+                if (r < m_cap) {
+                    Mk[r] = k[q];
+                    Mv[r] = v[q];
+                } else {  // only if the update list broke its sortedness invariant
+                    atomicOr(&st->sticky, ERR_INTERNAL);
+                    st->err_info[1] = 4;
+                }
             }
         }
         __syncwarp();
@@ -1010,8 +1017,9 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
 __global__ void __launch_bounds__(TPB) k_gather_ins(const TileJob *__restrict__ jobs, uint32_t njobs, Geo src,
                                                     const uint32_t *__restrict__ PQ,
                                                     const uint32_t *__restrict__ US, const UpdList u,
-                                                    const DevStatus *st, uint32_t n_cap, uint32_t thres,
-                                                    uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv) {
+                                                    DevStatus *st, uint32_t n_cap, uint32_t thres,
+                                                    uint64_t *__restrict__ Mk, uint8_t *__restrict__ Mv,
+                                                    uint64_t m_cap) {
     const uint32_t nu = min(st->n_u, n_cap);
     for (uint32_t x = blockIdx.x * TPB + threadIdx.x; x < nu; x += gridDim.x * TPB) {
         if (u.kind[x] != KIND_INS) continue;
@@ -1042,16 +1050,21 @@ __global__ void __launch_bounds__(TPB) k_gather_ins(const TileJob *__restrict__ 
                 expired_below += (sv[t] != VAL_TOMB && (sk[t] & TIME_MASK) < (uint64_t)thres) ? 1u : 0u;
         }
         const uint64_t r = (uint64_t)PQ[s] + ri + (pos - tomb_below - expired_below);
-        Mk[r] = y;
-        Mv[r] = u.val[x];
+        if (r < m_cap) {
+            Mk[r] = y;
+            Mv[r] = u.val[x];
+        } else {  // only if the update list broke its sortedness invariant
+            atomicOr(&st->sticky, ERR_INTERNAL);
+            st->err_info[1] = 5;
+        }
     }
 }
 
 __global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
                                                    Geo dst, const uint64_t *__restrict__ Mk,
-                                                   const uint8_t *__restrict__ Mv, const uint32_t *__restrict__ PQ,
-                                                   uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent, uint32_t V,
-                                                   DevStatus *st) {
+                                                   const uint8_t *__restrict__ Mv, uint64_t m_cap,
+                                                   const uint32_t *__restrict__ PQ, uint8_t *cnt_d, ulonglong2 *fl_d,
+                                                   uint32_t *sent, uint32_t V, DevStatus *st) {
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const TileJob J = jobs[find_job(jobs, njobs, tile, true)];
@@ -1062,6 +1075,7 @@ __global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ j
             atomicOr(&st->sticky, ERR_INTERNAL);
             st->err_info[1] = 2;
         }
+        if (mb + J.m > m_cap) continue;  // reported above; never read past M
         const uint64_t ds = J.da + k;
         const uint64_t j = heap_of_linear(ds, dst.H);
         const uint64_t f0 = first_rank(k, J.m, J.df), f1 = first_rank(k + 1, J.m, J.df);
@@ -1228,19 +1242,21 @@ void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *q
 
 void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
                      const uint32_t *PQ, const uint32_t *US, const UpdList u, uint32_t n_upd, uint32_t thres,
-                     uint64_t *Mk, uint8_t *Mv, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d, uint32_t *sent,
-                     uint32_t V, DevStatus *st, cudaStream_t s) {
+                     uint64_t *Mk, uint8_t *Mv, uint64_t m_cap, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
+                     uint32_t *sent, uint32_t V, DevStatus *st, cudaStream_t s) {
     if (!njobs) return;
     {
         ProfScope ps_("exec_gather", s);
-        k_gather<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv);
+        k_gather<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv,
+                                                                 m_cap, st);
         if (n_upd)
-            k_gather_ins<<<grid_for(n_upd, TPB), TPB, 0, s>>>(jobs, njobs, src, PQ, US, u, st, n_upd, thres, Mk, Mv);
+            k_gather_ins<<<grid_for(n_upd, TPB), TPB, 0, s>>>(jobs, njobs, src, PQ, US, u, st, n_upd, thres, Mk, Mv,
+                                                              m_cap);
     }
     {
         ProfScope ps_("exec_spread", s);
-        k_spread<<<grid_for(dtiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, dtiles, dst, Mk, Mv, PQ, cnt_d, fl_d,
-                                                                 sent, V, st);
+        k_spread<<<grid_for(dtiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, dtiles, dst, Mk, Mv, m_cap, PQ, cnt_d,
+                                                                 fl_d, sent, V, st);
     }
     note_launch(n_upd ? 3 : 2);
 }
