@@ -46,7 +46,8 @@ typedef enum {
     LPMA_ERR_INTERNAL = 6,         /* a device-side consistency check failed */
     LPMA_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
     LPMA_ERR_BUFFER_TOO_SMALL = 8,
-    LPMA_ERR_SCRATCH_LIMIT = 9     /* n above the fixed scratch of lpma_shuffle_static */
+    LPMA_ERR_SCRATCH_LIMIT = 9,    /* n above the fixed scratch of lpma_shuffle_static */
+    LPMA_ERR_IO = 10               /* a file is missing, unreadable or malformed */
 } lpma_status_t;
 
 enum { LPMA_KEY_PACKED = 0, LPMA_KEY_PAIR32 = 1 };
@@ -158,6 +159,70 @@ LPMA_API lpma_status_t lpma_info(const LpmaHandle *h, uint32_t *height, uint64_t
 LPMA_API lpma_status_t lpma_destroy(LpmaHandle *h);
 
 LPMA_API const char *lpma_status_string(lpma_status_t s);
+
+/* ---- read paths: they read the structure in place (no CSR view is built)
+ * and order after earlier work on `stream` (use the update stream). ---- */
+
+/* Replaces query_rpma(RPMA&, DEV_VEC_SIZE& srcs, DEV_VEC_KEY& constraints,
+ * offset, len, edgelist, v_list) (rpma.cuh:1974-2036): for query i, the
+ * neighbours of d_srcs[i] whose timestamp t has lb <= t <= ub, where
+ * d_windows[i] = lb << 32 | ub, in key order (dst ascending, then t).
+ * d_offsets (n + 1 device entries) receives the start of each list (its
+ * last entry the total), d_nbrs / d_vals (device, cap entries) the neighbour
+ * ids and values, *total the number of neighbours.  With d_nbrs NULL only
+ * the offsets and the total are produced; with total > cap the call returns
+ * LPMA_ERR_BUFFER_TOO_SMALL after the offsets.  The reference sorts the
+ * caller's queries and returns the lists in that order with sentinel markers
+ * between them; here the lists follow the caller's order and hold
+ * neighbours only.  A query with src >= V gets an empty list.  Synchronises
+ * the stream once, to read the total. */
+LPMA_API lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const uint64_t *d_windows, size_t n,
+                                            uint32_t *d_offsets, uint32_t *d_nbrs, uint8_t *d_vals, size_t cap,
+                                            size_t *total, lpma_stream_t stream);
+
+/* Edge query (check_edge_kernel rpma.cuh:2040-2066; result check
+ * test.cu:46-62): d_counts[i] = number of stored keys (src, dst, t') for
+ * query key (src, dst, t) with t - window <= t' <= t.  window = t = 0xFFFFF
+ * counts every timestamp, as check_edge_kernel (which ignores time) does.
+ * src >= V or dst >= 0x3FFFFE counts 0.  Asynchronous. */
+LPMA_API lpma_status_t lpma_edge_query(LpmaHandle *h, const uint64_t *d_keys, size_t n, uint32_t window,
+                                       uint32_t *d_counts, lpma_stream_t stream);
+
+/* Directed BFS over the stored edges from d_sources, the analytics step of
+ * test.cu:168-183 (nvGRAPH BFS over the exported CSR): d_dist (V int32,
+ * device) receives hop counts from the nearest source, INT32_MAX where
+ * unreached (nvGRAPH's convention).  max_depth bounds the levels (0: no
+ * bound; 2 for a 2-hop BFS from many seeds).  levels / reached (may be
+ * NULL) receive the levels expanded and the vertices reached.  Synchronises
+ * once per level. */
+LPMA_API lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_sources, uint32_t max_depth,
+                                int32_t *d_dist, uint32_t *levels, uint64_t *reached, lpma_stream_t stream);
+
+/* PageRank over the stored edges (test_algos.cu:44-90 runs nvGRAPH's on the
+ * CSR), in f64: from rank = 1/V, `iterations` times
+ *   rank[v] = (1 - alpha)/V + alpha * (sum over edges u->v of rank[u]/outdeg(u) + dangling/V)
+ * where dangling sums the rank of vertices without out-edges.  d_rank: V
+ * doubles on the device.  Asynchronous. */
+LPMA_API lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, double *d_rank,
+                                     lpma_stream_t stream);
+
+/* ---- edgelist files (README.md:9-20) ---- */
+
+/* read_edgelist (test_update_rpma.cu:175-192) and
+ * read_edgelist_and_timestamps (test.cu:191-221): "N E" then E lines
+ * "src dst"; timestamps_path (may be NULL) holds E timestamps, one per
+ * edge.  Writes keys src << 42 | dst << 20 | t into h_keys (host).  With
+ * cap < E it returns LPMA_ERR_BUFFER_TOO_SMALL after setting *num_vertices
+ * and *num_edges (h_keys may then be NULL).  LPMA_ERR_IO for a missing or
+ * malformed file, an id >= N, an id >= 0x3FFFFE or a timestamp >= 2^20. */
+LPMA_API lpma_status_t lpma_read_edgelist(const char *path, const char *timestamps_path, uint64_t *h_keys, size_t cap,
+                                          uint32_t *num_vertices, size_t *num_edges);
+
+/* read_queries (test.cu:223-241): "Q" then Q lines "src lb ub"; writes
+ * h_srcs[i] = src and h_windows[i] = lb << 32 | ub (host).  Sizing and
+ * errors as lpma_read_edgelist. */
+LPMA_API lpma_status_t lpma_read_queries(const char *path, uint32_t *h_srcs, uint64_t *h_windows, size_t cap,
+                                         size_t *num_queries);
 
 /* ---- synthetic workload (device generator; the same integer arithmetic
  * as the CPU workload generator used by the tests) ---- */

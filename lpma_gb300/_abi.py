@@ -13,7 +13,7 @@ LPMA_OK = 0
 STATUS_NAMES = {
     0: "LPMA_OK", 1: "LPMA_ERR_INVALID_ARGUMENT", 2: "LPMA_ERR_INVALID_KEY", 3: "LPMA_ERR_OUT_OF_MEMORY",
     4: "LPMA_ERR_CUDA", 5: "LPMA_ERR_CAPACITY", 6: "LPMA_ERR_INTERNAL", 7: "LPMA_ERR_TIMEOUT",
-    8: "LPMA_ERR_BUFFER_TOO_SMALL", 9: "LPMA_ERR_SCRATCH_LIMIT",
+    8: "LPMA_ERR_BUFFER_TOO_SMALL", 9: "LPMA_ERR_SCRATCH_LIMIT", 10: "LPMA_ERR_IO",
 }
 KEY_PACKED, KEY_PAIR32 = 0, 1
 MAX_HEIGHT = 24
@@ -23,7 +23,8 @@ EXPORTS = [
     "lpma_config_default", "lpma_create", "lpma_build", "lpma_update", "lpma_update_host", "lpma_csr_view",
     "lpma_to_csr", "lpma_export_sorted", "lpma_export_layout", "lpma_info", "lpma_destroy", "lpma_status_string",
     "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches", "lpma_prof_enable", "lpma_prof_report",
-    "lpma_shuffle_static",
+    "lpma_shuffle_static", "lpma_query_neighbors", "lpma_edge_query", "lpma_bfs", "lpma_pagerank",
+    "lpma_read_edgelist", "lpma_read_queries",
 ]
 SHUFFLE_STATIC_MAX_KEYS = 65536
 
@@ -89,6 +90,12 @@ def load():
         "lpma_gen_rmat": [U64, U32, U32, U32, U32, U32, P, SZ, P, P],
         "lpma_shuffle": [U64, P, SZ, P],
         "lpma_shuffle_static": [U64, P, SZ, P],
+        "lpma_query_neighbors": [P, P, P, SZ, P, P, P, SZ, P, P],
+        "lpma_edge_query": [P, P, SZ, U32, P, P],
+        "lpma_bfs": [P, P, SZ, U32, P, P, P, P],
+        "lpma_pagerank": [P, ctypes.c_double, U32, P, P],
+        "lpma_read_edgelist": [ctypes.c_char_p, ctypes.c_char_p, P, SZ, P, P],
+        "lpma_read_queries": [ctypes.c_char_p, P, P, SZ, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -102,6 +102,13 @@ struct LpmaHandle {
     std::vector<FrontGraph> graphs;
     uint64_t graph_clock = 0;
     bool host_staged = false;    // h2d already holds the staged input bytes
+    // read paths (neighbour query, BFS, PageRank)
+    uint32_t *q_cnt = nullptr, *q_tmp = nullptr;
+    size_t q_cap = 0;
+    uint32_t *bfs_a = nullptr, *bfs_b = nullptr, *bfs_cnt = nullptr;
+    uint32_t *pr_deg = nullptr;
+    double *pr_contrib = nullptr, *pr_acc = nullptr, *pr_dangling = nullptr;
+    uint32_t *pin_word = nullptr;  // pinned: totals read back by the read paths
 };
 
 namespace {
@@ -678,6 +685,9 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     dfree(h->jobs_d);
     dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
     dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals), dfree(h->exp_keys), dfree(h->exp_vals);
+    dfree(h->q_cnt), dfree(h->q_tmp), dfree(h->bfs_a), dfree(h->bfs_b), dfree(h->bfs_cnt);
+    dfree(h->pr_deg), dfree(h->pr_contrib), dfree(h->pr_acc), dfree(h->pr_dangling);
+    if (h->pin_word) cudaFreeHost(h->pin_word);
     delete h;
     return LPMA_OK;
 }
@@ -881,6 +891,107 @@ lpma_status_t lpma_info(const LpmaHandle *h, uint32_t *height, uint64_t *num_ite
     return LPMA_OK;
 }
 
+lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const uint64_t *d_windows, size_t n,
+                                   uint32_t *d_offsets, uint32_t *d_nbrs, uint8_t *d_vals, size_t cap, size_t *total,
+                                   lpma_stream_t stream) {
+    if (!h || !total || (n && (!d_srcs || !d_windows)) || !d_offsets || (d_nbrs && !d_vals))
+        return LPMA_ERR_INVALID_ARGUMENT;
+    if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!h->pin_word) CK(cudaMallocHost(&h->pin_word, 2 * sizeof(uint32_t)));
+    if (n > h->q_cap) {
+        dfree(h->q_cnt), dfree(h->q_tmp);
+        h->q_cap = 0;
+        const size_t c = std::max<size_t>(n, 1024);
+        CK(dalloc(&h->q_cnt, c));
+        CK(dalloc(&h->q_tmp, scan_tmp_words((uint32_t)c) + 64));
+        h->q_cap = c;
+    }
+    Geo g{h->c.keys, h->c.vals, h->H};
+    if (n) {
+        launch_nbr_count(d_srcs, d_windows, (uint32_t)n, g, h->c.cnt, h->sent, h->V, h->q_cnt, s);
+        CK(scan_u32(h->q_cnt, d_offsets, (uint32_t)n, d_offsets + n, h->q_tmp, s));
+    } else {
+        CK(cudaMemsetAsync(d_offsets, 0, sizeof(uint32_t), s));
+    }
+    CK(cudaMemcpyAsync(h->pin_word, d_offsets + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *total = h->pin_word[0];
+    if (!d_nbrs || !n) return LPMA_OK;
+    if (*total > cap) return LPMA_ERR_BUFFER_TOO_SMALL;
+    launch_nbr_fill(d_srcs, d_windows, (uint32_t)n, g, h->c.cnt, h->sent, h->V, d_offsets, d_nbrs, d_vals, s);
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_edge_query(LpmaHandle *h, const uint64_t *d_keys, size_t n, uint32_t window, uint32_t *d_counts,
+                              lpma_stream_t stream) {
+    if (!h || (n && (!d_keys || !d_counts)) || n >= (1u << 31)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    if (!n) return LPMA_OK;
+    launch_edge_query(d_keys, (uint32_t)n, window, Geo{h->c.keys, h->c.vals, h->H}, h->c.cnt, h->c.fl, h->sent, h->V,
+                      d_counts, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_sources, uint32_t max_depth, int32_t *d_dist,
+                       uint32_t *levels, uint64_t *reached, lpma_stream_t stream) {
+    if (!h || !d_dist || (n_sources && !d_sources) || n_sources >= (1u << 31)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!h->pin_word) CK(cudaMallocHost(&h->pin_word, 2 * sizeof(uint32_t)));
+    if (!h->bfs_a) {
+        CK(dalloc(&h->bfs_a, h->V));
+        CK(dalloc(&h->bfs_b, h->V));
+        CK(dalloc(&h->bfs_cnt, 2));
+    }
+    CK(cudaMemsetAsync(h->bfs_cnt, 0, 2 * sizeof(uint32_t), s));
+    launch_bfs_init(d_sources, (uint32_t)n_sources, h->V, d_dist, h->bfs_a, h->bfs_cnt, s);
+    CK(cudaMemcpyAsync(h->pin_word, h->bfs_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    uint32_t nf = h->pin_word[0], lv = 0;
+    uint64_t total = nf;
+    uint32_t *cur = h->bfs_a, *nxt = h->bfs_b;
+    const Geo g{h->c.keys, h->c.vals, h->H};
+    while (nf > 0 && (max_depth == 0 || lv < max_depth)) {
+        CK(cudaMemsetAsync(h->bfs_cnt + 1, 0, sizeof(uint32_t), s));
+        launch_bfs_expand(cur, h->bfs_cnt, nf, (int32_t)lv, g, h->c.cnt, h->sent, d_dist, nxt, h->bfs_cnt + 1, s);
+        CK(cudaMemcpyAsync(h->bfs_cnt, h->bfs_cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(h->pin_word, h->bfs_cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        nf = h->pin_word[0];
+        total += nf;
+        lv++;
+        std::swap(cur, nxt);
+    }
+    if (levels) *levels = lv;
+    if (reached) *reached = total;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, double *d_rank, lpma_stream_t stream) {
+    if (!h || !d_rank || !(alpha >= 0.0 && alpha <= 1.0)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!h->pr_deg) {
+        CK(dalloc(&h->pr_deg, h->V));
+        CK(dalloc(&h->pr_contrib, h->V));
+        CK(dalloc(&h->pr_acc, h->V));
+        CK(dalloc(&h->pr_dangling, 1));
+    }
+    const Geo g{h->c.keys, h->c.vals, h->H};
+    CK(cudaMemsetAsync(h->pr_deg, 0, sizeof(uint32_t) * h->V, s));
+    CK(cudaMemsetAsync(h->pr_acc, 0, sizeof(double) * h->V, s));
+    launch_outdeg(g, h->c.cnt, h->pr_deg, s);
+    launch_fill_f64(d_rank, h->V, 1.0 / (double)h->V, s);
+    for (uint32_t it = 0; it < iterations; it++)
+        launch_pr_iteration(g, h->c.cnt, h->pr_deg, h->V, alpha, d_rank, h->pr_contrib, h->pr_acc, h->pr_dangling, s);
+    CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
 const char *lpma_status_string(lpma_status_t s) {
     switch (s) {
         case LPMA_OK: return "ok";
@@ -893,6 +1004,7 @@ const char *lpma_status_string(lpma_status_t s) {
         case LPMA_ERR_TIMEOUT: return "bounded device wait gave up";
         case LPMA_ERR_BUFFER_TOO_SMALL: return "buffer too small";
         case LPMA_ERR_SCRATCH_LIMIT: return "n exceeds the fixed scratch of this entry point";
+        case LPMA_ERR_IO: return "file missing, unreadable or malformed";
     }
     return "unknown status";
 }

@@ -107,4 +107,23 @@ void launch_unique_flags(const uint64_t *keys, uint64_t n, uint32_t *flags, cuda
 void launch_scatter_flags(const uint64_t *keys, const uint32_t *pos, const uint32_t *flags, uint64_t n,
                           uint64_t *out, cudaStream_t s);
 
+
+// ---- read paths over the PMA (query.cu)
+void launch_nbr_count(const uint32_t *srcs, const uint64_t *windows, uint32_t n, Geo g, const uint8_t *cnt,
+                      const uint32_t *sent, uint32_t V, uint32_t *qcnt, cudaStream_t s);
+void launch_nbr_fill(const uint32_t *srcs, const uint64_t *windows, uint32_t n, Geo g, const uint8_t *cnt,
+                     const uint32_t *sent, uint32_t V, const uint32_t *offsets, uint32_t *nbrs, uint8_t *vals,
+                     cudaStream_t s);
+void launch_edge_query(const uint64_t *q, uint32_t n, uint32_t window, Geo g, const uint8_t *cnt,
+                       const ulonglong2 *fl, const uint32_t *sent, uint32_t V, uint32_t *res, cudaStream_t s);
+void launch_bfs_init(const uint32_t *sources, uint32_t n, uint32_t V, int32_t *dist, uint32_t *frontier,
+                     uint32_t *count, cudaStream_t s);
+void launch_bfs_expand(const uint32_t *frontier, const uint32_t *nf, uint32_t nf_host, int32_t level, Geo g,
+                       const uint8_t *cnt, const uint32_t *sent, int32_t *dist, uint32_t *next, uint32_t *next_count,
+                       cudaStream_t s);
+void launch_outdeg(Geo g, const uint8_t *cnt, uint32_t *deg, cudaStream_t s);
+void launch_fill_f64(double *p, uint64_t n, double x, cudaStream_t s);
+void launch_pr_iteration(Geo g, const uint8_t *cnt, const uint32_t *deg, uint32_t V, double alpha, double *rank,
+                         double *contrib, double *acc, double *dangling, cudaStream_t s);
+
 }  // namespace lpma

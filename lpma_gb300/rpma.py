@@ -179,6 +179,57 @@ class Lpma:
                                          _stream_ptr(self.stream)), "lpma_export_layout")
         return k, v, sent, h.value
 
+    # -------------------------------------------------------------- read paths
+    def query_neighbors(self, srcs, windows=None):
+        """query_rpma: neighbour lists of srcs (torch CUDA uint32/int32) with time
+        windows (torch CUDA int64, lb << 32 | ub; default every timestamp).
+        Returns torch tensors (offsets [n+1] int32, nbrs int32, values uint8)."""
+        import torch
+        n = srcs.numel()
+        dev = srcs.device
+        srcs = srcs.to(torch.int32).contiguous()
+        if windows is None:
+            windows = torch.full((n,), 0xFFFFFFFF, dtype=torch.int64, device=dev)
+        windows = windows.to(torch.int64).contiguous()
+        offsets = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        total = ctypes.c_size_t()
+        sp = _stream_ptr(self.stream)
+        check(self._L.lpma_query_neighbors(self._h, srcs.data_ptr(), windows.data_ptr(), n, offsets.data_ptr(), None,
+                                           None, 0, ctypes.byref(total), sp), "lpma_query_neighbors")
+        nbrs = torch.empty(max(total.value, 1), dtype=torch.int32, device=dev)
+        vals = torch.empty(max(total.value, 1), dtype=torch.uint8, device=dev)
+        check(self._L.lpma_query_neighbors(self._h, srcs.data_ptr(), windows.data_ptr(), n, offsets.data_ptr(),
+                                           nbrs.data_ptr(), vals.data_ptr(), nbrs.numel(), ctypes.byref(total), sp),
+              "lpma_query_neighbors")
+        return offsets, nbrs[:total.value], vals[:total.value]
+
+    def edge_query(self, keys, window=0xFFFFF):
+        """Count of stored keys (src, dst, t') with t - window <= t' <= t per query key (torch CUDA int64)."""
+        import torch
+        keys = keys.to(torch.int64).contiguous()
+        res = torch.empty(keys.numel(), dtype=torch.int32, device=keys.device)
+        check(self._L.lpma_edge_query(self._h, keys.data_ptr(), keys.numel(), int(window), res.data_ptr(),
+                                      _stream_ptr(self.stream)), "lpma_edge_query")
+        return res
+
+    def bfs(self, sources, max_depth=0):
+        """Directed BFS hop counts (torch int32 [V], INT32_MAX when unreached), levels, vertices reached."""
+        import torch
+        sources = sources.to(torch.int32).contiguous()
+        dist = torch.empty(self.num_vertices, dtype=torch.int32, device=sources.device)
+        lv, reached = ctypes.c_uint32(), ctypes.c_uint64()
+        check(self._L.lpma_bfs(self._h, sources.data_ptr(), sources.numel(), int(max_depth), dist.data_ptr(),
+                               ctypes.byref(lv), ctypes.byref(reached), _stream_ptr(self.stream)), "lpma_bfs")
+        return dist, lv.value, reached.value
+
+    def pagerank(self, alpha=0.85, iterations=20, device="cuda"):
+        """PageRank ranks (torch float64 [V]) after `iterations` power iterations."""
+        import torch
+        rank = torch.empty(self.num_vertices, dtype=torch.float64, device=device)
+        check(self._L.lpma_pagerank(self._h, float(alpha), int(iterations), rank.data_ptr(), _stream_ptr(self.stream)),
+              "lpma_pagerank")
+        return rank
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.lpma_destroy(self._h)
@@ -214,6 +265,44 @@ def destroy_rpma(rpma):
 
 
 # ------------------------------------------------------ workload generator
+def query_rpma(rpma, srcs, constraints=None):
+    """query_rpma (rpma.cuh:1974-2036): (offsets, nbrs, values), lists in the callers' query order."""
+    return rpma.query_neighbors(srcs, constraints)
+
+
+def edge_query_rpma(rpma, keys, window=0xFFFFF):
+    """Edge query (rpma.cuh:2040-2066, result check test.cu:46-62)."""
+    return rpma.edge_query(keys, window)
+
+
+def read_edgelist(path, timestamps_path=None):
+    """read_edgelist / read_edgelist_and_timestamps: (numpy uint64 keys, num_vertices)."""
+    L = _abi.load()
+    V, E = ctypes.c_uint32(), ctypes.c_size_t()
+    tp = timestamps_path.encode() if timestamps_path else None
+    rc = L.lpma_read_edgelist(path.encode(), tp, None, 0, ctypes.byref(V), ctypes.byref(E))
+    if rc not in (0, 8):
+        check(rc, "lpma_read_edgelist")
+    keys = np.empty(max(E.value, 1), np.uint64)
+    check(L.lpma_read_edgelist(path.encode(), tp, keys.ctypes.data_as(ctypes.c_void_p), keys.size, ctypes.byref(V),
+                               ctypes.byref(E)), "lpma_read_edgelist")
+    return keys[:E.value], V.value
+
+
+def read_queries(path):
+    """read_queries: (numpy uint32 srcs, numpy uint64 windows lb << 32 | ub)."""
+    L = _abi.load()
+    Q = ctypes.c_size_t()
+    rc = L.lpma_read_queries(path.encode(), None, None, 0, ctypes.byref(Q))
+    if rc not in (0, 8):
+        check(rc, "lpma_read_queries")
+    srcs = np.empty(max(Q.value, 1), np.uint32)
+    wins = np.empty(max(Q.value, 1), np.uint64)
+    check(L.lpma_read_queries(path.encode(), srcs.ctypes.data_as(ctypes.c_void_p), wins.ctypes.data_as(ctypes.c_void_p),
+                              srcs.size, ctypes.byref(Q)), "lpma_read_queries")
+    return srcs[:Q.value], wins[:Q.value]
+
+
 def rmat_thresholds(a=0.57, b=0.19, c=0.19):
     """Integer quadrant thresholds floor(p * 2^32) (IEEE double)."""
     return int(a * 4294967296.0), int((a + b) * 4294967296.0), int((a + b + c) * 4294967296.0)

@@ -235,3 +235,97 @@ def shuffle(keys, seed):
 
 def sentinel_key(v):
     return (int(v) << SRC_SHIFT) + DST_AND_TIME_END
+
+
+# ---------------------------------------------------------------- read paths
+# Restatements of the reference's read paths over a sorted key set (the
+# oracle's export_sorted()): what the device read kernels must return.
+
+TIME_MASK = 0xFFFFF
+NBR_END = 0x3FFFFE
+
+
+def _split(keys):
+    keys = np.asarray(keys, dtype=np.uint64)
+    src = (keys >> np.uint64(SRC_SHIFT)).astype(np.int64)
+    dst = ((keys >> np.uint64(20)) & np.uint64(0x3FFFFF)).astype(np.int64)
+    t = (keys & np.uint64(TIME_MASK)).astype(np.int64)
+    return src, dst, t
+
+
+def neighbors(keys, vals, srcs, windows, V):
+    """query_rpma (rpma.cuh:1827-2036) with the result check of test.cu:16-42:
+    for query i, the dst of every key of srcs[i] with lb <= t <= ub
+    (windows[i] = lb << 32 | ub), in key order; lists in query order."""
+    keys = np.asarray(keys, dtype=np.uint64)
+    vals = np.asarray(vals, dtype=np.uint8)
+    src, dst, t = _split(keys)
+    live = dst != NBR_END
+    src, dst, t, vv = src[live], dst[live], t[live], vals[live]
+    starts = np.searchsorted(src, np.arange(V + 1))
+    offs, nb, nv = [0], [], []
+    for s, w in zip(np.asarray(srcs, dtype=np.int64), np.asarray(windows, dtype=np.uint64)):
+        lb, ub = int(w) >> 32, int(w) & 0xFFFFFFFF
+        if s >= V:
+            offs.append(offs[-1])
+            continue
+        a, b = starts[s], starts[s + 1]
+        m = (t[a:b] >= lb) & (t[a:b] <= ub)
+        nb.append(dst[a:b][m])
+        nv.append(vv[a:b][m])
+        offs.append(offs[-1] + int(m.sum()))
+    cat = (lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt))
+    return np.array(offs, np.int64), cat(nb, np.int64), cat(nv, np.uint8)
+
+
+def edge_query_counts(keys, queries, window):
+    """Edge query counts (test.cu:46-62): stored keys (src, dst, t') with
+    t - window <= t' <= t for each query key (src, dst, t)."""
+    keys = np.asarray(keys, dtype=np.uint64)
+    q = np.asarray(queries, dtype=np.uint64)
+    pre = q & ~np.uint64(TIME_MASK)
+    t = (q & np.uint64(TIME_MASK)).astype(np.int64)
+    lb = np.maximum(t - int(window), 0).astype(np.uint64)
+    lo = np.searchsorted(keys, pre | lb, side="left")
+    hi = np.searchsorted(keys, pre | t.astype(np.uint64), side="right")
+    src, dst, _ = _split(q)
+    return np.where(dst >= NBR_END, 0, hi - lo).astype(np.int64)
+
+
+def bfs(keys, V, sources, max_depth=0):
+    """Directed BFS hop counts from the sources over the stored edges
+    (nvGRAPH BFS of test.cu:168-183 / test_algos.cu:136-186); 2^31-1 where
+    unreached; at most max_depth levels (0: no bound)."""
+    src, dst, _ = _split(keys)
+    live = dst != NBR_END
+    src, dst = src[live], dst[live]
+    starts = np.searchsorted(src, np.arange(V + 1))
+    INF = 2**31 - 1
+    dist = np.full(V, INF, np.int64)
+    front = np.unique(np.asarray([s for s in sources if s < V], dtype=np.int64))
+    dist[front] = 0
+    level = 0
+    while front.size and (max_depth == 0 or level < max_depth):
+        nxt = np.concatenate([dst[starts[u]:starts[u + 1]] for u in front]) if front.size else np.zeros(0, np.int64)
+        nxt = np.unique(nxt)
+        nxt = nxt[dist[nxt] == INF]
+        dist[nxt] = level + 1
+        front = nxt
+        level += 1
+    return dist
+
+
+def pagerank(keys, V, alpha, iterations):
+    """Power-iteration PageRank in float64 (test_algos.cu:44-90 runs nvGRAPH's):
+    rank = (1-alpha)/V + alpha (sum over u->v of rank[u]/outdeg(u) + dangling/V)."""
+    src, dst, _ = _split(keys)
+    live = dst != NBR_END
+    src, dst = src[live], dst[live]
+    deg = np.bincount(src, minlength=V).astype(np.float64)
+    rank = np.full(V, 1.0 / V)
+    for _ in range(iterations):
+        contrib = np.where(deg > 0, rank / np.maximum(deg, 1), 0.0)
+        dangling = rank[deg == 0].sum()
+        acc = np.bincount(dst, weights=contrib[src], minlength=V)
+        rank = (1 - alpha) / V + alpha * (acc + dangling / V)
+    return rank
