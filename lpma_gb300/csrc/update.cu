@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
                                                   Window *small, Window *big, const UpdList u,
                                                   const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
     // updates of segments that no window absorbed stay pending (overflow)
-    {
+    if (st->ovf) {  // the marks are read only on the overflow paths
         const uint32_t x = blockIdx.x * TPB + threadIdx.x;
         if (x < st->n_u && x < n_cap) pend[x] = seg_e[u.seg[x]] == EXEC_OVF;
     }
