@@ -51,13 +51,19 @@ typedef enum {
 } lpma_status_t;
 
 enum { LPMA_KEY_PACKED = 0, LPMA_KEY_PAIR32 = 1 };
+/* LPMA_FLAG_CONCURRENT: the handle's calls may run while other handles'
+ * calls run on other streams (a worker pool).  Its batch sort then uses
+ * ordinary launches instead of the one cooperative launch, because two
+ * cooperative grids that each hold part of the GPU could wait on each
+ * other. */
+enum { LPMA_FLAG_CONCURRENT = 1 };
 enum { LPMA_MAX_HEIGHT = 24 };
 
 typedef struct {
     uint32_t segment_length;   /* slots per segment; 32 (rpma.cuh:1769) */
     uint32_t key_format;       /* LPMA_KEY_PACKED or LPMA_KEY_PAIR32 */
     uint32_t skip_rule;        /* 1: the reference's big-grain skip state machine (rpma.cuh:1609-1619) */
-    uint32_t reserved0;
+    uint32_t flags;            /* LPMA_FLAG_* */
     double density_lower_root; /* 0.42 (rpma.cuh:77) */
     double density_upper_root; /* 1.0 (rpma.cuh:78) */
 } LpmaConfig;
@@ -205,6 +211,57 @@ LPMA_API lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t
  * doubles on the device.  Asynchronous. */
 LPMA_API lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, double *d_rank,
                                      lpma_stream_t stream);
+
+/* Device bytes the handle holds (structure, scratch, views). */
+LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
+
+/* ---- request pool: many resident graphs, batched or served ----
+ * Worker threads, each with its own stream, run submitted requests.
+ * Requests on different graphs run concurrently; requests on one graph run
+ * one at a time in submission order.  A request is admitted while the
+ * resident graphs plus the scratch of the requests in flight fit
+ * hbm_budget_bytes (0: no budget; one request is always admitted when none
+ * runs).  Graphs given to a pool should be created with
+ * LPMA_FLAG_CONCURRENT.  The caller owns each LpmaRequest and keeps it
+ * valid until done is set; its timestamps are host steady-clock
+ * nanoseconds.  (The reference has no counterpart: its drivers update one
+ * graph at a time.) */
+typedef struct LpmaPool LpmaPool;
+enum { LPMA_REQ_UPDATE = 0, LPMA_REQ_NEIGHBORS = 1, LPMA_REQ_BFS = 2, LPMA_REQ_EDGE_QUERY = 3 };
+typedef struct {
+    uint32_t kind;              /* LPMA_REQ_* */
+    uint32_t host_inputs;       /* update: 1 when keys0/vals0/keys1 are host memory */
+    LpmaHandle *graph;
+    const uint64_t *keys0;      /* update: inserts; edge query: query keys */
+    const uint8_t *vals0;       /* update: insert values (NULL: 1) */
+    size_t n0;
+    const uint64_t *keys1;      /* update: deletes */
+    size_t n1;
+    const uint32_t *vertices;   /* neighbours: query sources; BFS: sources */
+    const uint64_t *windows;    /* neighbours: lb << 32 | ub per query */
+    size_t nv;
+    uint32_t thres;             /* update: expiry threshold; edge query: window */
+    uint32_t max_depth;         /* BFS */
+    uint32_t *out_u32;          /* neighbours: offsets (nv + 1); edge query: counts */
+    uint32_t *out_nbrs;         /* neighbours */
+    uint8_t *out_vals;          /* neighbours */
+    int32_t *out_dist;          /* BFS: V entries */
+    size_t cap;                 /* neighbours: capacity of out_nbrs / out_vals */
+    /* filled by the pool */
+    lpma_status_t status;
+    uint32_t levels;            /* BFS */
+    uint64_t reached;           /* BFS: vertices reached; neighbours: total */
+    LpmaStats stats;            /* update */
+    uint64_t t_submit_ns, t_start_ns, t_end_ns;
+    volatile uint32_t done;
+    uint32_t reserved;
+} LpmaRequest;
+
+LPMA_API lpma_status_t lpma_pool_create(uint32_t n_workers, uint64_t hbm_budget_bytes, LpmaPool **out);
+LPMA_API lpma_status_t lpma_pool_submit(LpmaPool *p, LpmaRequest *req);
+LPMA_API lpma_status_t lpma_pool_wait(LpmaPool *p, LpmaRequest *req);
+LPMA_API lpma_status_t lpma_pool_drain(LpmaPool *p);
+LPMA_API lpma_status_t lpma_pool_destroy(LpmaPool *p);
 
 /* ---- edgelist files (README.md:9-20) ---- */
 

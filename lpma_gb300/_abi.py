@@ -16,6 +16,7 @@ STATUS_NAMES = {
     8: "LPMA_ERR_BUFFER_TOO_SMALL", 9: "LPMA_ERR_SCRATCH_LIMIT", 10: "LPMA_ERR_IO",
 }
 KEY_PACKED, KEY_PAIR32 = 0, 1
+FLAG_CONCURRENT = 1
 MAX_HEIGHT = 24
 
 # every entry point include/lpma.h declares
@@ -24,14 +25,16 @@ EXPORTS = [
     "lpma_to_csr", "lpma_export_sorted", "lpma_export_layout", "lpma_info", "lpma_destroy", "lpma_status_string",
     "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches", "lpma_prof_enable", "lpma_prof_report",
     "lpma_shuffle_static", "lpma_query_neighbors", "lpma_edge_query", "lpma_bfs", "lpma_pagerank",
-    "lpma_read_edgelist", "lpma_read_queries",
+    "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
+    "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy",
 ]
+REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
 SHUFFLE_STATIC_MAX_KEYS = 65536
 
 
 class LpmaConfig(ctypes.Structure):
     _fields_ = [("segment_length", ctypes.c_uint32), ("key_format", ctypes.c_uint32),
-                ("skip_rule", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("skip_rule", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("density_lower_root", ctypes.c_double), ("density_upper_root", ctypes.c_double)]
 
 
@@ -54,6 +57,20 @@ class LpmaStats(ctypes.Structure):
 
     def __getitem__(self, name):
         return getattr(self, name)
+
+
+class LpmaRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("host_inputs", ctypes.c_uint32), ("graph", ctypes.c_void_p),
+                ("keys0", ctypes.c_void_p), ("vals0", ctypes.c_void_p), ("n0", ctypes.c_size_t),
+                ("keys1", ctypes.c_void_p), ("n1", ctypes.c_size_t),
+                ("vertices", ctypes.c_void_p), ("windows", ctypes.c_void_p), ("nv", ctypes.c_size_t),
+                ("thres", ctypes.c_uint32), ("max_depth", ctypes.c_uint32),
+                ("out_u32", ctypes.c_void_p), ("out_nbrs", ctypes.c_void_p), ("out_vals", ctypes.c_void_p),
+                ("out_dist", ctypes.c_void_p), ("cap", ctypes.c_size_t),
+                ("status", ctypes.c_int), ("levels", ctypes.c_uint32), ("reached", ctypes.c_uint64),
+                ("stats", LpmaStats),
+                ("t_submit_ns", ctypes.c_uint64), ("t_start_ns", ctypes.c_uint64), ("t_end_ns", ctypes.c_uint64),
+                ("done", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class LpmaError(RuntimeError):
@@ -96,6 +113,12 @@ def load():
         "lpma_pagerank": [P, ctypes.c_double, U32, P, P],
         "lpma_read_edgelist": [ctypes.c_char_p, ctypes.c_char_p, P, SZ, P, P],
         "lpma_read_queries": [ctypes.c_char_p, P, P, SZ, P],
+        "lpma_memory_bytes": [P, P],
+        "lpma_pool_create": [U32, U64, P],
+        "lpma_pool_submit": [P, P],
+        "lpma_pool_wait": [P, P],
+        "lpma_pool_drain": [P],
+        "lpma_pool_destroy": [P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

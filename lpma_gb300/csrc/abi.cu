@@ -109,6 +109,8 @@ struct LpmaHandle {
     uint32_t *pr_deg = nullptr;
     double *pr_contrib = nullptr, *pr_acc = nullptr, *pr_dangling = nullptr;
     uint32_t *pin_word = nullptr;  // pinned: totals read back by the read paths
+    uint64_t recent_shapes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // front shapes seen, for the capture policy
+    uint32_t recent_pos = 0;
 };
 
 namespace {
@@ -452,6 +454,18 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         for (FrontGraph &f : h->graphs)
             if (!memcmp(f.key, key, sizeof(key))) fg = &f;
         if (!fg) {
+            // capture a shape only when it repeats: a stream of varying batch
+            // sizes would otherwise pay a capture and instantiation per call
+            uint64_t hk = 1469598103934665603ull;
+            for (uint64_t w : key) hk = (hk ^ w) * 1099511628211ull;
+            bool seen = false;
+            for (uint64_t x : h->recent_shapes) seen |= x == hk;
+            if (!seen) {
+                h->recent_shapes[h->recent_pos++ % 8] = hk;
+                return enqueue_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal);
+            }
+        }
+        if (!fg) {
             if (h->graphs.size() >= 16) {
                 auto lru = std::min_element(h->graphs.begin(), h->graphs.end(),
                                             [](const FrontGraph &a, const FrontGraph &b) { return a.stamp < b.stamp; });
@@ -716,8 +730,9 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         cudaMallocHost(&h->hinit, sizeof(DevStatus)) || dalloc(&h->sent, num_vertices) ||
         dalloc(&h->sort.hist, 8 * 256) || dalloc(&h->sort.counters, 16) || dalloc(&h->sort_err, 1))
         return fail(LPMA_ERR_OUT_OF_MEMORY);
-    // batches up to coop_sort_max_keys() sort in one cooperative launch
-    h->sort.bar = h->sort.counters;
+    // batches up to coop_sort_max_keys() sort in one cooperative launch,
+    // unless the handle shares the GPU with concurrent calls
+    h->sort.bar = (c.flags & LPMA_FLAG_CONCURRENT) ? nullptr : h->sort.counters;
     h->sort.err = &h->dst->error;
     std::memset(h->hinit, 0, sizeof(DevStatus));
     h->hinit->min_t_ins = 0xFFFFFFFFu;
@@ -989,6 +1004,21 @@ lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, do
     for (uint32_t it = 0; it < iterations; it++)
         launch_pr_iteration(g, h->c.cnt, h->pr_deg, h->V, alpha, d_rank, h->pr_contrib, h->pr_acc, h->pr_dangling, s);
     CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
+    if (!h || !bytes) return LPMA_ERR_INVALID_ARGUMENT;
+    uint64_t b = 0;
+    if (h->c.Hc || h->c.keys) {
+        const uint64_t ns = nslots_of(h->c.Hc), nseg = nseg_of(h->c.Hc);
+        b += 18 * ns + nseg * (5 + 16 + 7 * 4) + bitmap_words(h->c.Hc) * 4;
+    }
+    b += 4ull * h->V + h->bcap * 64ull + h->view_cap * 9ull + h->exp_cap * 9ull + h->stage_cap * 17ull;
+    if (h->bfs_a) b += 8ull * h->V;
+    if (h->pr_deg) b += 20ull * h->V;
+    b += h->q_cap * 8ull;
+    *bytes = b;
     return LPMA_OK;
 }
 

@@ -774,7 +774,9 @@ uint32_t coop_sort_max_keys() {
 }
 
 cudaError_t sort_prepare() {
+    static std::mutex mu;
     static bool done = false;
+    std::lock_guard<std::mutex> lk(mu);
     if (done) return cudaSuccess;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_small_sort<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -265,6 +265,71 @@ def destroy_rpma(rpma):
 
 
 # ------------------------------------------------------ workload generator
+class Pool:
+    """Worker pool over many resident graphs (lpma_pool_*): submit update,
+    neighbour, BFS and edge-query requests; different graphs run
+    concurrently, one graph's requests run in submission order.  Inputs and
+    outputs are torch CUDA tensors, kept alive by the request until done."""
+
+    def __init__(self, workers=8, hbm_budget_bytes=0):
+        self._L = _abi.load()
+        p = ctypes.c_void_p()
+        check(self._L.lpma_pool_create(int(workers), int(hbm_budget_bytes), ctypes.byref(p)), "lpma_pool_create")
+        self._p = p
+
+    def _submit(self, req, keep):
+        req._keep = keep
+        check(self._L.lpma_pool_submit(self._p, ctypes.byref(req)), "lpma_pool_submit")
+        return req
+
+    def update(self, graph, ins=None, dels=None, ins_vals=None, thres=0):
+        r = _abi.LpmaRequest()
+        r.kind, r.graph, r.thres = _abi.REQ_UPDATE, graph._h, int(thres)
+        if ins is not None:
+            r.keys0, r.n0 = _dev(ins, "uint64")
+        if ins_vals is not None:
+            r.vals0 = _dev(ins_vals, "uint8")[0]
+        if dels is not None:
+            r.keys1, r.n1 = _dev(dels, "uint64")
+        return self._submit(r, (ins, dels, ins_vals))
+
+    def neighbors(self, graph, srcs, windows, offsets, nbrs, vals):
+        r = _abi.LpmaRequest()
+        r.kind, r.graph = _abi.REQ_NEIGHBORS, graph._h
+        r.vertices, r.windows, r.nv = srcs.data_ptr(), windows.data_ptr(), srcs.numel()
+        r.out_u32, r.out_nbrs, r.out_vals, r.cap = offsets.data_ptr(), nbrs.data_ptr(), vals.data_ptr(), nbrs.numel()
+        return self._submit(r, (srcs, windows, offsets, nbrs, vals))
+
+    def bfs(self, graph, sources, dist, max_depth=0):
+        r = _abi.LpmaRequest()
+        r.kind, r.graph, r.max_depth = _abi.REQ_BFS, graph._h, int(max_depth)
+        r.vertices, r.nv, r.out_dist = sources.data_ptr(), sources.numel(), dist.data_ptr()
+        return self._submit(r, (sources, dist))
+
+    def wait(self, req):
+        return self._L.lpma_pool_wait(self._p, ctypes.byref(req))
+
+    def drain(self):
+        check(self._L.lpma_pool_drain(self._p), "lpma_pool_drain")
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self._L.lpma_pool_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def memory_bytes(g):
+    b = ctypes.c_uint64()
+    check(_abi.load().lpma_memory_bytes(g._h, ctypes.byref(b)), "lpma_memory_bytes")
+    return b.value
+
+
 def query_rpma(rpma, srcs, constraints=None):
     """query_rpma (rpma.cuh:1974-2036): (offsets, nbrs, values), lists in the callers' query order."""
     return rpma.query_neighbors(srcs, constraints)

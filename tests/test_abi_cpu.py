@@ -76,3 +76,21 @@ def test_build_flags_target_sm103a():
     b = __graft_entry__._load_builder()
     assert "arch=compute_103a,code=sm_103a" in " ".join(b.ARCH)
     assert "-lineinfo" in b.FLAGS
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """ctypes mirrors of LpmaConfig / LpmaStats / LpmaRequest have the C layout."""
+    import ctypes
+    import subprocess
+    from lpma_gb300 import _abi
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lpma.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(LpmaConfig), sizeof(LpmaStats),'
+                   ' sizeof(LpmaRequest), offsetof(LpmaRequest, stats), offsetof(LpmaRequest, done),'
+                   ' offsetof(LpmaRequest, cap));return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    want = [ctypes.sizeof(_abi.LpmaConfig), ctypes.sizeof(_abi.LpmaStats), ctypes.sizeof(_abi.LpmaRequest),
+            _abi.LpmaRequest.stats.offset, _abi.LpmaRequest.done.offset, _abi.LpmaRequest.cap.offset]
+    assert got == want
