@@ -49,6 +49,15 @@ def parse():
     ap.add_argument("--sweep-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served"],
+                    help="stream: the single-graph update stream (the headline line); multigraph: 256 graphs, one "
+                         "batch each per round, pooled vs one plain call per graph; served: Poisson arrivals over "
+                         "64 resident graphs, pooled vs one request at a time")
+    ap.add_argument("--graphs", type=int, default=256)
+    ap.add_argument("--rounds", type=int, default=6)
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--rates", default="500,2000,8000", help="served: Poisson arrival rates (requests/s)")
+    ap.add_argument("--duration", type=float, default=3.0, help="served: seconds of arrivals per rate")
     return ap.parse_args()
 
 
@@ -341,8 +350,205 @@ def cpu_baseline(host_edges, B, steps, threads):
     return {"value": B * steps / sum(lat), "lat": lat, "load_s": t_load}
 
 
+# ------------------------------------------------------------ many graphs
+class GraphSet:
+    """Independent directed R-MAT graphs, a = .57 b = .19 c = .19: vertex
+    counts log-uniform over 2^10..2^18 (powers of two), edge factor uniform
+    in 8..32, 50% preloaded, each with its own insert / delete pools."""
+
+    def __init__(self, n, seed, flags=0, device="cuda"):
+        import torch
+        import lpma_gb300 as L
+        from lpma_gb300 import rpma
+        rng = np.random.default_rng(seed)
+        self.graphs = []
+        for i in range(n):
+            scale = int(rng.integers(10, 19))
+            ef = int(rng.integers(8, 33))
+            raw = torch.empty((1 << scale) * ef, dtype=torch.int64, device=device)
+            m = L.gen_rmat_device(seed * 100003 + i, scale, ef, raw)
+            e = raw[:m].clone()
+            del raw
+            L.shuffle_device(seed + i, e)
+            half = m // 2
+            g = L.Lpma(1 << scale, config=rpma.default_config(flags=flags))
+            g.build(e[:half])
+            self.graphs.append({"g": g, "V": 1 << scale, "st": Stream(torch.cat([e[half:], e[:half]]),
+                                                                      torch.cat([e[:half], e[half:]])),
+                                "edges": m, "stored": half, "pool_left": m - half})
+        torch.cuda.synchronize()
+
+    def batch(self, gi, rng, lo=100, hi=100000, kind=None):
+        """(kind, device batch) for graph gi: insert or delete (even odds), size
+        log-uniform in [lo, hi], clamped to what the graph can take."""
+        G = self.graphs[gi]
+        kind = kind or ("ins" if rng.random() < 0.5 else "del")
+        b = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        avail = G["pool_left"] if kind == "ins" else G["stored"]
+        b = max(1, min(b, avail - 1)) if avail > 1 else 0
+        if b == 0:
+            kind = "del" if kind == "ins" else "ins"
+            b = 1
+        if G["st"].ci + b > G["st"].n or G["st"].cd + b > G["st"].n:
+            G["st"].ci = G["st"].cd = 0  # wrap the cyclic pools (a fresh pass over the same edges)
+        x = G["st"].next(kind, b)
+        if kind == "ins":
+            G["stored"] += b
+            G["pool_left"] -= b
+        else:
+            G["stored"] -= b
+            G["pool_left"] += b
+        return kind, x
+
+    def close(self):
+        for G in self.graphs:
+            G["g"].close()
+
+
+def multigraph_arm(args):
+    """256 graphs, one batch per graph per round: every batch of a round
+    submitted at once to the pool (concurrent workers, each graph's calls in
+    order) vs one plain update call per graph on one stream."""
+    import torch
+    from lpma_gb300 import rpma
+    gs = GraphSet(args.graphs, args.seed, flags=0)
+    rng = np.random.default_rng(args.seed + 1)
+    pool = rpma.Pool(args.workers, 0)
+    res = {"plain": [], "pooled": []}
+    for r in range(args.rounds + 2):
+        mode = "plain" if r % 2 == 0 else "pooled"
+        work = [gs.batch(i, rng) for i in range(len(gs.graphs))]
+        edges = sum(int(x.numel()) for _, x in work)
+        torch.cuda.synchronize()
+        lat = []
+        t0 = time.perf_counter()
+        if mode == "plain":
+            for G, (k, x) in zip(gs.graphs, work):
+                G["g"].set_flags(0)
+                a = time.perf_counter()
+                G["g"].update(ins=x) if k == "ins" else G["g"].update(dels=x)
+                torch.cuda.synchronize()
+                lat.append(time.perf_counter() - a)
+        else:
+            reqs = []
+            for G, (k, x) in zip(gs.graphs, work):
+                G["g"].set_flags(1)
+                reqs.append(pool.update(G["g"], ins=x) if k == "ins" else pool.update(G["g"], dels=x))
+            pool.drain()
+            for q in reqs:
+                assert q.status == 0, q.status
+                lat.append((q.t_end_ns - q.t_start_ns) / 1e9)
+        t = time.perf_counter() - t0
+        if r >= 2:  # first round of each mode is warm-up
+            res[mode].append({"edges": edges, "t": t, "lat": lat})
+    pool.close()
+    out = {}
+    for mode, rounds in res.items():
+        E = sum(x["edges"] for x in rounds)
+        T = sum(x["t"] for x in rounds)
+        lat = [l for x in rounds for l in x["lat"]]
+        out[mode] = {"edges_per_s": E / T, "round_ms": 1e3 * T / len(rounds),
+                     "batch_p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                     "batch_p99_ms": 1e3 * float(np.percentile(lat, 99))}
+    gs.close()
+    line = {"metric": "aggregate updated edges/s over a round of one batch per graph", "workload":
+            "%d R-MAT graphs, V log-uniform 2^10..2^18, edge factor 8..32, 50%% preloaded; one insert or delete batch "
+            "per graph per round, size log-uniform 100..100K" % args.graphs,
+            "unit": "edges/s", "rounds_per_mode": args.rounds // 2, "workers": args.workers,
+            "plain": out["plain"], "pooled": out["pooled"],
+            "speedup": out["pooled"]["edges_per_s"] / out["plain"]["edges_per_s"],
+            "note": "plain: one lpma_update per graph, one stream, wall clock per round (host + device); pooled: "
+                    "all batches of the round submitted to lpma_pool, wall clock until drained; batch latency = "
+                    "service time of one batch"}
+    print(json.dumps(line))
+
+
+def served_arm(args):
+    """Poisson arrivals over 64 resident graphs under a 150 GB admission
+    budget: 70% updates (size log-uniform 1..1M, insert:delete 3:1), 30%
+    reads (half neighbour list of a random vertex, half 2-hop BFS from 1,024
+    random seeds).  The pool (continuous admission, concurrent graphs) vs the
+    same arrivals served one request at a time."""
+    import torch
+    from lpma_gb300 import rpma
+    gs = GraphSet(min(64, args.graphs), args.seed, flags=1)
+    budget = 150 << 30
+    # read outputs: one buffer set per graph (a graph's requests run one at a time)
+    for G in gs.graphs:
+        G["nbr_out"] = (torch.empty(2, dtype=torch.int32, device="cuda"),
+                        torch.empty(1 << 20, dtype=torch.int32, device="cuda"),
+                        torch.empty(1 << 20, dtype=torch.uint8, device="cuda"))
+        G["dist"] = torch.empty(G["V"], dtype=torch.int32, device="cuda")
+    out = {"rates": []}
+    for rate in [float(x) for x in args.rates.split(",") if x]:
+        row = {"rate_per_s": rate}
+        for mode, workers in (("one_at_a_time", 1), ("pooled", args.workers)):
+            rng = np.random.default_rng(int(rate) + 17)
+            n_req = max(1, int(rate * args.duration))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+            plan = []
+            for i in range(n_req):
+                gi = int(rng.integers(0, len(gs.graphs)))
+                G = gs.graphs[gi]
+                u = rng.random()
+                if u < 0.7:
+                    kind = "ins" if rng.random() < 0.75 else "del"
+                    k, x = gs.batch(gi, rng, 1, 1000000, kind)
+                    plan.append(("upd", gi, k, x))
+                elif u < 0.85:
+                    src = torch.tensor([int(rng.integers(0, G["V"]))], dtype=torch.int32, device="cuda")
+                    win = torch.full((1,), 0xFFFFFFFF, dtype=torch.int64, device="cuda")
+                    plan.append(("nbr", gi, src, win) + G["nbr_out"])
+                else:
+                    seeds = torch.from_numpy(rng.integers(0, G["V"], 1024).astype(np.int32)).cuda()
+                    plan.append(("bfs", gi, seeds, G["dist"]))
+            torch.cuda.synchronize()
+            pool = rpma.Pool(workers, budget)
+            reqs = []
+            t0 = time.perf_counter()
+            t0_ns = time.perf_counter_ns()  # the pool's clock (steady_clock) runs on the same monotonic source
+            for at, p in zip(arrivals, plan):
+                d = t0 + at - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                if p[0] == "upd":
+                    G = gs.graphs[p[1]]["g"]
+                    q = pool.update(G, ins=p[3]) if p[2] == "ins" else pool.update(G, dels=p[3])
+                elif p[0] == "nbr":
+                    q = pool.neighbors(gs.graphs[p[1]]["g"], *p[2:])
+                else:
+                    q = pool.bfs(gs.graphs[p[1]]["g"], p[2], p[3], 2)
+                q.arrival_ns = t0_ns + int(at * 1e9)
+                reqs.append((p[0], q, int(p[3].numel()) if p[0] == "upd" else 0))
+            pool.drain()
+            t = time.perf_counter() - t0
+            pool.close()
+            stat = {"wall_s": t, "updated_edges_per_s": sum(e for _, _, e in reqs) / t}
+            for kind in ("upd", "nbr", "bfs"):
+                lat = [(q.t_end_ns - min(q.t_submit_ns, q.arrival_ns)) / 1e6 for k, q, _ in reqs if k == kind]
+                bad = sum(1 for k, q, _ in reqs if k == kind and q.status != 0)
+                if lat:
+                    stat[kind] = {"n": len(lat), "p50_ms": float(np.percentile(lat, 50)),
+                                  "p99_ms": float(np.percentile(lat, 99)), "errors": bad}
+            row[mode] = stat
+        out["rates"].append(row)
+    gs.close()
+    line = {"metric": "served p50/p99 request latency and updated edges/s at Poisson arrival rates",
+            "workload": "%d resident R-MAT graphs (V 2^10..2^18, edge factor 8..32), 150 GB admission budget; 70%% "
+                        "updates (log-uniform 1..1M, insert:delete 3:1), 15%% neighbour lists, 15%% 2-hop BFS from "
+                        "1,024 seeds" % len(gs.graphs), "unit": "ms / edges/s", "workers": args.workers,
+            "duration_s_per_rate": args.duration, **out,
+            "note": "latency = completion - planned arrival (queueing and submission lag included); one_at_a_time = "
+                    "a pool of one worker"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.workload != "stream":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        return multigraph_arm(args) if args.workload == "multigraph" else served_arm(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -212,6 +212,15 @@ LPMA_API lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t
 LPMA_API lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, double *d_rank,
                                      lpma_stream_t stream);
 
+/* After LPMA_ERR_INTERNAL: the device check that failed (1 multi-segment
+ * window size, 2 big-window item count, 3 single-segment window size, 4/5
+ * big-window staging bounds), 0 when none. */
+LPMA_API lpma_status_t lpma_error_detail(const LpmaHandle *h, uint32_t *site);
+
+/* Change the handle's LPMA_FLAG_* bits; no call on the handle may be in
+ * flight. */
+LPMA_API lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags);
+
 /* Device bytes the handle holds (structure, scratch, views). */
 LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
 

@@ -111,6 +111,10 @@ struct LpmaHandle {
     uint32_t *pin_word = nullptr;  // pinned: totals read back by the read paths
     uint64_t recent_shapes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // front shapes seen, for the capture policy
     uint32_t recent_pos = 0;
+    // Bumped whenever a buffer the front reads or writes is (re)allocated,
+    // or the sort mode changes: cached front graphs hold raw pointers to
+    // every such buffer, so they are all dropped when it moves.
+    uint64_t buf_gen = 1, graph_gen = 0;
 };
 
 namespace {
@@ -131,12 +135,30 @@ lpma_status_t cuda_fail(cudaError_t e) {
     return e == cudaErrorMemoryAllocation ? LPMA_ERR_OUT_OF_MEMORY : LPMA_ERR_CUDA;
 }
 
+// LPMA_POISON=1 fills every new buffer with 0xA5 bytes: a debugging aid
+// that makes a read of memory no kernel wrote show up deterministically.
+bool poison_enabled() {
+    const char *e = getenv("LPMA_POISON");  // read per allocation: tests switch it
+    return e && e[0] == '1';
+}
+
+// LPMA_POISON_ONLY=<text> restricts the poisoning to buffers whose name
+// contains <text>.
+bool poison_this(const char *name) {
+    if (!poison_enabled()) return false;
+    const char *only = getenv("LPMA_POISON_ONLY");
+    return !only || !only[0] || strstr(name, only) != nullptr;
+}
+
 template <typename T>
-cudaError_t dalloc(T **p, size_t count) {
+cudaError_t dalloc_named(const char *name, T **p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    return cudaMalloc((void **)p, count * sizeof(T));
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e == cudaSuccess && poison_this(name)) e = cudaMemset(*p, 0xA5, count * sizeof(T));
+    return e;
 }
+#define dalloc(p, n) dalloc_named(#p, p, n)
 template <typename T>
 void dfree(T *&p) {
     if (p) cudaFree((void *)p);
@@ -198,11 +220,13 @@ lpma_status_t grow_to(LpmaHandle *h, uint32_t hneed, cudaStream_t s) {
     }
     free_cap(o);
     h->c = n;
+    h->buf_gen++;
     return LPMA_OK;
 }
 
 lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
     if (n <= h->bcap) return LPMA_OK;
+    h->buf_gen++;
     size_t cap = std::max<size_t>(n, 4096);
     cap = cap + cap / 4;
     dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
@@ -390,6 +414,7 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
         CK(cudaStreamSynchronize(s));
         free_cap(h->c);
         h->c = fresh;
+        h->buf_gen++;
     } else if (hh < H) {
         CK(cudaMemsetAsync(h->c.cnt + nseg_of(hh), 0, nseg_of(H) - nseg_of(hh) + 64, s));
     }
@@ -450,6 +475,14 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         const uint64_t key[12] = {n_ins, n_del, h->H, thres, (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1),
                                   (uint64_t)h->c.keys, (uint64_t)h->c.vals, (uint64_t)h->c.cnt, (uint64_t)h->c.fl,
                                   (uint64_t)h->bk0, (uint64_t)h->c.cnt_live, (uint64_t)h->c.bitmap};
+        if (h->graph_gen != h->buf_gen) {
+            for (FrontGraph &f : h->graphs) {
+                cudaGraphExecDestroy(f.exec);
+                cudaGraphDestroy(f.graph);
+            }
+            h->graphs.clear();
+            h->graph_gen = h->buf_gen;
+        }
         FrontGraph *fg = nullptr;
         for (FrontGraph &f : h->graphs)
             if (!memcmp(f.key, key, sizeof(key))) fg = &f;
@@ -1004,6 +1037,20 @@ lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, do
     for (uint32_t it = 0; it < iterations; it++)
         launch_pr_iteration(g, h->c.cnt, h->pr_deg, h->V, alpha, d_rank, h->pr_contrib, h->pr_acc, h->pr_dangling, s);
     CK(cudaGetLastError());
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_error_detail(const LpmaHandle *h, uint32_t *site) {
+    if (!h || !site) return LPMA_ERR_INVALID_ARGUMENT;
+    *site = h->hst ? h->hst->sticky_site : 0u;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags) {
+    if (!h || (flags & ~(uint32_t)LPMA_FLAG_CONCURRENT)) return LPMA_ERR_INVALID_ARGUMENT;
+    h->cfg.flags = flags;
+    h->sort.bar = (flags & LPMA_FLAG_CONCURRENT) ? nullptr : h->sort.counters;
+    h->buf_gen++;  // cached fronts hold the other sort
     return LPMA_OK;
 }
 

@@ -91,6 +91,7 @@ struct DevStatus {
     // Not reset per call (the reset copies the fields above only): the
     // executors set ERR_INTERNAL here after the call may have returned.
     uint32_t sticky;
+    uint32_t sticky_site;  // which internal check set ERR_INTERNAL (first one)
 };
 
 // A rebalance window chosen by the planner (maximal executed window).

@@ -435,20 +435,26 @@ __global__ void __launch_bounds__(TPB) k_pending_scatter(const UpdList in, const
 }
 
 // ------------------------------------------------------------------ planner
-__device__ inline uint32_t sum_cnt(const uint8_t *cnt, uint64_t a, uint32_t l) {
+// Sum of the counts of the window [a, a + 2^l) clipped to nseg segments.
+// The last window of a level reaches one entry past the last segment
+// (a + 2^l = nseg + 1); that entry is not a segment and may hold a stale
+// count from another height, so it is taken back out.
+__device__ inline uint32_t sum_cnt(const uint8_t *cnt, uint64_t a, uint32_t l, uint64_t nseg) {
     uint32_t s = 0;
     if (l < 4) {
-        for (uint32_t t = 0; t < (1u << l); t++) s += cnt[a + t];
-    } else {
-        const uint4 *p = reinterpret_cast<const uint4 *>(cnt + a);
-        for (uint32_t t = 0; t < (1u << (l - 4)); t++) {
-            uint4 v = p[t];
-            s = __dp4a(v.x, 0x01010101u, s);
-            s = __dp4a(v.y, 0x01010101u, s);
-            s = __dp4a(v.z, 0x01010101u, s);
-            s = __dp4a(v.w, 0x01010101u, s);
-        }
+        for (uint32_t t = 0; t < (1u << l); t++)
+            if (a + t < nseg) s += cnt[a + t];
+        return s;
     }
+    const uint4 *p = reinterpret_cast<const uint4 *>(cnt + a);
+    for (uint32_t t = 0; t < (1u << (l - 4)); t++) {
+        uint4 v = p[t];
+        s = __dp4a(v.x, 0x01010101u, s);
+        s = __dp4a(v.y, 0x01010101u, s);
+        s = __dp4a(v.z, 0x01010101u, s);
+        s = __dp4a(v.w, 0x01010101u, s);
+    }
+    if (a + (1ull << l) > nseg) s -= cnt[nseg];
     return s;
 }
 
@@ -490,7 +496,7 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
             if (l == H + 1)
                 live = (int64_t)total_live;
             else if (l <= LSUM || !use_P)
-                live = sum_cnt(cnt, a, l);
+                live = sum_cnt(cnt, a, l, nseg);
             else
                 live = (int64_t)P[b] - (int64_t)P[a];
             const int64_t net = 2 * ((int64_t)u.ip[hi] - (int64_t)u.ip[lo]) - (int64_t)(hi - lo);
@@ -717,7 +723,7 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
         if (total != W.m || W.m > 32u * W.f) {
             if (ug == 0 && gl == 0) {
                 atomicOr(&st->sticky, ERR_INTERNAL);
-                st->err_info[1] = 1;
+                atomicCAS(&st->sticky_site, 0u, 1u);
             }
         } else if (active) {
             // destination segment ug of the even spread
@@ -875,7 +881,7 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restr
         const bool ok = active && m == W.m && m <= 32;
         if (active && !ok && gl == 0) {
             atomicOr(&st->sticky, ERR_INTERNAL);
-            st->err_info[1] = 3;
+            atomicCAS(&st->sticky_site, 0u, 3u);
         }
         if (ok) {
             uint64_t o[4];
@@ -1001,7 +1007,7 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
                     Mv[r] = v[q];
                 } else {  // only if the update list broke its sortedness invariant
                     atomicOr(&st->sticky, ERR_INTERNAL);
-                    st->err_info[1] = 4;
+                    atomicCAS(&st->sticky_site, 0u, 4u);
                 }
             }
         }
@@ -1055,7 +1061,7 @@ __global__ void __launch_bounds__(TPB) k_gather_ins(const TileJob *__restrict__ 
             Mv[r] = u.val[x];
         } else {  // only if the update list broke its sortedness invariant
             atomicOr(&st->sticky, ERR_INTERNAL);
-            st->err_info[1] = 5;
+            atomicCAS(&st->sticky_site, 0u, 5u);
         }
     }
 }
@@ -1073,7 +1079,7 @@ __global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ j
         const uint64_t mb = PQ[J.sa];
         if (k == 0 && gl == 0 && PQ[J.sa + J.sf] - mb != J.m) {  // the gather must account for m items
             atomicOr(&st->sticky, ERR_INTERNAL);
-            st->err_info[1] = 2;
+            atomicCAS(&st->sticky_site, 0u, 2u);
         }
         if (mb + J.m > m_cap) continue;  // reported above; never read past M
         const uint64_t ds = J.da + k;

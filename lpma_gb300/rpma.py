@@ -179,6 +179,10 @@ class Lpma:
                                          _stream_ptr(self.stream)), "lpma_export_layout")
         return k, v, sent, h.value
 
+    def set_flags(self, flags):
+        """LPMA_FLAG_* bits (1: calls may run concurrently with other handles')."""
+        check(self._L.lpma_set_flags(self._h, int(flags)), "lpma_set_flags")
+
     # -------------------------------------------------------------- read paths
     def query_neighbors(self, srcs, windows=None):
         """query_rpma: neighbour lists of srcs (torch CUDA uint32/int32) with time

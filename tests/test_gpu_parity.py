@@ -230,3 +230,53 @@ def test_scale18_stream(engine, oracle, batch):
                 if s[k]:
                     events.add(k)
     assert_csr(g, o)
+
+
+def test_cached_front_survives_buffer_moves(engine, oracle):
+    """A repeated batch shape replays a captured front; batch buffers that
+    grow in between, and a sort-mode change, must not leave a stale one."""
+    V = 1 << 11
+    e = oracle.shuffle(oracle.rmat_edges(31, 11, 16), 4)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    d = _dev(e)
+    pos = 0
+    plan = [100, 100, 100, 5000, 100, 100, 9000, 100, 100]
+    for i, b in enumerate(plan):
+        if i == 7:
+            g.set_flags(1)
+        if i == 8:
+            g.set_flags(0)
+        g.update(ins=d[pos:pos + b])
+        o.update(ins=e[pos:pos + b])
+        pos += b
+        assert_same(g, o, "step %d (batch %d)" % (i, b))
+    g.close()
+
+
+def test_shrink_then_grow_with_poisoned_buffers(engine, oracle, monkeypatch):
+    """Heights move down and up again through rebuilds, an eager level-up and
+    the one-level growth path, with every new device buffer filled with
+    garbage (LPMA_POISON=1): no kernel may read a count, key or flag that
+    no kernel wrote (the last window of a level once read one count past
+    the last segment)."""
+    monkeypatch.setenv("LPMA_POISON", "1")
+    V = 1 << 12
+    e = oracle.shuffle(oracle.rmat_edges(26, 12, 16), 27)
+    half = e.size // 2
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    d = _dev(e)
+    g.update(ins=d[:half])
+    o.update(ins=e[:half])
+    assert_same(g, o, "bulk")
+    steps = [("del", 0, int(half * 0.95)), ("del", int(half * 0.95), int(half * 0.955)),
+             ("del", int(half * 0.955), int(half * 0.985)), ("ins", half, e.size), ("ins", 0, int(half * 0.3))]
+    for kind, a, b in steps:
+        if kind == "del":
+            g.update(dels=d[a:b])
+            o.update(dels=e[a:b])
+        else:
+            g.update(ins=d[a:b])
+            o.update(ins=e[a:b])
+        assert_same(g, o, "%s %d:%d" % (kind, a, b))
+    assert_csr(g, o)
+    g.close()
