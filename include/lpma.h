@@ -268,6 +268,9 @@ typedef struct {
 
 LPMA_API lpma_status_t lpma_pool_create(uint32_t n_workers, uint64_t hbm_budget_bytes, LpmaPool **out);
 LPMA_API lpma_status_t lpma_pool_submit(LpmaPool *p, LpmaRequest *req);
+/* Submits reqs[0..n) (a contiguous array the caller keeps valid until all
+ * are done) in array order, under one lock. */
+LPMA_API lpma_status_t lpma_pool_submit_many(LpmaPool *p, LpmaRequest *reqs, size_t n);
 LPMA_API lpma_status_t lpma_pool_wait(LpmaPool *p, LpmaRequest *req);
 LPMA_API lpma_status_t lpma_pool_drain(LpmaPool *p);
 LPMA_API lpma_status_t lpma_pool_destroy(LpmaPool *p);

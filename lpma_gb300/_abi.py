@@ -26,7 +26,7 @@ EXPORTS = [
     "lpma_gen_rmat", "lpma_shuffle", "lpma_kernel_launches", "lpma_prof_enable", "lpma_prof_report",
     "lpma_shuffle_static", "lpma_query_neighbors", "lpma_edge_query", "lpma_bfs", "lpma_pagerank",
     "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
-    "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail",
+    "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
 ]
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
 SHUFFLE_STATIC_MAX_KEYS = 65536
@@ -118,6 +118,7 @@ def load():
         "lpma_error_detail": [P, P],
         "lpma_pool_create": [U32, U64, P],
         "lpma_pool_submit": [P, P],
+        "lpma_pool_submit_many": [P, P, SZ],
         "lpma_pool_wait": [P, P],
         "lpma_pool_drain": [P],
         "lpma_pool_destroy": [P],

@@ -168,6 +168,25 @@ lpma_status_t lpma_pool_submit(LpmaPool *p, LpmaRequest *r) {
     return LPMA_OK;
 }
 
+lpma_status_t lpma_pool_submit_many(LpmaPool *p, LpmaRequest *reqs, size_t n) {
+    if (!p || (n && !reqs)) return LPMA_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < n; i++)
+        if (!reqs[i].graph || reqs[i].kind > LPMA_REQ_EDGE_QUERY) return LPMA_ERR_INVALID_ARGUMENT;
+    const uint64_t t = now_ns();
+    std::lock_guard<std::mutex> lk(p->mu);
+    for (size_t i = 0; i < n; i++) {
+        LpmaRequest *r = &reqs[i];
+        r->done = 0;
+        r->status = LPMA_OK;
+        r->t_submit_ns = t;
+        r->t_start_ns = r->t_end_ns = 0;
+        p->queue.push_back(r);
+    }
+    p->pending += (uint32_t)n;
+    p->work_cv.notify_all();
+    return LPMA_OK;
+}
+
 lpma_status_t lpma_pool_wait(LpmaPool *p, LpmaRequest *r) {
     if (!p || !r) return LPMA_ERR_INVALID_ARGUMENT;
     std::unique_lock<std::mutex> lk(p->mu);

@@ -589,6 +589,105 @@ __global__ void __launch_bounds__(SORT_TPB) k_small_sort(uint64_t *keys, V *vals
     }
 }
 
+// ---------------------------------------------------------------- one-CTA sort, 8K keys
+// Keys stay in registers between passes; each pass ranks them (ballots),
+// places them in shared memory at their stable position and reloads them
+// in that order.  One launch and one SM for batches up to 8192 pairs, so
+// that many small batches of different graphs sort side by side.
+struct BlockSortSmem {
+    uint64_t k[BLOCK_SORT_MAX];
+    uint16_t v[BLOCK_SORT_MAX];
+    uint32_t whist[BLOCK_SORT_TPB / 32][256];
+    uint32_t ldig[256];
+    uint32_t wsum[8];
+};
+
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys, uint16_t *vals, uint32_t n,
+                                                                   SortMask mask) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BlockSortSmem &S = *reinterpret_cast<BlockSortSmem *>(smem_raw);
+    constexpr int IPT = BLOCK_SORT_IPT, NW = BLOCK_SORT_TPB / 32;
+    const uint32_t act = active_bytes(mask);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    uint64_t k[IPT];
+    uint16_t v[IPT];
+    uint32_t vmask = 0;
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+        const uint32_t p = w * 32 * IPT + i * 32 + lane;
+        if (p < n) {
+            k[i] = keys[p];
+            v[i] = vals[p];
+            vmask |= 1u << i;
+        } else {
+            k[i] = ~0ull;
+            v[i] = 0;
+        }
+    }
+    for (int byte = 0; byte < 8; byte++) {
+        if (!((act >> byte) & 1u)) continue;
+        const int sh = 8 * byte;
+        for (int i = tid; i < NW * 256; i += BLOCK_SORT_TPB) (&S.whist[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t rank[IPT];
+        warp_rank<IPT>(k, vmask, sh, S.whist[w], rank);
+        __syncthreads();
+        // digit d (thread d < 256): warp-exclusive offsets and the tile count
+        uint32_t tcount = 0;
+        if (tid < 256) {
+            for (int ww = 0; ww < NW; ww++) {
+                const uint32_t c = S.whist[ww][tid];
+                S.whist[ww][tid] = tcount;
+                tcount += c;
+            }
+        }
+        // exclusive scan of the 256 digit counts by the first eight warps
+        uint32_t incl = tcount;
+        if (tid < 256) {
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) S.wsum[w] = incl;
+        }
+        __syncthreads();
+        if (tid < 256) {
+            uint32_t base = 0;
+            for (int ww = 0; ww < w; ww++) base += S.wsum[ww];
+            S.ldig[tid] = base + incl - tcount;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < IPT; i++) {
+            if ((vmask >> i) & 1u) {
+                const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+                S.k[pos] = k[i];
+                S.v[pos] = v[i];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < IPT; i++) {
+            const uint32_t p = w * 32 * IPT + i * 32 + lane;
+            if (p < n) {
+                k[i] = S.k[p];
+                v[i] = S.v[p];
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+        const uint32_t p = w * 32 * IPT + i * 32 + lane;
+        if (p < n) {
+            keys[p] = k[i];
+            vals[p] = v[i];
+        }
+    }
+}
+
 // ---------------------------------------------------------------- scans
 constexpr int SCAN_TPB = 256, SCAN_IPT = 8, SCAN_TILE = SCAN_TPB * SCAN_IPT;
 
@@ -711,6 +810,12 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
                              cudaStream_t st) {
     if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
+    if (sizeof(V) == 2 && n > (uint32_t)SORT_TILE && n <= (uint32_t)BLOCK_SORT_MAX) {
+        ProfScope ps("sort_block", st);
+        k_block_sort<<<1, BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(k0, reinterpret_cast<uint16_t *>(v0), n, mask);
+        note_launch();
+        return cudaGetLastError();
+    }
     // cooperative sort: tiles of at least COOP_MIN_TILE keys, spread over
     // every resident CTA slot so that the SMs carry equal work
     const uint32_t maxG = g_coop_max_ctas[coop_slot<V>()] < 512u ? g_coop_max_ctas[coop_slot<V>()] : 512u;
@@ -791,6 +896,9 @@ cudaError_t sort_prepare() {
     if ((e = cudaFuncSetAttribute(k_downsweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(PassSmem<uint64_t>))))
         return e;
+    if ((e = cudaFuncSetAttribute(k_block_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(BlockSortSmem))))
+        return e;
     {
         int dev = 0, sms = 0, per[3] = {0, 0, 0};
         if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
@@ -822,7 +930,7 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
     uint32_t byte_mask = 0;
     for (int b = 0; b < 8; b++)
         if ((diff_bits >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
-    *which = (n > (uint32_t)SORT_TILE) ? (__builtin_popcount(byte_mask) & 1) : 0;
+    *which = (n > in_place_sort_max<V>()) ? (__builtin_popcount(byte_mask) & 1) : 0;
     cudaError_t e = sort_prepare();
     if (e != cudaSuccess) return e;
     return sort_impl<V>(k0, v0, k1, v1, n, SortMask{nullptr, byte_mask}, s, st);

@@ -43,14 +43,26 @@ __device__ inline uint32_t active_bytes(SortMask m) {
     return r & m.host_mask;
 }
 
-// true when sort_pairs_dev left its result in the second buffer pair
-__device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
-    return n > (uint32_t)SORT_TILE && (__popc(active_bytes(m)) & 1);
+// One CTA of BLOCK_SORT_TPB threads sorts a batch of up to BLOCK_SORT_MAX
+// (key, u16 payload) pairs in shared memory, in place.
+constexpr int BLOCK_SORT_TPB = 1024, BLOCK_SORT_IPT = 8;
+constexpr int BLOCK_SORT_MAX = BLOCK_SORT_TPB * BLOCK_SORT_IPT;  // 8192
+
+// the largest batch sorted in place in (k0, v0) by one CTA, per payload size
+template <typename V>
+__host__ __device__ constexpr uint32_t in_place_sort_max() {
+    return sizeof(V) == 2 ? (uint32_t)BLOCK_SORT_MAX : (uint32_t)SORT_TILE;
 }
 
-// Device-decided variant: the result lands in (k1, v1) when n > SORT_TILE
-// and the number of active bytes is odd, else in (k0, v0); kernels that
-// consume it compute the same parity (sort_result_odd).
+// true when sort_pairs_dev<uint16_t> left its result in the second buffer pair
+__device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
+    return n > in_place_sort_max<uint16_t>() && (__popc(active_bytes(m)) & 1);
+}
+
+// Device-decided variant: the result lands in (k1, v1) when n is above
+// in_place_sort_max<V>() and the number of active bytes is odd, else in
+// (k0, v0); kernels that consume it compute the same parity
+// (sort_result_odd).
 template <typename V>
 cudaError_t sort_pairs_dev(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
                            cudaStream_t st);

@@ -310,6 +310,24 @@ class Pool:
         r.vertices, r.nv, r.out_dist = sources.data_ptr(), sources.numel(), dist.data_ptr()
         return self._submit(r, (sources, dist))
 
+    def update_many(self, graphs, batches, kinds):
+        """One update request per (graph, device batch, "ins" | "del"),
+        submitted in one call; returns the request array (keep it alive
+        until drained)."""
+        n = len(graphs)
+        reqs = (_abi.LpmaRequest * n)()
+        for i, (g, x, k) in enumerate(zip(graphs, batches, kinds)):
+            r = reqs[i]
+            r.kind, r.graph = _abi.REQ_UPDATE, g._h
+            ptr, cnt = x.data_ptr(), x.numel()
+            if k == "ins":
+                r.keys0, r.n0 = ptr, cnt
+            else:
+                r.keys1, r.n1 = ptr, cnt
+        reqs._keep = batches
+        check(self._L.lpma_pool_submit_many(self._p, reqs, n), "lpma_pool_submit_many")
+        return reqs
+
     def wait(self, req):
         return self._L.lpma_pool_wait(self._p, ctypes.byref(req))
 
