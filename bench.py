@@ -49,10 +49,11 @@ def parse():
     ap.add_argument("--sweep-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served", "skew"],
                     help="stream: the single-graph update stream (the headline line); multigraph: 256 graphs, one "
                          "batch each per round, pooled vs one plain call per graph; served: Poisson arrivals over "
-                         "64 resident graphs, pooled vs one request at a time")
+                         "64 resident graphs, pooled vs one request at a time; skew: hub-heavy mixed batches on "
+                         "2^20 vertices with 64M edges (resize stress)")
     ap.add_argument("--graphs", type=int, default=256)
     ap.add_argument("--rounds", type=int, default=6)
     ap.add_argument("--workers", type=int, default=16)
@@ -546,12 +547,75 @@ def served_arm(args):
     print(json.dumps(line))
 
 
+def skew_arm(args):
+    """Skew and resize stress: 2^20 vertices, 32M uniform + 32M R-MAT
+    (a = .7, b = c = .1) edges, 25% preloaded; every batch is 1M edges, half
+    inserts (90% with a source among the top 1% out-degrees) and half deletes
+    of preloaded edges."""
+    import torch
+    import lpma_gb300 as L
+    scale, ef, B = 20, 32, args.batch
+    V = 1 << scale
+    raw = torch.empty(2 * V * ef, dtype=torch.int64, device="cuda")
+    n1 = L.gen_rmat_device(args.seed, scale, ef, raw[:V * ef], a=0.25, b=0.25, c=0.25)
+    n2 = L.gen_rmat_device(args.seed + 1, scale, ef, raw[V * ef:], a=0.7, b=0.1, c=0.1)
+    e = torch.unique(torch.cat([raw[:n1], raw[V * ef:V * ef + n2]]))
+    del raw
+    L.shuffle_device(args.seed + 2, e)
+    deg = torch.bincount(e >> 42, minlength=V)
+    hub = torch.zeros(V, dtype=torch.bool, device="cuda")
+    hub[torch.topk(deg, V // 100).indices] = True
+    nb = e.numel() // 4
+    bulk, rest = e[:nb], e[nb:]
+    rest_hub = hub[rest >> 42]
+    hub_pool, cold_pool = rest[rest_hub], rest[~rest_hub]
+    g = L.Lpma(V)
+    g.build(bulk)
+    torch.cuda.synchronize()
+    nh, nc, nd = int(B // 2 * 0.9), B // 2 - int(B // 2 * 0.9), B // 2
+    steps = min(args.steps, hub_pool.numel() // nh - args.warmup, cold_pool.numel() // nc - args.warmup,
+                nb // nd - args.warmup)
+
+    def batch(i):
+        ins = torch.cat([hub_pool[i * nh:(i + 1) * nh], cold_pool[i * nc:(i + 1) * nc]])
+        return ins, bulk[i * nd:(i + 1) * nd]
+
+    for i in range(args.warmup):
+        ins, dels = batch(i)
+        g.update(ins=ins, dels=dels)
+    stream = torch.cuda.current_stream()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    stats = []
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for i in range(steps):
+        ins, dels = batch(args.warmup + i)
+        stats.append(g.update(ins=ins, dels=dels).as_dict())
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    t = sum(lat) / 1e3
+    info = g.info()
+    g.close()
+    ev = {k: sum(x[k] for x in stats) for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path",
+                                                 "fill_empty", "windows_big")}
+    line = {"metric": "updated edges/s on hub-heavy mixed batches (skew and resize stress)", "value": B * steps / t,
+            "unit": "edges/s", "steps": steps, "warmup": args.warmup,
+            "workload": "2^20 vertices, %d edges (32M uniform + 32M R-MAT .7/.1/.1, deduplicated), 25%% preloaded; "
+                        "batches of %d: %d inserts (90%% from the top-1%% out-degree sources) + %d deletes of stored "
+                        "edges" % (e.numel(), B, B // 2, nd),
+            "batch_p50_ms": float(np.percentile(lat, 50)), "batch_p99_ms": float(np.percentile(lat, 99)),
+            "events": ev, "height_after": info["height"], "items_after": info["num_items"],
+            "data": "synthetic (seeded device generators)"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.workload != "stream":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        return multigraph_arm(args) if args.workload == "multigraph" else served_arm(args)
+        return {"multigraph": multigraph_arm, "served": served_arm, "skew": skew_arm}[args.workload](args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

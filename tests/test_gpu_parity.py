@@ -280,3 +280,55 @@ def test_shrink_then_grow_with_poisoned_buffers(engine, oracle, monkeypatch):
         assert_same(g, o, "%s %d:%d" % (kind, a, b))
     assert_csr(g, o)
     g.close()
+
+
+def _skew_stream(oracle, seed, scale, ef, batch, n_batches, bulk_frac=0.25, hub_frac=0.9):
+    """Config-3 shape: half uniform (Erdos-Renyi) and half R-MAT (.7, .1, .1)
+    edges; a quarter preloaded; batches of batch/2 inserts (hub_frac of them
+    with a source among the top 1% out-degrees) and batch/2 deletes of
+    stored edges."""
+    er = oracle.rmat_edges(seed, scale, ef, a=0.25, b=0.25, c=0.25)
+    rm = oracle.rmat_edges(seed + 1, scale, ef, a=0.7, b=0.1, c=0.1)
+    e = oracle.shuffle(np.union1d(er, rm), seed + 2)
+    src = (e >> np.uint64(42)).astype(np.int64)
+    deg = np.bincount(src, minlength=1 << scale)
+    hubs = np.zeros(1 << scale, bool)
+    hubs[np.argsort(-deg)[:max(1, (1 << scale) // 100)]] = True
+    nb = int(e.size * bulk_frac)
+    bulk, pool = e[:nb], e[nb:]
+    is_hub = hubs[(pool >> np.uint64(42)).astype(np.int64)]
+    hub_pool, cold_pool = pool[is_hub], pool[~is_hub]
+    rng = np.random.default_rng(seed)
+    stored = set(bulk.tolist())
+    batches, ph, pc = [], 0, 0
+    for _ in range(n_batches):
+        nh = int(batch // 2 * hub_frac)
+        nc = batch // 2 - nh
+        ins = np.concatenate([hub_pool[ph:ph + nh], cold_pool[pc:pc + nc]])
+        ph, pc = ph + nh, pc + nc
+        dels = rng.choice(np.array(sorted(stored), np.uint64), size=min(batch // 2, len(stored)), replace=False)
+        stored = (stored - set(dels.tolist())) | set(ins.tolist())
+        batches.append((ins, dels))
+    return bulk, batches
+
+
+@pytest.mark.parametrize("scale,batch", [(11, 2048), (13, 8192)])
+def test_skewed_mixed_batches(engine, oracle, scale, batch):
+    """Hub-heavy inserts with uniform deletes force windows up to the root,
+    level-ups and shrinking rebuilds: slot-for-slot parity after each batch."""
+    V = 1 << scale
+    bulk, batches = _skew_stream(oracle, 40 + scale, scale, 16, batch, 8)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    g.update(ins=_dev(bulk))
+    o.update(ins=bulk)
+    assert_same(g, o, "bulk")
+    big = 0
+    for i, (ins, dels) in enumerate(batches):
+        sg = g.update(ins=_dev(ins), dels=_dev(dels))
+        so = o.update(ins=ins, dels=dels)
+        assert sg["n_ins_applied"] == so["n_ins_applied"] and sg["n_del_applied"] == so["n_del_applied"]
+        big += sg["windows_big"] + sg["rebuilt"] + sg["levelup_path"] + sg["root_executed"]
+        assert_same(g, o, "skewed batch %d" % i)
+    assert big > 0  # the stress reached the big-window / resize paths
+    assert_csr(g, o)
+    g.close()
