@@ -111,9 +111,9 @@ struct LpmaHandle {
     uint32_t *pin_word = nullptr;  // pinned: totals read back by the read paths
     uint64_t recent_shapes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // front shapes seen, for the capture policy
     uint32_t recent_pos = 0;
-    // Bumped whenever a buffer the front reads or writes is (re)allocated,
-    // or the sort mode changes: cached front graphs hold raw pointers to
-    // every such buffer, so they are all dropped when it moves.
+    // Bumped whenever a buffer the front reads or writes is (re)allocated:
+    // cached front graphs hold raw pointers to every such buffer, so they
+    // are all dropped when one moves.  (The sort mode is part of their key.)
     uint64_t buf_gen = 1, graph_gen = 0;
 };
 
@@ -472,7 +472,9 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     if (internal || prof_enabled() || !graphs_enabled()) {
         CKS(enqueue_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
     } else {
-        const uint64_t key[12] = {n_ins, n_del, h->H, thres, (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1),
+        const uint64_t key[12] = {n_ins, n_del, h->H, thres,
+                                  (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1) |
+                                      ((uint64_t)(h->sort.bar != nullptr) << 2),
                                   (uint64_t)h->c.keys, (uint64_t)h->c.vals, (uint64_t)h->c.cnt, (uint64_t)h->c.fl,
                                   (uint64_t)h->bk0, (uint64_t)h->c.cnt_live, (uint64_t)h->c.bitmap};
         if (h->graph_gen != h->buf_gen) {
@@ -1050,8 +1052,7 @@ lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags) {
     if (!h || (flags & ~(uint32_t)LPMA_FLAG_CONCURRENT)) return LPMA_ERR_INVALID_ARGUMENT;
     h->cfg.flags = flags;
     h->sort.bar = (flags & LPMA_FLAG_CONCURRENT) ? nullptr : h->sort.counters;
-    h->buf_gen++;  // cached fronts hold the other sort
-    return LPMA_OK;
+    return LPMA_OK;  // cached fronts are keyed by the sort mode
 }
 
 lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
