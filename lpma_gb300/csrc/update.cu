@@ -125,15 +125,15 @@ __device__ inline uint64_t descend(uint64_t key, const ulonglong2 *top, uint32_t
 }
 
 // ------------------------------------------------------------------ pack
-__global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, const uint8_t *__restrict__ ins_vals,
+__device__ __forceinline__ void k_pack_body(const uint64_t *__restrict__ ins, const uint8_t *__restrict__ ins_vals,
                                               uint32_t n_ins, const uint64_t *__restrict__ del, uint32_t n_del,
                                               uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                                               uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
-                                              DevStatus *st) {
+                                              DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     const uint32_t n = n_ins + n_del;
     unsigned long long kand = ~0ull, kor = 0;
     uint32_t mint = 0xFFFFFFFFu, bad = 0xFFFFFFFFu;
-    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
+    for (uint32_t i = bid_ * TPB + threadIdx.x; i < n; i += nblk_ * TPB) {
         uint64_t k;
         uint16_t pay;
         bool ok;
@@ -192,6 +192,14 @@ __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, 
     }
 }
 
+__global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, const uint8_t *__restrict__ ins_vals,
+                                              uint32_t n_ins, const uint64_t *__restrict__ del, uint32_t n_del,
+                                              uint32_t V, uint32_t thres, uint32_t key_format, int internal,
+                                              uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
+                                              DevStatus *st) {
+    k_pack_body(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, blockIdx.x, gridDim.x);
+}
+
 // ------------------------------------------------------------------ live counts
 __global__ void __launch_bounds__(TPB) k_live_counts(const uint64_t *__restrict__ keys, uint32_t H, uint32_t thres,
                                                      uint8_t *cnt_live, DevStatus *st) {
@@ -209,13 +217,13 @@ __global__ void __launch_bounds__(TPB) k_live_counts(const uint64_t *__restrict_
 }
 
 // ------------------------------------------------------------------ resolve + locate
-__global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restrict__ k0,
+__device__ __forceinline__ void k_resolve_locate_body(const uint64_t *__restrict__ k0,
                                                         const uint16_t *__restrict__ p0,
                                                         const uint64_t *__restrict__ k1,
                                                         const uint16_t *__restrict__ p1, uint32_t n, SortMask mask,
                                                         Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
-                                                        uint32_t *blk_ins, DevStatus *st) {
+                                                        uint32_t *blk_ins, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     const bool odd = sort_result_odd(mask, n);
     const uint64_t *__restrict__ skey = odd ? k1 : k0;
     const uint16_t *__restrict__ spay = odd ? p1 : p0;
@@ -231,7 +239,7 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
     __syncthreads();
     const uint32_t nchunks = (n + TPB - 1) / TPB;
     uint32_t ups = 0, noop = 0;
-    for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    for (uint32_t chunk = bid_; chunk < nchunks; chunk += nblk_) {
         const uint32_t i = chunk * TPB + threadIdx.x;
         uint32_t kd = KIND_NOP, sg = 0;
         if (i < n && !rejected) {
@@ -293,9 +301,19 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
     }
 }
 
+__global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restrict__ k0,
+                                                        const uint16_t *__restrict__ p0,
+                                                        const uint64_t *__restrict__ k1,
+                                                        const uint16_t *__restrict__ p1, uint32_t n, SortMask mask,
+                                                        Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
+                                                        uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
+                                                        uint32_t *blk_ins, DevStatus *st) {
+    k_resolve_locate_body(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg, blk_nn, blk_ins, st, blockIdx.x, gridDim.x);
+}
+
 // exclusive scans of the two block-count arrays (one CTA); totals -> status
-__global__ void __launch_bounds__(1024) k_scan_pairs(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
-                                                     DevStatus *st) {
+__device__ __forceinline__ void k_scan_pairs_body(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
+                                                     DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     __shared__ uint32_t wa[32], wb[32];
     __shared__ uint32_t ca, cb;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -338,6 +356,11 @@ __global__ void __launch_bounds__(1024) k_scan_pairs(uint32_t *a, uint32_t *b, u
     }
 }
 
+__global__ void __launch_bounds__(1024) k_scan_pairs(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
+                                                     DevStatus *st) {
+    k_scan_pairs_body(a, b, nb, ip, st, blockIdx.x, gridDim.x);
+}
+
 __device__ inline uint32_t block_excl_scan(uint32_t x, uint32_t *wsum) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t v = x;
@@ -363,28 +386,36 @@ __device__ inline uint32_t block_excl_scan(uint32_t x, uint32_t *wsum) {
     return r;
 }
 
-__global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
+__device__ __forceinline__ void k_compact_body(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
                                                  const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
                                                  SortMask mask, const uint8_t *__restrict__ kind,
                                                  const uint32_t *__restrict__ seg, uint32_t n,
-                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u) {
+                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u, uint32_t bid_, uint32_t nblk_) {
     const bool odd = sort_result_odd(mask, n);
     const uint64_t *__restrict__ skey = odd ? k1 : k0;
     const uint16_t *__restrict__ spay = odd ? p1 : p0;
     __shared__ uint32_t wsum[TPB / 32];
-    const uint32_t i = blockIdx.x * TPB + threadIdx.x;
+    const uint32_t i = bid_ * TPB + threadIdx.x;
     const uint32_t kd = i < n ? kind[i] : KIND_NOP;
     // pack (kept, insert) flags into one scan word
     const uint32_t x = (kd != KIND_NOP ? 1u : 0u) | (kd == KIND_INS ? 1u << 16 : 0u);
     const uint32_t ex = block_excl_scan(x, wsum);
     if (kd != KIND_NOP) {
-        const uint32_t pos = blk_nn[blockIdx.x] + (ex & 0xFFFF);
+        const uint32_t pos = blk_nn[bid_] + (ex & 0xFFFF);
         u.key[pos] = skey[i];
         u.val[pos] = (uint8_t)(spay[i] & 0xFF);
         u.kind[pos] = (uint8_t)kd;
         u.seg[pos] = seg[i];
-        u.ip[pos] = blk_ins[blockIdx.x] + (ex >> 16);
+        u.ip[pos] = blk_ins[bid_] + (ex >> 16);
     }
+}
+
+__global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
+                                                 const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
+                                                 SortMask mask, const uint8_t *__restrict__ kind,
+                                                 const uint32_t *__restrict__ seg, uint32_t n,
+                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u) {
+    k_compact_body(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ relocate / pending
@@ -462,16 +493,16 @@ __device__ inline uint64_t bit_of(uint32_t H, uint32_t l, uint64_t widx) {
     return ((1ull << (H + 2)) - (1ull << (H + 2 - l))) + widx;
 }
 
-__global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
+__device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
                                               const uint32_t *__restrict__ P, int use_P, uint64_t total_live_host,
                                               const unsigned long long *__restrict__ total_live_dev, uint32_t H,
                                               Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
-                                              uint8_t *pend, DevStatus *st) {
+                                              uint8_t *pend, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     const uint64_t total_live = total_live_dev ? *total_live_dev : total_live_host;
     __shared__ uint32_t wsum[TPB / 32];
     __shared__ uint32_t base_s;
     const uint32_t nu = st->n_u;
-    const uint32_t x = blockIdx.x * TPB + threadIdx.x;
+    const uint32_t x = bid_ * TPB + threadIdx.x;
     uint32_t s = 0;
     bool lead = false;
     if (x < nu && x < n_cap) {
@@ -539,21 +570,29 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
     if (own) cand[base_s + ex] = Window{(uint32_t)wa, (uint32_t)wf, (uint32_t)wm, e, lo, hi};
 }
 
+__global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
+                                              const uint32_t *__restrict__ P, int use_P, uint64_t total_live_host,
+                                              const unsigned long long *__restrict__ total_live_dev, uint32_t H,
+                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
+                                              uint8_t *pend, DevStatus *st) {
+    k_plan_body(u, n_cap, cnt, P, use_P, total_live_host, total_live_dev, H, tb, bitmap, cand, seg_e, pend, st, blockIdx.x, gridDim.x);
+}
+
 // Keep the candidates not inside a larger executed window; sort them into
 // single-segment, small (<= 32 segments) and big lists.
-__global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
+__device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
                                                   Window *small, Window *big, const UpdList u,
-                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
+                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     // updates of segments that no window absorbed stay pending (overflow)
     if (st->ovf) {  // the marks are read only on the overflow paths
-        const uint32_t x = blockIdx.x * TPB + threadIdx.x;
+        const uint32_t x = bid_ * TPB + threadIdx.x;
         if (x < st->n_u && x < n_cap) pend[x] = seg_e[u.seg[x]] == EXEC_OVF;
     }
     __shared__ uint32_t wsum[TPB / 32];
     __shared__ uint32_t base_s[4];
     __shared__ unsigned long long sl[2][TPB / 32];
-    const uint32_t c = blockIdx.x * TPB + threadIdx.x;
+    const uint32_t c = bid_ * TPB + threadIdx.x;
     // classes: 0 single segment, 1 two to four, 2 five to 32, 3 larger, 4 none
     uint32_t cls = 4;
     Window w{};
@@ -604,6 +643,13 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
     }
 }
 
+__global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
+                                                  const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
+                                                  Window *small, Window *big, const UpdList u,
+                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
+    k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend, st, blockIdx.x, gridDim.x);
+}
+
 // ------------------------------------------------------------------ multi-segment windows
 // A unit of G groups of 8 lanes rewrites one window of 2..G segments in
 // shared memory: group g loads segment a+g (16-byte loads, 4 slots a lane),
@@ -632,16 +678,16 @@ __device__ inline void unit_sync() {
 }
 
 template <int G>
-__global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
+__device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
                                                        uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
                                                        uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
-                                                       DevStatus *st) {
+                                                       DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     __shared__ MultiSmem<G> S;
     constexpr int UNITS = 32 / G;
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     const int unit = grp / G, ug = grp % G;
     const uint32_t nwin = min(*n_win, n_cap);
-    for (uint32_t wi = blockIdx.x * UNITS + unit; wi < nwin; wi += gridDim.x * UNITS) {
+    for (uint32_t wi = bid_ * UNITS + unit; wi < nwin; wi += nblk_ * UNITS) {
         const Window W = wins[wi];
         const bool active = (uint32_t)ug < W.f;
         const uint32_t s = W.a + ug;
@@ -757,6 +803,14 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
     }
 }
 
+template <int G>
+__global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
+                                                       uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
+                                                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
+                                                       DevStatus *st) {
+    k_exec_multi_body<G>(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
+}
+
 // ------------------------------------------------------------------ single-segment windows
 // The level-0 windows (one segment, about 94% of the executed windows) get a
 // group of 8 lanes each, so a warp keeps 4 windows in flight.  Lane gl of a
@@ -767,20 +821,20 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
 constexpr int ES_TPB = 256;
 constexpr int ES_GROUPS = ES_TPB / 8;
 
-__global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restrict__ wins,
+__device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wins,
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
-                                                        const UpdList u, uint32_t thres, DevStatus *st) {
+                                                        const UpdList u, uint32_t thres, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     __shared__ __align__(16) uint64_t sk[ES_GROUPS][32];
     __shared__ __align__(16) uint8_t sv[ES_GROUPS][32];
     __shared__ uint64_t kk[ES_GROUPS][32];  // kept keys of the window, compacted
     __shared__ uint64_t ik[ES_GROUPS][32];  // insert keys of the window
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
-    const uint32_t stride = gridDim.x * ES_GROUPS;
+    const uint32_t stride = nblk_ * ES_GROUPS;
     // software pipeline: the next window's record, segment slots and update
     // bounds are loaded while the current one is merged
-    uint32_t wi = blockIdx.x * ES_GROUPS + grp;
+    uint32_t wi = bid_ * ES_GROUPS + grp;
     Window Wn{};
     ulonglong2 na = make_ulonglong2(KEY_NONE, KEY_NONE), nb = na;
     uint32_t nv4 = 0, nip0 = 0, nip1 = 0;
@@ -907,6 +961,13 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restr
         }
         __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restrict__ wins,
+                                                        const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
+                                                        uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
+                                                        const UpdList u, uint32_t thres, DevStatus *st) {
+    k_exec_single_body(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ tile grain
