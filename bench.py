@@ -407,19 +407,22 @@ class GraphSet:
 
 
 def multigraph_arm(args):
-    """256 graphs, one batch per graph per round: every batch of a round
-    submitted at once to the pool (concurrent workers, each graph's calls in
-    order) vs one plain update call per graph on one stream."""
+    """256 graphs, one batch per graph per round, three ways: one plain
+    update call per graph on one stream; every batch of a round submitted at
+    once to the pool (concurrent workers, each graph's calls in order); and
+    one lpma_update_batch call over all graphs (shared front launches)."""
     import torch
     from lpma_gb300 import rpma
     gs = GraphSet(args.graphs, args.seed, flags=0)
     rng = np.random.default_rng(args.seed + 1)
     pool = rpma.Pool(args.workers, 0)
-    mode_flags = {"plain": 0, "pooled": 1}
-    res = {"plain": [], "pooled": []}
-    warm = 4  # two rounds of each form: sizes seen twice get their captured front
+    batcher = rpma.Batcher()
+    modes = ("plain", "pooled", "batched")
+    mode_flags = {"plain": 0, "pooled": 1, "batched": 0}
+    res = {m: [] for m in modes}
+    warm = 2 * len(modes)  # two rounds of each form: sizes seen twice get their captured front
     for r in range(args.rounds + warm):
-        mode = "plain" if r % 2 == 0 else "pooled"
+        mode = modes[r % len(modes)]
         for G in gs.graphs:  # plain: the one-launch sort; pooled: sorts that may run side by side
             G["g"].set_flags(mode_flags[mode])
         work = [gs.batch(i, rng) for i in range(len(gs.graphs))]
@@ -437,16 +440,23 @@ def multigraph_arm(args):
                 evs[i + 1].record(stream)
             torch.cuda.synchronize()
             lat = [evs[i].elapsed_time(evs[i + 1]) / 1e3 for i in range(len(work))]
-        else:
+        elif mode == "pooled":
             reqs = pool.update_many([G["g"] for G in gs.graphs], [x for _, x in work], [k for k, _ in work])
             pool.drain()
             for q in reqs:
                 assert q.status == 0, q.status
                 lat.append((q.t_end_ns - q.t_start_ns) / 1e9)
+        else:
+            # every batch completes with the call: its latency is the call's
+            _, status = batcher.update([G["g"] for G in gs.graphs],
+                                       [{"ins": x} if k == "ins" else {"dels": x} for k, x in work])
+            assert all(q == 0 for q in status), status
+            lat = [time.perf_counter() - t0] * len(work)
         t = time.perf_counter() - t0
         if r >= warm:
             res[mode].append({"edges": edges, "t": t, "lat": lat})
     pool.close()
+    batcher.close()
     out = {}
     for mode, rounds in res.items():
         E = sum(x["edges"] for x in rounds)
@@ -459,12 +469,14 @@ def multigraph_arm(args):
     line = {"metric": "aggregate updated edges/s over a round of one batch per graph", "workload":
             "%d R-MAT graphs, V log-uniform 2^10..2^18, edge factor 8..32, 50%% preloaded; one insert or delete batch "
             "per graph per round, size log-uniform 100..100K" % args.graphs,
-            "unit": "edges/s", "rounds_per_mode": args.rounds // 2, "workers": args.workers,
-            "plain": out["plain"], "pooled": out["pooled"],
+            "unit": "edges/s", "rounds_per_mode": args.rounds // len(modes), "workers": args.workers,
+            "plain": out["plain"], "pooled": out["pooled"], "batched": out["batched"],
             "speedup": out["pooled"]["edges_per_s"] / out["plain"]["edges_per_s"],
+            "speedup_batched": out["batched"]["edges_per_s"] / out["plain"]["edges_per_s"],
             "note": "plain: one lpma_update per graph back to back on one stream, wall clock per round (host + "
                     "device), batch latency from CUDA events between calls; pooled: all batches of the round "
-                    "submitted to lpma_pool at once, wall clock until drained, batch latency = service time"}
+                    "submitted to lpma_pool at once, wall clock until drained, batch latency = service time; "
+                    "batched: one lpma_update_batch call per round, wall clock, batch latency = the call's"}
     print(json.dumps(line))
 
 

@@ -221,6 +221,34 @@ LPMA_API lpma_status_t lpma_error_detail(const LpmaHandle *h, uint32_t *site);
  * flight. */
 LPMA_API lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags);
 
+/* ---- one update per graph for many graphs at once ----
+ * The update batches of many graphs go through shared launches: one launch
+ * per step of the update front (status reset, pack, sort, locate, compact,
+ * plan) covers every graph, instead of a dozen launches per graph.  Each
+ * graph then goes on as after its own front (window executors, root,
+ * overflow, resize), so each graph ends exactly as lpma_update would leave
+ * it.  Batches with an expiry threshold, above 131,072 keys, or whose
+ * first level loop allows windows of 2^9+ segments take lpma_update inside
+ * the call.  A graph may appear once per call; its buffers are the handle's
+ * own, the batcher keeps the shared tables between calls.  stats and
+ * status (NULL or n entries) receive each graph's result; the return value
+ * is the first error, or LPMA_OK.  Synchronises the stream once.  (No
+ * counterpart in the reference: its drivers update one graph at a time.) */
+typedef struct LpmaBatcher LpmaBatcher;
+typedef struct {
+    const uint64_t *ins;       /* device */
+    const uint8_t *ins_vals;   /* device, may be NULL */
+    size_t n_ins;
+    const uint64_t *del;       /* device */
+    size_t n_del;
+    uint32_t thres;
+    uint32_t reserved;
+} LpmaBatch;
+LPMA_API lpma_status_t lpma_batcher_create(LpmaBatcher **out);
+LPMA_API lpma_status_t lpma_batcher_destroy(LpmaBatcher *b);
+LPMA_API lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const LpmaBatch *batches,
+                                         size_t n, lpma_stream_t stream, LpmaStats *stats, lpma_status_t *status);
+
 /* Device bytes the handle holds (structure, scratch, views). */
 LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
 

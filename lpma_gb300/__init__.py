@@ -8,10 +8,10 @@ from . import _abi
 
 _abi.load()
 
-from .rpma import (Lpma, LpmaError, default_config, destroy_rpma, gen_rmat_device, get_data_rpma,  # noqa: E402
+from .rpma import (Batcher, Lpma, LpmaError, default_config, destroy_rpma, gen_rmat_device, get_data_rpma,  # noqa: E402
                    init_csr_rpma, kernel_launches, pack_key, profile_enable, profile_report, sentinel_key,
                    shuffle_device, to_csr_rpma, update_rpma)
 
-__all__ = ["Lpma", "LpmaError", "default_config", "init_csr_rpma", "update_rpma", "to_csr_rpma", "get_data_rpma",
+__all__ = ["Lpma", "Batcher", "LpmaError", "default_config", "init_csr_rpma", "update_rpma", "to_csr_rpma", "get_data_rpma",
            "destroy_rpma", "pack_key", "sentinel_key", "gen_rmat_device", "shuffle_device", "kernel_launches",
            "profile_enable", "profile_report"]

@@ -27,6 +27,7 @@ EXPORTS = [
     "lpma_shuffle_static", "lpma_query_neighbors", "lpma_edge_query", "lpma_bfs", "lpma_pagerank",
     "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
+    "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
 ]
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
 SHUFFLE_STATIC_MAX_KEYS = 65536
@@ -71,6 +72,12 @@ class LpmaRequest(ctypes.Structure):
                 ("stats", LpmaStats),
                 ("t_submit_ns", ctypes.c_uint64), ("t_start_ns", ctypes.c_uint64), ("t_end_ns", ctypes.c_uint64),
                 ("done", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class LpmaBatch(ctypes.Structure):
+    _fields_ = [("ins", ctypes.c_void_p), ("ins_vals", ctypes.c_void_p), ("n_ins", ctypes.c_size_t),
+                ("dels", ctypes.c_void_p), ("n_del", ctypes.c_size_t),
+                ("thres", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class LpmaError(RuntimeError):
@@ -122,6 +129,9 @@ def load():
         "lpma_pool_wait": [P, P],
         "lpma_pool_drain": [P],
         "lpma_pool_destroy": [P],
+        "lpma_batcher_create": [P],
+        "lpma_batcher_destroy": [P],
+        "lpma_update_batch": [P, P, P, SZ, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -572,35 +572,12 @@ lpma_status_t wait_front(LpmaHandle *h, cudaStream_t s) {
     return LPMA_OK;
 }
 
-lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins,
-                        const uint64_t *del, size_t n_del, uint32_t thres, cudaStream_t s, LpmaStats *out,
-                        bool internal) {
-    if (h->sticky != LPMA_OK) return h->sticky;
-    if (!internal && !h->host_staged) h->h2d = 0;
-    h->host_staged = false;
-    h->d2h = 0;
-    LpmaStats st{};
-    st.height_before = h->H;
-    const size_t n = n_ins + n_del;
-    if ((n_ins && !ins) || (n_del && !del)) return LPMA_ERR_INVALID_ARGUMENT;
-    if (n == 0) {
-        st.height_after = h->H;
-        st.num_items = h->total;
-        if (out) *out = st;
-        return LPMA_OK;
-    }
-    if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
-    if (thres > 0xFFFFF) return LPMA_ERR_INVALID_ARGUMENT;
-    if (min_height(h->total + n_ins) > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
-    CKS(ensure_batch(h, n));
-    h->view_valid = false;
-    const bool thres_active = thres > h->min_t;
-
-    // pack, sort, resolve + locate, compact, plan (one CUDA graph when the
-    // batch shape repeats), then the one host round trip of the common path;
-    // a rejected batch turns every kernel after k_pack into a no-op
-    CKS(run_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
-    lpma_status_t rs = wait_front(h, s);
+// Everything after the front's status read-back (rs is the read-back's
+// verdict, h->hst holds the status block): the window executors, the
+// root / overflow / resize paths and the stats.  Shared by lpma_update and
+// the graphs of a batched update that need more than the common executors.
+lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t thres, bool thres_active,
+                            cudaStream_t s, LpmaStats &st, LpmaStats *out) {
     // a sort that gave up a bounded wait turned the front into a no-op:
     // nothing changed, so the handle stays usable
     if (rs == LPMA_ERR_TIMEOUT && h->hst->sticky == 0) return rs;
@@ -696,9 +673,80 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     return LPMA_OK;
 }
 
+lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins,
+                        const uint64_t *del, size_t n_del, uint32_t thres, cudaStream_t s, LpmaStats *out,
+                        bool internal) {
+    if (h->sticky != LPMA_OK) return h->sticky;
+    if (!internal && !h->host_staged) h->h2d = 0;
+    h->host_staged = false;
+    h->d2h = 0;
+    LpmaStats st{};
+    st.height_before = h->H;
+    const size_t n = n_ins + n_del;
+    if ((n_ins && !ins) || (n_del && !del)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (n == 0) {
+        st.height_after = h->H;
+        st.num_items = h->total;
+        if (out) *out = st;
+        return LPMA_OK;
+    }
+    if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (thres > 0xFFFFF) return LPMA_ERR_INVALID_ARGUMENT;
+    if (min_height(h->total + n_ins) > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
+    CKS(ensure_batch(h, n));
+    h->view_valid = false;
+    const bool thres_active = thres > h->min_t;
+
+    // pack, sort, resolve + locate, compact, plan (one CUDA graph when the
+    // batch shape repeats), then the one host round trip of the common path;
+    // a rejected batch turns every kernel after k_pack into a no-op
+    CKS(run_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
+    return finish_update(h, wait_front(h, s), n, thres, thres_active, s, st, out);
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
+// Device and pinned tables of a batched update (lpma_update_batch), kept
+// between calls.
+struct LpmaBatcher {
+    size_t cap_g = 0;
+    ForestGraph *dF = nullptr, *hF = nullptr;
+    uint32_t *dB = nullptr, *hB = nullptr;  // block offsets: 5 phases x (G + 1)
+    ForestSortJob *dJ = nullptr, *hJ = nullptr;
+    DevStatus *dS = nullptr, *hS = nullptr;
+};
+
+namespace {
+
+void batcher_free(LpmaBatcher *b) {
+    dfree(b->dF), dfree(b->dB), dfree(b->dJ), dfree(b->dS);
+    if (b->hF) cudaFreeHost(b->hF);
+    if (b->hB) cudaFreeHost(b->hB);
+    if (b->hJ) cudaFreeHost(b->hJ);
+    if (b->hS) cudaFreeHost(b->hS);
+    b->hF = nullptr, b->hB = nullptr, b->hJ = nullptr, b->hS = nullptr;
+    b->cap_g = 0;
+}
+
+lpma_status_t batcher_reserve(LpmaBatcher *b, size_t G) {
+    if (G <= b->cap_g) return LPMA_OK;
+    batcher_free(b);
+    const size_t c = std::max<size_t>(G, 64);
+    CK(dalloc(&b->dF, c));
+    CK(dalloc(&b->dB, 5 * (c + 1)));
+    CK(dalloc(&b->dJ, c));
+    CK(dalloc(&b->dS, c));
+    CK(cudaMallocHost(&b->hF, c * sizeof(ForestGraph)));
+    CK(cudaMallocHost(&b->hB, 5 * (c + 1) * sizeof(uint32_t)));
+    CK(cudaMallocHost(&b->hJ, c * sizeof(ForestSortJob)));
+    CK(cudaMallocHost(&b->hS, c * sizeof(DevStatus)));
+    b->cap_g = c;
+    return LPMA_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 lpma_status_t lpma_config_default(LpmaConfig *cfg) {
@@ -1068,6 +1116,149 @@ lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
     b += h->q_cap * 8ull;
     *bytes = b;
     return LPMA_OK;
+}
+
+lpma_status_t lpma_batcher_create(LpmaBatcher **out) {
+    if (!out) return LPMA_ERR_INVALID_ARGUMENT;
+    *out = new LpmaBatcher();
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_batcher_destroy(LpmaBatcher *b) {
+    if (!b) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    batcher_free(b);
+    delete b;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const LpmaBatch *items, size_t n,
+                                lpma_stream_t stream, LpmaStats *stats, lpma_status_t *status) {
+    if (!b || (n && (!graphs || !items)) || n > (1u << 20)) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<lpma_status_t> res(n, LPMA_OK);
+    std::vector<LpmaStats> sts(n);
+    std::vector<size_t> forest, plain;
+    std::vector<LpmaHandle *> seen;
+    seen.reserve(n);
+    for (size_t i = 0; i < n; i++) {
+        LpmaHandle *h = graphs[i];
+        const LpmaBatch &it = items[i];
+        sts[i] = LpmaStats{};
+        if (!h || (it.n_ins && !it.ins) || (it.n_del && !it.del)) {
+            res[i] = LPMA_ERR_INVALID_ARGUMENT;
+            continue;
+        }
+        if (std::find(seen.begin(), seen.end(), h) != seen.end()) {  // one batch per graph per call
+            res[i] = LPMA_ERR_INVALID_ARGUMENT;
+            continue;
+        }
+        seen.push_back(h);
+        if (h->sticky != LPMA_OK) {
+            res[i] = h->sticky;
+            continue;
+        }
+        const size_t m = it.n_ins + it.n_del;
+        sts[i].height_before = sts[i].height_after = h->H;
+        sts[i].num_items = h->total;
+        if (m == 0) continue;
+        // the shared launches take batches without expiry that one CTA sorts
+        // and whose first level loop plans from segment counts alone
+        if (it.thres == 0 && m <= FOREST_SORT_MAX && !needs_prefix(make_tables(h, h->H, true), h->H) &&
+            min_height(h->total + it.n_ins) <= LPMA_MAX_HEIGHT)
+            forest.push_back(i);
+        else
+            plain.push_back(i);
+    }
+    lpma_status_t r = LPMA_OK;
+    const uint32_t G = (uint32_t)forest.size();
+    if (G) {
+        if ((r = batcher_reserve(b, G)) != LPMA_OK) return r;
+        uint32_t *boff = b->hB, nblk[5] = {0, 0, 0, 0, 0};
+        std::vector<size_t> ready;
+        for (uint32_t k = 0; k < G; k++) {
+            const size_t i = forest[k];
+            LpmaHandle *h = graphs[i];
+            const LpmaBatch &it = items[i];
+            const size_t m = it.n_ins + it.n_del;
+            if ((res[i] = ensure_batch(h, m)) != LPMA_OK) return res[i];
+        }
+        for (uint32_t k = 0; k < G; k++) {
+            const size_t i = forest[k];
+            LpmaHandle *h = graphs[i];
+            const LpmaBatch &it = items[i];
+            const uint32_t m = (uint32_t)(it.n_ins + it.n_del);
+            h->view_valid = false;
+            h->h2d = sizeof(ForestGraph);
+            h->d2h = sizeof(DevStatus);
+            ForestGraph &f = b->hF[k];
+            f = ForestGraph{};
+            f.g = Geo{h->c.keys, h->c.vals, h->H};
+            f.fl = h->c.fl;
+            f.cnt = h->c.cnt;
+            f.V = h->V;
+            f.key_format = h->cfg.key_format;
+            f.ins = it.ins, f.ins_vals = it.ins_vals, f.del = it.del;
+            f.n_ins = (uint32_t)it.n_ins, f.n_del = (uint32_t)it.n_del;
+            f.bk0 = h->bk0, f.bp0 = h->bp0, f.kind = h->kind, f.seg = h->seg;
+            f.blk_nn = h->blk_nn, f.blk_ins = h->blk_ins, f.u = h->u;
+            f.bitmap = h->c.bitmap, f.bitmap_words = bitmap_words(h->H);
+            f.cand = h->cand, f.wsingle = h->wsingle, f.wsmall4 = h->wsmall4, f.wsmall = h->wsmall, f.wbig = h->wbig;
+            f.seg_e = h->c.seg_e, f.pend = h->pend;
+            f.tb = make_tables(h, h->H, true);
+            f.total_items = h->total;
+            f.st = h->dst;
+            b->hJ[k] = ForestSortJob{h->bk0, h->bk1, h->bp0, h->bp1, &h->dst->key_and, m, 0};
+            const uint32_t chunks = (m + 255) / 256;
+            // pack strides over its keys; resolve stages the top of the tree
+            // once per CTA, so each of its CTAs takes 8 or more chunks
+            const uint32_t per[5] = {std::min<uint32_t>(chunks, 64),
+                                     std::min<uint32_t>(chunks, std::max<uint32_t>(8, (chunks + 7) / 8)), chunks,
+                                     chunks, chunks};
+            for (int ph = 0; ph < 5; ph++) {
+                boff[ph * (G + 1) + k] = nblk[ph];
+                nblk[ph] += per[ph];
+            }
+        }
+        for (int ph = 0; ph < 5; ph++) boff[ph * (G + 1) + G] = nblk[ph];
+        CK(cudaMemcpyAsync(b->dF, b->hF, G * sizeof(ForestGraph), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(b->dB, b->hB, 5 * (G + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(b->dJ, b->hJ, G * sizeof(ForestSortJob), cudaMemcpyHostToDevice, s));
+        const uint32_t *B = b->dB;
+        launch_forest_phase(0, b->dF, nullptr, G, G, nullptr, s);
+        launch_forest_phase(1, b->dF, B, G, nblk[0], nullptr, s);
+        CK(forest_sort(b->dJ, G, s));
+        launch_forest_phase(2, b->dF, B + (G + 1), G, nblk[1], nullptr, s);
+        launch_forest_phase(3, b->dF, nullptr, G, G, nullptr, s);
+        launch_forest_phase(4, b->dF, B + 2 * (G + 1), G, nblk[2], nullptr, s);
+        launch_forest_phase(5, b->dF, B + 3 * (G + 1), G, nblk[3], nullptr, s);
+        launch_forest_phase(6, b->dF, B + 4 * (G + 1), G, nblk[4], nullptr, s);
+        launch_forest_phase(7, b->dF, nullptr, G, G, b->dS, s);
+        CK(cudaMemcpyAsync(b->hS, b->dS, G * sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        // each graph goes on as after its own front
+        for (uint32_t k = 0; k < G; k++) {
+            const size_t i = forest[k];
+            LpmaHandle *h = graphs[i];
+            memcpy(h->hst, &b->hS[k], sizeof(DevStatus));
+            const uint32_t e = h->hst->error | h->hst->sticky;
+            const lpma_status_t rs = (e & ERR_TIMEOUT) ? LPMA_ERR_TIMEOUT
+                                                       : ((e & ERR_INTERNAL) ? LPMA_ERR_INTERNAL : LPMA_OK);
+            sts[i].height_before = h->H;
+            res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, s, sts[i], &sts[i]);
+        }
+    }
+    for (size_t i : plain) {
+        const LpmaBatch &it = items[i];
+        res[i] = do_update(graphs[i], it.ins, it.ins_vals, it.n_ins, it.del, it.n_del, it.thres, s, &sts[i], false);
+    }
+    for (size_t i = 0; i < n; i++) {
+        if (stats) stats[i] = sts[i];
+        if (status) status[i] = res[i];
+        if (r == LPMA_OK && res[i] != LPMA_OK) r = res[i];
+    }
+    return r;
 }
 
 const char *lpma_status_string(lpma_status_t s) {

@@ -126,4 +126,37 @@ void launch_fill_f64(double *p, uint64_t n, double x, cudaStream_t s);
 void launch_pr_iteration(Geo g, const uint8_t *cnt, const uint32_t *deg, uint32_t V, double alpha, double *rank,
                          double *contrib, double *acc, double *dangling, cudaStream_t s);
 
+
+// ---- batched update of many graphs (forest launches): one launch per front
+// phase over all graphs; block b of a launch works for graph g with
+// boff[g] <= b < boff[g + 1] (boff: one table per phase).
+struct ForestGraph {
+    Geo g;
+    const ulonglong2 *fl;
+    uint8_t *cnt;
+    uint32_t V;
+    uint32_t key_format;
+    const uint64_t *ins;
+    const uint8_t *ins_vals;
+    const uint64_t *del;
+    uint32_t n_ins, n_del;
+    uint64_t *bk0;
+    uint16_t *bp0;
+    uint8_t *kind;
+    uint32_t *seg, *blk_nn, *blk_ins;
+    UpdList u;
+    uint32_t *bitmap;
+    uint64_t bitmap_words;
+    Window *cand, *wsingle, *wsmall4, *wsmall, *wbig;
+    uint8_t *seg_e, *pend;
+    Tables tb;
+    unsigned long long total_items;
+    DevStatus *st;
+};
+// phases: 0 reset statuses and planner bitmaps, 1 pack, 2 resolve + locate,
+// 3 insert-prefix scan, 4 compact, 5 plan, 6 maximal windows, 7 status copy
+// into out[g]
+void launch_forest_phase(int phase, const ForestGraph *F, const uint32_t *boff, uint32_t ngraphs,
+                         uint32_t nblocks, DevStatus *out, cudaStream_t s);
+
 }  // namespace lpma

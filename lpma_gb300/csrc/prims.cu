@@ -602,12 +602,11 @@ struct BlockSortSmem {
     uint32_t wsum[8];
 };
 
-__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys, uint16_t *vals, uint32_t n,
-                                                                   SortMask mask) {
+// in place, keys in registers; act = the digit bytes to sort
+__device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals, uint32_t n, uint32_t act) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BlockSortSmem &S = *reinterpret_cast<BlockSortSmem *>(smem_raw);
     constexpr int IPT = BLOCK_SORT_IPT, NW = BLOCK_SORT_TPB / 32;
-    const uint32_t act = active_bytes(mask);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     uint64_t k[IPT];
     uint16_t v[IPT];
@@ -684,6 +683,119 @@ __global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys
         if (p < n) {
             keys[p] = k[i];
             vals[p] = v[i];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys, uint16_t *vals, uint32_t n,
+                                                                   SortMask mask) {
+    block_sort_inreg(keys, vals, n, active_bytes(mask));
+}
+
+// ---------------------------------------------------------------- one CTA per graph
+// The batches of many graphs, one CTA each, in one launch.  Up to
+// BLOCK_SORT_MAX pairs sort in registers; larger batches (up to
+// FOREST_SORT_MAX) run an LSD sort through global memory: per digit a
+// histogram, then 8192-key chunks in input order, each ranked in registers
+// and scattered at (digit base + running digit count + stable rank).  The
+// result always ends in (k0, p0).
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_forest_sort(const ForestSortJob *__restrict__ jobs) {
+    const ForestSortJob J = jobs[blockIdx.x];
+    if (J.n < 2) return;
+    const uint32_t act = active_bytes(SortMask{J.andor, 0xFFu});
+    if (J.n <= (uint32_t)BLOCK_SORT_MAX) {
+        block_sort_inreg(J.k0, J.p0, J.n, act);
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BlockSortSmem &S = *reinterpret_cast<BlockSortSmem *>(smem_raw);
+    constexpr int IPT = BLOCK_SORT_IPT, NW = BLOCK_SORT_TPB / 32;
+    uint32_t *base = reinterpret_cast<uint32_t *>(S.k), *run = base + 256, *hist = base + 512;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t n = J.n;
+    int pass = 0;
+    for (int byte = 0; byte < 8; byte++) {
+        if (!((act >> byte) & 1u)) continue;
+        const int sh = 8 * byte;
+        const uint64_t *ki = (pass & 1) ? J.k1 : J.k0;
+        const uint16_t *vi = (pass & 1) ? J.p1 : J.p0;
+        uint64_t *ko = (pass & 1) ? J.k0 : J.k1;
+        uint16_t *vo = (pass & 1) ? J.p0 : J.p1;
+        if (tid < 256) hist[tid] = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < n; i += BLOCK_SORT_TPB) atomicAdd(&hist[(ki[i] >> sh) & 0xFF], 1u);
+        __syncthreads();
+        // digit bases: exclusive scan of the histogram by the first eight warps
+        {
+            const uint32_t x = tid < 256 ? hist[tid] : 0u;
+            uint32_t incl = x;
+            if (tid < 256) {
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane == 31) S.wsum[w] = incl;
+            }
+            __syncthreads();
+            if (tid < 256) {
+                uint32_t b0 = 0;
+                for (int ww = 0; ww < w; ww++) b0 += S.wsum[ww];
+                base[tid] = b0 + incl - x;
+                run[tid] = 0;
+            }
+            __syncthreads();
+        }
+        for (uint32_t c0 = 0; c0 < n; c0 += (uint32_t)BLOCK_SORT_MAX) {
+            uint64_t k[IPT];
+            uint16_t v[IPT];
+            uint32_t vmask = 0;
+#pragma unroll
+            for (int i = 0; i < IPT; i++) {
+                const uint32_t p = c0 + w * 32 * IPT + i * 32 + lane;
+                if (p < n) {
+                    k[i] = ki[p];
+                    v[i] = vi[p];
+                    vmask |= 1u << i;
+                } else {
+                    k[i] = ~0ull;
+                    v[i] = 0;
+                }
+            }
+            for (int i = tid; i < NW * 256; i += BLOCK_SORT_TPB) (&S.whist[0][0])[i] = 0;
+            __syncthreads();
+            uint32_t rank[IPT];
+            warp_rank<IPT>(k, vmask, sh, S.whist[w], rank);
+            __syncthreads();
+            if (tid < 256) {  // warp-exclusive offsets of digit tid, and its chunk count
+                uint32_t t = 0;
+                for (int ww = 0; ww < NW; ww++) {
+                    const uint32_t c = S.whist[ww][tid];
+                    S.whist[ww][tid] = t;
+                    t += c;
+                }
+                S.ldig[tid] = t;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < IPT; i++) {
+                if ((vmask >> i) & 1u) {
+                    const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                    const uint32_t g = base[d] + run[d] + S.whist[w][d] + rank[i];
+                    ko[g] = k[i];
+                    vo[g] = v[i];
+                }
+            }
+            __syncthreads();
+            if (tid < 256) run[tid] += S.ldig[tid];
+            __syncthreads();
+        }
+        pass++;
+    }
+    if (pass & 1) {
+        for (uint32_t i = tid; i < n; i += BLOCK_SORT_TPB) {
+            J.k0[i] = J.k1[i];
+            J.p0[i] = J.p1[i];
         }
     }
 }
@@ -873,6 +985,16 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
 
 // Shared-memory opt-ins of the sort kernels, set once outside any stream
 // capture.
+cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t n_jobs, cudaStream_t st) {
+    if (!n_jobs) return cudaSuccess;
+    cudaError_t e = sort_prepare();
+    if (e != cudaSuccess) return e;
+    ProfScope ps("sort_forest", st);
+    k_forest_sort<<<n_jobs, BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(d_jobs);
+    note_launch();
+    return cudaGetLastError();
+}
+
 uint32_t coop_sort_max_keys() {
     const uint32_t g = g_coop_max_ctas[0] < 512u ? g_coop_max_ctas[0] : 512u;
     return g * (uint32_t)COOP_TILE;
@@ -897,6 +1019,8 @@ cudaError_t sort_prepare() {
                                   (int)sizeof(PassSmem<uint64_t>))))
         return e;
     if ((e = cudaFuncSetAttribute(k_block_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(BlockSortSmem))) ||
+        (e = cudaFuncSetAttribute(k_forest_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))))
         return e;
     {

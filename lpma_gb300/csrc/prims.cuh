@@ -90,6 +90,20 @@ constexpr size_t sort_status_words(uint32_t n) {
 // One-time kernel attribute setup (outside stream capture).
 cudaError_t sort_prepare();
 
+// The batches of many graphs sorted in one launch, one CTA per graph
+// (k_forest_sort): (k0, p0) is sorted in place with (k1, p1) as the second
+// buffer, over the digit bytes where andor[0] (AND) and andor[1] (OR) of
+// the batch differ.  n <= FOREST_SORT_MAX.
+constexpr uint32_t FOREST_SORT_MAX = 1u << 17;
+struct ForestSortJob {
+    uint64_t *k0, *k1;
+    uint16_t *p0, *p1;
+    const unsigned long long *andor;
+    uint32_t n;
+    uint32_t pad;
+};
+cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t n_jobs, cudaStream_t st);
+
 // Keys per tile of the cooperative sort, and the largest batch it takes on
 // this device (tiles that can be resident at once x tile); valid after
 // sort_prepare().

@@ -1346,4 +1346,107 @@ void launch_sum_cnt(const uint8_t *cnt, uint64_t nseg, DevStatus *st, cudaStream
     note_launch();
 }
 
+// ------------------------------------------------------------------ forest launches
+namespace {
+
+__device__ inline uint32_t forest_graph(const uint32_t *__restrict__ boff, uint32_t G, uint32_t b) {
+    uint32_t lo = 0, hi = G;  // last g with boff[g] <= b
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (boff[mid] <= b)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// per-call status reset (the single-graph front copies a host template) and
+// the planner bitmap; one block per graph
+__global__ void __launch_bounds__(TPB) k_forest_reset(const ForestGraph *__restrict__ F) {
+    const ForestGraph &f = F[blockIdx.x];
+    uint32_t *w = reinterpret_cast<uint32_t *>(f.st);
+    constexpr uint32_t NW = offsetof(DevStatus, sticky) / 4;
+    for (uint32_t i = threadIdx.x; i < NW; i += TPB) w[i] = 0;
+    for (uint64_t i = threadIdx.x; i < f.bitmap_words; i += TPB) f.bitmap[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        f.st->min_t_ins = 0xFFFFFFFFu;
+        f.st->key_and = ~0ull;
+        f.st->err_info[0] = 0xFFFFFFFFu;
+        f.st->total_items = f.total_items;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_forest_pack(const ForestGraph *__restrict__ F, const uint32_t *boff,
+                                                     uint32_t G) {
+    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const ForestGraph &f = F[g];
+    k_pack_body(f.ins, f.ins_vals, f.n_ins, f.del, f.n_del, f.V, 0, f.key_format, 0, f.bk0, f.bp0, f.st,
+                blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+// the batch was sorted in place (forest sort): parity mask {nullptr, 0}
+__global__ void __launch_bounds__(TPB) k_forest_resolve(const ForestGraph *__restrict__ F, const uint32_t *boff,
+                                                        uint32_t G) {
+    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const ForestGraph &f = F[g];
+    k_resolve_locate_body(f.bk0, f.bp0, f.bk0, f.bp0, f.n_ins + f.n_del, SortMask{nullptr, 0u}, f.g, f.fl, 0, f.kind,
+                          f.seg, f.blk_nn, f.blk_ins, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+__global__ void __launch_bounds__(1024) k_forest_scan_pairs(const ForestGraph *__restrict__ F) {
+    const ForestGraph &f = F[blockIdx.x];
+    const uint32_t n = f.n_ins + f.n_del;
+    k_scan_pairs_body(f.blk_nn, f.blk_ins, (n + TPB - 1) / TPB, f.u.ip, f.st, 0, 1);
+}
+
+__global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__restrict__ F, const uint32_t *boff,
+                                                        uint32_t G) {
+    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const ForestGraph &f = F[g];
+    k_compact_body(f.bk0, f.bp0, f.bk0, f.bp0, SortMask{nullptr, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
+                   f.blk_ins, f.u, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+__global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restrict__ F, const uint32_t *boff,
+                                                     uint32_t G) {
+    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const ForestGraph &f = F[g];
+    k_plan_body(f.u, f.n_ins + f.n_del, f.cnt, nullptr, 0, 0, &f.st->total_items, f.g.H, f.tb, f.bitmap, f.cand,
+                f.seg_e, f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+__global__ void __launch_bounds__(TPB) k_forest_plan_max(const ForestGraph *__restrict__ F, const uint32_t *boff,
+                                                         uint32_t G) {
+    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const ForestGraph &f = F[g];
+    k_plan_max_body(f.cand, f.n_ins + f.n_del, f.g.H, f.bitmap, f.wsingle, f.wsmall4, f.wsmall, f.wbig, f.u, f.seg_e,
+                    f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+__global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restrict__ F, DevStatus *out) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(F[blockIdx.x].st);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(out + blockIdx.x);
+    for (uint32_t i = threadIdx.x; i < sizeof(DevStatus) / 4; i += 64) dst[i] = src[i];
+}
+
+}  // namespace
+
+void launch_forest_phase(int phase, const ForestGraph *F, const uint32_t *boff, uint32_t G, uint32_t nblocks,
+                         DevStatus *out, cudaStream_t s) {
+    if (!G || (phase >= 1 && phase <= 6 && phase != 3 && !nblocks)) return;
+    switch (phase) {
+        case 0: k_forest_reset<<<G, TPB, 0, s>>>(F); break;
+        case 1: k_forest_pack<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 2: k_forest_resolve<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 3: k_forest_scan_pairs<<<G, 1024, 0, s>>>(F); break;
+        case 4: k_forest_compact<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 5: k_forest_plan<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 6: k_forest_plan_max<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 7: k_forest_status<<<G, 64, 0, s>>>(F, out); break;
+    }
+    note_launch();
+}
+
 }  // namespace lpma

@@ -346,6 +346,58 @@ class Pool:
             pass
 
 
+class Batcher:
+    """Updates of many graphs in one call (lpma_update_batch): the update
+    fronts of all graphs share their launches, then each graph runs its own
+    executors.  Each graph appears at most once per call; batches are torch
+    CUDA tensors."""
+
+    def __init__(self):
+        self._L = _abi.load()
+        b = ctypes.c_void_p()
+        check(self._L.lpma_batcher_create(ctypes.byref(b)), "lpma_batcher_create")
+        self._b = b
+
+    def update(self, graphs, batches, stream=None, raise_on_error=True):
+        """graphs: Lpma objects; batches: per graph a dict with any of ins,
+        ins_vals, dels, thres (or an (ins, dels) pair).  Returns (stats,
+        statuses), one entry per graph."""
+        n = len(graphs)
+        items = (_abi.LpmaBatch * n)()
+        hs = (ctypes.c_void_p * n)()
+        keep = []
+        for i, (g, b) in enumerate(zip(graphs, batches)):
+            if not isinstance(b, dict):
+                b = {"ins": b[0], "dels": b[1]}
+            hs[i] = g._h.value
+            it = items[i]
+            if b.get("ins") is not None:
+                it.ins, it.n_ins = _dev(b["ins"], "uint64")
+            if b.get("ins_vals") is not None:
+                it.ins_vals = _dev(b["ins_vals"], "uint8")[0]
+            if b.get("dels") is not None:
+                it.dels, it.n_del = _dev(b["dels"], "uint64")
+            it.thres = int(b.get("thres", 0))
+            keep.append(b)
+        stats = (LpmaStats * n)()
+        status = (ctypes.c_int * n)()
+        rc = self._L.lpma_update_batch(self._b, hs, items, n, _stream_ptr(stream), stats, status)
+        if raise_on_error:
+            check(rc, "lpma_update_batch")
+        return list(stats), list(status)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._L.lpma_batcher_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def memory_bytes(g):
     b = ctypes.c_uint64()
     check(_abi.load().lpma_memory_bytes(g._h, ctypes.byref(b)), "lpma_memory_bytes")
