@@ -334,14 +334,18 @@ lpma_status_t upload_jobs(LpmaHandle *h, cudaStream_t s) {
 }
 
 // Execute the planned maximal windows (status already synced).
+// small_done: the single / 4 / 32-segment windows were already launched
+// (the shared executors of a batched update).
 lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32_t thres, bool thres_active,
-                        cudaStream_t s, LpmaStats *st) {
+                        cudaStream_t s, LpmaStats *st, bool small_done = false) {
     const uint32_t n_single = h->hst->n_single, n_small4 = h->hst->n_small4, n_small = h->hst->n_small,
                    n_big = h->hst->n_big;
     Geo g{h->c.keys, h->c.vals, h->H};
-    launch_exec_small(h->wsingle, n_single, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-    launch_exec_small(h->wsmall4, n_small4, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-    launch_exec_small(h->wsmall, n_small, 2, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    if (!small_done) {
+        launch_exec_small(h->wsingle, n_single, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        launch_exec_small(h->wsmall4, n_small4, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        launch_exec_small(h->wsmall, n_small, 2, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+    }
     st->windows_single += n_single;
     st->windows_small += n_single + n_small4 + n_small;
     st->slots_rewritten += h->hst->slots_small;
@@ -575,9 +579,10 @@ lpma_status_t wait_front(LpmaHandle *h, cudaStream_t s) {
 // Everything after the front's status read-back (rs is the read-back's
 // verdict, h->hst holds the status block): the window executors, the
 // root / overflow / resize paths and the stats.  Shared by lpma_update and
-// the graphs of a batched update that need more than the common executors.
+// the graphs of a batched update (small_done: their first loop's common
+// executors ran in the shared launches).
 lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t thres, bool thres_active,
-                            cudaStream_t s, LpmaStats &st, LpmaStats *out) {
+                            cudaStream_t s, LpmaStats &st, LpmaStats *out, bool small_done = false) {
     // a sort that gave up a bounded wait turned the front into a no-op:
     // nothing changed, so the handle stays usable
     if (rs == LPMA_ERR_TIMEOUT && h->hst->sticky == 0) return rs;
@@ -599,7 +604,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
     lpma_status_t r = LPMA_OK;
     if (n_u > 0 && !h->hst->ovf) {
         const bool root = h->hst->root != 0;
-        r = exec_plan(h, h->u, (uint32_t)n, thres, thres_active, s, &st);
+        r = exec_plan(h, h->u, (uint32_t)n, thres, thres_active, s, &st, small_done);
         if (r == LPMA_OK && root) {
             st.root_executed = 1;
             if (min_height((uint64_t)live_after) + 1 > h->H) {  // eager level-up
@@ -712,20 +717,26 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
 struct LpmaBatcher {
     size_t cap_g = 0;
     ForestGraph *dF = nullptr, *hF = nullptr;
-    uint32_t *dB = nullptr, *hB = nullptr;  // block offsets: 5 phases x (G + 1)
+    uint32_t *dB = nullptr, *hB = nullptr;  // block offsets: FOREST_TABLES tables of G + 1
     ForestSortJob *dJ = nullptr, *hJ = nullptr;
     DevStatus *dS = nullptr, *hS = nullptr;
+    ForestExec *dE = nullptr, *hE = nullptr;
+    uint32_t *dX = nullptr, *hX = nullptr;  // executor block offsets: 3 tables of G + 1
+    cudaEvent_t done = nullptr;             // after the last shared executor of the previous call
+    bool pending = false;
 };
 
 namespace {
 
+// block-offset tables of a batched update: pack, resolve, compact, plan,
+// maximal windows, then the sort's tile launch and merge rounds
+constexpr int FOREST_TABLES = 6 + (int)FOREST_MERGE_ROUNDS_MAX;
+
 void batcher_free(LpmaBatcher *b) {
-    dfree(b->dF), dfree(b->dB), dfree(b->dJ), dfree(b->dS);
-    if (b->hF) cudaFreeHost(b->hF);
-    if (b->hB) cudaFreeHost(b->hB);
-    if (b->hJ) cudaFreeHost(b->hJ);
-    if (b->hS) cudaFreeHost(b->hS);
-    b->hF = nullptr, b->hB = nullptr, b->hJ = nullptr, b->hS = nullptr;
+    dfree(b->dF), dfree(b->dB), dfree(b->dJ), dfree(b->dS), dfree(b->dE), dfree(b->dX);
+    for (void *p : {(void *)b->hF, (void *)b->hB, (void *)b->hJ, (void *)b->hS, (void *)b->hE, (void *)b->hX})
+        if (p) cudaFreeHost(p);
+    b->hF = nullptr, b->hB = nullptr, b->hJ = nullptr, b->hS = nullptr, b->hE = nullptr, b->hX = nullptr;
     b->cap_g = 0;
 }
 
@@ -734,13 +745,17 @@ lpma_status_t batcher_reserve(LpmaBatcher *b, size_t G) {
     batcher_free(b);
     const size_t c = std::max<size_t>(G, 64);
     CK(dalloc(&b->dF, c));
-    CK(dalloc(&b->dB, 5 * (c + 1)));
+    CK(dalloc(&b->dB, FOREST_TABLES * (c + 1)));
     CK(dalloc(&b->dJ, c));
     CK(dalloc(&b->dS, c));
     CK(cudaMallocHost(&b->hF, c * sizeof(ForestGraph)));
-    CK(cudaMallocHost(&b->hB, 5 * (c + 1) * sizeof(uint32_t)));
+    CK(cudaMallocHost(&b->hB, FOREST_TABLES * (c + 1) * sizeof(uint32_t)));
     CK(cudaMallocHost(&b->hJ, c * sizeof(ForestSortJob)));
     CK(cudaMallocHost(&b->hS, c * sizeof(DevStatus)));
+    CK(dalloc(&b->dE, c));
+    CK(dalloc(&b->dX, 3 * (c + 1)));
+    CK(cudaMallocHost(&b->hE, c * sizeof(ForestExec)));
+    CK(cudaMallocHost(&b->hX, 3 * (c + 1) * sizeof(uint32_t)));
     b->cap_g = c;
     return LPMA_OK;
 }
@@ -1128,6 +1143,7 @@ lpma_status_t lpma_batcher_destroy(LpmaBatcher *b) {
     if (!b) return LPMA_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
     batcher_free(b);
+    if (b->done) cudaEventDestroy(b->done);
     delete b;
     return LPMA_OK;
 }
@@ -1173,8 +1189,13 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
     lpma_status_t r = LPMA_OK;
     const uint32_t G = (uint32_t)forest.size();
     if (G) {
+        // the previous call's shared executors read the tables rewritten below
+        if (b->pending) {
+            CK(cudaEventSynchronize(b->done));
+            b->pending = false;
+        }
         if ((r = batcher_reserve(b, G)) != LPMA_OK) return r;
-        uint32_t *boff = b->hB, nblk[5] = {0, 0, 0, 0, 0};
+        uint32_t *boff = b->hB, nblk[FOREST_TABLES] = {}, rounds = 0;
         std::vector<size_t> ready;
         for (uint32_t k = 0; k < G; k++) {
             const size_t i = forest[k];
@@ -1209,25 +1230,30 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             f.total_items = h->total;
             f.st = h->dst;
             b->hJ[k] = ForestSortJob{h->bk0, h->bk1, h->bp0, h->bp1, &h->dst->key_and, m, 0};
+            const uint32_t rk = forest_sort_rounds(m);
+            rounds = std::max(rounds, rk);
+            f.sk = (rk & 1) ? h->bk1 : h->bk0;
+            f.sp = (rk & 1) ? h->bp1 : h->bp0;
             const uint32_t chunks = (m + 255) / 256;
             // pack strides over its keys; resolve stages the top of the tree
             // once per CTA, so each of its CTAs takes 8 or more chunks
-            const uint32_t per[5] = {std::min<uint32_t>(chunks, 64),
-                                     std::min<uint32_t>(chunks, std::max<uint32_t>(8, (chunks + 7) / 8)), chunks,
-                                     chunks, chunks};
-            for (int ph = 0; ph < 5; ph++) {
+            uint32_t per[FOREST_TABLES] = {std::min<uint32_t>(chunks, 64),
+                                           std::min<uint32_t>(chunks, std::max<uint32_t>(8, (chunks + 7) / 8)),
+                                           chunks, chunks, chunks, m > 1 ? forest_sort_tiles(m) : 0};
+            for (uint32_t r = 0; r < rk; r++) per[6 + r] = forest_merge_ctas(m);
+            for (int ph = 0; ph < FOREST_TABLES; ph++) {
                 boff[ph * (G + 1) + k] = nblk[ph];
                 nblk[ph] += per[ph];
             }
         }
-        for (int ph = 0; ph < 5; ph++) boff[ph * (G + 1) + G] = nblk[ph];
+        for (int ph = 0; ph < FOREST_TABLES; ph++) boff[ph * (G + 1) + G] = nblk[ph];
         CK(cudaMemcpyAsync(b->dF, b->hF, G * sizeof(ForestGraph), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(b->dB, b->hB, 5 * (G + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(b->dB, b->hB, FOREST_TABLES * (G + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(b->dJ, b->hJ, G * sizeof(ForestSortJob), cudaMemcpyHostToDevice, s));
         const uint32_t *B = b->dB;
         launch_forest_phase(0, b->dF, nullptr, G, G, nullptr, s);
         launch_forest_phase(1, b->dF, B, G, nblk[0], nullptr, s);
-        CK(forest_sort(b->dJ, G, s));
+        CK(forest_sort(b->dJ, G, B + 5 * (G + 1), nblk + 5, rounds, s));
         launch_forest_phase(2, b->dF, B + (G + 1), G, nblk[1], nullptr, s);
         launch_forest_phase(3, b->dF, nullptr, G, G, nullptr, s);
         launch_forest_phase(4, b->dF, B + 2 * (G + 1), G, nblk[2], nullptr, s);
@@ -1237,6 +1263,44 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
         CK(cudaMemcpyAsync(b->hS, b->dS, G * sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         CK(cudaGetLastError());
+        // graphs whose first loop needs only the common executors (no
+        // error, no overflow, no window of 2^6+ segments): one launch per
+        // executor over all of them
+        std::vector<uint8_t> shared(G, 0);
+        uint32_t GS = 0, xblk[3] = {0, 0, 0};
+        uint32_t *xoff = b->hX;
+        for (uint32_t k = 0; k < G; k++) {
+            const DevStatus &d = b->hS[k];
+            if ((d.error | d.sticky) || d.n_u == 0 || d.ovf || d.n_big) continue;
+            LpmaHandle *h = graphs[forest[k]];
+            shared[k] = 1;
+            ForestExec &e = b->hE[GS];
+            e = ForestExec{};
+            e.g = Geo{h->c.keys, h->c.vals, h->H};
+            e.cnt = h->c.cnt, e.fl = h->c.fl, e.sent = h->sent, e.V = h->V;
+            e.n[0] = d.n_single, e.n[1] = d.n_small4, e.n[2] = d.n_small;
+            e.w[0] = h->wsingle, e.w[1] = h->wsmall4, e.w[2] = h->wsmall;
+            e.u = h->u;
+            e.st = h->dst;
+            for (int kind = 0; kind < 3; kind++) {
+                xoff[kind * (G + 1) + GS] = xblk[kind];
+                xblk[kind] += exec_ctas(kind, e.n[kind]);
+            }
+            GS++;
+        }
+        if (GS) {
+            for (int kind = 0; kind < 3; kind++) {
+                xoff[kind * (G + 1) + GS] = xblk[kind];
+                if (kind) memmove(xoff + kind * (GS + 1), xoff + kind * (G + 1), (GS + 1) * sizeof(uint32_t));
+            }
+            CK(cudaMemcpyAsync(b->dE, b->hE, GS * sizeof(ForestExec), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(b->dX, b->hX, 3 * (GS + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+            for (int kind = 0; kind < 3; kind++)
+                launch_forest_exec(kind, b->dE, b->dX + kind * (GS + 1), GS, xblk[kind], s);
+            if (!b->done) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+            CK(cudaEventRecord(b->done, s));
+            b->pending = true;
+        }
         // each graph goes on as after its own front
         for (uint32_t k = 0; k < G; k++) {
             const size_t i = forest[k];
@@ -1246,7 +1310,8 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             const lpma_status_t rs = (e & ERR_TIMEOUT) ? LPMA_ERR_TIMEOUT
                                                        : ((e & ERR_INTERNAL) ? LPMA_ERR_INTERNAL : LPMA_OK);
             sts[i].height_before = h->H;
-            res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, s, sts[i], &sts[i]);
+            res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, s, sts[i], &sts[i],
+                                   shared[k] != 0);
         }
     }
     for (size_t i : plain) {

@@ -140,8 +140,10 @@ struct ForestGraph {
     const uint8_t *ins_vals;
     const uint64_t *del;
     uint32_t n_ins, n_del;
-    uint64_t *bk0;
+    uint64_t *bk0;  // packed batch (pack output, sort input)
     uint16_t *bp0;
+    const uint64_t *sk;  // sorted batch: (bk0, bp0) or the second buffer pair
+    const uint16_t *sp;
     uint8_t *kind;
     uint32_t *seg, *blk_nn, *blk_ins;
     UpdList u;
@@ -153,6 +155,25 @@ struct ForestGraph {
     unsigned long long total_items;
     DevStatus *st;
 };
+// The common executors of many graphs in one launch each (lpma_update_batch):
+// per graph its geometry and the window lists of the single, 4-segment and
+// 32-segment executors with their host-known counts.
+struct ForestExec {
+    Geo g;
+    uint8_t *cnt;
+    ulonglong2 *fl;
+    uint32_t *sent;
+    uint32_t V;
+    uint32_t n[3];
+    const Window *w[3];
+    UpdList u;
+    DevStatus *st;
+};
+// kind 0: single-segment windows, 1: up to 4 segments, 2: up to 32
+void launch_forest_exec(int kind, const ForestExec *E, const uint32_t *boff, uint32_t ngraphs, uint32_t nblocks,
+                        cudaStream_t s);
+// CTAs the executor of `kind` gets for n windows (as in lpma_update)
+uint32_t exec_ctas(int kind, uint32_t n);
 // phases: 0 reset statuses and planner bitmaps, 1 pack, 2 resolve + locate,
 // 3 insert-prefix scan, 4 compact, 5 plan, 6 maximal windows, 7 status copy
 // into out[g]

@@ -692,111 +692,91 @@ __global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys
     block_sort_inreg(keys, vals, n, active_bytes(mask));
 }
 
-// ---------------------------------------------------------------- one CTA per graph
-// The batches of many graphs, one CTA each, in one launch.  Up to
-// BLOCK_SORT_MAX pairs sort in registers; larger batches (up to
-// FOREST_SORT_MAX) run an LSD sort through global memory: per digit a
-// histogram, then 8192-key chunks in input order, each ranked in registers
-// and scattered at (digit base + running digit count + stable rank).  The
-// result always ends in (k0, p0).
-__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_forest_sort(const ForestSortJob *__restrict__ jobs) {
-    const ForestSortJob J = jobs[blockIdx.x];
-    if (J.n < 2) return;
-    const uint32_t act = active_bytes(SortMask{J.andor, 0xFFu});
-    if (J.n <= (uint32_t)BLOCK_SORT_MAX) {
-        block_sort_inreg(J.k0, J.p0, J.n, act);
-        return;
+// ---------------------------------------------------------------- many graphs' batches
+// tile sort: one CTA per FOREST_SORT_TILE pairs of a batch, in place in (k0, p0)
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_forest_tile_sort(const ForestSortJob *__restrict__ jobs,
+                                                                         const uint32_t *__restrict__ boff,
+                                                                         uint32_t G) {
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestSortJob J = jobs[g];
+    const uint32_t off = (blockIdx.x - boff[g]) * FOREST_SORT_TILE;
+    if (off >= J.n) return;
+    const uint32_t len = J.n - off < FOREST_SORT_TILE ? J.n - off : FOREST_SORT_TILE;
+    block_sort_inreg(J.k0 + off, J.p0 + off, len, active_bytes(SortMask{J.andor, 0xFFu}));
+}
+
+// merge path: how many of the first d outputs of the stable merge of A
+// (a keys) and B (b keys) come from A (ties go to A)
+__device__ __forceinline__ uint32_t merge_split(const uint64_t *A, uint32_t a, const uint64_t *B, uint32_t b,
+                                                uint32_t d) {
+    uint32_t lo = d > b ? d - b : 0, hi = d < a ? d : a;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (A[mid] <= B[d - mid - 1])
+            lo = mid + 1;
+        else
+            hi = mid;
     }
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    BlockSortSmem &S = *reinterpret_cast<BlockSortSmem *>(smem_raw);
-    constexpr int IPT = BLOCK_SORT_IPT, NW = BLOCK_SORT_TPB / 32;
-    uint32_t *base = reinterpret_cast<uint32_t *>(S.k), *run = base + 256, *hist = base + 512;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const uint32_t n = J.n;
-    int pass = 0;
-    for (int byte = 0; byte < 8; byte++) {
-        if (!((act >> byte) & 1u)) continue;
-        const int sh = 8 * byte;
-        const uint64_t *ki = (pass & 1) ? J.k1 : J.k0;
-        const uint16_t *vi = (pass & 1) ? J.p1 : J.p0;
-        uint64_t *ko = (pass & 1) ? J.k0 : J.k1;
-        uint16_t *vo = (pass & 1) ? J.p0 : J.p1;
-        if (tid < 256) hist[tid] = 0;
-        __syncthreads();
-        for (uint32_t i = tid; i < n; i += BLOCK_SORT_TPB) atomicAdd(&hist[(ki[i] >> sh) & 0xFF], 1u);
-        __syncthreads();
-        // digit bases: exclusive scan of the histogram by the first eight warps
-        {
-            const uint32_t x = tid < 256 ? hist[tid] : 0u;
-            uint32_t incl = x;
-            if (tid < 256) {
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                if (lane == 31) S.wsum[w] = incl;
-            }
-            __syncthreads();
-            if (tid < 256) {
-                uint32_t b0 = 0;
-                for (int ww = 0; ww < w; ww++) b0 += S.wsum[ww];
-                base[tid] = b0 + incl - x;
-                run[tid] = 0;
-            }
-            __syncthreads();
-        }
-        for (uint32_t c0 = 0; c0 < n; c0 += (uint32_t)BLOCK_SORT_MAX) {
-            uint64_t k[IPT];
-            uint16_t v[IPT];
-            uint32_t vmask = 0;
-#pragma unroll
-            for (int i = 0; i < IPT; i++) {
-                const uint32_t p = c0 + w * 32 * IPT + i * 32 + lane;
-                if (p < n) {
-                    k[i] = ki[p];
-                    v[i] = vi[p];
-                    vmask |= 1u << i;
-                } else {
-                    k[i] = ~0ull;
-                    v[i] = 0;
-                }
-            }
-            for (int i = tid; i < NW * 256; i += BLOCK_SORT_TPB) (&S.whist[0][0])[i] = 0;
-            __syncthreads();
-            uint32_t rank[IPT];
-            warp_rank<IPT>(k, vmask, sh, S.whist[w], rank);
-            __syncthreads();
-            if (tid < 256) {  // warp-exclusive offsets of digit tid, and its chunk count
-                uint32_t t = 0;
-                for (int ww = 0; ww < NW; ww++) {
-                    const uint32_t c = S.whist[ww][tid];
-                    S.whist[ww][tid] = t;
-                    t += c;
-                }
-                S.ldig[tid] = t;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int i = 0; i < IPT; i++) {
-                if ((vmask >> i) & 1u) {
-                    const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
-                    const uint32_t g = base[d] + run[d] + S.whist[w][d] + rank[i];
-                    ko[g] = k[i];
-                    vo[g] = v[i];
-                }
-            }
-            __syncthreads();
-            if (tid < 256) run[tid] += S.ldig[tid];
-            __syncthreads();
-        }
-        pass++;
+    return lo;
+}
+
+constexpr int MERGE_TPB = 256, MERGE_IPT = FOREST_MERGE_SLICE / MERGE_TPB;
+
+// merge round r: runs of FOREST_SORT_TILE << r pairs merged two by two;
+// each CTA writes FOREST_MERGE_SLICE consecutive outputs of one pair
+__global__ void __launch_bounds__(MERGE_TPB) k_forest_merge(const ForestSortJob *__restrict__ jobs,
+                                                            const uint32_t *__restrict__ boff, uint32_t G,
+                                                            uint32_t round) {
+    __shared__ uint64_t sk[FOREST_MERGE_SLICE];
+    __shared__ uint16_t sv[FOREST_MERGE_SLICE];
+    __shared__ uint32_t split[2];
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestSortJob J = jobs[g];
+    const uint64_t *__restrict__ ks = (round & 1) ? J.k1 : J.k0;
+    const uint16_t *__restrict__ vs = (round & 1) ? J.p1 : J.p0;
+    uint64_t *__restrict__ kd = (round & 1) ? J.k0 : J.k1;
+    uint16_t *__restrict__ vd = (round & 1) ? J.p0 : J.p1;
+    const uint32_t n = J.n, L = FOREST_SORT_TILE << round;
+    const uint32_t o0 = (blockIdx.x - boff[g]) * FOREST_MERGE_SLICE;
+    if (o0 >= n) return;
+    const uint32_t base = o0 / (2 * L) * (2 * L);
+    const uint32_t a = n - base < L ? n - base : L;
+    const uint32_t b = n - base > L ? (n - base - L < L ? n - base - L : L) : 0;
+    const uint64_t *A = ks + base, *B = A + a;  // b > 0 only when a == L
+    const uint32_t d0 = o0 - base, d1 = d0 + FOREST_MERGE_SLICE < a + b ? d0 + FOREST_MERGE_SLICE : a + b;
+    if (threadIdx.x == 0) split[0] = merge_split(A, a, B, b, d0);
+    if (threadIdx.x == 32) split[1] = merge_split(A, a, B, b, d1);
+    __syncthreads();
+    const uint32_t i0 = split[0], i1 = split[1], j0 = d0 - i0;
+    const uint32_t na = i1 - i0, nt = d1 - d0;  // nt <= FOREST_MERGE_SLICE
+    for (uint32_t t = threadIdx.x; t < nt; t += MERGE_TPB) {
+        const uint32_t src = t < na ? base + i0 + t : base + a + j0 + (t - na);
+        sk[t] = ks[src];
+        sv[t] = vs[src];
     }
-    if (pass & 1) {
-        for (uint32_t i = tid; i < n; i += BLOCK_SORT_TPB) {
-            J.k0[i] = J.k1[i];
-            J.p0[i] = J.p1[i];
+    __syncthreads();
+    const uint32_t nb = nt - na;
+    const uint32_t q0 = threadIdx.x * MERGE_IPT < nt ? threadIdx.x * MERGE_IPT : nt;
+    uint32_t i = merge_split(sk, na, sk + na, nb, q0), j = q0 - i;
+    uint64_t ok[MERGE_IPT];
+    uint16_t ov[MERGE_IPT];
+#pragma unroll
+    for (int q = 0; q < MERGE_IPT; q++) {
+        if (q0 + q < nt) {
+            const bool take_a = j >= nb || (i < na && sk[i] <= sk[na + j]);
+            const uint32_t p = take_a ? i++ : na + j++;
+            ok[q] = sk[p];
+            ov[q] = sv[p];
         }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < MERGE_IPT; q++)
+        if (q0 + q < nt) sk[q0 + q] = ok[q], sv[q0 + q] = ov[q];
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < nt; t += MERGE_TPB) {
+        kd[o0 + t] = sk[t];
+        vd[o0 + t] = sv[t];
     }
 }
 
@@ -985,13 +965,22 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
 
 // Shared-memory opt-ins of the sort kernels, set once outside any stream
 // capture.
-cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t n_jobs, cudaStream_t st) {
-    if (!n_jobs) return cudaSuccess;
+cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t G, const uint32_t *d_boff, const uint32_t *nblk,
+                        uint32_t rounds, cudaStream_t st) {
+    if (!G) return cudaSuccess;
     cudaError_t e = sort_prepare();
     if (e != cudaSuccess) return e;
-    ProfScope ps("sort_forest", st);
-    k_forest_sort<<<n_jobs, BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(d_jobs);
-    note_launch();
+    {
+        ProfScope ps("forest_tile_sort", st);
+        if (nblk[0]) k_forest_tile_sort<<<nblk[0], BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(d_jobs, d_boff, G);
+        note_launch();
+    }
+    for (uint32_t r = 0; r < rounds; r++) {
+        if (!nblk[1 + r]) continue;
+        ProfScope ps("forest_merge", st);
+        k_forest_merge<<<nblk[1 + r], MERGE_TPB, 0, st>>>(d_jobs, d_boff + (size_t)(1 + r) * (G + 1), G, r);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -1020,7 +1009,7 @@ cudaError_t sort_prepare() {
         return e;
     if ((e = cudaFuncSetAttribute(k_block_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))) ||
-        (e = cudaFuncSetAttribute(k_forest_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (e = cudaFuncSetAttribute(k_forest_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))))
         return e;
     {

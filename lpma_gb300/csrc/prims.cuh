@@ -90,11 +90,26 @@ constexpr size_t sort_status_words(uint32_t n) {
 // One-time kernel attribute setup (outside stream capture).
 cudaError_t sort_prepare();
 
-// The batches of many graphs sorted in one launch, one CTA per graph
-// (k_forest_sort): (k0, p0) is sorted in place with (k1, p1) as the second
-// buffer, over the digit bytes where andor[0] (AND) and andor[1] (OR) of
-// the batch differ.  n <= FOREST_SORT_MAX.
+// The batches of many graphs sorted together (lpma_update_batch).  Each
+// batch is cut into tiles of FOREST_SORT_TILE pairs; one launch sorts every
+// tile of every batch in registers, one CTA per tile, over the digit bytes
+// where andor[0] (AND) and andor[1] (OR) of the batch differ.  Then rounds
+// of stable merge-path merges join runs pairwise, one launch per round over
+// all batches that still hold more than one run, FOREST_MERGE_SLICE outputs
+// per CTA.  Round r reads (k0, p0) when r is even and (k1, p1) when odd, so
+// a batch of forest_sort_rounds(n) rounds ends in (k1, p1) when that count
+// is odd.  n <= FOREST_SORT_MAX.
+constexpr uint32_t FOREST_SORT_TILE = BLOCK_SORT_MAX;
+constexpr uint32_t FOREST_MERGE_SLICE = 2048;
 constexpr uint32_t FOREST_SORT_MAX = 1u << 17;
+constexpr uint32_t FOREST_MERGE_ROUNDS_MAX = 4;  // 16 tiles
+inline uint32_t forest_sort_tiles(uint32_t n) { return (n + FOREST_SORT_TILE - 1) / FOREST_SORT_TILE; }
+inline uint32_t forest_sort_rounds(uint32_t n) {
+    uint32_t r = 0;
+    while ((1u << r) < forest_sort_tiles(n)) r++;
+    return r;
+}
+inline uint32_t forest_merge_ctas(uint32_t n) { return (n + FOREST_MERGE_SLICE - 1) / FOREST_MERGE_SLICE; }
 struct ForestSortJob {
     uint64_t *k0, *k1;
     uint16_t *p0, *p1;
@@ -102,7 +117,25 @@ struct ForestSortJob {
     uint32_t n;
     uint32_t pad;
 };
-cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t n_jobs, cudaStream_t st);
+// d_boff: (1 + rounds) tables of G + 1 cumulative CTA counts per job (the
+// tile launch, then merge rounds 0 .. rounds-1); nblk: the CTA total of
+// each launch (host).
+cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t G, const uint32_t *d_boff, const uint32_t *nblk,
+                        uint32_t rounds, cudaStream_t st);
+
+// Which job block b of a launch over many jobs belongs to: the last g with
+// boff[g] <= b (boff holds G + 1 cumulative block counts).
+__device__ inline uint32_t forest_job_of(const uint32_t *__restrict__ boff, uint32_t G, uint32_t b) {
+    uint32_t lo = 0, hi = G;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (boff[mid] <= b)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
 
 // Keys per tile of the cooperative sort, and the largest batch it takes on
 // this device (tiles that can be resident at once x tile); valid after

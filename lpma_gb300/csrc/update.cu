@@ -1349,18 +1349,6 @@ void launch_sum_cnt(const uint8_t *cnt, uint64_t nseg, DevStatus *st, cudaStream
 // ------------------------------------------------------------------ forest launches
 namespace {
 
-__device__ inline uint32_t forest_graph(const uint32_t *__restrict__ boff, uint32_t G, uint32_t b) {
-    uint32_t lo = 0, hi = G;  // last g with boff[g] <= b
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (boff[mid] <= b)
-            lo = mid;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
 // per-call status reset (the single-graph front copies a host template) and
 // the planner bitmap; one block per graph
 __global__ void __launch_bounds__(TPB) k_forest_reset(const ForestGraph *__restrict__ F) {
@@ -1380,18 +1368,19 @@ __global__ void __launch_bounds__(TPB) k_forest_reset(const ForestGraph *__restr
 
 __global__ void __launch_bounds__(TPB) k_forest_pack(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                      uint32_t G) {
-    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_pack_body(f.ins, f.ins_vals, f.n_ins, f.del, f.n_del, f.V, 0, f.key_format, 0, f.bk0, f.bp0, f.st,
                 blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
-// the batch was sorted in place (forest sort): parity mask {nullptr, 0}
+// the sorted batch is (f.sk, f.sp), wherever the forest sort left it:
+// parity mask {nullptr, 0}
 __global__ void __launch_bounds__(TPB) k_forest_resolve(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                         uint32_t G) {
-    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
-    k_resolve_locate_body(f.bk0, f.bp0, f.bk0, f.bp0, f.n_ins + f.n_del, SortMask{nullptr, 0u}, f.g, f.fl, 0, f.kind,
+    k_resolve_locate_body(f.sk, f.sp, f.sk, f.sp, f.n_ins + f.n_del, SortMask{nullptr, 0u}, f.g, f.fl, 0, f.kind,
                           f.seg, f.blk_nn, f.blk_ins, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
@@ -1403,15 +1392,15 @@ __global__ void __launch_bounds__(1024) k_forest_scan_pairs(const ForestGraph *_
 
 __global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                         uint32_t G) {
-    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
-    k_compact_body(f.bk0, f.bp0, f.bk0, f.bp0, SortMask{nullptr, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
+    k_compact_body(f.sk, f.sp, f.sk, f.sp, SortMask{nullptr, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
                    f.blk_ins, f.u, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                      uint32_t G) {
-    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_plan_body(f.u, f.n_ins + f.n_del, f.cnt, nullptr, 0, 0, &f.st->total_items, f.g.H, f.tb, f.bitmap, f.cand,
                 f.seg_e, f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
@@ -1419,10 +1408,28 @@ __global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restri
 
 __global__ void __launch_bounds__(TPB) k_forest_plan_max(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                          uint32_t G) {
-    const uint32_t g = forest_graph(boff, G, blockIdx.x);
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_plan_max_body(f.cand, f.n_ins + f.n_del, f.g.H, f.bitmap, f.wsingle, f.wsmall4, f.wsmall, f.wbig, f.u, f.seg_e,
                     f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+__global__ void __launch_bounds__(ES_TPB, 4) k_forest_exec_single(const ForestExec *__restrict__ E,
+                                                                   const uint32_t *boff, uint32_t G) {
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestExec &e = E[g];
+    k_exec_single_body(e.w[0], &e.st->n_single, e.n[0], e.g, e.cnt, e.fl, e.sent, e.V, e.u, 0, e.st,
+                       blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+}
+
+template <int GS>
+__global__ void __launch_bounds__(EM_TPB) k_forest_exec_multi(const ForestExec *__restrict__ E, const uint32_t *boff,
+                                                              uint32_t G) {
+    constexpr int K = GS == 4 ? 1 : 2;
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestExec &e = E[g];
+    k_exec_multi_body<GS>(e.w[K], K == 1 ? &e.st->n_small4 : &e.st->n_small, e.n[K], e.g, e.cnt, e.fl, e.sent, e.V,
+                          e.u, 0, e.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restrict__ F, DevStatus *out) {
@@ -1433,9 +1440,33 @@ __global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restr
 
 }  // namespace
 
+uint32_t exec_ctas(int kind, uint32_t n) {
+    if (!n) return 0;
+    return grid_for(n, kind == 0 ? ES_GROUPS : (kind == 1 ? 8 : 1), 152 * 8);
+}
+
+void launch_forest_exec(int kind, const ForestExec *E, const uint32_t *boff, uint32_t G, uint32_t nblocks,
+                        cudaStream_t s) {
+    if (!G || !nblocks) return;
+    if (kind == 0) {
+        ProfScope ps_("forest_exec_single", s);
+        k_forest_exec_single<<<nblocks, ES_TPB, 0, s>>>(E, boff, G);
+    } else if (kind == 1) {
+        ProfScope ps_("forest_exec_small4", s);
+        k_forest_exec_multi<4><<<nblocks, EM_TPB, 0, s>>>(E, boff, G);
+    } else {
+        ProfScope ps_("forest_exec_small32", s);
+        k_forest_exec_multi<32><<<nblocks, EM_TPB, 0, s>>>(E, boff, G);
+    }
+    note_launch();
+}
+
 void launch_forest_phase(int phase, const ForestGraph *F, const uint32_t *boff, uint32_t G, uint32_t nblocks,
                          DevStatus *out, cudaStream_t s) {
     if (!G || (phase >= 1 && phase <= 6 && phase != 3 && !nblocks)) return;
+    static const char *const names[8] = {"forest_reset",   "forest_pack", "forest_resolve", "forest_scan_pairs",
+                                         "forest_compact", "forest_plan", "forest_plan_max", "forest_status"};
+    ProfScope ps_(names[phase & 7], s);
     switch (phase) {
         case 0: k_forest_reset<<<G, TPB, 0, s>>>(F); break;
         case 1: k_forest_pack<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
