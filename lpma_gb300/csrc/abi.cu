@@ -14,10 +14,15 @@
 //      second plan with every level allowed, then fill_empty_segs; any
 //      other h rebuilds from the pre-batch array plus every update.
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "kernels.cuh"
@@ -712,6 +717,94 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
 }  // namespace
 
 // ====================================================================== C ABI
+// Host threads that finish the graphs of a batched update that need more
+// than the shared executors (big windows, overflow, resize: paths with host
+// round trips), each on its own stream so that their round trips overlap.
+struct BatchWorkers {
+    std::mutex mu;
+    std::condition_variable cv, done_cv;
+    std::vector<std::thread> th;
+    std::vector<cudaStream_t> st;
+    std::vector<cudaEvent_t> ev;
+    std::vector<uint8_t> used;
+    std::function<void(size_t, cudaStream_t)> fn;
+    std::atomic<size_t> next{0};
+    size_t n = 0;
+    uint64_t gen = 0;
+    int busy = 0;
+    bool stop = false;
+
+    cudaError_t start(int nthreads) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e) return e;
+        st.assign(nthreads, nullptr);
+        ev.assign(nthreads, nullptr);
+        used.assign(nthreads, 0);
+        for (int w = 0; w < nthreads; w++) {
+            if ((e = cudaStreamCreateWithFlags(&st[w], cudaStreamNonBlocking)) ||
+                (e = cudaEventCreateWithFlags(&ev[w], cudaEventDisableTiming)))
+                return e;
+        }
+        for (int w = 0; w < nthreads; w++) th.emplace_back([this, w, dev] { loop(w, dev); });
+        return cudaSuccess;
+    }
+
+    void loop(int w, int dev) {
+        cudaSetDevice(dev);
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || gen != seen; });
+                if (stop) return;
+                seen = gen;
+            }
+            bool any = false;
+            for (size_t i; (i = next.fetch_add(1)) < n;) {
+                fn(i, st[w]);
+                any = true;
+            }
+            if (any) cudaEventRecord(ev[w], st[w]);
+            std::lock_guard<std::mutex> lk(mu);
+            used[w] = any;
+            if (--busy == 0) done_cv.notify_all();
+        }
+    }
+
+    // runs fn(i, stream) for i < count on the workers and the calling thread
+    // (which uses s); afterwards s waits for the workers' streams
+    void run(size_t count, cudaStream_t s, std::function<void(size_t, cudaStream_t)> f) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            fn = std::move(f);
+            n = count;
+            next = 0;
+            busy = (int)th.size();
+            gen++;
+        }
+        cv.notify_all();
+        for (size_t i; (i = next.fetch_add(1)) < count;) fn(i, s);
+        std::unique_lock<std::mutex> lk(mu);
+        done_cv.wait(lk, [&] { return busy == 0; });
+        for (size_t w = 0; w < th.size(); w++)
+            if (used[w]) cudaStreamWaitEvent(s, ev[w], 0);
+    }
+
+    ~BatchWorkers() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        for (std::thread &t : th) t.join();
+        for (cudaStream_t x : st)
+            if (x) cudaStreamDestroy(x);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
 // Device and pinned tables of a batched update (lpma_update_batch), kept
 // between calls.
 struct LpmaBatcher {
@@ -724,6 +817,7 @@ struct LpmaBatcher {
     uint32_t *dX = nullptr, *hX = nullptr;  // executor block offsets: 3 tables of G + 1
     cudaEvent_t done = nullptr;             // after the last shared executor of the previous call
     bool pending = false;
+    BatchWorkers *workers = nullptr;
 };
 
 namespace {
@@ -1142,6 +1236,7 @@ lpma_status_t lpma_batcher_create(LpmaBatcher **out) {
 lpma_status_t lpma_batcher_destroy(LpmaBatcher *b) {
     if (!b) return LPMA_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
+    delete b->workers;
     batcher_free(b);
     if (b->done) cudaEventDestroy(b->done);
     delete b;
@@ -1301,8 +1396,11 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             CK(cudaEventRecord(b->done, s));
             b->pending = true;
         }
-        // each graph goes on as after its own front
-        for (uint32_t k = 0; k < G; k++) {
+        // each graph goes on as after its own front: first those of the
+        // shared executors (host work, maybe an eager level-up), then the
+        // rest, whose paths wait on the device, on several host threads
+        std::vector<uint32_t> rest;
+        auto finish = [&](uint32_t k, cudaStream_t st) {
             const size_t i = forest[k];
             LpmaHandle *h = graphs[i];
             memcpy(h->hst, &b->hS[k], sizeof(DevStatus));
@@ -1310,8 +1408,24 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             const lpma_status_t rs = (e & ERR_TIMEOUT) ? LPMA_ERR_TIMEOUT
                                                        : ((e & ERR_INTERNAL) ? LPMA_ERR_INTERNAL : LPMA_OK);
             sts[i].height_before = h->H;
-            res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, s, sts[i], &sts[i],
+            res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, st, sts[i], &sts[i],
                                    shared[k] != 0);
+        };
+        for (uint32_t k = 0; k < G; k++) {
+            if (shared[k])
+                finish(k, s);
+            else
+                rest.push_back(k);
+        }
+        if (rest.size() > 1 && !prof_enabled()) {
+            if (!b->workers) {
+                b->workers = new BatchWorkers();
+                const unsigned hw = std::thread::hardware_concurrency();
+                CK(b->workers->start((int)std::max(1u, std::min(7u, hw > 1 ? hw - 1 : 1u))));
+            }
+            b->workers->run(rest.size(), s, [&](size_t j, cudaStream_t st) { finish(rest[j], st); });
+        } else {
+            for (uint32_t k : rest) finish(k, s);
         }
     }
     for (size_t i : plain) {
