@@ -104,6 +104,7 @@ struct LpmaHandle {
     bool view_valid = false;
     uint64_t h2d = 0, d2h = 0;  // bytes copied by the current call
     cudaStream_t cap_stream = nullptr;  // private stream for graph capture
+    cudaEvent_t front_ev = nullptr;     // recorded after the front's status read-back
     std::vector<FrontGraph> graphs;
     uint64_t graph_clock = 0;
     bool host_staged = false;    // h2d already holds the staged input bytes
@@ -458,6 +459,19 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
                  thres_active ? &h->dst->live_total : &h->dst->total_items));
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    // an event record node when the front is being captured into a graph
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s, &cs));
+    CK(cudaEventRecordWithFlags(h->front_ev, s,
+                                cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
+    // the first loop's single / 4 / 32-segment windows follow without a host
+    // round trip: they read their counts on the device and do nothing when
+    // the plan overflowed.  The host waits for the read-back only, so they
+    // run while it decides what else the call needs.
+    Geo ge{h->c.keys, h->c.vals, h->H};
+    launch_exec_small(h->wsingle, (uint32_t)n, 0, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
+    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
+    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
     return LPMA_OK;
 }
 
@@ -572,8 +586,8 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     return LPMA_OK;
 }
 
-lpma_status_t wait_front(LpmaHandle *h, cudaStream_t s) {
-    CK(cudaStreamSynchronize(s));
+lpma_status_t wait_front(LpmaHandle *h, cudaStream_t) {
+    CK(cudaEventSynchronize(h->front_ev));
     CK(cudaGetLastError());
     const uint32_t e = h->hst->error | h->hst->sticky;
     if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
@@ -584,8 +598,9 @@ lpma_status_t wait_front(LpmaHandle *h, cudaStream_t s) {
 // Everything after the front's status read-back (rs is the read-back's
 // verdict, h->hst holds the status block): the window executors, the
 // root / overflow / resize paths and the stats.  Shared by lpma_update and
-// the graphs of a batched update (small_done: their first loop's common
-// executors ran in the shared launches).
+// the graphs of a batched update.  small_done: the first loop's single / 4 /
+// 32-segment executors already ran (in lpma_update's front, guarded, or in
+// the shared launches of a batched update).
 lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t thres, bool thres_active,
                             cudaStream_t s, LpmaStats &st, LpmaStats *out, bool small_done = false) {
     // a sort that gave up a bounded wait turned the front into a no-op:
@@ -672,7 +687,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
         rs = sync_status(h, s);
         if (rs != LPMA_OK) return h->sticky = rs;
     }
-    // the common path returns here while the executors run on the stream
+    // the common path returns here (big windows may still run on the stream)
     h->total = thres_active ? h->hst->cnt_total : (uint64_t)live_after;
     if (n_new && min_t_ins < h->min_t) h->min_t = min_t_ins;
     st.height_after = h->H;
@@ -711,7 +726,7 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     // batch shape repeats), then the one host round trip of the common path;
     // a rejected batch turns every kernel after k_pack into a no-op
     CKS(run_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
-    return finish_update(h, wait_front(h, s), n, thres, thres_active, s, st, out);
+    return finish_update(h, wait_front(h, s), n, thres, thres_active, s, st, out, true);
 }
 
 }  // namespace
@@ -878,6 +893,7 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     }
     h->graphs.clear();
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->front_ev) cudaEventDestroy(h->front_ev);
     free_cap(h->c);
     dfree(h->sent), dfree(h->dst);
     if (h->hst) cudaFreeHost(h->hst);
@@ -934,7 +950,8 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         return fail(LPMA_ERR_OUT_OF_MEMORY);
     // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
     h->H = 0;
-    if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) || sort_prepare())
+    if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) ||
+        cudaEventCreateWithFlags(&h->front_ev, cudaEventDisableTiming) || sort_prepare())
         return fail(LPMA_ERR_CUDA);
     if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), s) || cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) ||
         cudaMemsetAsync(h->c.vals, 0, 32, s) ||

@@ -63,9 +63,12 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
 
 // in-place executors for windows of <= 32 segments: kind 0 the
 // single-segment list (DevStatus::n_single), 1 windows of 2..4 segments
-// (n_small4), 2 windows of 5..32 segments (n_small)
+// (n_small4), 2 windows of 5..32 segments (n_small).  guarded: launched
+// before the host has read the plan (n_cap an upper bound), the executor
+// does nothing when the plan overflowed or the batch was rejected.
 void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s);
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s,
+                       bool guarded = false);
 
 // per-segment counts for the tile grain: qi/qd from the update list
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,

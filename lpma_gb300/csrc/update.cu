@@ -803,11 +803,15 @@ __device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ win
     }
 }
 
+// a plan that overflowed or a rejected batch: the guarded executors skip
+__device__ __forceinline__ bool plan_void(const DevStatus *st) { return (st->ovf | st->error) != 0; }
+
 template <int G>
 __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
                                                        uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
                                                        uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
-                                                       DevStatus *st) {
+                                                       DevStatus *st, int guarded) {
+    if (guarded && plan_void(st)) return;
     k_exec_multi_body<G>(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
 
@@ -966,7 +970,9 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
 __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restrict__ wins,
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
-                                                        const UpdList u, uint32_t thres, DevStatus *st) {
+                                                        const UpdList u, uint32_t thres, DevStatus *st,
+                                                        int guarded) {
+    if (guarded && plan_void(st)) return;
     k_exec_single_body(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
 
@@ -1274,20 +1280,22 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
 }
 
 void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s) {
+                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s,
+                       bool guarded) {
     if (!n_cap) return;
+    const int gd = guarded ? 1 : 0;
     if (kind == 0) {
         ProfScope ps_("exec_single", s);
         k_exec_single<<<grid_for(n_cap, ES_GROUPS, 152 * 8), ES_TPB, 0, s>>>(w, &st->n_single, n_cap, g, cnt, fl, sent,
-                                                                         V, u, thres, st);
+                                                                         V, u, thres, st, gd);
     } else if (kind == 1) {
         ProfScope ps_("exec_small4", s);
         k_exec_multi<4><<<grid_for(n_cap, 8, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small4, n_cap, g, cnt, fl, sent, V, u,
-                                                                       thres, st);
+                                                                       thres, st, gd);
     } else {
         ProfScope ps_("exec_small32", s);
         k_exec_multi<32><<<grid_for(n_cap, 1, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small, n_cap, g, cnt, fl, sent, V, u,
-                                                                        thres, st);
+                                                                        thres, st, gd);
     }
     note_launch();
 }
