@@ -314,10 +314,11 @@ __global__ void __launch_bounds__(SORT_TPB) k_downsweep(uint64_t *k0, V *v0, uin
 // ---------------------------------------------------------------- cooperative sort
 // All digit passes of one sort in one cooperative launch: CTA t owns tile t
 // (COOP_TILE keys) in every pass.  A pass is: load the tile, rank it by the
-// pass digit, publish the tile's digit counts; grid barrier; CTAs scan the
-// count columns (one digit each); grid barrier; every CTA adds its column
-// offsets to the global digit bases, reorders its tile through shared
-// memory and writes it out; grid barrier before the next pass reads.  The
+// pass digit, publish the tile's digit counts; grid barrier (the tile is
+// reordered in shared memory while the CTA waits); CTAs scan the count
+// columns (one digit each); grid barrier; every CTA adds its column offsets
+// to the global digit bases and writes its reordered tile out; grid
+// barrier before the next pass reads.  The
 // three grid barriers replace the reduce-then-scan sort's three launches
 // per digit and its separate histogram pass.  Every barrier wait is bounded:
 // after BAR_SPIN_LIMIT polls the CTA records ERR_TIMEOUT and goes on, so
@@ -331,11 +332,17 @@ __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
     return v;
 }
 
-__device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t target, uint32_t *err) {
+// Split grid barrier.  Arrive: after the CTA's barrier, one release add
+// (it orders every write the CTA made before it, at GPU scope).  Wait: one
+// thread polls with acquire loads, then the CTA's barrier passes the order
+// on.  Work that needs no other CTA's data can run between the two.
+__device__ __forceinline__ void grid_arrive(uint32_t *bar) {
     __syncthreads();
+    if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+}
+
+__device__ __forceinline__ void grid_wait(uint32_t *bar, uint32_t target, uint32_t *err) {
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(bar, 1u);
         uint32_t it = 0;
         while (ld_acquire_gpu(bar) < target) {
             if (++it > BAR_SPIN_LIMIT) {
@@ -344,9 +351,13 @@ __device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t target, uin
             }
             if (it > 64) __nanosleep(64);
         }
-        __threadfence();
     }
     __syncthreads();
+}
+
+__device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t target, uint32_t *err) {
+    grid_arrive(bar);
+    grid_wait(bar, target, err);
 }
 
 template <typename V>
@@ -428,7 +439,19 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
         counts[(size_t)tid * G + tile] = tcount;
         S.ldig[tid] = block_excl_scan_256(tcount, S.wsum, nullptr);
         target += G;
-        grid_barrier(bar, target, err);
+        grid_arrive(bar);
+        // while the other tiles publish their counts: reorder this tile by
+        // the pass digit in shared memory (local offsets only)
+#pragma unroll
+        for (int i = 0; i < COOP_IPT; i++) {
+            if ((vmask >> i) & 1u) {
+                const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
+                S.k[pos] = k[i];
+                S.v[pos] = v[i];
+            }
+        }
+        grid_wait(bar, target, err);
         // column scans: offs[d][t] = sum of counts[d][t' < t], totals[d].
         // Groups of S threads (S = G rounded up to a power of two) scan one
         // column each, so the 256 columns take one or two rounds of the grid
@@ -489,15 +512,6 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
             const uint32_t o = __ldcg(offs + (size_t)tile * 256 + tid);
             const uint32_t gb = block_excl_scan_256(T, S.wsum, nullptr);
             S.gbase[tid] = gb + o;
-        }
-#pragma unroll
-        for (int i = 0; i < COOP_IPT; i++) {
-            if ((vmask >> i) & 1u) {
-                const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
-                const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
-                S.k[pos] = k[i];
-                S.v[pos] = v[i];
-            }
         }
         __syncthreads();
         for (uint32_t p = tid; p < nvalid; p += SORT_TPB) {
@@ -963,8 +977,6 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
     return cudaGetLastError();
 }
 
-// Shared-memory opt-ins of the sort kernels, set once outside any stream
-// capture.
 cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t G, const uint32_t *d_boff, const uint32_t *nblk,
                         uint32_t rounds, cudaStream_t st) {
     if (!G) return cudaSuccess;
@@ -989,6 +1001,8 @@ uint32_t coop_sort_max_keys() {
     return g * (uint32_t)COOP_TILE;
 }
 
+// Shared-memory opt-ins of the sort kernels, set once outside any stream
+// capture.
 cudaError_t sort_prepare() {
     static std::mutex mu;
     static bool done = false;
