@@ -565,7 +565,7 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
     }
     // block-aggregated append of the windows this block owns
     const uint32_t ex = block_excl_scan(own ? 1u : 0u, wsum);
-    if (threadIdx.x == TPB - 1) base_s = atomicAdd(&st->n_cand, ex + (own ? 1u : 0u));
+    if (threadIdx.x == TPB - 1 && ex + (own ? 1u : 0u)) base_s = atomicAdd(&st->n_cand, ex + (own ? 1u : 0u));
     __syncthreads();
     if (own) cand[base_s + ex] = Window{(uint32_t)wa, (uint32_t)wf, (uint32_t)wm, e, lo, hi};
 }
@@ -623,11 +623,13 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
     }
     if ((threadIdx.x & 31) == 0) sl[0][threadIdx.x >> 5] = s_small, sl[1][threadIdx.x >> 5] = s_big;
     if (threadIdx.x == TPB - 1) {
+        // the status words share a cache line: only the lists this block
+        // appends to take an atomic
         const uint32_t ta = exa + pa, tb = exb + pb;
-        base_s[0] = atomicAdd(&st->n_single, ta & 0xFFFFu);
-        base_s[1] = atomicAdd(&st->n_small4, ta >> 16);
-        base_s[2] = atomicAdd(&st->n_small, tb & 0xFFFFu);
-        base_s[3] = atomicAdd(&st->n_big, tb >> 16);
+        if (ta & 0xFFFFu) base_s[0] = atomicAdd(&st->n_single, ta & 0xFFFFu);
+        if (ta >> 16) base_s[1] = atomicAdd(&st->n_small4, ta >> 16);
+        if (tb & 0xFFFFu) base_s[2] = atomicAdd(&st->n_small, tb & 0xFFFFu);
+        if (tb >> 16) base_s[3] = atomicAdd(&st->n_big, tb >> 16);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
