@@ -92,9 +92,15 @@ struct LpmaHandle {
     std::vector<TileJob> jobs_h;
     std::vector<Window> big_h;
     // host-copy staging (lpma_update_host)
-    uint64_t *stage_ins = nullptr, *stage_del = nullptr;
-    uint8_t *stage_vals = nullptr;
+    // host-batch staging, two buffer sets: the copy of one call runs on
+    // copy_stream while the previous call's executors still run
+    uint64_t *stage_ins[2] = {nullptr, nullptr}, *stage_del[2] = {nullptr, nullptr};
+    uint8_t *stage_vals[2] = {nullptr, nullptr};
     size_t stage_cap = 0;
+    int stage_next = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t stage_free[2] = {nullptr, nullptr};  // after the last call that read the set
+    cudaEvent_t copy_done = nullptr;
     // view / export
     uint32_t *row_offset = nullptr, *col_index = nullptr;
     uint8_t *view_vals = nullptr;
@@ -905,7 +911,12 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
         dfree(h->sort.hist),
         dfree(h->sort.counters);
     dfree(h->jobs_d);
-    dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
+    for (int b = 0; b < 2; b++) {
+        dfree(h->stage_ins[b]), dfree(h->stage_del[b]), dfree(h->stage_vals[b]);
+        if (h->stage_free[b]) cudaEventDestroy(h->stage_free[b]);
+    }
+    if (h->copy_done) cudaEventDestroy(h->copy_done);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals), dfree(h->exp_keys), dfree(h->exp_vals);
     dfree(h->q_cnt), dfree(h->q_tmp), dfree(h->bfs_a), dfree(h->bfs_b), dfree(h->bfs_cnt);
     dfree(h->pr_deg), dfree(h->pr_contrib), dfree(h->pr_acc), dfree(h->pr_dangling);
@@ -989,23 +1000,47 @@ lpma_status_t lpma_update_host(LpmaHandle *h, const uint64_t *h_ins, const uint8
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
     if ((n_ins && !h_ins) || (n_del && !h_del)) return LPMA_ERR_INVALID_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    if (!h->copy_stream) {
+        if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) ||
+            cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&h->stage_free[0], cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&h->stage_free[1], cudaEventDisableTiming))
+            return LPMA_ERR_CUDA;
+    }
     const size_t need = std::max(n_ins, n_del);
     if (need > h->stage_cap) {
-        dfree(h->stage_ins), dfree(h->stage_del), dfree(h->stage_vals);
+        // no copy or front may still use the old sets
+        if (cudaStreamSynchronize(s) || cudaStreamSynchronize(h->copy_stream)) return LPMA_ERR_CUDA;
+        for (int b = 0; b < 2; b++) dfree(h->stage_ins[b]), dfree(h->stage_del[b]), dfree(h->stage_vals[b]);
         h->stage_cap = 0;
         size_t cap = need + need / 4;
-        if (dalloc(&h->stage_ins, cap) || dalloc(&h->stage_del, cap) || dalloc(&h->stage_vals, cap))
-            return LPMA_ERR_OUT_OF_MEMORY;
+        for (int b = 0; b < 2; b++)
+            if (dalloc(&h->stage_ins[b], cap) || dalloc(&h->stage_del[b], cap) || dalloc(&h->stage_vals[b], cap))
+                return LPMA_ERR_OUT_OF_MEMORY;
         h->stage_cap = cap;
     }
-    if (n_ins && cudaMemcpyAsync(h->stage_ins, h_ins, n_ins * 8, cudaMemcpyHostToDevice, s)) return LPMA_ERR_CUDA;
-    if (n_ins && h_ins_vals && cudaMemcpyAsync(h->stage_vals, h_ins_vals, n_ins, cudaMemcpyHostToDevice, s))
+    // the copy waits only for the call before last (the one that read this
+    // set); the front waits for the copy
+    const int b = h->stage_next;
+    h->stage_next ^= 1;
+    cudaStream_t c = h->copy_stream;
+    CK(cudaStreamWaitEvent(c, h->stage_free[b], 0));
+    if (n_ins && cudaMemcpyAsync(h->stage_ins[b], h_ins, n_ins * 8, cudaMemcpyHostToDevice, c)) return LPMA_ERR_CUDA;
+    if (n_ins && h_ins_vals && cudaMemcpyAsync(h->stage_vals[b], h_ins_vals, n_ins, cudaMemcpyHostToDevice, c))
         return LPMA_ERR_CUDA;
-    if (n_del && cudaMemcpyAsync(h->stage_del, h_del, n_del * 8, cudaMemcpyHostToDevice, s)) return LPMA_ERR_CUDA;
+    if (n_del && cudaMemcpyAsync(h->stage_del[b], h_del, n_del * 8, cudaMemcpyHostToDevice, c)) return LPMA_ERR_CUDA;
+    CK(cudaEventRecord(h->copy_done, c));
+    CK(cudaStreamWaitEvent(s, h->copy_done, 0));
     h->h2d = n_ins * 8 + (h_ins_vals ? n_ins : 0) + n_del * 8;
     h->host_staged = true;
-    return do_update(h, h->stage_ins, h_ins_vals ? h->stage_vals : nullptr, n_ins, h->stage_del, n_del, thres, s,
-                     stats, false);
+    const lpma_status_t r = do_update(h, h->stage_ins[b], h_ins_vals ? h->stage_vals[b] : nullptr, n_ins,
+                                      h->stage_del[b], n_del, thres, s, stats, false);
+    CK(cudaEventRecord(h->stage_free[b], s));
+    // a call that ended before its front ran has not waited for the copy;
+    // the caller may reuse the host batch once the call returns
+    if (r != LPMA_OK) cudaEventSynchronize(h->copy_done);
+    return r;
 }
 
 static lpma_status_t fill_view(LpmaHandle *h, cudaStream_t s, bool csr, bool exp) {
@@ -1236,7 +1271,7 @@ lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
         const uint64_t ns = nslots_of(h->c.Hc), nseg = nseg_of(h->c.Hc);
         b += 18 * ns + nseg * (5 + 16 + 7 * 4) + bitmap_words(h->c.Hc) * 4;
     }
-    b += 4ull * h->V + h->bcap * 64ull + h->view_cap * 9ull + h->exp_cap * 9ull + h->stage_cap * 17ull;
+    b += 4ull * h->V + h->bcap * 64ull + h->view_cap * 9ull + h->exp_cap * 9ull + h->stage_cap * 34ull;
     if (h->bfs_a) b += 8ull * h->V;
     if (h->pr_deg) b += 20ull * h->V;
     b += h->q_cap * 8ull;
