@@ -193,6 +193,38 @@ def test_host_entry_point_and_pair32(engine, oracle):
     assert np.array_equal(k1, k2)
 
 
+def test_host_batches_back_to_back(engine, oracle):
+    """lpma_update_host calls in a row through one reused host buffer: each
+    call's copy runs on the handle's copy stream while the previous call's
+    executors may still run, and the buffer is overwritten as soon as the
+    call returns.  Sizes grow past the staging capacity twice."""
+    V = 1 << 12
+    e = oracle.shuffle(oracle.rmat_edges(21, 12, 16), 4)
+    import torch
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    pinned = torch.empty(e.size, dtype=torch.int64, pin_memory=True)  # asynchronous copies
+    buf = pinned.numpy().view(np.uint64)
+    rng = np.random.default_rng(2)
+    pos = 0
+    for i, n in enumerate([700, 3000, 64, 9000, 1, 20000, 500, 40000]):
+        ins = e[pos:pos + n]
+        pos += ins.size
+        k, _ = o.export_sorted()
+        live = k[((k >> np.uint64(20)) & np.uint64(0x3FFFFF)) != np.uint64(0x3FFFFE)]
+        dels = rng.choice(live, size=min(n // 3, live.size), replace=False) if live.size else live
+        if i % 2:
+            buf[:ins.size] = ins
+            g.update(ins=buf[:ins.size], dels=dels)
+        else:
+            buf[:dels.size] = dels
+            g.update(ins=ins, dels=buf[:dels.size])
+        buf[:] = np.uint64(0xFFFFFFFFFFFFFFFF)  # the call has returned: its copy must be done
+        o.update(ins=ins, dels=dels)
+        assert_same(g, o, "host batch %d" % i)
+    assert_csr(g, o)
+    g.close()
+
+
 def test_timestamp_expiry(engine, oracle):
     V = 1 << 10
     e = oracle.shuffle(oracle.rmat_edges(6, 10, 16), 8)
