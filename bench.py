@@ -330,25 +330,40 @@ def roofline(res, B, peak, peak_kind):
             "kernel_ms_per_step": {k: round(v[1] / len(pst), 4) for k, v in prof.items()}}
 
 
-REBALANCE_KERNELS = ("exec_single", "exec_small4", "exec_small32", "exec_gather", "exec_spread", "seg_counts",
-                     "seg_q", "scan")
+REBALANCE_CLASSES = (
+    ("single", ("exec_single",)),
+    ("small", ("exec_small4", "exec_small32")),
+    ("big", ("exec_gather", "exec_spread", "seg_counts", "seg_q", "scan")),
+)
 
 
 def rebalance_roofline(res, peak, peak_kind):
-    """All window rewrites of a step together (the single, 4- and 32-segment
-    executors and the big-window gather / spread with its tile preparation):
+    """Window rewrites of the profiled steps, by executor class and in total:
     18 B per rewritten slot (8 B key + 1 B value, read and written) over the
-    summed device time of those kernels."""
+    summed device time of the class's kernels.  single: one-segment windows;
+    small: 2..32 segments; big: larger windows, the root and rebuilds
+    (gather / spread with their tile preparation)."""
     prof, pst = res["prof"], res["pstats"]
     if not prof or not pst:
         return None
-    ks = [k for k in REBALANCE_KERNELS if k in prof]
-    ms = sum(prof[k][1] for k in ks) / len(pst)
-    slots = sum(s["slots_rewritten"] for s in pst) / len(pst)
-    achieved = 18 * slots / (ms / 1e3) / 1e9 if ms else 0.0
-    return {"kernels": ks, "bytes_per_step": 18 * slots, "ms_per_step": ms, "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "per_kernel_ms_per_step": {k: round(prof[k][1] / len(pst), 4) for k in ks}}
+    n = len(pst)
+    single = sum(32 * s["windows_single"] for s in pst) / n
+    small = sum(s["slots_small"] for s in pst) / n - single
+    big = sum(s["slots_rewritten"] - s["slots_small"] for s in pst) / n
+    out = {"peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "steps": n,
+           "big_window_steps": sum(1 for s in pst if s["slots_rewritten"] > s["slots_small"])}
+    tot_b = tot_ms = 0.0
+    for (name, ks), slots in zip(REBALANCE_CLASSES, (single, small, big)):
+        ms = sum(prof[k][1] for k in ks if k in prof) / n
+        b = 18 * slots
+        tot_b += b
+        tot_ms += ms
+        out[name] = {"bytes_per_step": b, "ms_per_step": ms,
+                     "achieved": b / (ms / 1e3) / 1e9 if ms else 0.0,
+                     "frac": (b / (ms / 1e3) / 1e9 / peak) if ms else 0.0}
+    out["all"] = {"bytes_per_step": tot_b, "ms_per_step": tot_ms, "achieved": tot_b / (tot_ms / 1e3) / 1e9,
+                  "frac": tot_b / (tot_ms / 1e3) / 1e9 / peak}
+    return out
 
 
 def cpu_baseline(host_edges, B, steps, threads):
