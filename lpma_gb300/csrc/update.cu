@@ -541,7 +541,11 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
             }
         }
         seg_e[s] = (uint8_t)e;
-        if (e != EXEC_OVF) {
+        if (e == 0) {
+            // a single-segment window has one leader, and the maximality
+            // probe never reads level 0: no bitmap atomic on the common path
+            own = true;
+        } else if (e != EXEC_OVF) {
             const uint64_t bit = bit_of(H, e, (uint64_t)s >> e);
             const uint32_t mask = 1u << (bit & 31);
             own = !(atomicOr(&bitmap[bit >> 5], mask) & mask);
