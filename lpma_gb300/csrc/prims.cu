@@ -616,19 +616,23 @@ struct BlockSortSmem {
     uint32_t wsum[8];
 };
 
-// in place, keys in registers; act = the digit bytes to sort
+// in place, keys in registers; act = the digit bytes to sort.  Every warp
+// holds R = ceil(n / 1024) rounds of 32 consecutive keys (warp w the range
+// [32 R w, 32 R (w + 1))), so a small batch still spreads over all 32 warps
+// and each warp ranks only R rounds per pass.
 __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals, uint32_t n, uint32_t act) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BlockSortSmem &S = *reinterpret_cast<BlockSortSmem *>(smem_raw);
     constexpr int IPT = BLOCK_SORT_IPT, NW = BLOCK_SORT_TPB / 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int R = (int)((n + BLOCK_SORT_TPB - 1) / BLOCK_SORT_TPB);  // 1..IPT
     uint64_t k[IPT];
     uint16_t v[IPT];
     uint32_t vmask = 0;
 #pragma unroll
     for (int i = 0; i < IPT; i++) {
-        const uint32_t p = w * 32 * IPT + i * 32 + lane;
-        if (p < n) {
+        const uint32_t p = w * 32 * R + i * 32 + lane;
+        if (i < R && p < n) {
             k[i] = keys[p];
             v[i] = vals[p];
             vmask |= 1u << i;
@@ -643,7 +647,7 @@ __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals,
         for (int i = tid; i < NW * 256; i += BLOCK_SORT_TPB) (&S.whist[0][0])[i] = 0;
         __syncthreads();
         uint32_t rank[IPT];
-        warp_rank<IPT>(k, vmask, sh, S.whist[w], rank);
+        warp_rank<IPT>(k, vmask, sh, S.whist[w], rank, R);
         __syncthreads();
         // digit d (thread d < 256): warp-exclusive offsets and the tile count
         uint32_t tcount = 0;
@@ -683,8 +687,8 @@ __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals,
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < IPT; i++) {
-            const uint32_t p = w * 32 * IPT + i * 32 + lane;
-            if (p < n) {
+            const uint32_t p = w * 32 * R + i * 32 + lane;
+            if (i < R && p < n) {
                 k[i] = S.k[p];
                 v[i] = S.v[p];
             }
@@ -693,8 +697,8 @@ __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals,
     }
 #pragma unroll
     for (int i = 0; i < IPT; i++) {
-        const uint32_t p = w * 32 * IPT + i * 32 + lane;
-        if (p < n) {
+        const uint32_t p = w * 32 * R + i * 32 + lane;
+        if (i < R && p < n) {
             keys[p] = k[i];
             vals[p] = v[i];
         }
@@ -916,7 +920,7 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
                              cudaStream_t st) {
     if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
-    if (sizeof(V) == 2 && n > (uint32_t)SORT_TILE && n <= (uint32_t)BLOCK_SORT_MAX) {
+    if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) {
         ProfScope ps("sort_block", st);
         k_block_sort<<<1, BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(k0, reinterpret_cast<uint16_t *>(v0), n, mask);
         note_launch();
