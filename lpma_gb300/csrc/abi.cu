@@ -305,12 +305,17 @@ bool needs_prefix(const Tables &tb, uint32_t H) {
     return false;
 }
 
+// fresh: the plan counters and the bitmap are already clear (the call's
+// first plan), so no memset sits between the front's kernels
 lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thres_active, uint64_t total_live,
-                       const Tables &tb, cudaStream_t s, const unsigned long long *total_live_dev = nullptr) {
+                       const Tables &tb, cudaStream_t s, const unsigned long long *total_live_dev = nullptr,
+                       bool fresh = false) {
     const uint32_t H = h->H;
     const uint64_t nseg = nseg_of(H);
-    CK(cudaMemsetAsync(h->c.bitmap, 0, bitmap_words(H) * 4, s));
-    CK(reset_plan_counters(h, s));
+    if (!fresh) {
+        CK(cudaMemsetAsync(h->c.bitmap, 0, bitmap_words(H) * 4, s));
+        CK(reset_plan_counters(h, s));
+    }
     const uint8_t *cntp = thres_active ? h->c.cnt_live : h->c.cnt;
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
@@ -450,7 +455,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // the engine's own sentinel keys are always in the packed layout
     const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
     launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
-                h->bk0, h->bp0, h->dst, s);
+                h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), s);
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
     const SortMask mask{&h->dst->key_and, 0xFFu};
@@ -462,8 +467,9 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
                    h->dst, s);
     // plan the first loop
     Tables tb = make_tables(h, h->H, true);
+    // the status reset cleared the plan counters and k_pack the bitmap
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
-                 thres_active ? &h->dst->live_total : &h->dst->total_items));
+                 thres_active ? &h->dst->live_total : &h->dst->total_items, true));
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
     // an event record node when the front is being captured into a graph
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -580,7 +586,10 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         uint64_t *a_ko = h->bk0;
         uint16_t *a_po = h->bp0;
         DevStatus *a_st = h->dst;
-        void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st};
+        uint32_t *a_bm = h->c.bitmap;
+        uint32_t a_bmw = (uint32_t)bitmap_words(h->H);
+        void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st,
+                        &a_bm, &a_bmw};
         cudaKernelNodeParams kp = fg->pack_params;
         kp.kernelParams = args;
         kp.extra = nullptr;

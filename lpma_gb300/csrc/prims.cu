@@ -707,6 +707,7 @@ __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals,
 
 __global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys, uint16_t *vals, uint32_t n,
                                                                    SortMask mask) {
+    griddep_wait();
     block_sort_inreg(keys, vals, n, active_bytes(mask));
 }
 
@@ -922,7 +923,8 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
     cudaError_t e;
     if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) {
         ProfScope ps("sort_block", st);
-        k_block_sort<<<1, BLOCK_SORT_TPB, sizeof(BlockSortSmem), st>>>(k0, reinterpret_cast<uint16_t *>(v0), n, mask);
+        launch_pdl(k_block_sort, dim3(1), dim3(BLOCK_SORT_TPB), sizeof(BlockSortSmem), st, k0,
+                   reinterpret_cast<uint16_t *>(v0), n, mask);
         note_launch();
         return cudaGetLastError();
     }

@@ -158,6 +158,29 @@ void note_launch(int k = 1);
 
 // Optional per-kernel timing: when enabled, every launcher brackets its
 // launch with CUDA events on the launching stream.
+// Programmatic dependent launch.  A kernel launched with launch_pdl may
+// start (be scheduled, run its prologue) while its predecessor on the stream
+// drains; it calls griddep_wait() before it touches anything the
+// predecessor writes, which waits for the whole predecessor grid and its
+// memory.  Without a programmatic predecessor the wait returns at once.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct ProfScope {
     ProfScope(const char *name, cudaStream_t s);
     ~ProfScope();

@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, 
                                               uint32_t n_ins, const uint64_t *__restrict__ del, uint32_t n_del,
                                               uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                                               uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
-                                              DevStatus *st) {
+                                              DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words) {
+    // the planner bitmap of this call starts clear
+    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < bitmap_words; i += gridDim.x * TPB) bitmap[i] = 0;
     k_pack_body(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, blockIdx.x, gridDim.x);
 }
 
@@ -308,6 +310,7 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
                                                         Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
                                                         uint32_t *blk_ins, DevStatus *st) {
+    griddep_wait();
     k_resolve_locate_body(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg, blk_nn, blk_ins, st, blockIdx.x, gridDim.x);
 }
 
@@ -358,6 +361,7 @@ __device__ __forceinline__ void k_scan_pairs_body(uint32_t *a, uint32_t *b, uint
 
 __global__ void __launch_bounds__(1024) k_scan_pairs(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
                                                      DevStatus *st) {
+    griddep_wait();
     k_scan_pairs_body(a, b, nb, ip, st, blockIdx.x, gridDim.x);
 }
 
@@ -415,6 +419,7 @@ __global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ k0
                                                  SortMask mask, const uint8_t *__restrict__ kind,
                                                  const uint32_t *__restrict__ seg, uint32_t n,
                                                  const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u) {
+    griddep_wait();
     k_compact_body(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u, blockIdx.x, gridDim.x);
 }
 
@@ -579,6 +584,7 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
                                               const unsigned long long *__restrict__ total_live_dev, uint32_t H,
                                               Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
                                               uint8_t *pend, DevStatus *st) {
+    griddep_wait();
     k_plan_body(u, n_cap, cnt, P, use_P, total_live_host, total_live_dev, H, tb, bitmap, cand, seg_e, pend, st, blockIdx.x, gridDim.x);
 }
 
@@ -653,6 +659,7 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
                                                   Window *small, Window *big, const UpdList u,
                                                   const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
+    griddep_wait();
     k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend, st, blockIdx.x, gridDim.x);
 }
 
@@ -817,6 +824,7 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
                                                        uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
                                                        uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
                                                        DevStatus *st, int guarded) {
+    griddep_wait();
     if (guarded && plan_void(st)) return;
     k_exec_multi_body<G>(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
@@ -978,6 +986,7 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restr
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
                                                         const UpdList u, uint32_t thres, DevStatus *st,
                                                         int guarded) {
+    griddep_wait();
     if (guarded && plan_void(st)) return;
     k_exec_single_body(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
@@ -1219,10 +1228,10 @@ const void *pack_kernel_fn() { return reinterpret_cast<const void *>(&k_pack); }
 
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
-                 DevStatus *st, cudaStream_t s) {
+                 DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, cudaStream_t s) {
     ProfScope ps_("pack", s);
     k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
-                                                        keys_out, pay_out, st);
+                                                        keys_out, pay_out, st, bitmap, bitmap_words);
     note_launch();
 }
 
@@ -1238,8 +1247,8 @@ void launch_resolve_locate(const uint64_t *k0, const uint16_t *p0, const uint64_
                            uint32_t *blk_nn, uint32_t *blk_ins, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("resolve_locate", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
-    k_resolve_locate<<<nb < 152 * 8 ? nb : 152 * 8, TPB, 0, s>>>(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg,
-                                                                 blk_nn, blk_ins, st);
+    launch_pdl(k_resolve_locate, dim3(nb < 152 * 8 ? nb : 152 * 8), dim3(TPB), 0, s, k0, p0, k1, p1, n, mask, g, fl,
+               thres, kind, seg, blk_nn, blk_ins, st);
     note_launch();
 }
 
@@ -1248,8 +1257,8 @@ void launch_compact(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, 
                     UpdList u, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("compact", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
-    k_scan_pairs<<<1, 1024, 0, s>>>(blk_nn, blk_ins, nb, u.ip, st);
-    k_compact<<<nb, TPB, 0, s>>>(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u);
+    launch_pdl(k_scan_pairs, dim3(1), dim3(1024), 0, s, blk_nn, blk_ins, nb, u.ip, st);
+    launch_pdl(k_compact, dim3(nb), dim3(TPB), 0, s, k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u);
     note_launch(2);
 }
 
@@ -1279,9 +1288,10 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
     ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
-    k_plan<<<nb, TPB, 0, s>>>(u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap, cand, seg_e, pend,
-                              st);
-    k_plan_max<<<nb, TPB, 0, s>>>(cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend, st);
+    launch_pdl(k_plan, dim3(nb), dim3(TPB), 0, s, u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap,
+               cand, seg_e, pend, st);
+    launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend,
+               st);
     note_launch(2);
 }
 
@@ -1292,16 +1302,16 @@ void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t
     const int gd = guarded ? 1 : 0;
     if (kind == 0) {
         ProfScope ps_("exec_single", s);
-        k_exec_single<<<grid_for(n_cap, ES_GROUPS, 152 * 8), ES_TPB, 0, s>>>(w, &st->n_single, n_cap, g, cnt, fl, sent,
-                                                                         V, u, thres, st, gd);
+        launch_pdl(k_exec_single, dim3(grid_for(n_cap, ES_GROUPS, 152 * 8)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap,
+                   g, cnt, fl, sent, V, u, thres, st, gd);
     } else if (kind == 1) {
         ProfScope ps_("exec_small4", s);
-        k_exec_multi<4><<<grid_for(n_cap, 8, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small4, n_cap, g, cnt, fl, sent, V, u,
-                                                                       thres, st, gd);
+        launch_pdl(k_exec_multi<4>, dim3(grid_for(n_cap, 8, 152 * 8)), dim3(EM_TPB), 0, s, w, &st->n_small4, n_cap, g,
+                   cnt, fl, sent, V, u, thres, st, gd);
     } else {
         ProfScope ps_("exec_small32", s);
-        k_exec_multi<32><<<grid_for(n_cap, 1, 152 * 8), EM_TPB, 0, s>>>(w, &st->n_small, n_cap, g, cnt, fl, sent, V, u,
-                                                                        thres, st, gd);
+        launch_pdl(k_exec_multi<32>, dim3(grid_for(n_cap, 1, 152 * 8)), dim3(EM_TPB), 0, s, w, &st->n_small, n_cap, g,
+                   cnt, fl, sent, V, u, thres, st, gd);
     }
     note_launch();
 }
