@@ -317,14 +317,29 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
 // exclusive scans of the two block-count arrays (one CTA); totals -> status
 __device__ __forceinline__ void k_scan_pairs_body(uint32_t *a, uint32_t *b, uint32_t nb, uint32_t *ip,
                                                      DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+    // one pass per 8192 entries: each of the 1024 threads loads up to 8
+    // consecutive pairs at once, the thread sums are scanned, then each
+    // thread writes its run
+    constexpr uint32_t PER = 8;
     __shared__ uint32_t wa[32], wb[32];
     __shared__ uint32_t ca, cb;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) ca = cb = 0;
     __syncthreads();
-    for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
-        uint32_t i = b0 + threadIdx.x;
-        uint32_t xa = i < nb ? a[i] : 0, xb = i < nb ? b[i] : 0, va = xa, vb = xb;
+    for (uint32_t b0 = 0; b0 < nb; b0 += 1024 * PER) {
+        const uint32_t cnt = nb - b0 < 1024 * PER ? nb - b0 : 1024 * PER;
+        const uint32_t per = (cnt + 1023) / 1024;
+        const uint32_t beg = b0 + threadIdx.x * per, end = b0 + cnt;
+        uint32_t xa[PER], xb[PER], sa = 0, sb = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; q++) {
+            const bool in = q < per && beg + q < end;
+            xa[q] = in ? a[beg + q] : 0u;
+            xb[q] = in ? b[beg + q] : 0u;
+            sa += xa[q];
+            sb += xb[q];
+        }
+        uint32_t va = sa, vb = sb;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t ya = __shfl_up_sync(0xffffffffu, va, o), yb = __shfl_up_sync(0xffffffffu, vb, o);
@@ -333,19 +348,25 @@ __device__ __forceinline__ void k_scan_pairs_body(uint32_t *a, uint32_t *b, uint
         if (lane == 31) wa[w] = va, wb[w] = vb;
         __syncthreads();
         if (w == 0) {
-            uint32_t sa = wa[lane], sb = wb[lane];
+            uint32_t ta = wa[lane], tb = wb[lane];
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                uint32_t ya = __shfl_up_sync(0xffffffffu, sa, o), yb = __shfl_up_sync(0xffffffffu, sb, o);
-                if (lane >= o) sa += ya, sb += yb;
+                uint32_t ya = __shfl_up_sync(0xffffffffu, ta, o), yb = __shfl_up_sync(0xffffffffu, tb, o);
+                if (lane >= o) ta += ya, tb += yb;
             }
-            wa[lane] = sa;
-            wb[lane] = sb;
+            wa[lane] = ta;
+            wb[lane] = tb;
         }
         __syncthreads();
-        if (i < nb) {
-            a[i] = ca + (w ? wa[w - 1] : 0) + va - xa;
-            b[i] = cb + (w ? wb[w - 1] : 0) + vb - xb;
+        uint32_t ra = ca + (w ? wa[w - 1] : 0) + va - sa, rb = cb + (w ? wb[w - 1] : 0) + vb - sb;
+#pragma unroll
+        for (uint32_t q = 0; q < PER; q++) {
+            if (q < per && beg + q < end) {
+                a[beg + q] = ra;
+                b[beg + q] = rb;
+            }
+            ra += xa[q];
+            rb += xb[q];
         }
         __syncthreads();
         if (threadIdx.x == 0) ca += wa[31], cb += wb[31];
@@ -907,7 +928,9 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         const uint32_t lo = W.lo, hi = active ? W.hi : W.lo;
         const uint32_t ip0 = active ? ip0c : 0;
         const uint32_t nins = active ? ip1c - ip0 : 0;
-        const uint32_t rounds = __reduce_max_sync(0xffffffffu, (hi - lo + 7) / 8);
+        // deletes were applied as tombstones by the locate: a window without
+        // inserts needs no pass over its updates
+        const uint32_t rounds = __reduce_max_sync(0xffffffffu, nins ? (hi - lo + 7) / 8 : 0u);
         for (uint32_t r = 0; r < rounds; r++) {
             const uint32_t x = lo + 8 * r + gl;
             if (x < hi && u.kind[x] == KIND_INS) {
