@@ -4,10 +4,12 @@
 //   1. pack + validate the batch (a bad key turns the rest of the front
 //      into a no-op, so the structure does not change)
 //   2. radix sort, resolve + locate + membership, compaction
-//   3. count-only plan of the first level loop (skip rule on); steps 1-3
-//      replay as one CUDA graph, then the host reads the status block
-//      (the one synchronisation of a call without overflow)
-//   4. no overflow: execute the maximal windows once; if the root took
+//   3. count-only plan of the first level loop (skip rule on), the status
+//      block read back, then the windows of up to 32 segments executed
+//      (guarded on the device: nothing happens when the plan overflowed);
+//      steps 1-3 replay as one CUDA graph and the host waits for the
+//      read-back only (the one synchronisation of a call without overflow)
+//   4. no overflow: execute the bigger maximal windows; if the root took
 //      updates, the eager level-up of rpma.cuh:1646-1653
 //      overflow (rpma.cuh:1662-1712): resize to h; h == H+1 executes the
 //      first loop, adds a level, re-locates the pending updates and runs a
