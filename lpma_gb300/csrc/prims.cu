@@ -711,16 +711,19 @@ __global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys
     block_sort_inreg(keys, vals, n, active_bytes(mask));
 }
 
-// ---------------------------------------------------------------- many graphs' batches
-// tile sort: one CTA per FOREST_SORT_TILE pairs of a batch, in place in (k0, p0)
-__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_forest_tile_sort(const ForestSortJob *__restrict__ jobs,
-                                                                         const uint32_t *__restrict__ boff,
-                                                                         uint32_t G) {
-    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
-    const ForestSortJob J = jobs[g];
-    const uint32_t off = (blockIdx.x - boff[g]) * FOREST_SORT_TILE;
+// ---------------------------------------------------------------- tile-merge sort
+// A batch of 2049..TM_MAX pairs, or the batch of one graph in a batched
+// update: tiles of J.tile (1024 or 2048) pairs sorted in registers, one CTA
+// each, then stable merge-path rounds (runs of J.tile << r pairs merged two
+// by two, FOREST_MERGE_SLICE outputs per CTA).  Round r reads (k0, p0) when
+// r is even; the tile is chosen so that the round count is even, so the
+// result always ends in (k0, p0).
+
+// tile t of job J, in place
+__device__ __forceinline__ void tm_tile_body(const ForestSortJob &J, uint32_t t) {
+    const uint32_t off = t * J.tile;
     if (off >= J.n) return;
-    const uint32_t len = J.n - off < FOREST_SORT_TILE ? J.n - off : FOREST_SORT_TILE;
+    const uint32_t len = J.n - off < J.tile ? J.n - off : J.tile;
     block_sort_inreg(J.k0 + off, J.p0 + off, len, active_bytes(SortMask{J.andor, 0xFFu}));
 }
 
@@ -741,22 +744,17 @@ __device__ __forceinline__ uint32_t merge_split(const uint64_t *A, uint32_t a, c
 
 constexpr int MERGE_TPB = 256, MERGE_IPT = FOREST_MERGE_SLICE / MERGE_TPB;
 
-// merge round r: runs of FOREST_SORT_TILE << r pairs merged two by two;
-// each CTA writes FOREST_MERGE_SLICE consecutive outputs of one pair
-__global__ void __launch_bounds__(MERGE_TPB) k_forest_merge(const ForestSortJob *__restrict__ jobs,
-                                                            const uint32_t *__restrict__ boff, uint32_t G,
-                                                            uint32_t round) {
+// merge round r of job J, output slice c (FOREST_MERGE_SLICE outputs)
+__device__ __forceinline__ void tm_merge_body(const ForestSortJob &J, uint32_t round, uint32_t c) {
     __shared__ uint64_t sk[FOREST_MERGE_SLICE];
     __shared__ uint16_t sv[FOREST_MERGE_SLICE];
     __shared__ uint32_t split[2];
-    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
-    const ForestSortJob J = jobs[g];
     const uint64_t *__restrict__ ks = (round & 1) ? J.k1 : J.k0;
     const uint16_t *__restrict__ vs = (round & 1) ? J.p1 : J.p0;
     uint64_t *__restrict__ kd = (round & 1) ? J.k0 : J.k1;
     uint16_t *__restrict__ vd = (round & 1) ? J.p0 : J.p1;
-    const uint32_t n = J.n, L = FOREST_SORT_TILE << round;
-    const uint32_t o0 = (blockIdx.x - boff[g]) * FOREST_MERGE_SLICE;
+    const uint32_t n = J.n, L = J.tile << round;
+    const uint32_t o0 = c * FOREST_MERGE_SLICE;
     if (o0 >= n) return;
     const uint32_t base = o0 / (2 * L) * (2 * L);
     const uint32_t a = n - base < L ? n - base : L;
@@ -797,6 +795,34 @@ __global__ void __launch_bounds__(MERGE_TPB) k_forest_merge(const ForestSortJob 
         kd[o0 + t] = sk[t];
         vd[o0 + t] = sv[t];
     }
+}
+
+// one batch: CTA per tile / per output slice
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_tm_tiles(ForestSortJob J) {
+    griddep_wait();
+    tm_tile_body(J, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(MERGE_TPB) k_tm_merge(ForestSortJob J, uint32_t round) {
+    griddep_wait();
+    tm_merge_body(J, round, blockIdx.x);
+}
+
+// many graphs' batches: a block finds its job in the launch's offset table
+__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_forest_tile_sort(const ForestSortJob *__restrict__ jobs,
+                                                                         const uint32_t *__restrict__ boff,
+                                                                         uint32_t G) {
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestSortJob J = jobs[g];
+    tm_tile_body(J, blockIdx.x - boff[g]);
+}
+
+__global__ void __launch_bounds__(MERGE_TPB) k_forest_merge(const ForestSortJob *__restrict__ jobs,
+                                                            const uint32_t *__restrict__ boff, uint32_t G,
+                                                            uint32_t round) {
+    const uint32_t g = forest_job_of(boff, G, blockIdx.x);
+    const ForestSortJob J = jobs[g];
+    tm_merge_body(J, round, blockIdx.x - boff[g]);
 }
 
 // ---------------------------------------------------------------- scans
@@ -921,6 +947,23 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
                              cudaStream_t st) {
     if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
+    if (sizeof(V) == 2 && n > (uint32_t)TM_TILE_MAX && n <= (uint32_t)TM_MAX) {
+        // tile-merge: the round count is even, the result ends in (k0, v0)
+        const ForestSortJob J{k0, k1, reinterpret_cast<uint16_t *>(v0), reinterpret_cast<uint16_t *>(v1), mask.andor,
+                              n, tm_tile(n)};
+        {
+            ProfScope ps("sort_tiles", st);
+            launch_pdl(k_tm_tiles, dim3((n + J.tile - 1) / J.tile), dim3(BLOCK_SORT_TPB), sizeof(BlockSortSmem), st, J);
+            note_launch();
+        }
+        const uint32_t rounds = tm_rounds(n);
+        for (uint32_t r = 0; r < rounds; r++) {
+            ProfScope ps("sort_merge", st);
+            launch_pdl(k_tm_merge, dim3(forest_merge_ctas(n)), dim3(MERGE_TPB), 0, st, J, r);
+            note_launch();
+        }
+        return cudaGetLastError();
+    }
     if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) {
         ProfScope ps("sort_block", st);
         launch_pdl(k_block_sort, dim3(1), dim3(BLOCK_SORT_TPB), sizeof(BlockSortSmem), st, k0,
@@ -1030,6 +1073,8 @@ cudaError_t sort_prepare() {
     if ((e = cudaFuncSetAttribute(k_block_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))) ||
         (e = cudaFuncSetAttribute(k_forest_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(BlockSortSmem))) ||
+        (e = cudaFuncSetAttribute(k_tm_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))))
         return e;
     {

@@ -48,10 +48,11 @@ __device__ inline uint32_t active_bytes(SortMask m) {
 constexpr int BLOCK_SORT_TPB = 1024, BLOCK_SORT_IPT = 8;
 constexpr int BLOCK_SORT_MAX = BLOCK_SORT_TPB * BLOCK_SORT_IPT;  // 8192
 
-// the largest batch sorted in place in (k0, v0) by one CTA, per payload size
+// the largest batch whose sorted result is left in (k0, v0), per payload
+// size (one-CTA sorts; for 16-bit payloads also the tile-merge tier)
 template <typename V>
 __host__ __device__ constexpr uint32_t in_place_sort_max() {
-    return sizeof(V) == 2 ? (uint32_t)BLOCK_SORT_MAX : (uint32_t)SORT_TILE;
+    return sizeof(V) == 2 ? (uint32_t)(1u << 15) : (uint32_t)SORT_TILE;
 }
 
 // true when sort_pairs_dev<uint16_t> left its result in the second buffer pair
@@ -90,32 +91,39 @@ constexpr size_t sort_status_words(uint32_t n) {
 // One-time kernel attribute setup (outside stream capture).
 cudaError_t sort_prepare();
 
-// The batches of many graphs sorted together (lpma_update_batch).  Each
-// batch is cut into tiles of FOREST_SORT_TILE pairs; one launch sorts every
-// tile of every batch in registers, one CTA per tile, over the digit bytes
-// where andor[0] (AND) and andor[1] (OR) of the batch differ.  Then rounds
-// of stable merge-path merges join runs pairwise, one launch per round over
-// all batches that still hold more than one run, FOREST_MERGE_SLICE outputs
-// per CTA.  Round r reads (k0, p0) when r is even and (k1, p1) when odd, so
-// a batch of forest_sort_rounds(n) rounds ends in (k1, p1) when that count
-// is odd.  n <= FOREST_SORT_MAX.
-constexpr uint32_t FOREST_SORT_TILE = BLOCK_SORT_MAX;
+// Tile-merge sort of 16-bit-payload pairs: batches of TM_TILE_MAX + 1 ..
+// TM_MAX pairs on their own, and the batch of each graph of a batched
+// update (lpma_update_batch, any size up to FOREST_SORT_MAX).  The batch is
+// cut into tiles of 1024 or 2048 pairs, whichever makes the number of merge
+// rounds even; one launch sorts every tile in registers, one CTA per tile,
+// over the digit bytes where andor[0] (AND) and andor[1] (OR) of the batch
+// differ.  Then rounds of stable merge-path merges join runs pairwise, one
+// launch per round, FOREST_MERGE_SLICE outputs per CTA.  Round r reads
+// (k0, p0) when r is even and (k1, p1) when odd, so with an even round
+// count the result is in (k0, p0), as after an in-place sort.
+constexpr uint32_t TM_TILE_MAX = 2048;  // up to here one CTA sorts the whole batch
+constexpr uint32_t TM_MAX = 1u << 15;  // measured: the cooperative sort wins from ~48K keys
 constexpr uint32_t FOREST_MERGE_SLICE = 2048;
 constexpr uint32_t FOREST_SORT_MAX = 1u << 17;
-constexpr uint32_t FOREST_MERGE_ROUNDS_MAX = 4;  // 16 tiles
-inline uint32_t forest_sort_tiles(uint32_t n) { return (n + FOREST_SORT_TILE - 1) / FOREST_SORT_TILE; }
-inline uint32_t forest_sort_rounds(uint32_t n) {
+constexpr uint32_t FOREST_MERGE_ROUNDS_MAX = 7;  // 131072 / 1024 = 128 tiles
+static_assert(in_place_sort_max<uint16_t>() == TM_MAX, "tile-merge results stay in the first buffer pair");
+inline uint32_t tm_rounds_for(uint32_t n, uint32_t tile) {
+    const uint32_t t = (n + tile - 1) / tile;
     uint32_t r = 0;
-    while ((1u << r) < forest_sort_tiles(n)) r++;
+    while ((1u << r) < t) r++;
     return r;
 }
+inline uint32_t tm_tile(uint32_t n) { return (tm_rounds_for(n, 1024) & 1) ? 2048u : 1024u; }
+inline uint32_t tm_rounds(uint32_t n) { return tm_rounds_for(n, tm_tile(n)); }
+inline uint32_t forest_sort_tiles(uint32_t n) { return (n + tm_tile(n) - 1) / tm_tile(n); }
+inline uint32_t forest_sort_rounds(uint32_t n) { return tm_rounds(n); }
 inline uint32_t forest_merge_ctas(uint32_t n) { return (n + FOREST_MERGE_SLICE - 1) / FOREST_MERGE_SLICE; }
 struct ForestSortJob {
     uint64_t *k0, *k1;
     uint16_t *p0, *p1;
     const unsigned long long *andor;
     uint32_t n;
-    uint32_t pad;
+    uint32_t tile;  // tm_tile(n)
 };
 // d_boff: (1 + rounds) tables of G + 1 cumulative CTA counts per job (the
 // tile launch, then merge rounds 0 .. rounds-1); nblk: the CTA total of
