@@ -249,6 +249,33 @@ LPMA_API lpma_status_t lpma_batcher_destroy(LpmaBatcher *b);
 LPMA_API lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const LpmaBatch *batches,
                                          size_t n, lpma_stream_t stream, LpmaStats *stats, lpma_status_t *status);
 
+/* ---- autotuner: the batch-sort algorithm per batch-size bucket ----
+ * The update front sorts each batch with one of five algorithms ("tiers"):
+ * 1 one CTA through shared memory (<= 2048 keys), 2 one 1024-thread CTA
+ * with keys in registers (<= 8192), 3 register-sorted tiles plus
+ * merge-path rounds (<= 2^24), 4 one cooperative launch for all digit
+ * passes (handles without LPMA_FLAG_CONCURRENT), 5 three launches per digit
+ * pass.  All give the same order.  lpma_autotune times every usable tier on
+ * seeded batches of 2^b keys for b = 11 .. ceil(log2 max_keys), for both
+ * sort modes (concurrent 0: cooperative launches allowed, 1: not), keeps
+ * the fastest in a process-wide table that later update calls read, and
+ * reports one entry per (b, mode) (median microseconds per tier; 0 where a
+ * tier does not apply).  lpma_tune_set / lpma_tune_get read or override one
+ * entry (tier 0: the built-in cutovers).  Batches of 2^(b-1)+1 .. 2^b keys
+ * use entry b.  (The reference's cut-over is fixed: rebalance_batch,
+ * rpma.cuh:1214-1256.) */
+typedef struct {
+    uint32_t log2_keys;
+    uint32_t concurrent;
+    uint32_t tier;
+    uint32_t reserved;
+    float us[6];
+} LpmaTuneEntry;
+LPMA_API lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEntry *out, size_t cap,
+                                     size_t *n_out);
+LPMA_API lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier);
+LPMA_API lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, uint32_t *tier);
+
 /* Device bytes the handle holds (structure, scratch, views). */
 LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
 

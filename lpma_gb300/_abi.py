@@ -28,7 +28,9 @@ EXPORTS = [
     "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
+    "lpma_autotune", "lpma_tune_set", "lpma_tune_get",
 ]
+SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
 SHUFFLE_STATIC_MAX_KEYS = 65536
 
@@ -78,6 +80,11 @@ class LpmaBatch(ctypes.Structure):
     _fields_ = [("ins", ctypes.c_void_p), ("ins_vals", ctypes.c_void_p), ("n_ins", ctypes.c_size_t),
                 ("dels", ctypes.c_void_p), ("n_del", ctypes.c_size_t),
                 ("thres", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class LpmaTuneEntry(ctypes.Structure):
+    _fields_ = [("log2_keys", ctypes.c_uint32), ("concurrent", ctypes.c_uint32), ("tier", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("us", ctypes.c_float * 6)]
 
 
 class LpmaError(RuntimeError):
@@ -132,6 +139,9 @@ def load():
         "lpma_batcher_create": [P],
         "lpma_batcher_destroy": [P],
         "lpma_update_batch": [P, P, P, SZ, P, P, P],
+        "lpma_autotune": [U32, P, P, SZ, P],
+        "lpma_tune_set": [U32, U32, U32],
+        "lpma_tune_get": [U32, U32, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -460,8 +460,9 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
                 h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), s);
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
-    const SortMask mask{&h->dst->key_and, 0xFFu};
-    CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s));
+    const SortTier tier = sort_tier_for_update((uint32_t)n, h->sort);
+    const SortMask mask{&h->dst->key_and, 0xFFu, sort_tier_in_place(tier) ? 0u : 1u};
+    CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s, tier));
     Geo g{h->c.keys, h->c.vals, h->H};
     launch_resolve_locate(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, g, h->c.fl, thres, h->kind, h->seg,
                           h->blk_nn, h->blk_ins, h->dst, s);
@@ -511,7 +512,8 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     } else {
         const uint64_t key[12] = {n_ins, n_del, h->H, thres,
                                   (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1) |
-                                      ((uint64_t)(h->sort.bar != nullptr) << 2),
+                                      ((uint64_t)(h->sort.bar != nullptr) << 2) |
+                                      ((uint64_t)sort_tier_for_update((uint32_t)n, h->sort) << 3),
                                   (uint64_t)h->c.keys, (uint64_t)h->c.vals, (uint64_t)h->c.cnt, (uint64_t)h->c.fl,
                                   (uint64_t)h->bk0, (uint64_t)h->c.cnt_live, (uint64_t)h->c.bitmap};
         if (h->graph_gen != h->buf_gen) {
@@ -1575,6 +1577,127 @@ lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edge_factor,
     cudaStreamSynchronize(s);
     dfree(tmp), dfree(p0), dfree(p1), dfree(flags), dfree(pos), dfree(total), dfree(stmp), dfree(err);
     dfree(ss.status), dfree(ss.hist), dfree(ss.counters);
+    return r;
+}
+
+lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier) {
+    if (log2_keys > 32 || tier >= TIER_COUNT) return LPMA_ERR_INVALID_ARGUMENT;
+    sort_tier_set(log2_keys, concurrent ? 1 : 0, (SortTier)tier);
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, uint32_t *tier) {
+    if (log2_keys > 32 || !tier) return LPMA_ERR_INVALID_ARGUMENT;
+    *tier = (uint32_t)sort_tier_get(log2_keys, concurrent ? 1 : 0);
+    return LPMA_OK;
+}
+
+// Times every usable sort tier on seeded batches of 2^b keys (the update
+// path's key layout: 21-bit source and destination ids, six active digit
+// bytes), for b = 11 .. ceil(log2 max_keys) and both sort modes, and keeps
+// the fastest per (b, mode) in the process-wide table that update calls
+// read.  All tiers give the same order, so this changes speed only.
+lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEntry *out, size_t cap,
+                            size_t *n_out) {
+    if (max_keys < 2048 || max_keys > (1u << 24)) return LPMA_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(sort_prepare());
+    uint32_t bmax = 11;
+    while ((1u << bmax) < max_keys) bmax++;
+    const uint32_t N = 1u << bmax;
+    // seeded keys, their pristine copy and running AND / OR per prefix
+    std::vector<uint64_t> hk(N);
+    std::vector<uint16_t> hp(N);
+    uint64_t x = 0x5EEDull;
+    for (uint32_t i = 0; i < N; i++) {
+        x += 0x9E3779B97F4A7C15ull;
+        uint64_t z = x;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        hk[i] = ((z & 0x1FFFFFull) << 42) | (((z >> 21) & 0x1FFFFFull) << 20);
+        hp[i] = (uint16_t)((i & 0xFF) | ((i & 1) << 8));
+    }
+    uint64_t *k0 = nullptr, *k1 = nullptr, *kp = nullptr;
+    uint16_t *p0 = nullptr, *p1 = nullptr, *pp = nullptr;
+    unsigned long long *andor = nullptr;
+    uint32_t *err = nullptr;
+    SortScratch sc;
+    sc.status_words = sort_status_words(N);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    lpma_status_t r = LPMA_OK;
+    size_t nout = 0;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(s);
+        dfree(k0), dfree(k1), dfree(kp), dfree(p0), dfree(p1), dfree(pp), dfree(andor), dfree(err);
+        dfree(sc.status), dfree(sc.hist), dfree(sc.counters);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (dalloc(&k0, N) || dalloc(&k1, N) || dalloc(&kp, N) || dalloc(&p0, N) || dalloc(&p1, N) || dalloc(&pp, N) ||
+        dalloc(&andor, 2) || dalloc(&err, 1) || dalloc(&sc.status, sc.status_words) || dalloc(&sc.hist, 8 * 256) ||
+        dalloc(&sc.counters, 16) || cudaEventCreate(&e0) || cudaEventCreate(&e1)) {
+        cleanup();
+        return LPMA_ERR_OUT_OF_MEMORY;
+    }
+    sc.err = err;
+    if (cudaMemcpy(kp, hk.data(), N * 8ull, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(pp, hp.data(), N * 2ull, cudaMemcpyHostToDevice) || cudaMemset(err, 0, 4)) {
+        cleanup();
+        return LPMA_ERR_CUDA;
+    }
+    uint64_t a = ~0ull, o = 0;
+    uint32_t done = 0;
+    for (uint32_t b = 11; b <= bmax && r == LPMA_OK; b++) {
+        const uint32_t n = 1u << b;
+        for (; done < n; done++) a &= hk[done], o |= hk[done];
+        const unsigned long long ao[2] = {a, o};
+        if (cudaMemcpy(andor, ao, sizeof(ao), cudaMemcpyHostToDevice)) {
+            r = LPMA_ERR_CUDA;
+            break;
+        }
+        for (int conc = 0; conc < 2 && r == LPMA_OK; conc++) {
+            sc.bar = conc ? nullptr : sc.counters;
+            LpmaTuneEntry ent{};
+            ent.log2_keys = b;
+            ent.concurrent = (uint32_t)conc;
+            float best = 0.f;
+            uint32_t best_t = 0;
+            for (uint32_t t = TIER_SMALL; t < TIER_COUNT; t++) {
+                if (!sort_tier_usable((SortTier)t, n, sc)) continue;
+                const SortMask m{andor, 0xFFu, sort_tier_in_place((SortTier)t) ? 0u : 1u};
+                float ts[6];
+                for (int rep = 0; rep < 6; rep++) {  // one warm-up, five timed
+                    cudaError_t ce = cudaMemcpyAsync(k0, kp, n * 8ull, cudaMemcpyDeviceToDevice, s);
+                    if (!ce) ce = cudaMemcpyAsync(p0, pp, n * 2ull, cudaMemcpyDeviceToDevice, s);
+                    if (!ce) ce = cudaEventRecord(e0, s);
+                    if (!ce) ce = sort_pairs_dev<uint16_t>(k0, p0, k1, p1, n, m, sc, s, (SortTier)t);
+                    if (!ce) ce = cudaEventRecord(e1, s);
+                    if (!ce) ce = cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    if (!ce) ce = cudaEventElapsedTime(&ms, e0, e1);
+                    if (ce) {
+                        r = LPMA_ERR_CUDA;
+                        break;
+                    }
+                    ts[rep] = ms * 1000.f;
+                }
+                if (r != LPMA_OK) break;
+                std::sort(ts + 1, ts + 6);
+                ent.us[t] = ts[3];
+                if (!best_t || ts[3] < best) best = ts[3], best_t = t;
+            }
+            uint32_t herr = 0;
+            if (r == LPMA_OK && (cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost) || herr)) r = LPMA_ERR_TIMEOUT;
+            if (r != LPMA_OK) break;
+            ent.tier = best_t;
+            sort_tier_set(b, conc, (SortTier)best_t);
+            if (out && nout < cap) out[nout] = ent;
+            nout++;
+        }
+    }
+    if (n_out) *n_out = nout;
+    cleanup();
     return r;
 }
 

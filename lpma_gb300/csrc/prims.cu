@@ -724,7 +724,7 @@ __device__ __forceinline__ void tm_tile_body(const ForestSortJob &J, uint32_t t)
     const uint32_t off = t * J.tile;
     if (off >= J.n) return;
     const uint32_t len = J.n - off < J.tile ? J.n - off : J.tile;
-    block_sort_inreg(J.k0 + off, J.p0 + off, len, active_bytes(SortMask{J.andor, 0xFFu}));
+    block_sort_inreg(J.k0 + off, J.p0 + off, len, active_bytes(SortMask{J.andor, 0xFFu, 0u}));
 }
 
 // merge path: how many of the first d outputs of the stable merge of A
@@ -942,13 +942,61 @@ constexpr int coop_slot() {
     return sizeof(V) == 2 ? 0 : (sizeof(V) == 4 ? 1 : 2);
 }
 
+// cooperative-sort geometry for n keys: tiles of at least COOP_MIN_TILE
+// keys, spread over every resident CTA slot so that the SMs carry equal work
+template <typename V>
+static bool coop_geometry(uint32_t n, const SortScratch &s, uint32_t *tile_len_out, uint32_t *G_out) {
+    const uint32_t maxG = g_coop_max_ctas[coop_slot<V>()] < 512u ? g_coop_max_ctas[coop_slot<V>()] : 512u;
+    const uint32_t tile_len = maxG ? std::max<uint32_t>(COOP_MIN_TILE, (n + maxG - 1) / maxG) : 0u;
+    const uint32_t G = tile_len ? (n + tile_len - 1) / tile_len : 0u;
+    *tile_len_out = tile_len;
+    *G_out = G;
+    return s.bar && n > (uint32_t)SORT_TILE && tile_len && tile_len <= (uint32_t)COOP_TILE && G <= maxG &&
+           s.status_words >= 512 * (size_t)G + 256;
+}
+
+template <typename V>
+static bool tier_ok(SortTier t, uint32_t n, const SortScratch &s) {
+    uint32_t tl, G;
+    switch (t) {
+        case TIER_SMALL: return n <= (uint32_t)SORT_TILE;
+        case TIER_BLOCK: return sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX;
+        case TIER_TILE_MERGE: return sizeof(V) == 2 && n <= (1u << 24);
+        case TIER_COOP: return coop_geometry<V>(n, s, &tl, &G);
+        case TIER_MULTIPASS:
+            return n > (uint32_t)SORT_TILE &&
+                   s.status_words >= 2 * (size_t)((n + SORT_TILE - 1) / SORT_TILE) * 256;
+        default: return false;
+    }
+}
+
+// the measured cutovers of this build (used until a tuning run says otherwise)
+template <typename V>
+static SortTier tier_default(uint32_t n, const SortScratch &s) {
+    if (sizeof(V) == 2 && n > TM_TILE_MAX && n <= TM_MAX) return TIER_TILE_MERGE;
+    if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) return TIER_BLOCK;
+    if (tier_ok<V>(TIER_COOP, n, s)) return TIER_COOP;
+    if (n <= (uint32_t)SORT_TILE) return TIER_SMALL;
+    // without a cooperative launch (concurrent handles) the merge rounds beat
+    // three launches per digit pass up to 2^19 keys (measured: 113 against
+    // 148 us at 2^19, 226 against 187 at 2^20)
+    if (n <= (1u << 19) && tier_ok<V>(TIER_TILE_MERGE, n, s)) return TIER_TILE_MERGE;
+    return TIER_MULTIPASS;
+}
+
+// tuned tier per (sort mode, ceil(log2 n)) for 16-bit payloads; 0 = none
+static std::atomic<uint8_t> g_tier_table[2][33];
+
+static uint32_t log2_bucket(uint32_t n) { return n <= 1 ? 0u : 32u - (uint32_t)__builtin_clz(n - 1); }
+
 template <typename V>
 static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
-                             cudaStream_t st) {
+                             cudaStream_t st, SortTier tier) {
     if (n < 2 || mask.host_mask == 0) return cudaSuccess;
     cudaError_t e;
-    if (sizeof(V) == 2 && n > (uint32_t)TM_TILE_MAX && n <= (uint32_t)TM_MAX) {
-        // tile-merge: the round count is even, the result ends in (k0, v0)
+    if (tier == TIER_AUTO || !tier_ok<V>(tier, n, s)) tier = tier_default<V>(n, s);
+    if (tier == TIER_TILE_MERGE) {
+        // the round count is even: the result ends in (k0, v0)
         const ForestSortJob J{k0, k1, reinterpret_cast<uint16_t *>(v0), reinterpret_cast<uint16_t *>(v1), mask.andor,
                               n, tm_tile(n)};
         {
@@ -964,20 +1012,16 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         }
         return cudaGetLastError();
     }
-    if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) {
+    if (tier == TIER_BLOCK) {
         ProfScope ps("sort_block", st);
         launch_pdl(k_block_sort, dim3(1), dim3(BLOCK_SORT_TPB), sizeof(BlockSortSmem), st, k0,
                    reinterpret_cast<uint16_t *>(v0), n, mask);
         note_launch();
         return cudaGetLastError();
     }
-    // cooperative sort: tiles of at least COOP_MIN_TILE keys, spread over
-    // every resident CTA slot so that the SMs carry equal work
-    const uint32_t maxG = g_coop_max_ctas[coop_slot<V>()] < 512u ? g_coop_max_ctas[coop_slot<V>()] : 512u;
-    const uint32_t tile_len = maxG ? std::max<uint32_t>(COOP_MIN_TILE, (n + maxG - 1) / maxG) : 0u;
-    const uint32_t G = tile_len ? (n + tile_len - 1) / tile_len : 0u;
-    if (s.bar && n > (uint32_t)SORT_TILE && tile_len && tile_len <= (uint32_t)COOP_TILE && G <= maxG &&
-        s.status_words >= 512 * (size_t)G + 256) {
+    if (tier == TIER_COOP) {
+        uint32_t tile_len, G;
+        coop_geometry<V>(n, s, &tile_len, &G);
         if ((e = cudaMemsetAsync(s.bar, 0, sizeof(uint32_t), st))) return e;
         uint32_t *counts = s.status, *offs = s.status + 256 * (size_t)G, *totals = s.status + 512 * (size_t)G;
         uint32_t *bar = s.bar, *err = s.err;
@@ -989,7 +1033,7 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         note_launch();
         return e;
     }
-    if (n <= (uint32_t)SORT_TILE) {
+    if (tier == TIER_SMALL) {
         const size_t sm = sizeof(SmallSmem<V>);
         ProfScope ps("sort_small", st);
         k_small_sort<V><<<1, SORT_TPB, sm, st>>>(k0, v0, n, mask);
@@ -1108,20 +1152,37 @@ cudaError_t sort_pairs(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, uin
     uint32_t byte_mask = 0;
     for (int b = 0; b < 8; b++)
         if ((diff_bits >> (8 * b)) & 0xFF) byte_mask |= 1u << b;
-    *which = (n > in_place_sort_max<V>()) ? (__builtin_popcount(byte_mask) & 1) : 0;
     cudaError_t e = sort_prepare();
     if (e != cudaSuccess) return e;
-    return sort_impl<V>(k0, v0, k1, v1, n, SortMask{nullptr, byte_mask}, s, st);
+    const SortTier t = tier_default<V>(n, s);
+    *which = (n >= 2 && !sort_tier_in_place(t)) ? (__builtin_popcount(byte_mask) & 1) : 0;
+    return sort_impl<V>(k0, v0, k1, v1, n, SortMask{nullptr, byte_mask, 0u}, s, st, t);
+}
+
+SortTier sort_tier_for_update(uint32_t n, const SortScratch &s) {
+    const uint32_t t = g_tier_table[s.bar ? 1 : 0][log2_bucket(n)].load(std::memory_order_relaxed);
+    if (t && tier_ok<uint16_t>((SortTier)t, n, s)) return (SortTier)t;
+    return tier_default<uint16_t>(n, s);
+}
+
+bool sort_tier_usable(SortTier t, uint32_t n, const SortScratch &s) { return tier_ok<uint16_t>(t, n, s); }
+
+void sort_tier_set(uint32_t bucket, int concurrent, SortTier t) {
+    if (bucket < 33) g_tier_table[concurrent ? 0 : 1][bucket].store((uint8_t)t, std::memory_order_relaxed);
+}
+
+SortTier sort_tier_get(uint32_t bucket, int concurrent) {
+    return bucket < 33 ? (SortTier)g_tier_table[concurrent ? 0 : 1][bucket].load(std::memory_order_relaxed) : TIER_AUTO;
 }
 
 template <typename V>
 cudaError_t sort_pairs_dev(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
-                           cudaStream_t st) {
-    return sort_impl<V>(k0, v0, k1, v1, n, mask, s, st);
+                           cudaStream_t st, SortTier tier) {
+    return sort_impl<V>(k0, v0, k1, v1, n, mask, s, st, tier);
 }
 
 template cudaError_t sort_pairs_dev<uint16_t>(uint64_t *, uint16_t *, uint64_t *, uint16_t *, uint32_t, SortMask,
-                                              SortScratch &, cudaStream_t);
+                                              SortScratch &, cudaStream_t, SortTier);
 template cudaError_t sort_pairs<uint16_t>(uint64_t *, uint16_t *, uint64_t *, uint16_t *, uint32_t, uint64_t,
                                           SortScratch &, uint32_t *, cudaStream_t, int *);
 template cudaError_t sort_pairs<uint64_t>(uint64_t *, uint64_t *, uint64_t *, uint64_t *, uint32_t, uint64_t,

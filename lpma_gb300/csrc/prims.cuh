@@ -25,10 +25,36 @@ struct SortScratch {
 // Digit bytes to sort: host_mask, intersected (when andor is set) with the
 // bytes where the device words andor[0] (AND of all keys) and andor[1] (OR
 // of all keys) differ.
+// pingpong: the sort that produced the batch is a ping-pong one (one
+// buffer swap per digit pass), so its result is in the second buffer pair
+// when the number of active digit bytes is odd; 0: the result is in place.
 struct SortMask {
     const unsigned long long *andor;
     uint32_t host_mask;
+    uint32_t pingpong;
 };
+
+// The sort algorithms ("tiers") of a batch sort.  All give the same stable
+// order; they differ in speed per batch size and in where the result lands.
+enum SortTier : uint32_t {
+    TIER_AUTO = 0,        // the tuned choice, else the default cutovers
+    TIER_SMALL = 1,       // one CTA through shared memory, <= 2048 keys, in place
+    TIER_BLOCK = 2,       // one 1024-thread CTA, keys in registers, <= 8192 keys, in place
+    TIER_TILE_MERGE = 3,  // register-sorted tiles + merge-path rounds, <= 2^24 keys, in place
+    TIER_COOP = 4,        // one cooperative launch, all digit passes, ping-pong
+    TIER_MULTIPASS = 5,   // three launches per digit pass, ping-pong
+    TIER_COUNT = 6
+};
+inline __host__ __device__ bool sort_tier_in_place(SortTier t) {
+    return t == TIER_SMALL || t == TIER_BLOCK || t == TIER_TILE_MERGE;
+}
+// The tier the update front sorts a batch of n 16-bit-payload pairs with:
+// the tuned table's entry for ceil(log2 n) and the scratch's mode
+// (cooperative or concurrent), when set and usable, else the default.
+SortTier sort_tier_for_update(uint32_t n, const SortScratch &s);
+bool sort_tier_usable(SortTier t, uint32_t n, const SortScratch &s);
+void sort_tier_set(uint32_t bucket, int concurrent, SortTier t);
+SortTier sort_tier_get(uint32_t bucket, int concurrent);
 
 // Which digit bytes a sort pass must handle: either fixed by the host, or
 // read from the device (bytes where the keys' AND and OR differ, restricted
@@ -48,25 +74,21 @@ __device__ inline uint32_t active_bytes(SortMask m) {
 constexpr int BLOCK_SORT_TPB = 1024, BLOCK_SORT_IPT = 8;
 constexpr int BLOCK_SORT_MAX = BLOCK_SORT_TPB * BLOCK_SORT_IPT;  // 8192
 
-// the largest batch whose sorted result is left in (k0, v0), per payload
-// size (one-CTA sorts; for 16-bit payloads also the tile-merge tier)
-template <typename V>
-__host__ __device__ constexpr uint32_t in_place_sort_max() {
-    return sizeof(V) == 2 ? (uint32_t)(1u << 15) : (uint32_t)SORT_TILE;
-}
 
 // true when sort_pairs_dev<uint16_t> left its result in the second buffer pair
 __device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
-    return n > in_place_sort_max<uint16_t>() && (__popc(active_bytes(m)) & 1);
+    return n >= 2 && m.pingpong && (__popc(active_bytes(m)) & 1);
 }
 
-// Device-decided variant: the result lands in (k1, v1) when n is above
-// in_place_sort_max<V>() and the number of active bytes is odd, else in
-// (k0, v0); kernels that consume it compute the same parity
+// Device-decided variant, sorted with `tier` (TIER_AUTO: the tuned or
+// default choice): an in-place tier leaves the result in (k0, v0); a
+// ping-pong tier leaves it in (k1, v1) when the number of active bytes is
+// odd.  The caller sets mask.pingpong to match (sort_tier_in_place), and
+// kernels that consume the result compute the same parity
 // (sort_result_odd).
 template <typename V>
 cudaError_t sort_pairs_dev(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n, SortMask mask, SortScratch &s,
-                           cudaStream_t st);
+                           cudaStream_t st, SortTier tier);
 
 // Sorts n pairs by key (stable).  Only the bytes set in diff_bits are sorted
 // (bytes equal across all keys need no pass).  The result lands either in
@@ -106,7 +128,6 @@ constexpr uint32_t TM_MAX = 1u << 15;  // measured: the cooperative sort wins fr
 constexpr uint32_t FOREST_MERGE_SLICE = 2048;
 constexpr uint32_t FOREST_SORT_MAX = 1u << 17;
 constexpr uint32_t FOREST_MERGE_ROUNDS_MAX = 7;  // 131072 / 1024 = 128 tiles
-static_assert(in_place_sort_max<uint16_t>() == TM_MAX, "tile-merge results stay in the first buffer pair");
 inline uint32_t tm_rounds_for(uint32_t n, uint32_t tile) {
     const uint32_t t = (n + tile - 1) / tile;
     uint32_t r = 0;

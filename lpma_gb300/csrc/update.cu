@@ -1427,7 +1427,7 @@ __global__ void __launch_bounds__(TPB) k_forest_resolve(const ForestGraph *__res
                                                         uint32_t G) {
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
-    k_resolve_locate_body(f.sk, f.sp, f.sk, f.sp, f.n_ins + f.n_del, SortMask{nullptr, 0u}, f.g, f.fl, 0, f.kind,
+    k_resolve_locate_body(f.sk, f.sp, f.sk, f.sp, f.n_ins + f.n_del, SortMask{nullptr, 0u, 0u}, f.g, f.fl, 0, f.kind,
                           f.seg, f.blk_nn, f.blk_ins, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
@@ -1441,7 +1441,7 @@ __global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__res
                                                         uint32_t G) {
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
-    k_compact_body(f.sk, f.sp, f.sk, f.sp, SortMask{nullptr, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
+    k_compact_body(f.sk, f.sp, f.sk, f.sp, SortMask{nullptr, 0u, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
                    f.blk_ins, f.u, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 

@@ -398,6 +398,29 @@ class Batcher:
             pass
 
 
+def autotune(max_keys=1 << 20, stream=None):
+    """Time every usable batch-sort tier per batch-size bucket and keep the
+    fastest (lpma_autotune).  Returns one dict per (bucket, sort mode)."""
+    L = _abi.load()
+    cap = 2 * 32
+    ents = (_abi.LpmaTuneEntry * cap)()
+    n = ctypes.c_size_t()
+    check(L.lpma_autotune(int(max_keys), _stream_ptr(stream), ents, cap, ctypes.byref(n)), "lpma_autotune")
+    out = []
+    for e in ents[:n.value]:
+        out.append({"keys": 1 << e.log2_keys, "concurrent": bool(e.concurrent),
+                    "tier": _abi.SORT_TIERS.get(e.tier, e.tier),
+                    "us": {_abi.SORT_TIERS[t]: round(e.us[t], 1) for t in _abi.SORT_TIERS if e.us[t] > 0}})
+    return out
+
+
+def tune_set(log2_keys, tier, concurrent=False):
+    """Override one autotuner entry (tier name or number; 0 / None = built-in cutovers)."""
+    if isinstance(tier, str):
+        tier = {v: k for k, v in _abi.SORT_TIERS.items()}[tier]
+    check(_abi.load().lpma_tune_set(int(log2_keys), 1 if concurrent else 0, int(tier or 0)), "lpma_tune_set")
+
+
 def memory_bytes(g):
     b = ctypes.c_uint64()
     check(_abi.load().lpma_memory_bytes(g._h, ctypes.byref(b)), "lpma_memory_bytes")
