@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--sweep", default="1024,10240,102400")
     ap.add_argument("--sweep-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the batch-sort autotuner (lpma_autotune) before the stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served", "skew"],
                     help="stream: the single-graph update stream (the headline line); multigraph: 256 graphs, one "
@@ -177,6 +179,11 @@ def gpu_arm(args, rank, world):
     device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(device)
     V = 1 << args.scale
+    tiers = None
+    if not args.no_autotune:
+        # sort tier per batch-size bucket, timed on this GPU (outside every timed region)
+        from lpma_gb300 import rpma
+        tiers = {str(r["keys"]): r["tier"] for r in rpma.autotune(max(args.batch, 1 << 11)) if not r["concurrent"]}
     e, S, ins_seq, del_seq = build_workload(args, device, replica_seed(args.seed, rank))
     g = L.Lpma(V)
     g.build(S)
@@ -273,7 +280,7 @@ def gpu_arm(args, rank, world):
     info = g.info()
     res = {"t": t, "lat": lat, "wall": wall, "launches": launches, "clocks": clk.summary(), "stats": stats,
            "pstats": pstats, "prof": prof, "sweep": sweep, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
-           "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"]}
+           "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"], "sort_tiers": tiers}
     host_edges = None
     if rank == 0 and not args.no_cpu_baseline:
         host_edges = (e.cpu().numpy().view(np.uint64), int(S.shape[0]))
@@ -703,6 +710,7 @@ def main():
         "e2e": {"value": B * res["e2e_steps"] * world / res["t_e2e"], "unit": "edges/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"], "entry": "lpma_update_host (pinned host batch)"},
         "gpu_launches": res["launches"],
+        "sort_tiers": res["sort_tiers"],
         "clocks": res["clocks"],
     }
     s = res["stats"]
