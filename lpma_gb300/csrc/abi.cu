@@ -91,8 +91,6 @@ struct LpmaHandle {
     uint32_t *sort_err = nullptr;
     TileJob *jobs_d = nullptr;
     size_t jobs_cap = 0;
-    std::vector<TileJob> jobs_h;
-    std::vector<Window> big_h;
     // host-copy staging (lpma_update_host)
     // host-batch staging, two buffer sets: the copy of one call runs on
     // copy_stream while the previous call's executors still run
@@ -341,17 +339,6 @@ lpma_status_t tile_prep(LpmaHandle *h, const UpdList &u, uint32_t n_list, bool t
     return LPMA_OK;
 }
 
-lpma_status_t upload_jobs(LpmaHandle *h, cudaStream_t s) {
-    if (h->jobs_h.size() > h->jobs_cap) {
-        dfree(h->jobs_d);
-        h->jobs_cap = h->jobs_h.size() * 2;
-        CK(dalloc(&h->jobs_d, h->jobs_cap));
-    }
-    CK(cudaMemcpyAsync(h->jobs_d, h->jobs_h.data(), h->jobs_h.size() * sizeof(TileJob), cudaMemcpyHostToDevice, s));
-    h->h2d += h->jobs_h.size() * sizeof(TileJob);
-    return LPMA_OK;
-}
-
 // Execute the planned maximal windows (status already synced).
 // small_done: the single / 4 / 32-segment windows were already launched
 // (the shared executors of a batched update).
@@ -370,20 +357,19 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
     st->slots_rewritten += h->hst->slots_small;
     st->slots_small += h->hst->slots_small;
     if (n_big) {
-        h->big_h.resize(n_big);
-        CK(cudaMemcpyAsync(h->big_h.data(), h->wbig, n_big * sizeof(Window), cudaMemcpyDeviceToHost, s));
-        h->d2h += n_big * sizeof(Window);
-        CKS(tile_prep(h, u, n_list, thres_active, s));
-        CK(cudaStreamSynchronize(s));
-        std::sort(h->big_h.begin(), h->big_h.end(), [](const Window &a, const Window &b) { return a.a < b.a; });
-        h->jobs_h.clear();
-        uint32_t tiles = 0;
-        for (const Window &w : h->big_h) {
-            h->jobs_h.push_back(TileJob{w.a, w.f, w.a, w.f, w.m, tiles, tiles, 0});
-            tiles += (w.f + 31) / 32;
+        // the job list is built on the device (windows sorted by position,
+        // tile prefix); the tile count came with the status read-back, so
+        // the big windows need no host round trip
+        if (n_big > h->jobs_cap) {
+            CK(cudaStreamSynchronize(s));  // the old list may still be read
+            dfree(h->jobs_d);
+            h->jobs_cap = n_big * 2;
+            CK(dalloc(&h->jobs_d, h->jobs_cap));
         }
-        CKS(upload_jobs(h, s));
-        launch_exec_big(h->jobs_d, (uint32_t)h->jobs_h.size(), tiles, tiles, g, h->c.PQ, h->c.US, u, n_list,
+        CKS(tile_prep(h, u, n_list, thres_active, s));
+        launch_big_jobs(h->wbig, n_big, h->bk1, h->bk0, h->bp1, h->bp0, h->sort, h->jobs_d, s);
+        const uint32_t tiles = h->hst->big_tiles;
+        launch_exec_big(h->jobs_d, n_big, tiles, tiles, g, h->c.PQ, h->c.US, u, n_list,
                         thres_active ? thres : 0, h->c.keys_alt, h->c.vals_alt, nslots_of(h->c.Hc), g, h->c.cnt,
                         h->c.fl, h->sent, h->V, h->dst, s);
         CK(cudaGetLastError());
@@ -427,8 +413,11 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     uint8_t *cnt_d = grow ? fresh.cnt : h->c.cnt;
     ulonglong2 *fl_d = grow ? fresh.fl : h->c.fl;
     const uint32_t sf = (uint32_t)nseg_of(H), df = (uint32_t)nseg_of(hh);
-    h->jobs_h.assign(1, TileJob{0, sf, 0, df, (uint32_t)m, 0, 0, 0});
-    CKS(upload_jobs(h, s));
+    if (!h->jobs_d) {
+        CK(dalloc(&h->jobs_d, 64));
+        h->jobs_cap = 64;
+    }
+    launch_set_job(h->jobs_d, TileJob{0, sf, 0, df, (uint32_t)m, 0, 0, 0}, s);
     const uint64_t m_cap = nslots_of(grow ? fresh.Hc : h->c.Hc);
     launch_exec_big(h->jobs_d, 1, (sf + 31) / 32, (df + 31) / 32, src, h->c.PQ, h->c.US, u, n_list,
                     thres_active ? thres : 0, Mk, Mv, m_cap, dst, cnt_d, fl_d, h->sent, h->V, h->dst, s);

@@ -94,6 +94,16 @@ void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint3
                      uint64_t *Mk, uint8_t *Mv, uint64_t m_cap, Geo dst, uint8_t *cnt_d, ulonglong2 *fl_d,
                      uint32_t *sent, uint32_t V, DevStatus *st, cudaStream_t s);
 
+// The big windows (n, count known on the host) as tile jobs in order of
+// their first segment, built on the device: the window list is sorted by
+// position in the scratch arrays, then one CTA scans the tile counts.
+void launch_big_jobs(const Window *wbig, uint32_t n, uint64_t *kscratch, uint64_t *kscratch2, uint16_t *pscratch,
+                     uint16_t *pscratch2, SortScratch &ss, TileJob *jobs, cudaStream_t s);
+
+// one job written from the kernel argument (no host staging, no implicit
+// synchronisation of a pageable copy)
+void launch_set_job(TileJob *jobs, const TileJob &j, cudaStream_t s);
+
 // new level: cnt re-index (old s -> 2s+1), empty leaves
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s);
 void launch_check_empty_level(const uint8_t *cnt, uint32_t H, DevStatus *st, cudaStream_t s);

@@ -80,6 +80,7 @@ struct DevStatus {
     uint32_t n_u;             // compacted updates
     uint32_t n_ins, n_del, n_upsert, n_noop;
     uint32_t n_cand, n_single, n_small4, n_small, n_big;
+    uint32_t big_tiles;       // 32-segment tiles of the big windows
     uint32_t root, ovf;
     uint32_t exec_levels;     // bit l: some window of level l executes
     uint32_t empty_found;     // fill_empty_segs check

@@ -647,11 +647,14 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
     const uint32_t exa = block_excl_scan(pa, wsum);
     const uint32_t exb = block_excl_scan(pb, wsum);
     unsigned long long s_small = cls <= 2 ? 32ull * w.f : 0, s_big = cls == 3 ? 32ull * w.f : 0;
+    uint32_t t_big = cls == 3 ? (w.f + 31) / 32 : 0u;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         s_small += __shfl_xor_sync(0xffffffffu, s_small, o);
         s_big += __shfl_xor_sync(0xffffffffu, s_big, o);
+        t_big += __shfl_xor_sync(0xffffffffu, t_big, o);
     }
+    if ((threadIdx.x & 31) == 0 && t_big) atomicAdd(&st->big_tiles, t_big);
     if ((threadIdx.x & 31) == 0) sl[0][threadIdx.x >> 5] = s_small, sl[1][threadIdx.x >> 5] = s_big;
     if (threadIdx.x == TPB - 1) {
         // the status words share a cache line: only the lists this block
@@ -1373,6 +1376,83 @@ void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint3
                                                                  fl_d, sent, V, st);
     }
     note_launch(n_upd ? 3 : 2);
+}
+
+namespace {
+// big windows -> (first segment, index) pairs for the sort by position
+__global__ void __launch_bounds__(TPB) k_big_keys(const Window *__restrict__ w, uint32_t n, uint64_t *keys,
+                                                  uint16_t *pay) {
+    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
+        // the window index rides in the key's low half (a < 2^32), so the
+        // sort payload is unused
+        keys[i] = ((uint64_t)w[i].a << 32) | i;
+        pay[i] = 0;
+    }
+}
+
+// sorted big windows -> tile jobs: one CTA, a chunk of windows per thread
+__global__ void __launch_bounds__(1024) k_big_jobs(const uint64_t *__restrict__ sorted, const Window *__restrict__ w,
+                                                   uint32_t n, TileJob *jobs) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t b0 = 0; b0 < n; b0 += 1024) {
+        const uint32_t i = b0 + threadIdx.x;
+        Window W{};
+        uint32_t t = 0;
+        if (i < n) {
+            W = w[(uint32_t)sorted[i]];
+            t = (W.f + 31) / 32;
+        }
+        uint32_t v = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) wsum[wp] = v;
+        __syncthreads();
+        if (wp == 0) {
+            uint32_t x = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            wsum[lane] = x;
+        }
+        __syncthreads();
+        const uint32_t ex = carry + (wp ? wsum[wp - 1] : 0) + v - t;
+        if (i < n) jobs[i] = TileJob{W.a, W.f, W.a, W.f, W.m, ex, ex, 0};
+        __syncthreads();
+        if (threadIdx.x == 0) carry += wsum[31];
+        __syncthreads();
+    }
+}
+}  // namespace
+
+namespace {
+__global__ void k_set_job(TileJob *jobs, TileJob j) { jobs[0] = j; }
+}  // namespace
+
+void launch_set_job(TileJob *jobs, const TileJob &j, cudaStream_t s) {
+    k_set_job<<<1, 1, 0, s>>>(jobs, j);
+    note_launch();
+}
+
+void launch_big_jobs(const Window *wbig, uint32_t n, uint64_t *kscratch, uint64_t *kscratch2, uint16_t *pscratch,
+                     uint16_t *pscratch2, SortScratch &ss, TileJob *jobs, cudaStream_t s) {
+    ProfScope ps_("big_jobs", s);
+    k_big_keys<<<grid_for(n, TPB), TPB, 0, s>>>(wbig, n, kscratch, pscratch);
+    // first segments are unique: sorting (a << 32 | index) by its upper four
+    // bytes orders the windows; four passes leave ping-pong tiers in place
+    const SortTier t = sort_tier_for_update(n, ss);
+    sort_pairs_dev<uint16_t>(kscratch, pscratch, kscratch2, pscratch2, n,
+                             SortMask{nullptr, 0xF0u, sort_tier_in_place(t) ? 0u : 1u}, ss, s, t);
+    k_big_jobs<<<1, 1024, 0, s>>>(kscratch, wbig, n, jobs);
+    note_launch(3);
 }
 
 void launch_levelup_cnt(const uint8_t *cnt_old, uint8_t *cnt_new, uint32_t H_old, cudaStream_t s) {
