@@ -90,6 +90,7 @@ struct LpmaHandle {
     SortScratch sort{};
     uint32_t *sort_err = nullptr;
     TileJob *jobs_d = nullptr;
+    void *arena = nullptr;  // batch scratch: every per-key buffer of an update
     size_t jobs_cap = 0;
     // host-copy staging (lpma_update_host)
     // host-batch staging, two buffer sets: the copy of one call runs on
@@ -236,27 +237,67 @@ lpma_status_t grow_to(LpmaHandle *h, uint32_t hneed, cudaStream_t s) {
     return LPMA_OK;
 }
 
-lpma_status_t ensure_batch(LpmaHandle *h, size_t n) {
+// Stream-ordered pool of the batch scratch (one arena per handle): the
+// memory stays cached in the process, so a batch that outgrows its buffers
+// costs no device-wide synchronisation (a cudaFree would stall every stream,
+// the other graphs of a batched update included).
+cudaMemPool_t batch_pool() {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps p{};
+        p.allocType = cudaMemAllocationTypePinned;
+        p.location.type = cudaMemLocationTypeDevice;
+        p.location.id = dev;
+        if (cudaMemPoolCreate(&pools[dev], &p) != cudaSuccess) {
+            pools[dev] = nullptr;
+            return nullptr;
+        }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return pools[dev];
+}
+
+// Batch scratch for n update keys: capacity the next power of two (a graph's
+// buffers move O(log n) times), all arrays carved from one arena allocated
+// on the call's stream; the old arena is released in stream order.
+lpma_status_t ensure_batch(LpmaHandle *h, size_t n, cudaStream_t s) {
     if (n <= h->bcap) return LPMA_OK;
     h->buf_gen++;
-    size_t cap = std::max<size_t>(n, 4096);
-    cap = cap + cap / 4;
-    dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
-    dfree(h->blk_nn), dfree(h->blk_ins);
-    for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall4), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status);
-    h->bcap = 0;
+    size_t cap = 4096;
+    while (cap < n) cap <<= 1;
     const size_t nb = cap / 256 + 4;
-    CK(dalloc(&h->bk0, cap)); CK(dalloc(&h->bk1, cap)); CK(dalloc(&h->bp0, cap)); CK(dalloc(&h->bp1, cap));
-    CK(dalloc(&h->kind, cap)); CK(dalloc(&h->pend, cap)); CK(dalloc(&h->seg, cap));
-    CK(dalloc(&h->blk_nn, nb)); CK(dalloc(&h->blk_ins, nb));
-    for (UpdList *u : {&h->u, &h->u2}) {
-        CK(dalloc(&u->key, cap)); CK(dalloc(&u->val, cap)); CK(dalloc(&u->kind, cap)); CK(dalloc(&u->seg, cap));
-        CK(dalloc(&u->ip, cap + 1));
+    const size_t status_words = sort_status_words((uint32_t)cap);
+    size_t off = 0;
+    std::vector<std::pair<void **, size_t>> parts;
+    auto part = [&](auto **p, size_t count) {
+        parts.emplace_back(reinterpret_cast<void **>(p), off);
+        off += (count * sizeof(**p) + 255) & ~size_t(255);
+    };
+    part(&h->bk0, cap), part(&h->bk1, cap), part(&h->bp0, cap), part(&h->bp1, cap);
+    part(&h->kind, cap), part(&h->pend, cap), part(&h->seg, cap), part(&h->blk_nn, nb), part(&h->blk_ins, nb);
+    for (UpdList *u : {&h->u, &h->u2})
+        part(&u->key, cap), part(&u->val, cap), part(&u->kind, cap), part(&u->seg, cap), part(&u->ip, cap + 1);
+    part(&h->cand, cap), part(&h->wsingle, cap), part(&h->wsmall4, cap), part(&h->wsmall, cap), part(&h->wbig, cap);
+    part(&h->sort.status, status_words);
+    h->bcap = 0;
+    if (h->arena) {
+        CK(cudaFreeAsync(h->arena, s));
+        h->arena = nullptr;
     }
-    CK(dalloc(&h->cand, cap)); CK(dalloc(&h->wsingle, cap)); CK(dalloc(&h->wsmall4, cap)); CK(dalloc(&h->wsmall, cap)); CK(dalloc(&h->wbig, cap));
-    h->sort.status_words = sort_status_words((uint32_t)cap);
-    CK(dalloc(&h->sort.status, h->sort.status_words));
+    cudaMemPool_t pool = batch_pool();
+    if (pool) {
+        CK(cudaMallocFromPoolAsync(&h->arena, off, pool, s));
+    } else {
+        CK(cudaMallocAsync(&h->arena, off, s));
+    }
+    if (poison_this("batch")) CK(cudaMemsetAsync(h->arena, 0xA5, off, s));
+    for (auto &pp : parts) *pp.first = static_cast<char *>(h->arena) + pp.second;
+    h->sort.status_words = status_words;
     h->bcap = cap;
     return LPMA_OK;
 }
@@ -726,7 +767,7 @@ lpma_status_t do_update(LpmaHandle *h, const uint64_t *ins, const uint8_t *ins_v
     if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
     if (thres > 0xFFFFF) return LPMA_ERR_INVALID_ARGUMENT;
     if (min_height(h->total + n_ins) > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
-    CKS(ensure_batch(h, n));
+    CKS(ensure_batch(h, n, s));
     h->view_valid = false;
     const bool thres_active = thres > h->min_t;
 
@@ -906,12 +947,9 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     dfree(h->sent), dfree(h->dst);
     if (h->hst) cudaFreeHost(h->hst);
     if (h->hinit) cudaFreeHost(h->hinit);
-    dfree(h->bk0), dfree(h->bk1), dfree(h->bp0), dfree(h->bp1), dfree(h->kind), dfree(h->pend), dfree(h->seg);
-    dfree(h->blk_nn), dfree(h->blk_ins);
-    for (UpdList *u : {&h->u, &h->u2}) dfree(u->key), dfree(u->val), dfree(u->kind), dfree(u->seg), dfree(u->ip);
-    dfree(h->cand), dfree(h->wsingle), dfree(h->wsmall4), dfree(h->wsmall), dfree(h->wbig), dfree(h->sort.status),
-        dfree(h->sort.hist),
-        dfree(h->sort.counters);
+    if (h->arena) cudaFree(h->arena);  // the batch scratch (synchronises)
+    h->arena = nullptr;
+    dfree(h->sort.hist), dfree(h->sort.counters);
     dfree(h->jobs_d);
     for (int b = 0; b < 2; b++) {
         dfree(h->stage_ins[b]), dfree(h->stage_del[b]), dfree(h->stage_vals[b]);
@@ -1351,7 +1389,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             LpmaHandle *h = graphs[i];
             const LpmaBatch &it = items[i];
             const size_t m = it.n_ins + it.n_del;
-            if ((res[i] = ensure_batch(h, m)) != LPMA_OK) return res[i];
+            if ((res[i] = ensure_batch(h, m, s)) != LPMA_OK) return res[i];
         }
         for (uint32_t k = 0; k < G; k++) {
             const size_t i = forest[k];
