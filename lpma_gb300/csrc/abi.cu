@@ -51,6 +51,7 @@ struct Cap {
     uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
     uint32_t *bitmap = nullptr;
     uint32_t *scan_tmp = nullptr;
+    void *arena = nullptr;  // one stream-ordered allocation holding all of the above
 };
 
 // Replays of the front as a CUDA graph, one per batch shape and buffer set.
@@ -186,61 +187,11 @@ uint32_t min_height(uint64_t cnt) {
 
 uint64_t bitmap_words(uint32_t H) { return ((1ull << (H + 2)) + 31) / 32 + 1; }
 
-void free_cap(Cap &c) {
-    dfree(c.keys), dfree(c.keys_alt), dfree(c.vals), dfree(c.vals_alt);
-    dfree(c.cnt), dfree(c.cnt_alt), dfree(c.cnt_live), dfree(c.srcc), dfree(c.seg_e);
-    dfree(c.fl);
-    dfree(c.segP), dfree(c.q), dfree(c.qn), dfree(c.PQ), dfree(c.US), dfree(c.qi), dfree(c.qd);
-    dfree(c.bitmap), dfree(c.scan_tmp);
-    c.Hc = 0;
-}
-
-cudaError_t alloc_cap(Cap &c, uint32_t Hc) {
-    const uint64_t ns = nslots_of(Hc), nseg = nseg_of(Hc);
-    cudaError_t e;
-    c.Hc = Hc;
-#define A(p, n)                             \
-    if ((e = dalloc(&c.p, (n))) != cudaSuccess) { \
-        free_cap(c);                        \
-        return e;                           \
-    }
-    A(keys, ns) A(keys_alt, ns) A(vals, ns) A(vals_alt, ns);
-    A(cnt, nseg + 64) A(cnt_alt, nseg + 64) A(cnt_live, nseg + 64) A(srcc, nseg + 64) A(seg_e, nseg + 64);
-    A(fl, nseg);
-    A(segP, nseg + 2) A(q, nseg + 2) A(qn, nseg + 2) A(PQ, nseg + 2) A(US, nseg + 2) A(qi, nseg + 2) A(qd, nseg + 2);
-    A(bitmap, bitmap_words(Hc)) A(scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
-#undef A
-    if ((e = cudaMemset(c.cnt, 0, nseg + 64)) != cudaSuccess) return e;
-    if ((e = cudaMemset(c.cnt_live, 0, nseg + 64)) != cudaSuccess) return e;
-    return cudaSuccess;
-}
-
-// Grow the capacity to hold height h, keeping the current tree (prefix copy:
-// the heap layout of height H is a prefix of any larger one).
-lpma_status_t grow_to(LpmaHandle *h, uint32_t hneed, cudaStream_t s) {
-    if (hneed <= h->c.Hc) return LPMA_OK;
-    if (hneed > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
-    uint32_t Hc = std::min<uint32_t>(hneed + 1, LPMA_MAX_HEIGHT);
-    Cap n;
-    CK(alloc_cap(n, Hc));
-    Cap &o = h->c;
-    if (o.keys) {
-        CK(cudaMemcpyAsync(n.keys, o.keys, nslots_of(h->H) * 8, cudaMemcpyDeviceToDevice, s));
-        CK(cudaMemcpyAsync(n.vals, o.vals, nslots_of(h->H), cudaMemcpyDeviceToDevice, s));
-        CK(cudaMemcpyAsync(n.cnt, o.cnt, nseg_of(h->H), cudaMemcpyDeviceToDevice, s));
-        CK(cudaMemcpyAsync(n.fl, o.fl, nseg_of(h->H) * sizeof(ulonglong2), cudaMemcpyDeviceToDevice, s));
-        CK(cudaStreamSynchronize(s));
-    }
-    free_cap(o);
-    h->c = n;
-    h->buf_gen++;
-    return LPMA_OK;
-}
-
-// Stream-ordered pool of the batch scratch (one arena per handle): the
-// memory stays cached in the process, so a batch that outgrows its buffers
-// costs no device-wide synchronisation (a cudaFree would stall every stream,
-// the other graphs of a batched update included).
+// Stream-ordered memory pool of the structure and batch arenas: the memory
+// stays cached in the process, so a batch that outgrows its buffers or a
+// tree that outgrows its capacity costs no device-wide synchronisation (a
+// cudaFree would stall every stream, the other graphs of a batched update
+// included).
 cudaMemPool_t batch_pool() {
     static std::mutex mu;
     static cudaMemPool_t pools[64] = {};
@@ -260,6 +211,72 @@ cudaMemPool_t batch_pool() {
         cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
     }
     return pools[dev];
+}
+
+cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool = batch_pool();
+    return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMallocAsync(p, bytes, s);
+}
+
+// Releases the capacity's arena in stream order (s = nullptr: at once, with
+// a device synchronisation).
+void free_cap(Cap &c, cudaStream_t s, bool now = false) {
+    if (c.arena) {
+        if (now)
+            cudaFree(c.arena);
+        else
+            cudaFreeAsync(c.arena, s);
+    }
+    c = Cap{};
+}
+
+// One arena per capacity, from the stream-ordered pool, on stream s.
+cudaError_t alloc_cap(Cap &c, uint32_t Hc, cudaStream_t s) {
+    const uint64_t ns = nslots_of(Hc), nseg = nseg_of(Hc);
+    c = Cap{};
+    c.Hc = Hc;
+    size_t off = 0;
+    std::vector<std::pair<void **, size_t>> parts;
+    auto part = [&](auto **p, size_t count) {
+        parts.emplace_back(reinterpret_cast<void **>(p), off);
+        off += (count * sizeof(**p) + 255) & ~size_t(255);
+    };
+    part(&c.keys, ns), part(&c.keys_alt, ns), part(&c.vals, ns), part(&c.vals_alt, ns);
+    part(&c.cnt, nseg + 64), part(&c.cnt_alt, nseg + 64), part(&c.cnt_live, nseg + 64), part(&c.srcc, nseg + 64);
+    part(&c.seg_e, nseg + 64), part(&c.fl, nseg);
+    part(&c.segP, nseg + 2), part(&c.q, nseg + 2), part(&c.qn, nseg + 2), part(&c.PQ, nseg + 2);
+    part(&c.US, nseg + 2), part(&c.qi, nseg + 2), part(&c.qd, nseg + 2);
+    part(&c.bitmap, bitmap_words(Hc)), part(&c.scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
+    cudaError_t e = pool_alloc(&c.arena, off, s);
+    if (e != cudaSuccess) {
+        c = Cap{};
+        return e;
+    }
+    for (auto &pp : parts) *pp.first = static_cast<char *>(c.arena) + pp.second;
+    if (poison_this("cap") && (e = cudaMemsetAsync(c.arena, 0xA5, off, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c.cnt, 0, nseg + 64, s)) != cudaSuccess) return e;
+    return cudaMemsetAsync(c.cnt_live, 0, nseg + 64, s);
+}
+
+// Grow the capacity to hold height h, keeping the current tree (prefix copy:
+// the heap layout of height H is a prefix of any larger one).
+lpma_status_t grow_to(LpmaHandle *h, uint32_t hneed, cudaStream_t s) {
+    if (hneed <= h->c.Hc) return LPMA_OK;
+    if (hneed > LPMA_MAX_HEIGHT) return LPMA_ERR_CAPACITY;
+    uint32_t Hc = std::min<uint32_t>(hneed + 1, LPMA_MAX_HEIGHT);
+    Cap n;
+    CK(alloc_cap(n, Hc, s));
+    Cap &o = h->c;
+    if (o.keys) {
+        CK(cudaMemcpyAsync(n.keys, o.keys, nslots_of(h->H) * 8, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.vals, o.vals, nslots_of(h->H), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.cnt, o.cnt, nseg_of(h->H), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(n.fl, o.fl, nseg_of(h->H) * sizeof(ulonglong2), cudaMemcpyDeviceToDevice, s));
+    }
+    free_cap(o, s);  // in stream order, after the copies
+    h->c = n;
+    h->buf_gen++;
+    return LPMA_OK;
 }
 
 // Batch scratch for n update keys: capacity the next power of two (a graph's
@@ -444,7 +461,7 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     CKS(tile_prep(h, u, n_list, thres_active, s));
     Cap fresh;
     const bool grow = hh > h->c.Hc;
-    if (grow) CK(alloc_cap(fresh, std::min<uint32_t>(hh + 1, LPMA_MAX_HEIGHT)));
+    if (grow) CK(alloc_cap(fresh, std::min<uint32_t>(hh + 1, LPMA_MAX_HEIGHT), s));
     // gather into the alternate buffer, spread into the main buffer (of the
     // new capacity when the tree outgrows the current one)
     Geo src{h->c.keys, h->c.vals, H};
@@ -464,8 +481,7 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
                     thres_active ? thres : 0, Mk, Mv, m_cap, dst, cnt_d, fl_d, h->sent, h->V, h->dst, s);
     CK(cudaGetLastError());
     if (grow) {
-        CK(cudaStreamSynchronize(s));
-        free_cap(h->c);
+        free_cap(h->c, s);  // in stream order, after the gather read it
         h->c = fresh;
         h->buf_gen++;
     } else if (hh < H) {
@@ -943,7 +959,7 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     h->graphs.clear();
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     if (h->front_ev) cudaEventDestroy(h->front_ev);
-    free_cap(h->c);
+    free_cap(h->c, nullptr, true);
     dfree(h->sent), dfree(h->dst);
     if (h->hst) cudaFreeHost(h->hst);
     if (h->hinit) cudaFreeHost(h->hinit);
@@ -997,7 +1013,7 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
     h->hinit->min_t_ins = 0xFFFFFFFFu;
     h->hinit->key_and = ~0ull;
     h->hinit->err_info[0] = 0xFFFFFFFFu;
-    if (alloc_cap(h->c, std::min<uint32_t>(min_height(num_vertices) + 1, LPMA_MAX_HEIGHT)) != cudaSuccess)
+    if (alloc_cap(h->c, std::min<uint32_t>(min_height(num_vertices) + 1, LPMA_MAX_HEIGHT), s) != cudaSuccess)
         return fail(LPMA_ERR_OUT_OF_MEMORY);
     // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
     h->H = 0;
