@@ -113,6 +113,7 @@ struct LpmaHandle {
     uint64_t h2d = 0, d2h = 0;  // bytes copied by the current call
     cudaStream_t cap_stream = nullptr;  // private stream for graph capture
     cudaEvent_t front_ev = nullptr;     // recorded after the front's status read-back
+    cudaEvent_t front_ev_blk = nullptr; // the same, waited on without spinning (concurrent handles)
     std::vector<FrontGraph> graphs;
     uint64_t graph_clock = 0;
     bool host_staged = false;    // h2d already holds the staged input bytes
@@ -319,10 +320,13 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n, cudaStream_t s) {
     return LPMA_OK;
 }
 
+// a handle that shares the GPU with concurrent callers waits without spinning
+inline bool blocking_waits(const LpmaHandle *h) { return (h->cfg.flags & LPMA_FLAG_CONCURRENT) != 0; }
+
 lpma_status_t sync_status(LpmaHandle *h, cudaStream_t s) {
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
     h->d2h += sizeof(DevStatus);
-    CK(cudaStreamSynchronize(s));
+    CK(host_wait(s, blocking_waits(h)));
     CK(cudaGetLastError());
     const uint32_t e = h->hst->error | h->hst->sticky;
     if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
@@ -523,7 +527,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // an event record node when the front is being captured into a graph
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(s, &cs));
-    CK(cudaEventRecordWithFlags(h->front_ev, s,
+    CK(cudaEventRecordWithFlags(blocking_waits(h) ? h->front_ev_blk : h->front_ev, s,
                                 cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
     // the first loop's single / 4 / 32-segment windows follow without a host
     // round trip: they read their counts on the device and do nothing when
@@ -652,7 +656,7 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
 }
 
 lpma_status_t wait_front(LpmaHandle *h, cudaStream_t) {
-    CK(cudaEventSynchronize(h->front_ev));
+    CK(blocking_waits(h) ? event_wait(h->front_ev_blk) : cudaEventSynchronize(h->front_ev));
     CK(cudaGetLastError());
     const uint32_t e = h->hst->error | h->hst->sticky;
     if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
@@ -959,6 +963,7 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     h->graphs.clear();
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     if (h->front_ev) cudaEventDestroy(h->front_ev);
+    if (h->front_ev_blk) cudaEventDestroy(h->front_ev_blk);
     free_cap(h->c, nullptr, true);
     dfree(h->sent), dfree(h->dst);
     if (h->hst) cudaFreeHost(h->hst);
@@ -1018,7 +1023,8 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
     // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
     h->H = 0;
     if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) ||
-        cudaEventCreateWithFlags(&h->front_ev, cudaEventDisableTiming) || sort_prepare())
+        cudaEventCreateWithFlags(&h->front_ev, cudaEventDisableTiming) ||
+        cudaEventCreateWithFlags(&h->front_ev_blk, cudaEventDisableTiming | cudaEventBlockingSync) || sort_prepare())
         return fail(LPMA_ERR_CUDA);
     if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), s) || cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) ||
         cudaMemsetAsync(h->c.vals, 0, 32, s) ||
@@ -1231,7 +1237,7 @@ lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const 
         CK(cudaMemsetAsync(d_offsets, 0, sizeof(uint32_t), s));
     }
     CK(cudaMemcpyAsync(h->pin_word, d_offsets + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(host_wait(s, blocking_waits(h)));
     *total = h->pin_word[0];
     if (!d_nbrs || !n) return LPMA_OK;
     if (*total > cap) return LPMA_ERR_BUFFER_TOO_SMALL;
@@ -1265,7 +1271,7 @@ lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_source
     CK(cudaMemsetAsync(h->bfs_cnt, 0, 2 * sizeof(uint32_t), s));
     launch_bfs_init(d_sources, (uint32_t)n_sources, h->V, d_dist, h->bfs_a, h->bfs_cnt, s);
     CK(cudaMemcpyAsync(h->pin_word, h->bfs_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    CK(host_wait(s, blocking_waits(h)));
     uint32_t nf = h->pin_word[0], lv = 0;
     uint64_t total = nf;
     uint32_t *cur = h->bfs_a, *nxt = h->bfs_b;
@@ -1275,7 +1281,7 @@ lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_source
         launch_bfs_expand(cur, h->bfs_cnt, nf, (int32_t)lv, g, h->c.cnt, h->sent, d_dist, nxt, h->bfs_cnt + 1, s);
         CK(cudaMemcpyAsync(h->bfs_cnt, h->bfs_cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
         CK(cudaMemcpyAsync(h->pin_word, h->bfs_cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(host_wait(s, blocking_waits(h)));
         nf = h->pin_word[0];
         total += nf;
         lv++;

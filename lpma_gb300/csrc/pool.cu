@@ -20,6 +20,8 @@
 
 #include <cuda_runtime.h>
 
+#include "prims.cuh"
+
 #include "lpma.h"
 
 namespace {
@@ -130,7 +132,7 @@ struct LpmaPool {
                     st = lpma_edge_query(r->graph, r->keys0, r->n0, r->thres, r->out_u32, ls);
                     break;
             }
-            const cudaError_t ce = cudaStreamSynchronize(s);
+            const cudaError_t ce = lpma::host_wait(s, true);
             if (st == LPMA_OK && ce != cudaSuccess) st = LPMA_ERR_CUDA;
             r->status = st;
             r->t_end_ns = now_ns();

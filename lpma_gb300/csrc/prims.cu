@@ -10,6 +10,7 @@
 // sorted by one CTA in shared memory in a single launch.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -46,6 +47,33 @@ static cudaEvent_t pool_event() {
 }
 
 bool prof_enabled() { return g_prof_on; }
+
+cudaError_t host_wait(cudaStream_t s, bool blocking) {
+    if (!blocking) return cudaStreamSynchronize(s);
+    thread_local cudaEvent_t ev = nullptr;
+    thread_local int ev_dev = -1;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (!ev || ev_dev != dev) {
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming))) return e;
+        ev_dev = dev;
+    }
+    if ((e = cudaEventRecord(ev, s))) return e;
+    return event_wait(ev);
+}
+
+cudaError_t event_wait(cudaEvent_t ev) {
+    // short waits end in the spin; long ones sleep (the event was created
+    // with cudaEventBlockingSync)
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t q = cudaEventQuery(ev);
+        if (q != cudaErrorNotReady) return q;
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(40)) break;
+    }
+    return cudaEventSynchronize(ev);
+}
 
 ProfScope::ProfScope(const char *name, cudaStream_t st) : idx(-1), s(st) {
     if (!g_prof_on) return;

@@ -210,6 +210,15 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// Host wait for everything enqueued on s.  blocking: the calling thread
+// spins briefly, then sleeps until the GPU signals (an event created with
+// cudaEventBlockingSync); for the many threads of a request pool, whose
+// spins would crowd the host cores.
+cudaError_t host_wait(cudaStream_t s, bool blocking);
+// Wait for an event created with cudaEventBlockingSync: spin for up to 40 us,
+// then sleep until it completes.
+cudaError_t event_wait(cudaEvent_t ev);
+
 struct ProfScope {
     ProfScope(const char *name, cudaStream_t s);
     ~ProfScope();

@@ -37,7 +37,7 @@ def test_autotune_reports_and_sets(engine, reset_table):
     import ctypes
     for r in rows:
         assert r["tier"] in r["us"], r  # the chosen tier was timed
-        assert r["tier"] == min(r["us"], key=r["us"].get)
+        assert r["us"][r["tier"]] <= min(r["us"].values()) + 0.1  # the fastest (times reported to 0.1 us)
         if not r["concurrent"] and r["keys"] > 2048:
             assert "cooperative" in r["us"]
         if r["concurrent"]:
