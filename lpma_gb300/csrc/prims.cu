@@ -770,6 +770,32 @@ __device__ __forceinline__ uint32_t merge_split(const uint64_t *A, uint32_t a, c
     return lo;
 }
 
+// The same split found by one warp: each step evaluates the merge-path
+// predicate at 32 evenly spaced candidates at once (one memory round trip)
+// and keeps the interval between the last true and the first false, so a
+// run of 2^k keys takes about k / 5 round trips instead of k.
+__device__ __forceinline__ uint32_t merge_split_warp(const uint64_t *A, uint32_t a, const uint64_t *B, uint32_t b,
+                                                     uint32_t d) {
+    const int lane = threadIdx.x & 31;
+    uint32_t lo = d > b ? d - b : 0, hi = d < a ? d : a;  // answer in [lo, hi]
+    while (hi - lo > 32) {
+        const uint32_t span = hi - lo;
+        // candidate i = lo + span * (lane + 1) / 33, strictly inside (lo, hi)
+        const uint32_t i = lo + (uint32_t)(((uint64_t)span * (uint32_t)(lane + 1)) / 33u);
+        const bool p = A[i] <= B[d - i - 1];  // true: the answer is above i
+        const uint32_t t = __ballot_sync(0xffffffffu, p);
+        // the predicate is monotone (true then false): count the trues
+        const int nt = __popc(t);
+        const uint32_t new_lo = nt ? lo + (uint32_t)(((uint64_t)span * (uint32_t)nt) / 33u) + 1 : lo;
+        const uint32_t new_hi = nt < 32 ? lo + (uint32_t)(((uint64_t)span * (uint32_t)(nt + 1)) / 33u) : hi;
+        lo = new_lo, hi = new_hi;
+    }
+    // at most 32 candidates left: one more round over lo .. hi - 1
+    const uint32_t i = lo + (uint32_t)lane;
+    const bool p = i < hi && A[i] <= B[d - i - 1];
+    return lo + (uint32_t)__popc(__ballot_sync(0xffffffffu, p));
+}
+
 constexpr int MERGE_TPB = 256, MERGE_IPT = FOREST_MERGE_SLICE / MERGE_TPB;
 
 // merge round r of job J, output slice c (FOREST_MERGE_SLICE outputs)
@@ -789,8 +815,10 @@ __device__ __forceinline__ void tm_merge_body(const ForestSortJob &J, uint32_t r
     const uint32_t b = n - base > L ? (n - base - L < L ? n - base - L : L) : 0;
     const uint64_t *A = ks + base, *B = A + a;  // b > 0 only when a == L
     const uint32_t d0 = o0 - base, d1 = d0 + FOREST_MERGE_SLICE < a + b ? d0 + FOREST_MERGE_SLICE : a + b;
-    if (threadIdx.x == 0) split[0] = merge_split(A, a, B, b, d0);
-    if (threadIdx.x == 32) split[1] = merge_split(A, a, B, b, d1);
+    if (threadIdx.x < 64) {  // warp 0: the slice's start, warp 1: its end
+        const uint32_t r = merge_split_warp(A, a, B, b, threadIdx.x < 32 ? d0 : d1);
+        if ((threadIdx.x & 31) == 0) split[threadIdx.x >> 5] = r;
+    }
     __syncthreads();
     const uint32_t i0 = split[0], i1 = split[1], j0 = d0 - i0;
     const uint32_t na = i1 - i0, nt = d1 - d0;  // nt <= FOREST_MERGE_SLICE
