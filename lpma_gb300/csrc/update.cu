@@ -772,10 +772,12 @@ __device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ win
         uint64_t *outk = S.outk[unit];
         uint8_t *outv = S.outv[unit];
         // kept slots: rank = kept before + inserts of the segment below the key
+        // (a segment with deletes only needs no search: its deletes are
+        // tombstones already)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if ((kmask >> q) & 1u) {
-                const uint32_t below = ue > us ? u.ip[lb_key(u.key, us, ue, k[q])] - ip0 : 0;
+                const uint32_t below = nins ? u.ip[lb_key(u.key, us, ue, k[q])] - ip0 : 0;
                 const uint32_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
                 if (r < 32 * G) {
                     outk[r] = k[q];
@@ -784,7 +786,7 @@ __device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ win
             }
         }
         // inserts: rank = inserts before + kept keys below
-        for (uint32_t x = us + gl; x < ue; x += 8) {
+        for (uint32_t x = us + gl; nins && x < ue; x += 8) {
             if (u.kind[x] != KIND_INS) continue;
             const uint64_t y = u.key[x];
             uint32_t L = 0, R = nk;
