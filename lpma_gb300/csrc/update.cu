@@ -938,9 +938,13 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         const uint32_t rounds = __reduce_max_sync(0xffffffffu, nins ? (hi - lo + 7) / 8 : 0u);
         for (uint32_t r = 0; r < rounds; r++) {
             const uint32_t x = lo + 8 * r + gl;
-            if (x < hi && u.kind[x] == KIND_INS) {
-                const uint64_t yk = u.key[x];
-                const uint32_t ri = u.ip[x] - ip0;
+            // the update's fields load together (not behind the kind test)
+            uint8_t kd = KIND_NOP, yv = 0;
+            uint64_t yk = 0;
+            uint32_t yip = 0;
+            if (x < hi) kd = u.kind[x], yk = u.key[x], yip = u.ip[x], yv = u.val[x];
+            if (kd == KIND_INS) {
+                const uint32_t ri = yip - ip0;
                 uint32_t L = 0, R = nk;
                 while (L < R) {
                     const uint32_t mid = (L + R) >> 1;
@@ -952,7 +956,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
                 if (ri < 32) ik[grp][ri] = yk;
                 if (ri + L < 32) {
                     sk[grp][ri + L] = yk;
-                    sv[grp][ri + L] = u.val[x];
+                    sv[grp][ri + L] = yv;
                 }
             }
         }
