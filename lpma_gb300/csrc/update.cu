@@ -646,14 +646,12 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
     const uint32_t pb = (cls == 2 || cls == 3) ? 1u << (16 * (cls - 2)) : 0u;
     const uint32_t exa = block_excl_scan(pa, wsum);
     const uint32_t exb = block_excl_scan(pb, wsum);
-    unsigned long long s_small = cls <= 2 ? 32ull * w.f : 0, s_big = cls == 3 ? 32ull * w.f : 0;
+    // slots of disjoint maximal windows: a warp's sums stay below 2^32
+    uint32_t s_small = cls <= 2 ? 32u * w.f : 0u, s_big = cls == 3 ? 32u * w.f : 0u;
     uint32_t t_big = cls == 3 ? (w.f + 31) / 32 : 0u;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        s_small += __shfl_xor_sync(0xffffffffu, s_small, o);
-        s_big += __shfl_xor_sync(0xffffffffu, s_big, o);
-        t_big += __shfl_xor_sync(0xffffffffu, t_big, o);
-    }
+    s_small = __reduce_add_sync(0xffffffffu, s_small);
+    s_big = __reduce_add_sync(0xffffffffu, s_big);
+    t_big = __reduce_add_sync(0xffffffffu, t_big);
     if ((threadIdx.x & 31) == 0 && t_big) atomicAdd(&st->big_tiles, t_big);
     if ((threadIdx.x & 31) == 0) sl[0][threadIdx.x >> 5] = s_small, sl[1][threadIdx.x >> 5] = s_big;
     if (threadIdx.x == TPB - 1) {
