@@ -258,13 +258,17 @@ def gpu_arm(args, rank, world):
 
     # end to end through the host entry point: pinned host batch -> lpma_update_host
     e2e_steps = min(args.steps, 10)
+    e2e_warm = 2  # untimed: the host entry allocates its staging buffers on first use
     host_batches = []
-    for i in range(e2e_steps):
+    for i in range(e2e_warm + e2e_steps):
         k = (args.warmup + args.steps + prof_steps + i) % 2
         b = st.next(kinds[k], B)
         hb = torch.empty(B, dtype=torch.int64, pin_memory=True)
         hb.copy_(b)
         host_batches.append((k, hb.numpy().view(np.uint64)))
+    for k, hb in host_batches[:e2e_warm]:
+        g.update(ins=hb) if k == 0 else g.update(dels=hb)
+    host_batches = host_batches[e2e_warm:]
     torch.cuda.synchronize()
     e2e_stats = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
