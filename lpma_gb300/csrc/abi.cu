@@ -1438,7 +1438,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             f.tb = make_tables(h, h->H, true);
             f.total_items = h->total;
             f.st = h->dst;
-            b->hJ[k] = ForestSortJob{h->bk0, h->bk1, h->bp0, h->bp1, &h->dst->key_and, m, tm_tile(m)};
+            b->hJ[k] = ForestSortJob{h->bk0, h->bk1, h->bp0, h->bp1, &h->dst->key_and, m, tm_tile_forest(m)};
             const uint32_t rk = forest_sort_rounds(m);
             rounds = std::max(rounds, rk);
             f.sk = (rk & 1) ? h->bk1 : h->bk0;

@@ -136,8 +136,15 @@ inline uint32_t tm_rounds_for(uint32_t n, uint32_t tile) {
 }
 inline uint32_t tm_tile(uint32_t n) { return (tm_rounds_for(n, 1024) & 1) ? 2048u : 1024u; }
 inline uint32_t tm_rounds(uint32_t n) { return tm_rounds_for(n, tm_tile(n)); }
-inline uint32_t forest_sort_tiles(uint32_t n) { return (n + tm_tile(n) - 1) / tm_tile(n); }
-inline uint32_t forest_sort_rounds(uint32_t n) { return tm_rounds(n); }
+// A batched update sorts for throughput (many graphs' tiles fill the GPU):
+// one tile up to 8192 pairs, else tiles of 8192 or 4096 (even rounds);
+// bigger tiles sort more keys per SM-microsecond.
+inline uint32_t tm_tile_forest(uint32_t n) {
+    if (n <= 8192) return 8192;
+    return (tm_rounds_for(n, 8192) & 1) ? 4096u : 8192u;
+}
+inline uint32_t forest_sort_tiles(uint32_t n) { return (n + tm_tile_forest(n) - 1) / tm_tile_forest(n); }
+inline uint32_t forest_sort_rounds(uint32_t n) { return tm_rounds_for(n, tm_tile_forest(n)); }
 inline uint32_t forest_merge_ctas(uint32_t n) { return (n + FOREST_MERGE_SLICE - 1) / FOREST_MERGE_SLICE; }
 struct ForestSortJob {
     uint64_t *k0, *k1;
@@ -153,17 +160,24 @@ cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t G, const uint32_t 
                         uint32_t rounds, cudaStream_t st);
 
 // Which job block b of a launch over many jobs belongs to: the last g with
-// boff[g] <= b (boff holds G + 1 cumulative block counts).
+// boff[g] <= b (boff holds G + 1 cumulative block counts).  Called by whole
+// warps.
 __device__ inline uint32_t forest_job_of(const uint32_t *__restrict__ boff, uint32_t G, uint32_t b) {
-    uint32_t lo = 0, hi = G;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (boff[mid] <= b)
-            lo = mid;
-        else
-            hi = mid;
+    // every lane of the warp asks for the same b: 32 entries are probed per
+    // memory round trip (two for a few hundred jobs, instead of eight
+    // dependent loads of a plain binary search)
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t lo = 0, hi = G;  // boff[lo] <= b, and the answer is below hi
+    while (hi - lo > 32) {
+        const uint32_t span = hi - lo;
+        const uint32_t i = lo + (uint32_t)(((uint64_t)span * (lane + 1)) / 33u);
+        const int nt = __popc(__ballot_sync(0xffffffffu, boff[i] <= b));
+        const uint32_t new_lo = nt ? lo + (uint32_t)(((uint64_t)span * (uint32_t)nt) / 33u) : lo;
+        const uint32_t new_hi = nt < 32 ? lo + (uint32_t)(((uint64_t)span * (uint32_t)(nt + 1)) / 33u) : hi;
+        lo = new_lo, hi = new_hi;
     }
-    return lo;
+    const bool p = lo + lane < hi && boff[lo + lane] <= b;
+    return lo + (uint32_t)__popc(__ballot_sync(0xffffffffu, p)) - 1;
 }
 
 // Keys per tile of the cooperative sort, and the largest batch it takes on
