@@ -17,6 +17,7 @@ the host cores, the reference's CPU path) on the same workload and metric.
 """
 import argparse
 import ctypes
+import gc
 import json
 import os
 import statistics
@@ -579,31 +580,65 @@ def served_arm(args):
             torch.cuda.synchronize()
             pool = rpma.Pool(workers, budget)
             reqs = []
-            t0 = time.perf_counter()
-            t0_ns = time.perf_counter_ns()  # the pool's clock (steady_clock) runs on the same monotonic source
-            for at, p in zip(arrivals, plan):
-                d = t0 + at - time.perf_counter()
-                if d > 0:
-                    time.sleep(d)
-                if p[0] == "upd":
-                    G = gs.graphs[p[1]]["g"]
-                    q = pool.update(G, ins=p[3]) if p[2] == "ins" else pool.update(G, dels=p[3])
-                elif p[0] == "nbr":
-                    q = pool.neighbors(gs.graphs[p[1]]["g"], *p[2:])
-                else:
-                    q = pool.bfs(gs.graphs[p[1]]["g"], p[2], p[3], 2)
-                q.arrival_ns = t0_ns + int(at * 1e9)
-                reqs.append((p[0], q, int(p[3].numel()) if p[0] == "upd" else 0))
-            pool.drain()
-            t = time.perf_counter() - t0
+            # The load generator runs without Python's cyclic garbage
+            # collector: its full collections over the request objects
+            # stalled submissions by up to 54 ms at 8,000 requests/s, which
+            # showed up as queueing of every request behind them.
+            gc.collect()
+            gc.disable()
+            try:
+                t0 = time.perf_counter()
+                t0_ns = time.perf_counter_ns()  # the pool's clock (steady_clock) runs on the same monotonic source
+                for at, p in zip(arrivals, plan):
+                    d = t0 + at - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    if p[0] == "upd":
+                        G = gs.graphs[p[1]]["g"]
+                        q = pool.update(G, ins=p[3]) if p[2] == "ins" else pool.update(G, dels=p[3])
+                    elif p[0] == "nbr":
+                        q = pool.neighbors(gs.graphs[p[1]]["g"], *p[2:])
+                    else:
+                        q = pool.bfs(gs.graphs[p[1]]["g"], p[2], p[3], 2)
+                    q.arrival_ns = t0_ns + int(at * 1e9)
+                    reqs.append((p[0], q, int(p[3].numel()) if p[0] == "upd" else 0))
+                pool.drain()
+                t = time.perf_counter() - t0
+            finally:
+                gc.enable()
             pool.close()
             stat = {"wall_s": t, "updated_edges_per_s": sum(e for _, _, e in reqs) / t}
             for kind in ("upd", "nbr", "bfs"):
-                lat = [(q.t_end_ns - min(q.t_submit_ns, q.arrival_ns)) / 1e6 for k, q, _ in reqs if k == kind]
-                bad = sum(1 for k, q, _ in reqs if k == kind and q.status != 0)
+                sel = [(q, e) for k, q, e in reqs if k == kind]
+                lat = [(q.t_end_ns - min(q.t_submit_ns, q.arrival_ns)) / 1e6 for q, _ in sel]
+                bad = sum(1 for q, _ in sel if q.status != 0)
                 if lat:
+                    # latency = queueing (arrival to a worker taking it) + service
+                    wait = [(q.t_start_ns - min(q.t_submit_ns, q.arrival_ns)) / 1e6 for q, _ in sel]
+                    serv = [(q.t_end_ns - q.t_start_ns) / 1e6 for q, _ in sel]
                     stat[kind] = {"n": len(lat), "p50_ms": float(np.percentile(lat, 50)),
-                                  "p99_ms": float(np.percentile(lat, 99)), "errors": bad}
+                                  "p99_ms": float(np.percentile(lat, 99)), "errors": bad,
+                                  "queue_p99_ms": float(np.percentile(wait, 99)),
+                                  "service_p99_ms": float(np.percentile(serv, 99))}
+            # the slowest requests of the run: when each arrived, how long it
+            # queued, how long it ran, its graph and size
+            order = sorted(range(len(reqs)), key=lambda i: reqs[i][1].arrival_ns - reqs[i][1].t_end_ns)[:5]
+            stat["slowest"] = [{"kind": reqs[i][0], "at_ms": round((reqs[i][1].arrival_ns - t0_ns) / 1e6, 2),
+                                "queue_ms": round((reqs[i][1].t_start_ns - reqs[i][1].arrival_ns) / 1e6, 3),
+                                "submit_lag_ms": round((reqs[i][1].t_submit_ns - reqs[i][1].arrival_ns) / 1e6, 3),
+                                "service_ms": round((reqs[i][1].t_end_ns - reqs[i][1].t_start_ns) / 1e6, 3),
+                                "graph": plan[i][1], "edges": reqs[i][2]} for i in order]
+            order = sorted(range(len(reqs)), key=lambda i: reqs[i][1].t_start_ns - reqs[i][1].t_end_ns)[:5]
+            stat["longest_service"] = [
+                {"kind": reqs[i][0], "at_ms": round((reqs[i][1].arrival_ns - t0_ns) / 1e6, 2),
+                 "service_ms": round((reqs[i][1].t_end_ns - reqs[i][1].t_start_ns) / 1e6, 3), "graph": plan[i][1],
+                 "edges": reqs[i][2], "height": [reqs[i][1].stats.height_before, reqs[i][1].stats.height_after],
+                 "rebuilt": reqs[i][1].stats.rebuilt} for i in order]
+            stat["resident_gb"] = sum(rpma.memory_bytes(G["g"]) for G in gs.graphs) / 1e9
+            # how late the load generator submitted (a late submission is
+            # counted as queueing, so it is reported)
+            lag = [(q.t_submit_ns - q.arrival_ns) / 1e6 for _, q, _ in reqs]
+            stat["submit_lag_ms"] = {"p99": float(np.percentile(lag, 99)), "max": float(max(lag))}
             row[mode] = stat
         out["rates"].append(row)
     gs.close()
@@ -613,7 +648,7 @@ def served_arm(args):
                         "1,024 seeds" % len(gs.graphs), "unit": "ms / edges/s", "workers": args.workers,
             "duration_s_per_rate": args.duration, **out,
             "note": "latency = completion - planned arrival (queueing and submission lag included); one_at_a_time = "
-                    "a pool of one worker"}
+                    "a pool of one worker; the load generator runs with Python's cyclic GC off"}
     print(json.dumps(line))
 
 
