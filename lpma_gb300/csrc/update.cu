@@ -857,9 +857,13 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
 // The level-0 windows (one segment, about 94% of the executed windows) get a
 // group of 8 lanes each, so a warp keeps 4 windows in flight.  Lane gl of a
 // group moves slots 4gl..4gl+3 with two 16-byte key loads/stores and one
-// 4-byte value load/store.  Merged ranks come from binary searches over the
-// window's kept keys and insert keys staged in shared memory; the re-packed
-// segment is staged there too (800 bytes per group).
+// 4-byte value load/store.  The window's kept keys are compacted into shared
+// memory; an insert's merged slot is (inserts before it) + (kept keys below
+// it, a binary search), and the inserts mark their slots in a 32-bit mask.
+// Every output slot then reads its key without a search: a marked slot takes
+// the insert whose index is the count of marks below it, any other slot the
+// kept key whose index is the count of unmarked slots below it.  576 bytes of
+// shared memory per group.
 constexpr int ES_TPB = 256;
 constexpr int ES_GROUPS = ES_TPB / 8;
 
@@ -867,10 +871,10 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
                                                         const UpdList u, uint32_t thres, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
-    __shared__ __align__(16) uint64_t sk[ES_GROUPS][32];
-    __shared__ __align__(16) uint8_t sv[ES_GROUPS][32];
     __shared__ uint64_t kk[ES_GROUPS][32];  // kept keys of the window, compacted
-    __shared__ uint64_t ik[ES_GROUPS][32];  // insert keys of the window
+    __shared__ uint64_t ik[ES_GROUPS][32];  // insert keys of the window, in key order
+    __shared__ uint8_t kv[ES_GROUPS][32];   // their values
+    __shared__ uint8_t iv[ES_GROUPS][32];
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
     const uint32_t stride = nblk_ * ES_GROUPS;
@@ -878,11 +882,12 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
     // bounds are loaded while the current one is merged
     uint32_t wi = bid_ * ES_GROUPS + grp;
     Window Wn{};
+    uint64_t jn = 0;
     ulonglong2 na = make_ulonglong2(KEY_NONE, KEY_NONE), nb = na;
     uint32_t nv4 = 0, nip0 = 0, nip1 = 0;
     if (wi < nwin) {
         Wn = wins[wi];
-        const uint64_t jn = heap_of_linear(Wn.a, g.H);
+        jn = heap_of_linear(Wn.a, g.H);
         const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
         na = kp[0], nb = kp[1];
         nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
@@ -891,26 +896,23 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
     for (; __any_sync(0xffffffffu, wi < nwin); wi += stride) {
         const bool active = wi < nwin;
         const Window W = Wn;
+        const uint64_t j = jn;
         const ulonglong2 a = na, b = nb;
         const uint32_t v4 = nv4, ip0c = nip0, ip1c = nip1;
         if (wi + stride < nwin) {
             Wn = wins[wi + stride];
-            const uint64_t jn = heap_of_linear(Wn.a, g.H);
+            jn = heap_of_linear(Wn.a, g.H);
             const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
             na = kp[0], nb = kp[1];
             nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
             nip0 = u.ip[Wn.lo], nip1 = u.ip[Wn.hi];
         }
-        const uint64_t j = active ? heap_of_linear(W.a, g.H) : 0;
         uint64_t k[4];
-        uint8_t v[4];
         uint32_t kmask = 0;
         k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            v[q] = (uint8_t)(v4 >> (8 * q));
-            if (active && kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
-        }
+        for (int q = 0; q < 4; q++)
+            if (active && kept_slot(k[q], (uint8_t)(v4 >> (8 * q)), thres)) kmask |= 1u << q;
         // exclusive prefix of kept counts across the group
         const uint32_t nl = __popc(kmask);
         uint32_t incl = nl;
@@ -921,19 +923,23 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         }
         const uint32_t kbase = incl - nl;
         const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
-        // kept keys, compacted and sorted, for the insert ranks
+        // kept keys and values, compacted in order
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if ((kmask >> q) & 1u) kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
+            if ((kmask >> q) & 1u) {
+                const uint32_t x = kbase + __popc(kmask & ((1u << q) - 1));
+                kk[grp][x] = k[q];
+                kv[grp][x] = (uint8_t)(v4 >> (8 * q));
+            }
         __syncwarp();
-        // updates of the window, 8 per round (usually one round): an insert's
-        // rank is (inserts before it) + (kept keys below it)
+        // updates of the window, 8 per round (usually one round)
         const uint32_t lo = W.lo, hi = active ? W.hi : W.lo;
         const uint32_t ip0 = active ? ip0c : 0;
         const uint32_t nins = active ? ip1c - ip0 : 0;
         // deletes were applied as tombstones by the locate: a window without
         // inserts needs no pass over its updates
         const uint32_t rounds = __reduce_max_sync(0xffffffffu, nins ? (hi - lo + 7) / 8 : 0u);
+        uint32_t imask = 0;
         for (uint32_t r = 0; r < rounds; r++) {
             const uint32_t x = lo + 8 * r + gl;
             // the update's fields load together (not behind the kind test)
@@ -951,32 +957,17 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
                     else
                         R = mid;
                 }
-                if (ri < 32) ik[grp][ri] = yk;
-                if (ri + L < 32) {
-                    sk[grp][ri + L] = yk;
-                    sv[grp][ri + L] = yv;
+                if (ri < 32) {
+                    ik[grp][ri] = yk;
+                    iv[grp][ri] = yv;
                 }
+                if (ri + L < 32) imask |= 1u << (ri + L);
             }
         }
-        __syncwarp();
-        // a kept key's rank is (kept keys before it) + (inserts below it)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if ((kmask >> q) & 1u) {
-                uint32_t L = 0, R = nins < 32 ? nins : 32;
-                while (L < R) {
-                    const uint32_t mid = (L + R) >> 1;
-                    if (ik[grp][mid] < k[q])
-                        L = mid + 1;
-                    else
-                        R = mid;
-                }
-                const uint32_t rk = kbase + __popc(kmask & ((1u << q) - 1)) + L;
-                if (rk < 32) {
-                    sk[grp][rk] = k[q];
-                    sv[grp][rk] = v[q];
-                }
-            }
+        if (rounds) {  // warp-uniform: the group's marks in every lane
+            imask |= __shfl_xor_sync(0xffffffffu, imask, 1, 8);
+            imask |= __shfl_xor_sync(0xffffffffu, imask, 2, 8);
+            imask |= __shfl_xor_sync(0xffffffffu, imask, 4, 8);
         }
         __syncwarp();
         const uint32_t m = nk + nins;
@@ -991,11 +982,20 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const uint32_t slot = 4 * gl + q;
-                o[q] = slot < m ? sk[grp][slot] : KEY_NONE;
-                ov |= (slot < m ? (uint32_t)sv[grp][slot] : 0u) << (8 * q);
-                if (slot < m && is_sentinel(o[q])) {
-                    const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
-                    if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                o[q] = KEY_NONE;
+                if (slot < m) {
+                    const uint32_t below = __popc(imask & ((1u << slot) - 1));
+                    if ((imask >> slot) & 1u) {
+                        o[q] = ik[grp][below];
+                        ov |= (uint32_t)iv[grp][below] << (8 * q);
+                    } else {
+                        o[q] = kk[grp][slot - below];
+                        ov |= (uint32_t)kv[grp][slot - below] << (8 * q);
+                    }
+                    if (is_sentinel(o[q])) {
+                        const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
+                        if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                    }
                 }
             }
             ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(g.keys + 32 * j + 4 * gl);
@@ -1004,7 +1004,9 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
             *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ov;
             if (gl == 0) {
                 cnt[W.a] = (uint8_t)m;
-                fl[j] = m ? make_ulonglong2(sk[grp][0], sk[grp][m - 1]) : make_ulonglong2(KEY_NONE, KEY_NONE);
+                // the last slot holds the last insert or the last kept key
+                const uint64_t last = m ? (((imask >> (m - 1)) & 1u) ? ik[grp][nins - 1] : kk[grp][nk - 1]) : KEY_NONE;
+                fl[j] = make_ulonglong2(o[0], last);
             }
         }
         __syncwarp();
