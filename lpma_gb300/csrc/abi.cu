@@ -46,7 +46,7 @@ struct Cap {
     uint32_t Hc = 0;
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     uint8_t *vals = nullptr, *vals_alt = nullptr;
-    uint8_t *cnt = nullptr, *cnt_alt = nullptr, *cnt_live = nullptr, *srcc = nullptr, *seg_e = nullptr;
+    uint8_t *cnt = nullptr, *cnt_alt = nullptr, *cnt_live = nullptr, *srcc = nullptr;
     ulonglong2 *fl = nullptr;
     uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
     uint32_t *bitmap = nullptr;
@@ -244,7 +244,7 @@ cudaError_t alloc_cap(Cap &c, uint32_t Hc, cudaStream_t s) {
     };
     part(&c.keys, ns), part(&c.keys_alt, ns), part(&c.vals, ns), part(&c.vals_alt, ns);
     part(&c.cnt, nseg + 64), part(&c.cnt_alt, nseg + 64), part(&c.cnt_live, nseg + 64), part(&c.srcc, nseg + 64);
-    part(&c.seg_e, nseg + 64), part(&c.fl, nseg);
+    part(&c.fl, nseg);
     part(&c.segP, nseg + 2), part(&c.q, nseg + 2), part(&c.qn, nseg + 2), part(&c.PQ, nseg + 2);
     part(&c.US, nseg + 2), part(&c.qi, nseg + 2), part(&c.qd, nseg + 2);
     part(&c.bitmap, bitmap_words(Hc)), part(&c.scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
@@ -382,7 +382,7 @@ lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thr
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
     launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, total_live_dev, H, tb, h->c.bitmap, h->cand,
-                h->wsingle, h->wsmall4, h->wsmall, h->wbig, h->c.seg_e, h->pend, h->dst, s);
+                h->wsingle, h->wsmall4, h->wsmall, h->wbig, h->pend, h->dst, s);
     CK(cudaGetLastError());
     return LPMA_OK;
 }
@@ -1331,7 +1331,7 @@ lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
     uint64_t b = 0;
     if (h->c.Hc || h->c.keys) {
         const uint64_t ns = nslots_of(h->c.Hc), nseg = nseg_of(h->c.Hc);
-        b += 18 * ns + nseg * (5 + 16 + 7 * 4) + bitmap_words(h->c.Hc) * 4;
+        b += 18 * ns + nseg * (4 + 16 + 7 * 4) + bitmap_words(h->c.Hc) * 4;
     }
     b += 4ull * h->V + h->bcap * 64ull + h->view_cap * 9ull + h->exp_cap * 9ull + h->stage_cap * 34ull;
     if (h->bfs_a) b += 8ull * h->V;
@@ -1434,7 +1434,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             f.blk_nn = h->blk_nn, f.blk_ins = h->blk_ins, f.u = h->u;
             f.bitmap = h->c.bitmap, f.bitmap_words = bitmap_words(h->H);
             f.cand = h->cand, f.wsingle = h->wsingle, f.wsmall4 = h->wsmall4, f.wsmall = h->wsmall, f.wbig = h->wbig;
-            f.seg_e = h->c.seg_e, f.pend = h->pend;
+            f.pend = h->pend;
             f.tb = make_tables(h, h->H, true);
             f.total_items = h->total;
             f.st = h->dst;

@@ -61,7 +61,7 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
                  uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
-                 uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s);
+                 uint8_t *pend, DevStatus *st, cudaStream_t s);
 
 // in-place executors for windows of <= 32 segments: kind 0 the
 // single-segment list (DevStatus::n_single), 1 windows of 2..4 segments
@@ -165,7 +165,7 @@ struct ForestGraph {
     uint32_t *bitmap;
     uint64_t bitmap_words;
     Window *cand, *wsingle, *wsmall4, *wsmall, *wbig;
-    uint8_t *seg_e, *pend;
+    uint8_t *pend;
     Tables tb;
     unsigned long long total_items;
     DevStatus *st;

@@ -522,11 +522,14 @@ __device__ inline uint64_t bit_of(uint32_t H, uint32_t l, uint64_t widx) {
 __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
                                               const uint32_t *__restrict__ P, int use_P, uint64_t total_live_host,
                                               const unsigned long long *__restrict__ total_live_dev, uint32_t H,
-                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
-                                              uint8_t *pend, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *pend,
+                                              DevStatus *st, uint32_t bid_, uint32_t nblk_) {
     const uint64_t total_live = total_live_dev ? *total_live_dev : total_live_host;
     __shared__ uint32_t wsum[TPB / 32];
     __shared__ uint32_t base_s;
+    __shared__ uint32_t s_lv, s_fl;  // executed levels; bit 0 an overflow, bit 1 a root window
+    if (threadIdx.x == 0) s_lv = 0, s_fl = 0;
+    __syncthreads();
     const uint32_t nu = st->n_u;
     const uint32_t x = bid_ * TPB + threadIdx.x;
     uint32_t s = 0;
@@ -566,7 +569,9 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
                 break;
             }
         }
-        seg_e[s] = (uint8_t)e;
+        // the run's pending mark (read on the overflow paths; the other
+        // updates of the run copy it from here)
+        pend[x] = (uint8_t)(e == EXEC_OVF);
         if (e == 0) {
             // a single-segment window has one leader, and the maximality
             // probe never reads level 0: no bitmap atomic on the common path
@@ -577,20 +582,18 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
             own = !(atomicOr(&bitmap[bit >> 5], mask) & mask);
         }
     }
-    const int any_ovf = __syncthreads_or(lead && e == EXEC_OVF);
-    const int any_root = __syncthreads_or(lead && e == H + 1);
-    // levels with an executed window, for the maximality test
-    uint32_t lv = (lead && e != EXEC_OVF) ? 1u << e : 0u;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) lv |= __shfl_xor_sync(0xffffffffu, lv, o);
-    __shared__ uint32_t s_lv;
-    if (threadIdx.x == 0) s_lv = 0;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0 && lv) atomicOr(&s_lv, lv);
+    // levels with an executed window (for the maximality test), overflow
+    // and root flags: one block barrier for all three
+    const uint32_t lv = __reduce_or_sync(0xffffffffu, (lead && e != EXEC_OVF) ? 1u << e : 0u);
+    const uint32_t fg = __reduce_or_sync(0xffffffffu, (lead && e == EXEC_OVF ? 1u : 0u) | (lead && e == H + 1 ? 2u : 0u));
+    if ((threadIdx.x & 31) == 0) {
+        if (lv) atomicOr(&s_lv, lv);
+        if (fg) atomicOr(&s_fl, fg);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        if (any_ovf) atomicOr(&st->ovf, 1u);
-        if (any_root) atomicOr(&st->root, 1u);
+        if (s_fl & 1u) atomicOr(&st->ovf, 1u);
+        if (s_fl & 2u) atomicOr(&st->root, 1u);
         if (s_lv) atomicOr(&st->exec_levels, s_lv);
     }
     // block-aggregated append of the windows this block owns
@@ -603,22 +606,27 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
 __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, const uint8_t *__restrict__ cnt,
                                               const uint32_t *__restrict__ P, int use_P, uint64_t total_live_host,
                                               const unsigned long long *__restrict__ total_live_dev, uint32_t H,
-                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *seg_e,
-                                              uint8_t *pend, DevStatus *st) {
+                                              Tables tb, uint32_t *bitmap, Window *cand, uint8_t *pend,
+                                              DevStatus *st) {
     griddep_wait();
-    k_plan_body(u, n_cap, cnt, P, use_P, total_live_host, total_live_dev, H, tb, bitmap, cand, seg_e, pend, st, blockIdx.x, gridDim.x);
+    k_plan_body(u, n_cap, cnt, P, use_P, total_live_host, total_live_dev, H, tb, bitmap, cand, pend, st, blockIdx.x, gridDim.x);
 }
 
 // Keep the candidates not inside a larger executed window; sort them into
 // single-segment, small (<= 32 segments) and big lists.
 __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
-                                                  Window *small, Window *big, const UpdList u,
-                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
-    // updates of segments that no window absorbed stay pending (overflow)
-    if (st->ovf) {  // the marks are read only on the overflow paths
+                                                  Window *small, Window *big, const UpdList u, uint8_t *pend,
+                                                  DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+    // updates of segments that no window absorbed stay pending (overflow):
+    // each update copies the mark its run's first update (the planner's
+    // leader) wrote.  The marks are read only on the overflow paths.
+    if (st->ovf) {
         const uint32_t x = bid_ * TPB + threadIdx.x;
-        if (x < st->n_u && x < n_cap) pend[x] = seg_e[u.seg[x]] == EXEC_OVF;
+        if (x < st->n_u && x < n_cap) {
+            const uint32_t s = u.seg[x];
+            if (x > 0 && u.seg[x - 1] == s) pend[x] = pend[lb_back(u.seg, x, s)];
+        }
     }
     __shared__ uint32_t wsum[TPB / 32];
     __shared__ uint32_t base_s[4];
@@ -634,8 +642,9 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
         // without an early exit so that the loads are in flight together.
         uint32_t hit = 0;
         const uint32_t lv = st->exec_levels;
+        const uint32_t ltop = lv ? min(H + 1, 31u - __clz(lv)) : 0u;  // the highest executed level
 #pragma unroll 4
-        for (uint32_t l = w.level + 1; l <= H + 1; l++) {
+        for (uint32_t l = w.level + 1; l <= ltop; l++) {
             if (!((lv >> l) & 1u)) continue;  // no window of that level executes
             const uint64_t bit = bit_of(H, l, (uint64_t)w.a >> l);
             hit |= (bitmap[bit >> 5] >> (bit & 31)) & 1u;
@@ -679,10 +688,10 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
 
 __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
-                                                  Window *small, Window *big, const UpdList u,
-                                                  const uint8_t *__restrict__ seg_e, uint8_t *pend, DevStatus *st) {
+                                                  Window *small, Window *big, const UpdList u, uint8_t *pend,
+                                                  DevStatus *st) {
     griddep_wait();
-    k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend, st, blockIdx.x, gridDim.x);
+    k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ multi-segment windows
@@ -1316,14 +1325,13 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
                  uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
-                 uint8_t *seg_e, uint8_t *pend, DevStatus *st, cudaStream_t s) {
+                 uint8_t *pend, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
     launch_pdl(k_plan, dim3(nb), dim3(TPB), 0, s, u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap,
-               cand, seg_e, pend, st);
-    launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, seg_e, pend,
-               st);
+               cand, pend, st);
+    launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st);
     note_launch(2);
 }
 
@@ -1536,15 +1544,15 @@ __global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restri
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_plan_body(f.u, f.n_ins + f.n_del, f.cnt, nullptr, 0, 0, &f.st->total_items, f.g.H, f.tb, f.bitmap, f.cand,
-                f.seg_e, f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+                f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(TPB) k_forest_plan_max(const ForestGraph *__restrict__ F, const uint32_t *boff,
                                                          uint32_t G) {
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
-    k_plan_max_body(f.cand, f.n_ins + f.n_del, f.g.H, f.bitmap, f.wsingle, f.wsmall4, f.wsmall, f.wbig, f.u, f.seg_e,
-                    f.pend, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+    k_plan_max_body(f.cand, f.n_ins + f.n_del, f.g.H, f.bitmap, f.wsingle, f.wsmall4, f.wsmall, f.wbig, f.u, f.pend,
+                    f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(ES_TPB, 4) k_forest_exec_single(const ForestExec *__restrict__ E,

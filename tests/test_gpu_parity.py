@@ -264,6 +264,48 @@ def test_scale18_stream(engine, oracle, batch):
     assert_csr(g, o)
 
 
+PATH_FLAGS = ("overflow", "levelup_path", "rebuilt", "eager_levelup", "root_executed", "fill_empty")
+
+
+@pytest.mark.parametrize("V,frac,dfrac,path", [
+    (1 << 10, 0.8, 0.0, "levelup_path"),  # an overflow absorbed by one new level
+    (1 << 10, 0.8, 0.1, "levelup_path"),  # the same with deletes pending in the batch
+    (1 << 12, 0.8, 0.05, "fill_empty"),   # the level-up leaves an empty leaf: full respread
+    (1 << 12, 0.2, 0.1, "rebuilt"),       # an overflow that needs a rebuild
+])
+def test_overflow_paths(engine, oracle, V, frac, dfrac, path):
+    """Growing batches (each frac of what was inserted so far, plus deletes
+    of dfrac of the stored edges) drive the root window past its capacity.
+    The updates no window absorbed stay pending across the level-up; the
+    path each batch takes and the layout after it match the oracle."""
+    scale = int(V).bit_length() - 1
+    e = oracle.shuffle(oracle.rmat_edges(41, scale, 16), 3)
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    rng = np.random.default_rng(7)
+    pos = e.size // 8
+    g.update(ins=_dev(e[:pos]))
+    o.update(ins=e[:pos])
+    seen = set()
+    for i in range(6):
+        n = max(1, int(frac * pos))
+        if pos + n > e.size:
+            break
+        k, _ = o.export_sorted()
+        live = k[((k >> np.uint64(20)) & np.uint64(0x3FFFFF)) != np.uint64(0x3FFFFE)]
+        dels = rng.choice(live, size=int(dfrac * live.size), replace=False) if dfrac else np.empty(0, np.uint64)
+        sg = g.update(ins=_dev(e[pos:pos + n]), dels=_dev(dels))
+        so = o.update(ins=e[pos:pos + n], dels=dels)
+        pos += n
+        assert_same(g, o, "batch %d" % i)
+        for key in PATH_FLAGS:
+            assert bool(sg[key]) == bool(so[key]), "batch %d: %s %d vs %d" % (i, key, sg[key], so[key])
+            if sg[key]:
+                seen.add(key)
+    assert path in seen and "overflow" in seen, seen
+    assert_csr(g, o)
+    g.close()
+
+
 def test_cached_front_survives_buffer_moves(engine, oracle):
     """A repeated batch shape replays a captured front; batch buffers that
     grow in between, and a sort-mode change, must not leave a stale one."""
