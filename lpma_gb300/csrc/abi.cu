@@ -497,6 +497,14 @@ lpma_status_t rebuild(LpmaHandle *h, uint32_t hh, const UpdList &u, uint32_t n_l
     return LPMA_OK;
 }
 
+// Segments whose bounds and counts the pack kernel prefetches into L2: all
+// of them when the batch is large against the tree (the locate then touches
+// most of the deep levels), none for a small batch.
+uint64_t prefetch_segs(const LpmaHandle *h, size_t n) {
+    const uint64_t nseg = nseg_of(h->H);
+    return (h->c.fl && h->c.cnt && (uint64_t)n * 8 >= nseg) ? nseg : 0;
+}
+
 // Everything of an update call up to the host round trip: status reset,
 // pack, sort, resolve + locate, compaction, plan and the status read-back.
 lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, const uint8_t *ins_vals,
@@ -507,7 +515,8 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // the engine's own sentinel keys are always in the packed layout
     const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
     launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
-                h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), s);
+                h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), h->c.fl, h->c.cnt,
+                prefetch_segs(h, n), s);
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
     const SortTier tier = sort_tier_for_update((uint32_t)n, h->sort);
@@ -631,7 +640,8 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
             note_launch(-(int)f.launches);  // counted again on each replay
         }
         fg->stamp = ++h->graph_clock;
-        // k_pack(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st)
+        // k_pack(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, bitmap,
+        //        bitmap_words, fl, cnt, pf_segs)
         const uint64_t *a_ins = ins, *a_del = del;
         const uint8_t *a_vals = ins_vals;
         uint32_t a_nins = (uint32_t)n_ins, a_ndel = (uint32_t)n_del, a_V = h->V, a_thres = thres,
@@ -642,8 +652,11 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         DevStatus *a_st = h->dst;
         uint32_t *a_bm = h->c.bitmap;
         uint32_t a_bmw = (uint32_t)bitmap_words(h->H);
+        const ulonglong2 *a_fl = h->c.fl;
+        const uint8_t *a_cnt = h->c.cnt;
+        uint64_t a_pf = prefetch_segs(h, n);
         void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st,
-                        &a_bm, &a_bmw};
+                        &a_bm, &a_bmw, &a_fl, &a_cnt, &a_pf};
         cudaKernelNodeParams kp = fg->pack_params;
         kp.kernelParams = args;
         kp.extra = nullptr;
@@ -651,7 +664,6 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         CK(cudaGraphLaunch(fg->exec, s));
         note_launch((int)fg->launches);
     }
-    (void)n;
     return LPMA_OK;
 }
 

@@ -25,11 +25,12 @@ struct Geo {  // one tree geometry in HBM
 
 // validate + pack both input arrays into one key/payload array; payload bits
 // 0-7 = value, bit 8 = delete.  Also clears the planner bitmap (bitmap_words
-// 32-bit words) for the call's first plan.
+// 32-bit words) for the call's first plan, and prefetches the first pf_segs
+// entries of the segment bounds (fl) and counts (cnt) into L2.
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del,
                  uint32_t n_del, uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                  uint64_t *keys_out, uint16_t *pay_out, DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
-                 cudaStream_t s);
+                 const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs, cudaStream_t s);
 
 // the pack kernel's entry (graph replays update its input pointers)
 const void *pack_kernel_fn();

@@ -192,14 +192,34 @@ __device__ __forceinline__ void k_pack_body(const uint64_t *__restrict__ ins, co
     }
 }
 
+// Bulk L2 prefetch of [p, p + bytes) (p 16-byte aligned), spread over the
+// grid in 4 KB requests; bytes past the last multiple of 16 are left out.
+__device__ __forceinline__ void l2_prefetch(const void *p, uint64_t bytes) {
+    constexpr uint64_t CH = 4096;
+    const uint64_t nch = (bytes + CH - 1) / CH;
+    for (uint64_t c = (uint64_t)blockIdx.x * TPB + threadIdx.x; c < nch; c += (uint64_t)gridDim.x * TPB) {
+        const uint64_t off = c * CH;
+        const uint32_t len = (uint32_t)(umin64(CH, bytes - off) & ~15ull);
+        if (len) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char *)p + off), "r"(len) : "memory");
+    }
+}
+
 __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, const uint8_t *__restrict__ ins_vals,
                                               uint32_t n_ins, const uint64_t *__restrict__ del, uint32_t n_del,
                                               uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                                               uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
-                                              DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words) {
+                                              DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
+                                              const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs) {
     // the planner bitmap of this call starts clear
     for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < bitmap_words; i += gridDim.x * TPB) bitmap[i] = 0;
     k_pack_body(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, blockIdx.x, gridDim.x);
+    // the segment bounds and counts that the locate and the planner read at
+    // random come into L2 while the batch is sorted (the sort runs out of L2
+    // and leaves DRAM idle); issued after the block's own accesses
+    if (pf_segs) {
+        l2_prefetch(fl, 16 * pf_segs);
+        l2_prefetch(cnt, pf_segs);
+    }
 }
 
 // ------------------------------------------------------------------ live counts
@@ -1269,10 +1289,11 @@ const void *pack_kernel_fn() { return reinterpret_cast<const void *>(&k_pack); }
 
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
-                 DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, cudaStream_t s) {
+                 DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, const ulonglong2 *fl, const uint8_t *cnt,
+                 uint64_t pf_segs, cudaStream_t s) {
     ProfScope ps_("pack", s);
     k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
-                                                        keys_out, pay_out, st, bitmap, bitmap_words);
+                                                        keys_out, pay_out, st, bitmap, bitmap_words, fl, cnt, pf_segs);
     note_launch();
 }
 
