@@ -907,10 +907,11 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
     const uint32_t stride = nblk_ * ES_GROUPS;
-    // software pipeline: the next window's record, segment slots and update
-    // bounds are loaded while the current one is merged
+    // software pipeline: the segment slots and update bounds of the next
+    // window are loaded while the current one is merged, and the window
+    // record two ahead (its segment address is known when its slots load)
     uint32_t wi = bid_ * ES_GROUPS + grp;
-    Window Wn{};
+    Window Wn{}, Wnn{};
     uint64_t jn = 0;
     ulonglong2 na = make_ulonglong2(KEY_NONE, KEY_NONE), nb = na;
     uint32_t nv4 = 0, nip0 = 0, nip1 = 0;
@@ -922,6 +923,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
         nip0 = u.ip[Wn.lo], nip1 = u.ip[Wn.hi];
     }
+    if (wi + stride < nwin) Wnn = wins[wi + stride];
     for (; __any_sync(0xffffffffu, wi < nwin); wi += stride) {
         const bool active = wi < nwin;
         const Window W = Wn;
@@ -929,12 +931,13 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         const ulonglong2 a = na, b = nb;
         const uint32_t v4 = nv4, ip0c = nip0, ip1c = nip1;
         if (wi + stride < nwin) {
-            Wn = wins[wi + stride];
+            Wn = Wnn;
             jn = heap_of_linear(Wn.a, g.H);
             const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
             na = kp[0], nb = kp[1];
             nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
             nip0 = u.ip[Wn.lo], nip1 = u.ip[Wn.hi];
+            if (wi + 2 * stride < nwin) Wnn = wins[wi + 2 * stride];
         }
         uint64_t k[4];
         uint32_t kmask = 0;
