@@ -88,7 +88,8 @@ typedef struct {
     uint64_t num_items;        /* keys stored after the call, sentinels included */
     uint64_t h2d_bytes;        /* host->device bytes the call copied (inputs, control) */
     uint64_t d2h_bytes;        /* device->host bytes the call copied (status blocks) */
-    uint32_t sort_passes;      /* digit passes the batch sort ran (bytes that vary over the batch) */
+    uint32_t sort_passes;      /* digit passes the batch sort ran: one per byte that varies over the batch,
+                                  or, for the cooperative sort, one per 9-bit digit window */
     uint32_t reserved1;
 } LpmaStats;
 

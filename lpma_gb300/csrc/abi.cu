@@ -130,6 +130,9 @@ struct LpmaHandle {
     // cached front graphs hold raw pointers to every such buffer, so they
     // are all dropped when one moves.  (The sort mode is part of their key.)
     uint64_t buf_gen = 1, graph_gen = 0;
+    // the last front sorted with the cooperative sort's 9-bit digits (for
+    // the pass count in the stats)
+    bool front_sort_wide = false;
 };
 
 namespace {
@@ -289,7 +292,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n, cudaStream_t s) {
     size_t cap = 4096;
     while (cap < n) cap <<= 1;
     const size_t nb = cap / 256 + 4;
-    const size_t status_words = sort_status_words((uint32_t)cap);
+    const size_t status_words = sort_status_words_wide((uint32_t)cap);
     size_t off = 0;
     std::vector<std::pair<void **, size_t>> parts;
     auto part = [&](auto **p, size_t count) {
@@ -520,7 +523,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
     const SortTier tier = sort_tier_for_update((uint32_t)n, h->sort);
-    const SortMask mask{&h->dst->key_and, 0xFFu, sort_tier_in_place(tier) ? 0u : 1u};
+    const SortMask mask = update_sort_mask(&h->dst->key_and, tier, (uint32_t)n, h->sort);
     CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s, tier));
     Geo g{h->c.keys, h->c.vals, h->H};
     launch_resolve_locate(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, g, h->c.fl, thres, h->kind, h->seg,
@@ -566,6 +569,7 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     // the stored-key count reaches the planner through the status reset copy,
     // so that it is not a kernel argument of a cached graph
     h->hinit->total_items = h->total;
+    h->front_sort_wide = update_sort_mask(nullptr, sort_tier_for_update((uint32_t)n, h->sort), (uint32_t)n, h->sort).wide;
     if (internal || prof_enabled() || !graphs_enabled()) {
         CKS(enqueue_front(h, s, ins, ins_vals, n_ins, del, n_del, thres, thres_active, internal));
     } else {
@@ -690,8 +694,18 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
     if (rs != LPMA_OK) return h->sticky = rs;
     if (h->hst->error & ERR_KEY) return LPMA_ERR_INVALID_KEY;
     {
-        const uint64_t diff = h->hst->key_and ^ h->hst->key_or;
-        for (int b = 0; b < 8; b++) st.sort_passes += ((diff >> (8 * b)) & 0xFF) ? 1u : 0u;
+        // the digit passes the sort made: one per differing byte, or with
+        // 9-bit digits one per window (the greedy plan of the sort itself)
+        uint64_t diff = h->hst->key_and ^ h->hst->key_or;
+        if (h->front_sort_wide) {
+            while (diff) {
+                const int b = __builtin_ctzll(diff);
+                diff = b + WIDE_DIGIT_BITS >= 64 ? 0ull : (diff >> (b + WIDE_DIGIT_BITS)) << (b + WIDE_DIGIT_BITS);
+                st.sort_passes++;
+            }
+        } else {
+            for (int b = 0; b < 8; b++) st.sort_passes += ((diff >> (8 * b)) & 0xFF) ? 1u : 0u;
+        }
     }
     const uint32_t min_t_ins = h->hst->min_t_ins;
     const int64_t live_before = thres_active ? (int64_t)h->hst->live_total : (int64_t)h->total;
@@ -1534,6 +1548,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             const lpma_status_t rs = (e & ERR_TIMEOUT) ? LPMA_ERR_TIMEOUT
                                                        : ((e & ERR_INTERNAL) ? LPMA_ERR_INTERNAL : LPMA_OK);
             sts[i].height_before = h->H;
+            h->front_sort_wide = false;  // the shared tile-merge sort
             res[i] = finish_update(h, rs, items[i].n_ins + items[i].n_del, 0, false, st, sts[i], &sts[i],
                                    shared[k] != 0);
         };
@@ -1684,7 +1699,7 @@ lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEnt
     unsigned long long *andor = nullptr;
     uint32_t *err = nullptr;
     SortScratch sc;
-    sc.status_words = sort_status_words(N);
+    sc.status_words = sort_status_words_wide(N);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     lpma_status_t r = LPMA_OK;
     size_t nout = 0;
@@ -1726,7 +1741,7 @@ lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEnt
             uint32_t best_t = 0;
             for (uint32_t t = TIER_SMALL; t < TIER_COUNT; t++) {
                 if (!sort_tier_usable((SortTier)t, n, sc)) continue;
-                const SortMask m{andor, 0xFFu, sort_tier_in_place((SortTier)t) ? 0u : 1u};
+                const SortMask m = update_sort_mask(andor, (SortTier)t, n, sc);
                 float ts[6];
                 for (int rep = 0; rep < 6; rep++) {  // one warm-up, five timed
                     cudaError_t ce = cudaMemcpyAsync(k0, kp, n * 8ull, cudaMemcpyDeviceToDevice, s);

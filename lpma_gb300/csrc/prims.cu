@@ -162,15 +162,44 @@ __device__ inline uint32_t block_excl_scan_256(uint32_t x, uint32_t *wsum /*[8]*
     return r;
 }
 
+// The same over u64 values (two independent u32 scans in the halves, as
+// long as neither half's total reaches 2^32).
+__device__ inline uint64_t block_excl_scan_256_u64(uint64_t x, uint64_t *wsum /*[8]*/, uint64_t *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint64_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t s = lane < 8 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < 8) wsum[lane] = s;
+    }
+    __syncthreads();
+    const uint64_t base = w ? wsum[w - 1] : 0;
+    if (total) *total = wsum[7];
+    const uint64_t r = base + v - x;
+    __syncthreads();
+    return r;
+}
+
 // Rank the IPT keys each lane holds among the keys of its warp with the same
 // digit.  Keys of warp w are at tile positions w*32*IPT + i*32 + lane, so
-// the rank order is the input order.  whist[256] is this warp's digit
+// the rank order is the input order.  whist[2^RB] is this warp's digit
 // counter row (zeroed by the caller); on return it holds the warp's counts.
-// The lanes that share a digit are found with eight ballots (one per digit
+// The lanes that share a digit are found with RB ballots (one per digit
 // bit), which issue far faster than a match instruction; the lowest of them
 // adds the group's size to the warp's counter and shares the old value.
 // Counter updates of one warp land in program order, so ranks are stable.
-template <int IPT>
+template <int IPT, int RB = 8>
 __device__ inline void warp_rank(const uint64_t (&k)[IPT], uint32_t valid_mask, int sh, uint32_t *whist,
                                  uint32_t (&rank)[IPT], int rounds = IPT) {
     const uint32_t lt = lanemask_lt();
@@ -179,10 +208,10 @@ __device__ inline void warp_rank(const uint64_t (&k)[IPT], uint32_t valid_mask, 
     for (int i = 0; i < IPT; i++) {
         if (i >= rounds) break;  // warp-uniform: no valid key in rounds >= rounds
         const bool valid = (valid_mask >> i) & 1u;
-        const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+        const uint32_t d = (uint32_t)((k[i] >> sh) & ((1u << RB) - 1));
         uint32_t peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
+        for (int b = 0; b < RB; b++) {
             const bool bit = (d >> b) & 1u;
             const uint32_t bal = __ballot_sync(0xffffffffu, bit);
             peers &= bit ? bal : ~bal;
@@ -388,14 +417,15 @@ __device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t target, uin
     grid_wait(bar, target, err);
 }
 
-template <typename V>
+template <typename V, int NB>
 struct CoopSmem {
     uint64_t k[COOP_TILE];
     V v[COOP_TILE];
-    uint32_t whist[8][256];
-    uint32_t gbase[256];
-    uint32_t ldig[256];
+    uint32_t whist[8][NB];
+    uint32_t gbase[NB];
+    uint32_t ldig[NB];
     uint32_t wsum[8];
+    uint64_t wsum64[8];
 };
 
 template <typename V>
@@ -409,34 +439,36 @@ __device__ __forceinline__ uint16_t ld_cg<uint16_t>(const uint16_t *p) {
 
 // Tile t is keys [t * tile_len, min(n, (t+1) * tile_len)), tile_len <=
 // COOP_TILE; warp w of a tile takes a contiguous run of ceil(tile_len / 8)
-// of them.  counts is [256][G] (digit-major, for the column scans), offs
-// [G][256] (tile-major, one row per CTA), totals [256].
-template <typename V>
+// of them.  Digits of RB bits (NB = 2^RB of them, 8 or 9 bits: the digit
+// passes of sort_digit_next); thread tid owns the NB / 256 adjacent digits
+// from tid * NB / 256.  counts is [NB][G] (digit-major, for the column
+// scans), offs [G][NB] (tile-major, one row per CTA), totals [NB].
+template <typename V, int RB>
 __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t n,
                                                            uint32_t tile_len, SortMask mask, uint32_t *counts,
                                                            uint32_t *offs, uint32_t *totals, uint32_t *bar,
                                                            uint32_t *err) {
+    constexpr int NB = 1 << RB, PER = NB / SORT_TPB;
+    static_assert(PER >= 1 && NB % SORT_TPB == 0, "whole digits per thread");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CoopSmem<V> &S = *reinterpret_cast<CoopSmem<V> *>(smem_raw);
+    CoopSmem<V, NB> &S = *reinterpret_cast<CoopSmem<V, NB> *>(smem_raw);
     const uint32_t G = gridDim.x, tile = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const uint32_t act = active_bytes(mask);
+    uint64_t rem = sort_digit_bits(mask);  // bits the remaining passes cover
     const uint64_t base = (uint64_t)tile * tile_len;
     const uint32_t nvalid = (uint32_t)umin64(tile_len, n - base);
     const uint32_t pw = (tile_len + 7) / 8;  // keys per warp
     const uint32_t wbeg = (uint32_t)umin64((uint64_t)w * pw, nvalid), wend = (uint32_t)umin64(wbeg + pw, nvalid);
     const int rounds = (int)((wend - wbeg + 31) / 32);
     uint32_t target = 0;
-    int pass = 0;
-    for (int byte = 0; byte < 8; byte++) {
-        if (!((act >> byte) & 1u)) continue;
-        const int sh = 8 * byte;
+    for (uint32_t pass = 0; rem; pass++) {
+        const int sh = sort_digit_next(rem, RB);
         const bool odd = pass & 1;
         const uint64_t *ki = odd ? k1 : k0;
         const V *vi = odd ? v1 : v0;
         uint64_t *ko = odd ? k0 : k1;
         V *vo = odd ? v0 : v1;
-        for (int i = tid; i < 8 * 256; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
+        for (int i = tid; i < 8 * NB; i += SORT_TPB) (&S.whist[0][0])[i] = 0;
         __syncthreads();
         // keys written by other CTAs in the previous pass: load through L2
         uint64_t k[COOP_IPT];
@@ -455,17 +487,32 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
             }
         }
         uint32_t rank[COOP_IPT];
-        warp_rank<COOP_IPT>(k, vmask, sh, S.whist[w], rank, rounds);
+        warp_rank<COOP_IPT, RB>(k, vmask, sh, S.whist[w], rank, rounds);
         __syncthreads();
-        uint32_t tcount = 0;
+        // per digit: warp-exclusive offsets and the tile's count
+        uint32_t tc[PER], tsum = 0;
 #pragma unroll
-        for (int ww = 0; ww < 8; ww++) {
-            const uint32_t c = S.whist[ww][tid];
-            S.whist[ww][tid] = tcount;
-            tcount += c;
+        for (int r = 0; r < PER; r++) {
+            const int d = tid * PER + r;
+            uint32_t c0 = 0;
+#pragma unroll
+            for (int ww = 0; ww < 8; ww++) {
+                const uint32_t c = S.whist[ww][d];
+                S.whist[ww][d] = c0;
+                c0 += c;
+            }
+            counts[(size_t)d * G + tile] = c0;
+            tc[r] = c0;
+            tsum += c0;
         }
-        counts[(size_t)tid * G + tile] = tcount;
-        S.ldig[tid] = block_excl_scan_256(tcount, S.wsum, nullptr);
+        {
+            uint32_t run = block_excl_scan_256(tsum, S.wsum, nullptr);
+#pragma unroll
+            for (int r = 0; r < PER; r++) {
+                S.ldig[tid * PER + r] = run;
+                run += tc[r];
+            }
+        }
         target += G;
         grid_arrive(bar);
         // while the other tiles publish their counts: reorder this tile by
@@ -473,7 +520,7 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
 #pragma unroll
         for (int i = 0; i < COOP_IPT; i++) {
             if ((vmask >> i) & 1u) {
-                const uint32_t d = (uint32_t)((k[i] >> sh) & 0xFF);
+                const uint32_t d = (uint32_t)((k[i] >> sh) & (NB - 1));
                 const uint32_t pos = S.ldig[d] + S.whist[w][d] + rank[i];
                 S.k[pos] = k[i];
                 S.v[pos] = v[i];
@@ -482,27 +529,44 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
         grid_wait(bar, target, err);
         // column scans: offs[d][t] = sum of counts[d][t' < t], totals[d].
         // Groups of S threads (S = G rounded up to a power of two) scan one
-        // column each, so the 256 columns take one or two rounds of the grid
-        // whatever G is (G <= 512; above 256 a thread takes two entries).
-        if (G > 256) {
-            // thread tid takes the adjacent entries 2 tid and 2 tid + 1
+        // column each, so the NB columns take NB / 256 or 2 NB / 256 rounds
+        // of the grid whatever G is (G <= 512; above 256 a thread takes two
+        // entries).
+        if (G > 256 && NB == 512) {
+            // thread tid takes the adjacent entries 2 tid and 2 tid + 1 of
+            // the columns d and d + 256, scanned together in u64 halves
             const uint32_t i0 = 2 * (uint32_t)tid, i1 = i0 + 1;
             for (uint32_t d = tile; d < 256; d += G) {
+                const uint32_t *ca = counts + (size_t)d * G, *cb = counts + (size_t)(d + 256) * G;
+                const uint32_t a0 = i0 < G ? __ldcg(ca + i0) : 0u, a1 = i1 < G ? __ldcg(ca + i1) : 0u;
+                const uint32_t b0 = i0 < G ? __ldcg(cb + i0) : 0u, b1 = i1 < G ? __ldcg(cb + i1) : 0u;
+                uint64_t tot = 0;
+                const uint64_t e = block_excl_scan_256_u64((uint64_t)(a0 + a1) | ((uint64_t)(b0 + b1) << 32),
+                                                           S.wsum64, &tot);
+                const uint32_t ea = (uint32_t)e, eb = (uint32_t)(e >> 32);
+                if (i0 < G) offs[(size_t)i0 * NB + d] = ea, offs[(size_t)i0 * NB + d + 256] = eb;
+                if (i1 < G) offs[(size_t)i1 * NB + d] = ea + a0, offs[(size_t)i1 * NB + d + 256] = eb + b0;
+                if (tid == 0) totals[d] = (uint32_t)tot, totals[d + 256] = (uint32_t)(tot >> 32);
+            }
+        } else if (G > 256) {
+            // thread tid takes the adjacent entries 2 tid and 2 tid + 1
+            const uint32_t i0 = 2 * (uint32_t)tid, i1 = i0 + 1;
+            for (uint32_t d = tile; d < (uint32_t)NB; d += G) {
                 const uint32_t *c = counts + (size_t)d * G;
                 const uint32_t x0 = i0 < G ? __ldcg(c + i0) : 0u;
                 const uint32_t x1 = i1 < G ? __ldcg(c + i1) : 0u;
                 uint32_t tot = 0;
                 const uint32_t e = block_excl_scan_256(x0 + x1, S.wsum, &tot);
-                if (i0 < G) offs[(size_t)i0 * 256 + d] = e;
-                if (i1 < G) offs[(size_t)i1 * 256 + d] = e + x0;
+                if (i0 < G) offs[(size_t)i0 * NB + d] = e;
+                if (i1 < G) offs[(size_t)i1 * NB + d] = e + x0;
                 if (tid == 0) totals[d] = tot;
             }
         } else {
             const uint32_t Sg = G <= 1 ? 1u : 1u << (32 - __clz(G - 1));  // power of two >= G
             const uint32_t per = 256 / Sg, grp = tid / Sg, t = tid % Sg;
-            for (uint32_t d0 = tile * per; d0 < 256; d0 += G * per) {
+            for (uint32_t d0 = tile * per; d0 < (uint32_t)NB; d0 += G * per) {
                 const uint32_t d = d0 + grp;
-                const bool live = d < 256 && t < G;
+                const bool live = d < (uint32_t)NB && t < G;
                 const uint32_t x = live ? __ldcg(counts + (size_t)d * G + t) : 0u;
                 uint32_t v = x, tot;
                 if (Sg <= 32) {
@@ -529,30 +593,38 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
                     v += pre;
                     __syncthreads();
                 }
-                if (live) offs[(size_t)t * 256 + d] = v - x;
-                if (d < 256 && t == 0) totals[d] = tot;
+                if (live) offs[(size_t)t * NB + d] = v - x;
+                if (d < (uint32_t)NB && t == 0) totals[d] = tot;
             }
         }
         target += G;
         grid_barrier(bar, target, err);
         {
-            const uint32_t T = __ldcg(totals + tid);
-            const uint32_t o = __ldcg(offs + (size_t)tile * 256 + tid);
-            const uint32_t gb = block_excl_scan_256(T, S.wsum, nullptr);
-            S.gbase[tid] = gb + o;
+            uint32_t T[PER], tsum2 = 0;
+#pragma unroll
+            for (int r = 0; r < PER; r++) {
+                T[r] = __ldcg(totals + tid * PER + r);
+                tsum2 += T[r];
+            }
+            uint32_t run = block_excl_scan_256(tsum2, S.wsum, nullptr);
+#pragma unroll
+            for (int r = 0; r < PER; r++) {
+                const int d = tid * PER + r;
+                S.gbase[d] = run + __ldcg(offs + (size_t)tile * NB + d);
+                run += T[r];
+            }
         }
         __syncthreads();
         for (uint32_t p = tid; p < nvalid; p += SORT_TPB) {
             const uint64_t kk = S.k[p];
-            const uint32_t d = (uint32_t)((kk >> sh) & 0xFF);
+            const uint32_t d = (uint32_t)((kk >> sh) & (NB - 1));
             const uint32_t g = S.gbase[d] + (p - S.ldig[d]);
             if (g < n) {  // always, unless a barrier wait gave up
                 ko[g] = kk;
                 vo[g] = S.v[p];
             }
         }
-        pass++;
-        if (act >> (byte + 1)) {
+        if (rem) {
             target += G;
             grid_barrier(bar, target, err);
         }
@@ -991,24 +1063,31 @@ cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_
     return scan_impl<uint8_t>(in, out, n, total, tmp, st);
 }
 
-uint32_t g_coop_max_ctas[3];  // resident CTAs of k_coop_sort<u16/u32/u64>, set by sort_prepare
+// resident CTAs of k_coop_sort<u16/u32/u64, 8-bit digits> and of
+// k_coop_sort<u16, 9-bit digits>, set by sort_prepare
+uint32_t g_coop_max_ctas[4];
 
 template <typename V>
-constexpr int coop_slot() {
-    return sizeof(V) == 2 ? 0 : (sizeof(V) == 4 ? 1 : 2);
+constexpr int coop_slot(bool wide) {
+    return wide ? 3 : (sizeof(V) == 2 ? 0 : (sizeof(V) == 4 ? 1 : 2));
 }
 
 // cooperative-sort geometry for n keys: tiles of at least COOP_MIN_TILE
 // keys, spread over every resident CTA slot so that the SMs carry equal work
+// (wide: 9-bit digits, 16-bit payloads only)
 template <typename V>
-static bool coop_geometry(uint32_t n, const SortScratch &s, uint32_t *tile_len_out, uint32_t *G_out) {
-    const uint32_t maxG = g_coop_max_ctas[coop_slot<V>()] < 512u ? g_coop_max_ctas[coop_slot<V>()] : 512u;
+static bool coop_geometry(uint32_t n, const SortScratch &s, uint32_t *tile_len_out, uint32_t *G_out,
+                          bool wide = false) {
+    if (wide && sizeof(V) != 2) return false;
+    const uint32_t mc = g_coop_max_ctas[coop_slot<V>(wide)];
+    const uint32_t maxG = mc < 512u ? mc : 512u;
     const uint32_t tile_len = maxG ? std::max<uint32_t>(COOP_MIN_TILE, (n + maxG - 1) / maxG) : 0u;
     const uint32_t G = tile_len ? (n + tile_len - 1) / tile_len : 0u;
+    const size_t nb = wide ? 512 : 256;
     *tile_len_out = tile_len;
     *G_out = G;
     return s.bar && n > (uint32_t)SORT_TILE && tile_len && tile_len <= (uint32_t)COOP_TILE && G <= maxG &&
-           s.status_words >= 512 * (size_t)G + 256;
+           s.status_words >= 2 * nb * (size_t)G + nb;
 }
 
 template <typename V>
@@ -1075,17 +1154,31 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         note_launch();
         return cudaGetLastError();
     }
+    // the 9-bit digit plan belongs to the cooperative sort alone: the
+    // consumers of the result compute its parity from the same mask
+    if (mask.wide && (tier != TIER_COOP || sizeof(V) != 2)) return cudaErrorInvalidValue;
     if (tier == TIER_COOP) {
+        const bool wide = mask.wide != 0;
         uint32_t tile_len, G;
-        coop_geometry<V>(n, s, &tile_len, &G);
+        if (!coop_geometry<V>(n, s, &tile_len, &G, wide)) return cudaErrorInvalidValue;
         if ((e = cudaMemsetAsync(s.bar, 0, sizeof(uint32_t), st))) return e;
-        uint32_t *counts = s.status, *offs = s.status + 256 * (size_t)G, *totals = s.status + 512 * (size_t)G;
+        const size_t nb = wide ? 512 : 256;
+        uint32_t *counts = s.status, *offs = s.status + nb * G, *totals = s.status + 2 * nb * G;
         uint32_t *bar = s.bar, *err = s.err;
         uint32_t tl = tile_len;
         void *args[] = {&k0, &v0, &k1, &v1, &n, &tl, &mask, &counts, &offs, &totals, &bar, &err};
         ProfScope ps("sort_coop", st);
-        e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V>, dim3(G), dim3(SORT_TPB), args,
-                                        sizeof(CoopSmem<V>), st);
+        if constexpr (sizeof(V) == 2) {
+            if (wide)
+                e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, WIDE_DIGIT_BITS>, dim3(G),
+                                                dim3(SORT_TPB), args, sizeof(CoopSmem<V, 512>), st);
+            else
+                e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, 8>, dim3(G), dim3(SORT_TPB), args,
+                                                sizeof(CoopSmem<V, 256>), st);
+        } else {
+            e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, 8>, dim3(G), dim3(SORT_TPB), args,
+                                            sizeof(CoopSmem<V, 256>), st);
+        }
         note_launch();
         return e;
     }
@@ -1178,24 +1271,28 @@ cudaError_t sort_prepare() {
                                   (int)sizeof(BlockSortSmem))))
         return e;
     {
-        int dev = 0, sms = 0, per[3] = {0, 0, 0};
+        int dev = 0, sms = 0, per[4] = {0, 0, 0, 0};
         if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
             return e;
-        if ((e = cudaFuncSetAttribute(k_coop_sort<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(CoopSmem<uint16_t>))) ||
-            (e = cudaFuncSetAttribute(k_coop_sort<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(CoopSmem<uint32_t>))) ||
-            (e = cudaFuncSetAttribute(k_coop_sort<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(CoopSmem<uint64_t>))))
+        if ((e = cudaFuncSetAttribute(k_coop_sort<uint16_t, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint16_t, 256>))) ||
+            (e = cudaFuncSetAttribute(k_coop_sort<uint32_t, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint32_t, 256>))) ||
+            (e = cudaFuncSetAttribute(k_coop_sort<uint64_t, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(CoopSmem<uint64_t, 256>))) ||
+            (e = cudaFuncSetAttribute(k_coop_sort<uint16_t, WIDE_DIGIT_BITS>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CoopSmem<uint16_t, 512>))))
             return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_coop_sort<uint16_t>, SORT_TPB,
-                                                               sizeof(CoopSmem<uint16_t>))) ||
-            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_coop_sort<uint32_t>, SORT_TPB,
-                                                               sizeof(CoopSmem<uint32_t>))) ||
-            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_coop_sort<uint64_t>, SORT_TPB,
-                                                               sizeof(CoopSmem<uint64_t>))))
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_coop_sort<uint16_t, 8>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint16_t, 256>))) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_coop_sort<uint32_t, 8>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint32_t, 256>))) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_coop_sort<uint64_t, 8>, SORT_TPB,
+                                                               sizeof(CoopSmem<uint64_t, 256>))) ||
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], k_coop_sort<uint16_t, WIDE_DIGIT_BITS>,
+                                                               SORT_TPB, sizeof(CoopSmem<uint16_t, 512>))))
             return e;
-        for (int i = 0; i < 3; i++) g_coop_max_ctas[i] = (uint32_t)(per[i] * sms);
+        for (int i = 0; i < 4; i++) g_coop_max_ctas[i] = (uint32_t)(per[i] * sms);
     }
     done = true;
     return cudaSuccess;
@@ -1222,6 +1319,12 @@ SortTier sort_tier_for_update(uint32_t n, const SortScratch &s) {
 }
 
 bool sort_tier_usable(SortTier t, uint32_t n, const SortScratch &s) { return tier_ok<uint16_t>(t, n, s); }
+
+SortMask update_sort_mask(const unsigned long long *andor, SortTier t, uint32_t n, const SortScratch &s) {
+    uint32_t tl, G;
+    const bool wide = t == TIER_COOP && coop_geometry<uint16_t>(n, s, &tl, &G, true);
+    return SortMask{andor, 0xFFu, sort_tier_in_place(t) ? 0u : 1u, wide ? 1u : 0u};
+}
 
 void sort_tier_set(uint32_t bucket, int concurrent, SortTier t) {
     if (bucket < 33) g_tier_table[concurrent ? 0 : 1][bucket].store((uint8_t)t, std::memory_order_relaxed);

@@ -27,11 +27,15 @@ struct SortScratch {
 // of all keys) differ.
 // pingpong: the sort that produced the batch is a ping-pong one (one
 // buffer swap per digit pass), so its result is in the second buffer pair
-// when the number of active digit bytes is odd; 0: the result is in place.
+// when the number of digit passes is odd; 0: the result is in place.
+// wide: the cooperative sort's 9-bit digits (set only with andor and
+// host_mask 0xFF): digit windows of up to 9 bits placed greedily over the
+// bits where the keys differ, instead of one pass per differing byte.
 struct SortMask {
     const unsigned long long *andor;
     uint32_t host_mask;
     uint32_t pingpong;
+    uint32_t wide;
 };
 
 // The sort algorithms ("tiers") of a batch sort.  All give the same stable
@@ -53,6 +57,10 @@ inline __host__ __device__ bool sort_tier_in_place(SortTier t) {
 // (cooperative or concurrent), when set and usable, else the default.
 SortTier sort_tier_for_update(uint32_t n, const SortScratch &s);
 bool sort_tier_usable(SortTier t, uint32_t n, const SortScratch &s);
+// The mask of an update batch sorted with tier t: digits from the device
+// words andor (AND, OR of the keys), ping-pong parity for the ping-pong
+// tiers, 9-bit digits for the cooperative tier when its scratch allows.
+SortMask update_sort_mask(const unsigned long long *andor, SortTier t, uint32_t n, const SortScratch &s);
 void sort_tier_set(uint32_t bucket, int concurrent, SortTier t);
 SortTier sort_tier_get(uint32_t bucket, int concurrent);
 
@@ -75,9 +83,37 @@ constexpr int BLOCK_SORT_TPB = 1024, BLOCK_SORT_IPT = 8;
 constexpr int BLOCK_SORT_MAX = BLOCK_SORT_TPB * BLOCK_SORT_IPT;  // 8192
 
 
+// The digit passes of a sort.  The bits to cover: byte digits cover the
+// active bytes, wide digits the bits where the keys differ.  A pass takes
+// the window of W bits (8, or 9 when wide) that starts at the lowest bit
+// still to cover; sort_digit_next returns that shift and removes the window
+// from rem.  With byte digits this is one pass per active byte.
+constexpr int WIDE_DIGIT_BITS = 9;
+__device__ inline uint64_t sort_digit_bits(SortMask m) {
+    if (m.wide && m.andor) return m.andor[0] ^ m.andor[1];
+    const uint32_t act = active_bytes(m);
+    uint64_t r = 0;
+#pragma unroll
+    for (int b = 0; b < 8; b++)
+        if ((act >> b) & 1u) r |= 0xFFull << (8 * b);
+    return r;
+}
+__device__ __forceinline__ int sort_digit_next(uint64_t &rem, int W) {
+    const int sh = __ffsll((long long)rem) - 1;
+    rem = sh + W >= 64 ? 0ull : (rem >> (sh + W)) << (sh + W);
+    return sh;
+}
+__device__ inline uint32_t sort_digit_passes(SortMask m) {
+    uint64_t rem = sort_digit_bits(m);
+    const int W = m.wide ? WIDE_DIGIT_BITS : 8;
+    uint32_t np = 0;
+    for (; rem; np++) sort_digit_next(rem, W);
+    return np;
+}
+
 // true when sort_pairs_dev<uint16_t> left its result in the second buffer pair
 __device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
-    return n >= 2 && m.pingpong && (__popc(active_bytes(m)) & 1);
+    return n >= 2 && m.pingpong && (sort_digit_passes(m) & 1);
 }
 
 // Device-decided variant, sorted with `tier` (TIER_AUTO: the tuned or
@@ -108,6 +144,14 @@ constexpr size_t sort_status_words(uint32_t n) {
                    (512 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 256)
                ? (2 * (((size_t)n + SORT_TILE - 1) / SORT_TILE) * 256 + 2)
                : (512 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 256);
+}
+// The same with room for the cooperative sort's 9-bit digits (512 counts
+// and 512 offsets per tile, plus 512 digit totals): the scratch of the
+// update front.
+constexpr size_t sort_status_words_wide(uint32_t n) {
+    return sort_status_words(n) > 1024 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 512
+               ? sort_status_words(n)
+               : 1024 * (((size_t)n + COOP_MIN_TILE - 1) / COOP_MIN_TILE) + 512;
 }
 
 // One-time kernel attribute setup (outside stream capture).

@@ -19,6 +19,23 @@ def _bucket(n):
     return max(0, int(n - 1).bit_length())
 
 
+def _expected_passes(keys, tier):
+    """Digit passes of the batch sort: one per byte where the keys differ,
+    or for the cooperative sort one per 9-bit window, each starting at the
+    lowest differing bit the earlier windows left uncovered."""
+    if keys.size < 2:
+        return 0
+    diff = int(np.bitwise_and.reduce(keys)) ^ int(np.bitwise_or.reduce(keys))
+    if tier != "cooperative":
+        return sum(1 for b in range(8) if (diff >> (8 * b)) & 0xFF)
+    n = 0
+    while diff:
+        low = (diff & -diff).bit_length() - 1
+        diff = (diff >> (low + 9)) << (low + 9)
+        n += 1
+    return n
+
+
 @pytest.fixture
 def reset_table(engine):
     from lpma_gb300 import rpma
@@ -72,8 +89,9 @@ def test_every_tier_gives_the_same_layout(engine, oracle, reset_table, n, tiers)
             dels = rng.choice(live, size=min(nd, live.size), replace=False)
             if step == 2:  # the batch holds n keys in all
                 ins = ins[:n - dels.size]
-            g.update(ins=_dev(ins), dels=_dev(dels))
+            st = g.update(ins=_dev(ins), dels=_dev(dels))
             o.update(ins=ins, dels=dels)
             assert_same(g, o, "tier %s, batch of %d, step %d" % (tier, ins.size + dels.size, step))
+            assert st["sort_passes"] == _expected_passes(np.concatenate([ins, dels]), tier), (tier, st["sort_passes"])
         g.close()
         rp.tune_set(_bucket(n), 0)
