@@ -114,6 +114,10 @@ struct LpmaHandle {
     cudaStream_t cap_stream = nullptr;  // private stream for graph capture
     cudaEvent_t front_ev = nullptr;     // recorded after the front's status read-back
     cudaEvent_t front_ev_blk = nullptr; // the same, waited on without spinning (concurrent handles)
+    // the front's 4- and 32-segment executors run on side_stream, beside the
+    // single-segment one: fork after the status read-back, join after them
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::vector<FrontGraph> graphs;
     uint64_t graph_clock = 0;
     bool host_staged = false;    // h2d already holds the staged input bytes
@@ -545,10 +549,20 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // round trip: they read their counts on the device and do nothing when
     // the plan overflowed.  The host waits for the read-back only, so they
     // run while it decides what else the call needs.
+    // The windows of the three executors are disjoint, so the 4- and
+    // 32-segment ones run on a second stream beside the single-segment one
+    // (a parallel branch of the captured graph); the join makes everything
+    // after them on s wait for all three.
     Geo ge{h->c.keys, h->c.vals, h->H};
+    CK(cudaEventRecord(h->fork_ev, s));
+    CK(cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
+    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst,
+                      h->side_stream, true);
+    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst,
+                      h->side_stream, true);
+    CK(cudaEventRecord(h->join_ev, h->side_stream));
     launch_exec_small(h->wsingle, (uint32_t)n, 0, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
-    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
-    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
+    CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     return LPMA_OK;
 }
 
@@ -988,6 +1002,9 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     }
     h->graphs.clear();
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->side_stream) cudaStreamDestroy(h->side_stream);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->front_ev) cudaEventDestroy(h->front_ev);
     if (h->front_ev_blk) cudaEventDestroy(h->front_ev_blk);
     free_cap(h->c, nullptr, true);
@@ -1049,6 +1066,9 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
     // empty height-0 tree (init_rpma, rpma.cuh:1764-1795)
     h->H = 0;
     if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) ||
+        cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking) ||
+        cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) ||
+        cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) ||
         cudaEventCreateWithFlags(&h->front_ev, cudaEventDisableTiming) ||
         cudaEventCreateWithFlags(&h->front_ev_blk, cudaEventDisableTiming | cudaEventBlockingSync) || sort_prepare())
         return fail(LPMA_ERR_CUDA);
