@@ -940,6 +940,10 @@ struct LpmaBatcher {
     ForestExec *dE = nullptr, *hE = nullptr;
     uint32_t *dX = nullptr, *hX = nullptr;  // executor block offsets: 3 tables of G + 1
     cudaEvent_t done = nullptr;             // after the last shared executor of the previous call
+    // the shared 4- and 32-segment executors run on side beside the
+    // single-segment one (disjoint windows)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     bool pending = false;
     BatchWorkers *workers = nullptr;
 };
@@ -1399,6 +1403,9 @@ lpma_status_t lpma_batcher_destroy(LpmaBatcher *b) {
     delete b->workers;
     batcher_free(b);
     if (b->done) cudaEventDestroy(b->done);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->join_ev) cudaEventDestroy(b->join_ev);
+    if (b->side) cudaStreamDestroy(b->side);
     delete b;
     return LPMA_OK;
 }
@@ -1550,8 +1557,18 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             }
             CK(cudaMemcpyAsync(b->dE, b->hE, GS * sizeof(ForestExec), cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(b->dX, b->hX, 3 * (GS + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-            for (int kind = 0; kind < 3; kind++)
-                launch_forest_exec(kind, b->dE, b->dX + kind * (GS + 1), GS, xblk[kind], s);
+            if (!b->side) {
+                CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+                CK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+                CK(cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming));
+            }
+            CK(cudaEventRecord(b->fork_ev, s));
+            CK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
+            for (int kind = 1; kind < 3; kind++)
+                launch_forest_exec(kind, b->dE, b->dX + kind * (GS + 1), GS, xblk[kind], b->side);
+            CK(cudaEventRecord(b->join_ev, b->side));
+            launch_forest_exec(0, b->dE, b->dX, GS, xblk[0], s);
+            CK(cudaStreamWaitEvent(s, b->join_ev, 0));
             if (!b->done) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
             CK(cudaEventRecord(b->done, s));
             b->pending = true;
