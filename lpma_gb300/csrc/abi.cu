@@ -86,6 +86,7 @@ struct LpmaHandle {
     uint16_t *bp0 = nullptr, *bp1 = nullptr;
     uint8_t *kind = nullptr, *pend = nullptr;
     uint32_t *seg = nullptr, *blk_nn = nullptr, *blk_ins = nullptr;
+    uint32_t *sup = nullptr;  // the locate's (kept, insert) totals per 64 blocks of 256 keys
     UpdList u{}, u2{};
     Window *cand = nullptr, *wsingle = nullptr, *wsmall4 = nullptr, *wsmall = nullptr, *wbig = nullptr;
     SortScratch sort{};
@@ -305,6 +306,7 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n, cudaStream_t s) {
     };
     part(&h->bk0, cap), part(&h->bk1, cap), part(&h->bp0, cap), part(&h->bp1, cap);
     part(&h->kind, cap), part(&h->pend, cap), part(&h->seg, cap), part(&h->blk_nn, nb), part(&h->blk_ins, nb);
+    part(&h->sup, sup_words_for(cap));
     for (UpdList *u : {&h->u, &h->u2})
         part(&u->key, cap), part(&u->val, cap), part(&u->kind, cap), part(&u->seg, cap), part(&u->ip, cap + 1);
     part(&h->cand, cap), part(&h->wsingle, cap), part(&h->wsmall4, cap), part(&h->wsmall, cap), part(&h->wbig, cap);
@@ -523,7 +525,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
     launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
                 h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), h->c.fl, h->c.cnt,
-                prefetch_segs(h, n), s);
+                prefetch_segs(h, n), h->sup, sup_words_for(n), s);
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
     const SortTier tier = sort_tier_for_update((uint32_t)n, h->sort);
@@ -531,9 +533,9 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s, tier));
     Geo g{h->c.keys, h->c.vals, h->H};
     launch_resolve_locate(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, g, h->c.fl, thres, h->kind, h->seg,
-                          h->blk_nn, h->blk_ins, h->dst, s);
-    launch_compact(h->bk0, h->bp0, h->bk1, h->bp1, mask, h->kind, h->seg, (uint32_t)n, h->blk_nn, h->blk_ins, h->u,
-                   h->dst, s);
+                          h->blk_nn, h->blk_ins, h->sup, h->dst, s);
+    launch_compact(h->bk0, h->bp0, h->bk1, h->bp1, mask, h->kind, h->seg, (uint32_t)n, h->blk_nn, h->blk_ins, h->sup,
+                   h->u, h->dst, s);
     // plan the first loop
     Tables tb = make_tables(h, h->H, true);
     // the status reset cleared the plan counters and k_pack the bitmap
@@ -659,7 +661,7 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         }
         fg->stamp = ++h->graph_clock;
         // k_pack(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, bitmap,
-        //        bitmap_words, fl, cnt, pf_segs)
+        //        bitmap_words, fl, cnt, pf_segs, sup, sup_words)
         const uint64_t *a_ins = ins, *a_del = del;
         const uint8_t *a_vals = ins_vals;
         uint32_t a_nins = (uint32_t)n_ins, a_ndel = (uint32_t)n_del, a_V = h->V, a_thres = thres,
@@ -673,8 +675,10 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         const ulonglong2 *a_fl = h->c.fl;
         const uint8_t *a_cnt = h->c.cnt;
         uint64_t a_pf = prefetch_segs(h, n);
+        uint32_t *a_sup = h->sup;
+        uint32_t a_supw = sup_words_for(n);
         void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st,
-                        &a_bm, &a_bmw, &a_fl, &a_cnt, &a_pf};
+                        &a_bm, &a_bmw, &a_fl, &a_cnt, &a_pf, &a_sup, &a_supw};
         cudaKernelNodeParams kp = fg->pack_params;
         kp.kernelParams = args;
         kp.extra = nullptr;

@@ -25,12 +25,18 @@ struct Geo {  // one tree geometry in HBM
 
 // validate + pack both input arrays into one key/payload array; payload bits
 // 0-7 = value, bit 8 = delete.  Also clears the planner bitmap (bitmap_words
-// 32-bit words) for the call's first plan, and prefetches the first pf_segs
-// entries of the segment bounds (fl) and counts (cnt) into L2.
+// 32-bit words) for the call's first plan and the locate's chunk-group
+// totals (sup_words words), and prefetches the first pf_segs entries of the
+// segment bounds (fl) and counts (cnt) into L2.
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del,
                  uint32_t n_del, uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                  uint64_t *keys_out, uint16_t *pay_out, DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
-                 const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs, cudaStream_t s);
+                 const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs, uint32_t *sup, uint32_t sup_words,
+                 cudaStream_t s);
+
+// words of the locate's chunk-group totals for n keys (an (nn, inserts)
+// pair per 64 chunks of 256 keys)
+inline uint32_t sup_words_for(uint64_t n) { return 2 * (uint32_t)((n + 256 * 64 - 1) / (256 * 64)) + 2; }
 
 // the pack kernel's entry (graph replays update its input pointers)
 const void *pack_kernel_fn();
@@ -41,14 +47,19 @@ void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_
 
 // collapse duplicates, locate every key, membership test against its
 // segment, upsert/tombstone in place; per-256-block counts of kept entries
-// The sorted batch is (k0, p0) or (k1, p1), as sort_pairs_dev left it.
+// and inserts, and their totals per 64 blocks added into sup (cleared by
+// the pack).  The sorted batch is (k0, p0) or (k1, p1), as sort_pairs_dev
+// left it.
 void launch_resolve_locate(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, uint32_t n,
                            SortMask mask, Geo g, const ulonglong2 *fl, uint32_t thres, uint8_t *kind, uint32_t *seg,
-                           uint32_t *blk_nn, uint32_t *blk_ins, DevStatus *st, cudaStream_t s);
+                           uint32_t *blk_nn, uint32_t *blk_ins, uint32_t *sup, DevStatus *st, cudaStream_t s);
 
+// the update list: each 256-block's offsets from the group totals and the
+// block counts before it; the last block writes n_u, n_ins, n_del and the
+// end of ip
 void launch_compact(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, SortMask mask,
                     const uint8_t *kind, const uint32_t *seg, uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins,
-                    UpdList u, DevStatus *st, cudaStream_t s);
+                    const uint32_t *sup, UpdList u, DevStatus *st, cudaStream_t s);
 
 // locate only (second loop after a level-up): u.seg from u.key
 void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s);

@@ -22,7 +22,8 @@ namespace {
 constexpr int TPB = 256;
 constexpr int TOPL = 10;               // tree levels staged in shared memory by locate
 constexpr int TOPN = (1 << TOPL) - 1;  // 1023 heap entries = 16 KB of (first, last)
-constexpr int LSUM = 8;                // windows up to 2^8 segments sum counts directly
+constexpr int LSUM = 8;
+constexpr uint32_t SUP_CHUNKS = 64;     // chunks (of TPB keys) per group total of the locate                // windows up to 2^8 segments sum counts directly
 
 __device__ inline uint32_t warp_sum(uint32_t v) {
 #pragma unroll
@@ -209,9 +210,12 @@ __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, 
                                               uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                                               uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
                                               DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
-                                              const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs) {
-    // the planner bitmap of this call starts clear
+                                              const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs,
+                                              uint32_t *sup, uint32_t sup_words) {
+    // the planner bitmap and the locate's chunk-group totals of this call
+    // start clear
     for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < bitmap_words; i += gridDim.x * TPB) bitmap[i] = 0;
+    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < sup_words; i += gridDim.x * TPB) sup[i] = 0;
     k_pack_body(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, blockIdx.x, gridDim.x);
     // the segment bounds and counts that the locate and the planner read at
     // random come into L2 while the batch is sorted (the sort runs out of L2
@@ -245,7 +249,8 @@ __device__ __forceinline__ void k_resolve_locate_body(const uint64_t *__restrict
                                                         const uint16_t *__restrict__ p1, uint32_t n, SortMask mask,
                                                         Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
-                                                        uint32_t *blk_ins, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+                                                        uint32_t *blk_ins, uint32_t *sup, DevStatus *st, uint32_t bid_,
+                                                        uint32_t nblk_) {
     const bool odd = sort_result_odd(mask, n);
     const uint64_t *__restrict__ skey = odd ? k1 : k0;
     const uint16_t *__restrict__ spay = odd ? p1 : p0;
@@ -313,6 +318,11 @@ __device__ __forceinline__ void k_resolve_locate_body(const uint64_t *__restrict
         if (threadIdx.x == 0) {
             blk_nn[chunk] = c_nn;
             blk_ins[chunk] = c_ins;
+            // totals per group of SUP_CHUNKS chunks, for the compaction's offsets
+            if (sup && c_nn) {
+                atomicAdd(&sup[2 * (chunk / SUP_CHUNKS)], c_nn);
+                if (c_ins) atomicAdd(&sup[2 * (chunk / SUP_CHUNKS) + 1], c_ins);
+            }
         }
     }
     ups = warp_sum(ups);
@@ -329,9 +339,10 @@ __global__ void __launch_bounds__(TPB) k_resolve_locate(const uint64_t *__restri
                                                         const uint16_t *__restrict__ p1, uint32_t n, SortMask mask,
                                                         Geo g, const ulonglong2 *__restrict__ fl, uint32_t thres,
                                                         uint8_t *kind, uint32_t *seg, uint32_t *blk_nn,
-                                                        uint32_t *blk_ins, DevStatus *st) {
+                                                        uint32_t *blk_ins, uint32_t *sup, DevStatus *st) {
     griddep_wait();
-    k_resolve_locate_body(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg, blk_nn, blk_ins, st, blockIdx.x, gridDim.x);
+    k_resolve_locate_body(k0, p0, k1, p1, n, mask, g, fl, thres, kind, seg, blk_nn, blk_ins, sup, st, blockIdx.x,
+                          gridDim.x);
 }
 
 // exclusive scans of the two block-count arrays (one CTA); totals -> status
@@ -435,23 +446,57 @@ __device__ __forceinline__ void k_compact_body(const uint64_t *__restrict__ k0, 
                                                  const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
                                                  SortMask mask, const uint8_t *__restrict__ kind,
                                                  const uint32_t *__restrict__ seg, uint32_t n,
-                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u, uint32_t bid_, uint32_t nblk_) {
+                                                 const uint32_t *blk_nn, const uint32_t *blk_ins,
+                                                 const uint32_t *sup, UpdList u, DevStatus *st, uint32_t bid_,
+                                                 uint32_t nblk_) {
     const bool odd = sort_result_odd(mask, n);
     const uint64_t *__restrict__ skey = odd ? k1 : k0;
     const uint16_t *__restrict__ spay = odd ? p1 : p0;
     __shared__ uint32_t wsum[TPB / 32];
+    __shared__ uint64_t wsum64[TPB / 32];
+    // this chunk's offsets: with sup, the counts of the chunks before it
+    // (whole groups from the group totals, then the chunks of its own group;
+    // nn in the low half of the sum, inserts in the high half); without, the
+    // scanned chunk counts
+    uint32_t base_nn, base_ins;
+    if (sup) {
+        const uint32_t grp = bid_ / SUP_CHUNKS;
+        uint64_t acc = 0;
+        for (uint32_t t = threadIdx.x; t < grp; t += TPB)
+            acc += (uint64_t)sup[2 * t] | ((uint64_t)sup[2 * t + 1] << 32);
+        for (uint32_t t = grp * SUP_CHUNKS + threadIdx.x; t < bid_; t += TPB)
+            acc += (uint64_t)blk_nn[t] | ((uint64_t)blk_ins[t] << 32);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) wsum64[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        acc = 0;
+#pragma unroll
+        for (int w = 0; w < TPB / 32; w++) acc += wsum64[w];
+        base_nn = (uint32_t)acc, base_ins = (uint32_t)(acc >> 32);
+    } else {
+        base_nn = blk_nn[bid_], base_ins = blk_ins[bid_];
+    }
     const uint32_t i = bid_ * TPB + threadIdx.x;
     const uint32_t kd = i < n ? kind[i] : KIND_NOP;
     // pack (kept, insert) flags into one scan word
     const uint32_t x = (kd != KIND_NOP ? 1u : 0u) | (kd == KIND_INS ? 1u << 16 : 0u);
     const uint32_t ex = block_excl_scan(x, wsum);
     if (kd != KIND_NOP) {
-        const uint32_t pos = blk_nn[bid_] + (ex & 0xFFFF);
+        const uint32_t pos = base_nn + (ex & 0xFFFF);
         u.key[pos] = skey[i];
         u.val[pos] = (uint8_t)(spay[i] & 0xFF);
         u.kind[pos] = (uint8_t)kd;
         u.seg[pos] = seg[i];
-        u.ip[pos] = blk_ins[bid_] + (ex >> 16);
+        u.ip[pos] = base_ins + (ex >> 16);
+    }
+    // the last chunk knows the totals: list length, inserts, the end of ip
+    if (sup && bid_ == nblk_ - 1 && threadIdx.x == TPB - 1) {
+        const uint32_t t = ex + x, nu = base_nn + (t & 0xFFFF), ni = base_ins + (t >> 16);
+        st->n_u = nu;
+        st->n_ins = ni;
+        st->n_del = nu - ni;
+        u.ip[nu] = ni;
     }
 }
 
@@ -459,9 +504,10 @@ __global__ void __launch_bounds__(TPB) k_compact(const uint64_t *__restrict__ k0
                                                  const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
                                                  SortMask mask, const uint8_t *__restrict__ kind,
                                                  const uint32_t *__restrict__ seg, uint32_t n,
-                                                 const uint32_t *blk_nn, const uint32_t *blk_ins, UpdList u) {
+                                                 const uint32_t *blk_nn, const uint32_t *blk_ins,
+                                                 const uint32_t *sup, UpdList u, DevStatus *st) {
     griddep_wait();
-    k_compact_body(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u, blockIdx.x, gridDim.x);
+    k_compact_body(k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, sup, u, st, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ relocate / pending
@@ -1293,10 +1339,11 @@ const void *pack_kernel_fn() { return reinterpret_cast<const void *>(&k_pack); }
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
                  DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, const ulonglong2 *fl, const uint8_t *cnt,
-                 uint64_t pf_segs, cudaStream_t s) {
+                 uint64_t pf_segs, uint32_t *sup, uint32_t sup_words, cudaStream_t s) {
     ProfScope ps_("pack", s);
     k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
-                                                        keys_out, pay_out, st, bitmap, bitmap_words, fl, cnt, pf_segs);
+                                                        keys_out, pay_out, st, bitmap, bitmap_words, fl, cnt, pf_segs,
+                                                        sup, sup_words);
     note_launch();
 }
 
@@ -1309,22 +1356,21 @@ void launch_live_counts(const uint64_t *keys, uint32_t H, uint32_t thres, uint8_
 
 void launch_resolve_locate(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, uint32_t n,
                            SortMask mask, Geo g, const ulonglong2 *fl, uint32_t thres, uint8_t *kind, uint32_t *seg,
-                           uint32_t *blk_nn, uint32_t *blk_ins, DevStatus *st, cudaStream_t s) {
+                           uint32_t *blk_nn, uint32_t *blk_ins, uint32_t *sup, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("resolve_locate", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
     launch_pdl(k_resolve_locate, dim3(nb < 152 * 8 ? nb : 152 * 8), dim3(TPB), 0, s, k0, p0, k1, p1, n, mask, g, fl,
-               thres, kind, seg, blk_nn, blk_ins, st);
+               thres, kind, seg, blk_nn, blk_ins, sup, st);
     note_launch();
 }
 
 void launch_compact(const uint64_t *k0, const uint16_t *p0, const uint64_t *k1, const uint16_t *p1, SortMask mask,
                     const uint8_t *kind, const uint32_t *seg, uint32_t n, uint32_t *blk_nn, uint32_t *blk_ins,
-                    UpdList u, DevStatus *st, cudaStream_t s) {
+                    const uint32_t *sup, UpdList u, DevStatus *st, cudaStream_t s) {
     ProfScope ps_("compact", s);
     const uint32_t nb = (n + TPB - 1) / TPB;
-    launch_pdl(k_scan_pairs, dim3(1), dim3(1024), 0, s, blk_nn, blk_ins, nb, u.ip, st);
-    launch_pdl(k_compact, dim3(nb), dim3(TPB), 0, s, k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, u);
-    note_launch(2);
+    launch_pdl(k_compact, dim3(nb), dim3(TPB), 0, s, k0, p0, k1, p1, mask, kind, seg, n, blk_nn, blk_ins, sup, u, st);
+    note_launch();
 }
 
 void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStream_t s) {
@@ -1546,7 +1592,7 @@ __global__ void __launch_bounds__(TPB) k_forest_resolve(const ForestGraph *__res
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_resolve_locate_body(f.sk, f.sp, f.sk, f.sp, f.n_ins + f.n_del, SortMask{nullptr, 0u, 0u}, f.g, f.fl, 0, f.kind,
-                          f.seg, f.blk_nn, f.blk_ins, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+                          f.seg, f.blk_nn, f.blk_ins, nullptr, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(1024) k_forest_scan_pairs(const ForestGraph *__restrict__ F) {
@@ -1560,7 +1606,7 @@ __global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__res
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_compact_body(f.sk, f.sp, f.sk, f.sp, SortMask{nullptr, 0u, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
-                   f.blk_ins, f.u, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+                   f.blk_ins, nullptr, f.u, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restrict__ F, const uint32_t *boff,
