@@ -1490,6 +1490,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
             f.bk0 = h->bk0, f.bp0 = h->bp0, f.kind = h->kind, f.seg = h->seg;
             f.blk_nn = h->blk_nn, f.blk_ins = h->blk_ins, f.u = h->u;
             f.bitmap = h->c.bitmap, f.bitmap_words = bitmap_words(h->H);
+            f.sup = h->sup, f.sup_words = sup_words_for(m);
             f.cand = h->cand, f.wsingle = h->wsingle, f.wsmall4 = h->wsmall4, f.wsmall = h->wsmall, f.wbig = h->wbig;
             f.pend = h->pend;
             f.tb = make_tables(h, h->H, true);
@@ -1521,11 +1522,10 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
         launch_forest_phase(1, b->dF, B, G, nblk[0], nullptr, s);
         CK(forest_sort(b->dJ, G, B + 5 * (G + 1), nblk + 5, rounds, s));
         launch_forest_phase(2, b->dF, B + (G + 1), G, nblk[1], nullptr, s);
-        launch_forest_phase(3, b->dF, nullptr, G, G, nullptr, s);
-        launch_forest_phase(4, b->dF, B + 2 * (G + 1), G, nblk[2], nullptr, s);
-        launch_forest_phase(5, b->dF, B + 3 * (G + 1), G, nblk[3], nullptr, s);
-        launch_forest_phase(6, b->dF, B + 4 * (G + 1), G, nblk[4], nullptr, s);
-        launch_forest_phase(7, b->dF, nullptr, G, G, b->dS, s);
+        launch_forest_phase(3, b->dF, B + 2 * (G + 1), G, nblk[2], nullptr, s);
+        launch_forest_phase(4, b->dF, B + 3 * (G + 1), G, nblk[3], nullptr, s);
+        launch_forest_phase(5, b->dF, B + 4 * (G + 1), G, nblk[4], nullptr, s);
+        launch_forest_phase(6, b->dF, nullptr, G, G, b->dS, s);
         CK(cudaMemcpyAsync(b->hS, b->dS, G * sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         CK(cudaGetLastError());

@@ -173,6 +173,8 @@ struct ForestGraph {
     const uint16_t *sp;
     uint8_t *kind;
     uint32_t *seg, *blk_nn, *blk_ins;
+    uint32_t *sup;  // the locate's per-64-block totals (cleared by phase 0)
+    uint32_t sup_words;
     UpdList u;
     uint32_t *bitmap;
     uint64_t bitmap_words;
@@ -201,9 +203,9 @@ void launch_forest_exec(int kind, const ForestExec *E, const uint32_t *boff, uin
                         cudaStream_t s);
 // CTAs the executor of `kind` gets for n windows (as in lpma_update)
 uint32_t exec_ctas(int kind, uint32_t n);
-// phases: 0 reset statuses and planner bitmaps, 1 pack, 2 resolve + locate,
-// 3 insert-prefix scan, 4 compact, 5 plan, 6 maximal windows, 7 status copy
-// into out[g]
+// phases: 0 reset statuses, planner bitmaps and the locate's group totals,
+// 1 pack, 2 resolve + locate, 3 compact, 4 plan, 5 maximal windows, 6 status
+// copy into out[g]
 void launch_forest_phase(int phase, const ForestGraph *F, const uint32_t *boff, uint32_t ngraphs,
                          uint32_t nblocks, DevStatus *out, cudaStream_t s);
 

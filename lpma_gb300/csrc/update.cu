@@ -1568,6 +1568,7 @@ __global__ void __launch_bounds__(TPB) k_forest_reset(const ForestGraph *__restr
     constexpr uint32_t NW = offsetof(DevStatus, sticky) / 4;
     for (uint32_t i = threadIdx.x; i < NW; i += TPB) w[i] = 0;
     for (uint64_t i = threadIdx.x; i < f.bitmap_words; i += TPB) f.bitmap[i] = 0;
+    for (uint32_t i = threadIdx.x; i < f.sup_words; i += TPB) f.sup[i] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
         f.st->min_t_ins = 0xFFFFFFFFu;
@@ -1592,13 +1593,7 @@ __global__ void __launch_bounds__(TPB) k_forest_resolve(const ForestGraph *__res
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_resolve_locate_body(f.sk, f.sp, f.sk, f.sp, f.n_ins + f.n_del, SortMask{nullptr, 0u, 0u}, f.g, f.fl, 0, f.kind,
-                          f.seg, f.blk_nn, f.blk_ins, nullptr, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
-}
-
-__global__ void __launch_bounds__(1024) k_forest_scan_pairs(const ForestGraph *__restrict__ F) {
-    const ForestGraph &f = F[blockIdx.x];
-    const uint32_t n = f.n_ins + f.n_del;
-    k_scan_pairs_body(f.blk_nn, f.blk_ins, (n + TPB - 1) / TPB, f.u.ip, f.st, 0, 1);
+                          f.seg, f.blk_nn, f.blk_ins, f.sup, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__restrict__ F, const uint32_t *boff,
@@ -1606,7 +1601,7 @@ __global__ void __launch_bounds__(TPB) k_forest_compact(const ForestGraph *__res
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestGraph &f = F[g];
     k_compact_body(f.sk, f.sp, f.sk, f.sp, SortMask{nullptr, 0u, 0u}, f.kind, f.seg, f.n_ins + f.n_del, f.blk_nn,
-                   f.blk_ins, nullptr, f.u, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+                   f.blk_ins, f.sup, f.u, f.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(TPB) k_forest_plan(const ForestGraph *__restrict__ F, const uint32_t *boff,
@@ -1674,19 +1669,18 @@ void launch_forest_exec(int kind, const ForestExec *E, const uint32_t *boff, uin
 
 void launch_forest_phase(int phase, const ForestGraph *F, const uint32_t *boff, uint32_t G, uint32_t nblocks,
                          DevStatus *out, cudaStream_t s) {
-    if (!G || (phase >= 1 && phase <= 6 && phase != 3 && !nblocks)) return;
-    static const char *const names[8] = {"forest_reset",   "forest_pack", "forest_resolve", "forest_scan_pairs",
-                                         "forest_compact", "forest_plan", "forest_plan_max", "forest_status"};
-    ProfScope ps_(names[phase & 7], s);
+    if (!G || (phase >= 1 && phase <= 5 && !nblocks)) return;
+    static const char *const names[7] = {"forest_reset", "forest_pack",     "forest_resolve", "forest_compact",
+                                         "forest_plan",  "forest_plan_max", "forest_status"};
+    ProfScope ps_(names[phase % 7], s);
     switch (phase) {
         case 0: k_forest_reset<<<G, TPB, 0, s>>>(F); break;
         case 1: k_forest_pack<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
         case 2: k_forest_resolve<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
-        case 3: k_forest_scan_pairs<<<G, 1024, 0, s>>>(F); break;
-        case 4: k_forest_compact<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
-        case 5: k_forest_plan<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
-        case 6: k_forest_plan_max<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
-        case 7: k_forest_status<<<G, 64, 0, s>>>(F, out); break;
+        case 3: k_forest_compact<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 4: k_forest_plan<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 5: k_forest_plan_max<<<nblocks, TPB, 0, s>>>(F, boff, G); break;
+        case 6: k_forest_status<<<G, 64, 0, s>>>(F, out); break;
     }
     note_launch();
 }
