@@ -554,17 +554,22 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // The windows of the three executors are disjoint, so the 4- and
     // 32-segment ones run on a second stream beside the single-segment one
     // (a parallel branch of the captured graph); the join makes everything
-    // after them on s wait for all three.
+    // after them on s wait for all three.  The in-library profiler times
+    // each kernel alone, so it keeps them on one stream.
     Geo ge{h->c.keys, h->c.vals, h->H};
-    CK(cudaEventRecord(h->fork_ev, s));
-    CK(cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
-    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst,
-                      h->side_stream, true);
-    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst,
-                      h->side_stream, true);
-    CK(cudaEventRecord(h->join_ev, h->side_stream));
+    const bool fork = !prof_enabled();
+    cudaStream_t side = fork ? h->side_stream : s;
+    if (fork) {
+        CK(cudaEventRecord(h->fork_ev, s));
+        CK(cudaStreamWaitEvent(side, h->fork_ev, 0));
+    }
+    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
+                      true);
+    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
+                      true);
+    if (fork) CK(cudaEventRecord(h->join_ev, side));
     launch_exec_small(h->wsingle, (uint32_t)n, 0, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
-    CK(cudaStreamWaitEvent(s, h->join_ev, 0));
+    if (fork) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     return LPMA_OK;
 }
 
@@ -1566,13 +1571,18 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
                 CK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
                 CK(cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming));
             }
-            CK(cudaEventRecord(b->fork_ev, s));
-            CK(cudaStreamWaitEvent(b->side, b->fork_ev, 0));
+            // one stream while the in-library profiler times each kernel
+            const bool fork = !prof_enabled();
+            cudaStream_t side = fork ? b->side : s;
+            if (fork) {
+                CK(cudaEventRecord(b->fork_ev, s));
+                CK(cudaStreamWaitEvent(side, b->fork_ev, 0));
+            }
             for (int kind = 1; kind < 3; kind++)
-                launch_forest_exec(kind, b->dE, b->dX + kind * (GS + 1), GS, xblk[kind], b->side);
-            CK(cudaEventRecord(b->join_ev, b->side));
+                launch_forest_exec(kind, b->dE, b->dX + kind * (GS + 1), GS, xblk[kind], side);
+            if (fork) CK(cudaEventRecord(b->join_ev, side));
             launch_forest_exec(0, b->dE, b->dX, GS, xblk[0], s);
-            CK(cudaStreamWaitEvent(s, b->join_ev, 0));
+            if (fork) CK(cudaStreamWaitEvent(s, b->join_ev, 0));
             if (!b->done) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
             CK(cudaEventRecord(b->done, s));
             b->pending = true;
