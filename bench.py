@@ -548,6 +548,10 @@ def served_arm(args):
     from lpma_gb300 import rpma
     gs = GraphSet(min(64, args.graphs), args.seed, flags=1)
     budget = 150 << 30
+    # the update memory pool holds room for the graphs to grow before traffic
+    # starts (no new device memory mapped under load)
+    reserve = 32 << 30
+    rpma.memory_reserve(reserve)
     # read outputs: one buffer set per graph (a graph's requests run one at a time)
     for G in gs.graphs:
         G["nbr_out"] = (torch.empty(2, dtype=torch.int32, device="cuda"),
@@ -646,7 +650,7 @@ def served_arm(args):
             "workload": "%d resident R-MAT graphs (V 2^10..2^18, edge factor 8..32), 150 GB admission budget; 70%% "
                         "updates (log-uniform 1..1M, insert:delete 3:1), 15%% neighbour lists, 15%% 2-hop BFS from "
                         "1,024 seeds" % len(gs.graphs), "unit": "ms / edges/s", "workers": args.workers,
-            "duration_s_per_rate": args.duration, **out,
+            "duration_s_per_rate": args.duration, "memory_reserve_gb": reserve / 2 ** 30, **out,
             "note": "latency = completion - planned arrival (queueing and submission lag included); one_at_a_time = "
                     "a pool of one worker; the load generator runs with Python's cyclic GC off"}
     print(json.dumps(line))

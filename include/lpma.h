@@ -280,6 +280,15 @@ LPMA_API lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, ui
 /* Device bytes the handle holds (structure, scratch, views). */
 LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
 
+/* Grow the current device's update memory pool (the stream-ordered pool the
+ * handles' capacity and batch buffers come from) to hold at least `bytes`
+ * more: the bytes are allocated on `stream` and freed again, and the pool
+ * keeps them.  A server calls this before taking traffic, so that a graph
+ * growing a level under load is served from memory the pool already holds
+ * instead of mapping new memory then.  Synchronous; LPMA_ERR_OUT_OF_MEMORY
+ * if the device cannot provide them. */
+LPMA_API lpma_status_t lpma_memory_reserve(uint64_t bytes, lpma_stream_t stream);
+
 /* ---- request pool: many resident graphs, batched or served ----
  * Worker threads, each with its own stream, run submitted requests.
  * Requests on different graphs run concurrently; requests on one graph run

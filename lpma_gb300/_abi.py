@@ -28,7 +28,7 @@ EXPORTS = [
     "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
-    "lpma_autotune", "lpma_tune_set", "lpma_tune_get",
+    "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve",
 ]
 SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
@@ -128,6 +128,7 @@ def load():
         "lpma_read_edgelist": [ctypes.c_char_p, ctypes.c_char_p, P, SZ, P, P],
         "lpma_read_queries": [ctypes.c_char_p, P, P, SZ, P],
         "lpma_memory_bytes": [P, P],
+        "lpma_memory_reserve": [U64, P],
         "lpma_set_flags": [P, U32],
         "lpma_error_detail": [P, P],
         "lpma_pool_create": [U32, U64, P],

@@ -1385,6 +1385,23 @@ lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags) {
     return LPMA_OK;  // cached fronts are keyed by the sort mode
 }
 
+lpma_status_t lpma_memory_reserve(uint64_t bytes, lpma_stream_t stream) {
+    cudaMemPool_t pool = batch_pool();
+    if (!pool) return LPMA_ERR_CUDA;
+    if (bytes == 0) return LPMA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    void *p = nullptr;
+    const cudaError_t e = cudaMallocFromPoolAsync(&p, (size_t)bytes, pool, s);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return LPMA_ERR_OUT_OF_MEMORY;
+    }
+    CK(e);
+    CK(cudaFreeAsync(p, s));
+    CK(cudaStreamSynchronize(s));
+    return LPMA_OK;
+}
+
 lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
     if (!h || !bytes) return LPMA_ERR_INVALID_ARGUMENT;
     uint64_t b = 0;

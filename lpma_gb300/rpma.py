@@ -427,6 +427,12 @@ def memory_bytes(g):
     return b.value
 
 
+def memory_reserve(nbytes, stream=None):
+    """Grow the update memory pool by nbytes (lpma_memory_reserve), so that
+    graphs growing under load do not map new device memory then."""
+    check(_abi.load().lpma_memory_reserve(int(nbytes), _stream_ptr(stream)), "lpma_memory_reserve")
+
+
 def query_rpma(rpma, srcs, constraints=None):
     """query_rpma (rpma.cuh:1974-2036): (offsets, nbrs, values), lists in the callers' query order."""
     return rpma.query_neighbors(srcs, constraints)
