@@ -442,6 +442,33 @@ __device__ inline uint32_t block_excl_scan(uint32_t x, uint32_t *wsum) {
     return r;
 }
 
+// The same over u64 values (fields packed in the word add independently as
+// long as none of the block's sums overflows its field).
+__device__ inline uint64_t block_excl_scan_u64(uint64_t x, uint64_t *wsum) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint64_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t t = lane < TPB / 32 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < TPB / 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < TPB / 32) wsum[lane] = t;
+    }
+    __syncthreads();
+    const uint64_t r = (w ? wsum[w - 1] : 0) + v - x;
+    __syncthreads();
+    return r;
+}
+
 __device__ __forceinline__ void k_compact_body(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
                                                  const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
                                                  SortMask mask, const uint8_t *__restrict__ kind,
@@ -694,7 +721,7 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
             if (x > 0 && u.seg[x - 1] == s) pend[x] = pend[lb_back(u.seg, x, s)];
         }
     }
-    __shared__ uint32_t wsum[TPB / 32];
+    __shared__ uint64_t wsum[TPB / 32];
     __shared__ uint32_t base_s[4];
     __shared__ unsigned long long sl[2][TPB / 32];
     const uint32_t c = bid_ * TPB + threadIdx.x;
@@ -717,10 +744,12 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
         }
         if (hit) cls = 4;
     }
+    // the four classes' positions in one scan: a 16-bit field each (at most
+    // TPB per block), classes 0 and 1 in the low word, 2 and 3 in the high
     const uint32_t pa = cls < 2 ? 1u << (16 * cls) : 0u;
     const uint32_t pb = (cls == 2 || cls == 3) ? 1u << (16 * (cls - 2)) : 0u;
-    const uint32_t exa = block_excl_scan(pa, wsum);
-    const uint32_t exb = block_excl_scan(pb, wsum);
+    const uint64_t exab = block_excl_scan_u64((uint64_t)pa | ((uint64_t)pb << 32), wsum);
+    const uint32_t exa = (uint32_t)exab, exb = (uint32_t)(exab >> 32);
     // slots of disjoint maximal windows: a warp's sums stay below 2^32
     uint32_t s_small = cls <= 2 ? 32u * w.f : 0u, s_big = cls == 3 ? 32u * w.f : 0u;
     uint32_t t_big = cls == 3 ? (w.f + 31) / 32 : 0u;
