@@ -525,12 +525,15 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     const uint32_t key_format = internal ? (uint32_t)LPMA_KEY_PACKED : h->cfg.key_format;
     launch_pack(ins, ins_vals, (uint32_t)n_ins, del, (uint32_t)n_del, h->V, thres, key_format, internal ? 1 : 0,
                 h->bk0, h->bp0, h->dst, h->c.bitmap, (uint32_t)bitmap_words(h->H), h->c.fl, h->c.cnt,
-                prefetch_segs(h, n), h->sup, sup_words_for(n), s);
+                prefetch_segs(h, n), h->sup, sup_words_for(n), h->sort.bar, s);
     if (thres_active) launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
     // sort (digit bytes decided on the device), resolve + locate, compact
     const SortTier tier = sort_tier_for_update((uint32_t)n, h->sort);
     const SortMask mask = update_sort_mask(&h->dst->key_and, tier, (uint32_t)n, h->sort);
-    CK(sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s, tier));
+    h->sort.bar_cleared = h->sort.bar != nullptr;  // by k_pack
+    const cudaError_t se = sort_pairs_dev<uint16_t>(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, h->sort, s, tier);
+    h->sort.bar_cleared = false;
+    CK(se);
     Geo g{h->c.keys, h->c.vals, h->H};
     launch_resolve_locate(h->bk0, h->bp0, h->bk1, h->bp1, (uint32_t)n, mask, g, h->c.fl, thres, h->kind, h->seg,
                           h->blk_nn, h->blk_ins, h->sup, h->dst, s);
@@ -666,7 +669,7 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         }
         fg->stamp = ++h->graph_clock;
         // k_pack(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, bitmap,
-        //        bitmap_words, fl, cnt, pf_segs, sup, sup_words)
+        //        bitmap_words, fl, cnt, pf_segs, sup, sup_words, sort_bar)
         const uint64_t *a_ins = ins, *a_del = del;
         const uint8_t *a_vals = ins_vals;
         uint32_t a_nins = (uint32_t)n_ins, a_ndel = (uint32_t)n_del, a_V = h->V, a_thres = thres,
@@ -682,8 +685,9 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         uint64_t a_pf = prefetch_segs(h, n);
         uint32_t *a_sup = h->sup;
         uint32_t a_supw = sup_words_for(n);
+        uint32_t *a_bar = h->sort.bar;
         void *args[] = {&a_ins, &a_vals, &a_nins, &a_del, &a_ndel, &a_V, &a_thres, &a_fmt, &a_internal, &a_ko, &a_po, &a_st,
-                        &a_bm, &a_bmw, &a_fl, &a_cnt, &a_pf, &a_sup, &a_supw};
+                        &a_bm, &a_bmw, &a_fl, &a_cnt, &a_pf, &a_sup, &a_supw, &a_bar};
         cudaKernelNodeParams kp = fg->pack_params;
         kp.kernelParams = args;
         kp.extra = nullptr;

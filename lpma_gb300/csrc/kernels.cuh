@@ -25,14 +25,15 @@ struct Geo {  // one tree geometry in HBM
 
 // validate + pack both input arrays into one key/payload array; payload bits
 // 0-7 = value, bit 8 = delete.  Also clears the planner bitmap (bitmap_words
-// 32-bit words) for the call's first plan and the locate's chunk-group
-// totals (sup_words words), and prefetches the first pf_segs entries of the
-// segment bounds (fl) and counts (cnt) into L2.
+// 32-bit words) for the call's first plan, the locate's chunk-group totals
+// (sup_words words) and the cooperative sort's barrier counter (sort_bar,
+// may be null), and prefetches the first pf_segs entries of the segment
+// bounds (fl) and counts (cnt) into L2.
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del,
                  uint32_t n_del, uint32_t V, uint32_t thres, uint32_t key_format, int internal,
                  uint64_t *keys_out, uint16_t *pay_out, DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
                  const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs, uint32_t *sup, uint32_t sup_words,
-                 cudaStream_t s);
+                 uint32_t *sort_bar, cudaStream_t s);
 
 // words of the locate's chunk-group totals for n keys (an (nn, inserts)
 // pair per 64 chunks of 256 keys)

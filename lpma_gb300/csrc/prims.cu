@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(SORT_TPB, 2) k_coop_sort(uint64_t *k0, V *v0, 
                                                            uint32_t *err) {
     constexpr int NB = 1 << RB, PER = NB / SORT_TPB;
     static_assert(PER >= 1 && NB % SORT_TPB == 0, "whole digits per thread");
+    griddep_wait();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CoopSmem<V, NB> &S = *reinterpret_cast<CoopSmem<V, NB> *>(smem_raw);
     const uint32_t G = gridDim.x, tile = blockIdx.x;
@@ -1161,24 +1162,35 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         const bool wide = mask.wide != 0;
         uint32_t tile_len, G;
         if (!coop_geometry<V>(n, s, &tile_len, &G, wide)) return cudaErrorInvalidValue;
-        if ((e = cudaMemsetAsync(s.bar, 0, sizeof(uint32_t), st))) return e;
+        if (!s.bar_cleared && (e = cudaMemsetAsync(s.bar, 0, sizeof(uint32_t), st))) return e;
         const size_t nb = wide ? 512 : 256;
         uint32_t *counts = s.status, *offs = s.status + nb * G, *totals = s.status + 2 * nb * G;
         uint32_t *bar = s.bar, *err = s.err;
         uint32_t tl = tile_len;
         void *args[] = {&k0, &v0, &k1, &v1, &n, &tl, &mask, &counts, &offs, &totals, &bar, &err};
         ProfScope ps("sort_coop", st);
+        // cooperative, and a programmatic dependent of the kernel before it
+        // (the sort waits for it with griddepcontrol.wait)
+        cudaLaunchAttribute attr[2];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(G);
+        cfg.blockDim = dim3(SORT_TPB);
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 2;
+        const void *fn = (const void *)k_coop_sort<V, 8>;
+        cfg.dynamicSmemBytes = sizeof(CoopSmem<V, 256>);
         if constexpr (sizeof(V) == 2) {
-            if (wide)
-                e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, WIDE_DIGIT_BITS>, dim3(G),
-                                                dim3(SORT_TPB), args, sizeof(CoopSmem<V, 512>), st);
-            else
-                e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, 8>, dim3(G), dim3(SORT_TPB), args,
-                                                sizeof(CoopSmem<V, 256>), st);
-        } else {
-            e = cudaLaunchCooperativeKernel((const void *)k_coop_sort<V, 8>, dim3(G), dim3(SORT_TPB), args,
-                                            sizeof(CoopSmem<V, 256>), st);
+            if (wide) {
+                fn = (const void *)k_coop_sort<V, WIDE_DIGIT_BITS>;
+                cfg.dynamicSmemBytes = sizeof(CoopSmem<V, 512>);
+            }
         }
+        e = cudaLaunchKernelExC(&cfg, fn, args);
         note_launch();
         return e;
     }

@@ -20,6 +20,9 @@ struct SortScratch {
     // sort), err receives ERR_TIMEOUT if a bounded barrier wait gives up.
     uint32_t *bar = nullptr;
     uint32_t *err = nullptr;
+    // the caller's previous kernel on the stream cleared *bar (no memset
+    // before the cooperative launch)
+    bool bar_cleared = false;
 };
 
 // Digit bytes to sort: host_mask, intersected (when andor is set) with the

@@ -211,11 +211,13 @@ __global__ void __launch_bounds__(TPB) k_pack(const uint64_t *__restrict__ ins, 
                                               uint64_t *__restrict__ keys_out, uint16_t *__restrict__ pay_out,
                                               DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words,
                                               const ulonglong2 *fl, const uint8_t *cnt, uint64_t pf_segs,
-                                              uint32_t *sup, uint32_t sup_words) {
+                                              uint32_t *sup, uint32_t sup_words, uint32_t *sort_bar) {
     // the planner bitmap and the locate's chunk-group totals of this call
     // start clear
     for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < bitmap_words; i += gridDim.x * TPB) bitmap[i] = 0;
     for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < sup_words; i += gridDim.x * TPB) sup[i] = 0;
+    // the cooperative sort's barrier counter (the sort that follows)
+    if (sort_bar && blockIdx.x == 0 && threadIdx.x == 0) *sort_bar = 0;
     k_pack_body(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal, keys_out, pay_out, st, blockIdx.x, gridDim.x);
     // the segment bounds and counts that the locate and the planner read at
     // random come into L2 while the batch is sorted (the sort runs out of L2
@@ -1368,11 +1370,11 @@ const void *pack_kernel_fn() { return reinterpret_cast<const void *>(&k_pack); }
 void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, const uint64_t *del, uint32_t n_del,
                  uint32_t V, uint32_t thres, uint32_t key_format, int internal, uint64_t *keys_out, uint16_t *pay_out,
                  DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, const ulonglong2 *fl, const uint8_t *cnt,
-                 uint64_t pf_segs, uint32_t *sup, uint32_t sup_words, cudaStream_t s) {
+                 uint64_t pf_segs, uint32_t *sup, uint32_t sup_words, uint32_t *sort_bar, cudaStream_t s) {
     ProfScope ps_("pack", s);
     k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
                                                         keys_out, pay_out, st, bitmap, bitmap_words, fl, cnt, pf_segs,
-                                                        sup, sup_words);
+                                                        sup, sup_words, sort_bar);
     note_launch();
 }
 
