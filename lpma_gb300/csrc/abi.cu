@@ -544,21 +544,17 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // the status reset cleared the plan counters and k_pack the bitmap
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
                  thres_active ? &h->dst->live_total : &h->dst->total_items, true));
-    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
-    // an event record node when the front is being captured into a graph
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CK(cudaStreamIsCapturing(s, &cs));
-    CK(cudaEventRecordWithFlags(blocking_waits(h) ? h->front_ev_blk : h->front_ev, s,
-                                cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
-    // the first loop's single / 4 / 32-segment windows follow without a host
-    // round trip: they read their counts on the device and do nothing when
-    // the plan overflowed.  The host waits for the read-back only, so they
-    // run while it decides what else the call needs.
-    // The windows of the three executors are disjoint, so the 4- and
-    // 32-segment ones run on a second stream beside the single-segment one
-    // (a parallel branch of the captured graph); the join makes everything
-    // after them on s wait for all three.  The in-library profiler times
-    // each kernel alone, so it keeps them on one stream.
+    // The status read-back (the host waits on the event after it) and the
+    // first loop's single / 4 / 32-segment windows follow without a host
+    // round trip: the executors read their counts on the device and do
+    // nothing when the plan overflowed, so they run while the host decides
+    // what else the call needs.  The read-back and the 4- and 32-segment
+    // executors run on a second stream (a parallel branch of the captured
+    // graph): the single-segment executor follows the planner directly, as
+    // its programmatic dependent, and the windows of the three are
+    // disjoint.  The join makes everything after them on s wait for all.
+    // The in-library profiler times each kernel alone, so it keeps them on
+    // one stream.
     Geo ge{h->c.keys, h->c.vals, h->H};
     const bool fork = !prof_enabled();
     cudaStream_t side = fork ? h->side_stream : s;
@@ -566,6 +562,12 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
         CK(cudaEventRecord(h->fork_ev, s));
         CK(cudaStreamWaitEvent(side, h->fork_ev, 0));
     }
+    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, side));
+    // an event record node when the front is being captured into a graph
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s, &cs));
+    CK(cudaEventRecordWithFlags(blocking_waits(h) ? h->front_ev_blk : h->front_ev, side,
+                                cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
     launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
                       true);
     launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
