@@ -154,9 +154,14 @@ class Stream:
             a = self.cd
             self.cd += B
             seq = self.del_seq
-        if a + B > self.n:
-            raise RuntimeError("edge stream exhausted; use fewer steps")
-        return seq[a:a + B]
+        # cyclic: past the end the sequence starts over (inserts of U ++ S and
+        # deletes of S ++ U advance together, so a full cycle returns the
+        # stored set to S)
+        a %= self.n
+        if a + B <= self.n:
+            return seq[a:a + B]
+        import torch
+        return torch.cat([seq[a:], seq[:a + B - self.n]])
 
 
 def build_workload(args, device, seed):
@@ -390,8 +395,11 @@ def cpu_baseline(host_edges, B, steps, threads):
     c.load(S)
     t_load = time.perf_counter() - t0
     lat = []
+    n = ins_seq.size
     for i in range(steps):
-        b = (ins_seq if i % 2 == 0 else del_seq)[(i // 2) * B:(i // 2 + 1) * B]
+        seq = ins_seq if i % 2 == 0 else del_seq
+        a = ((i // 2) * B) % n  # cyclic, as the device stream
+        b = seq[a:a + B] if a + B <= n else np.concatenate([seq[a:], seq[:a + B - n]])
         t0 = time.perf_counter()
         (c.insert if i % 2 == 0 else c.delete)(b)
         lat.append(time.perf_counter() - t0)
