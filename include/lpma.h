@@ -5,8 +5,11 @@
  * entry point takes plain pointers and sizes, returns an lpma_status_t and
  * never prints.  Device pointers are borrowed for the duration of the call
  * and read only.  Calls on one handle are ordered on the stream passed in;
- * different handles are independent.  Every call that returns a count or a
- * host buffer synchronises with its stream before returning.
+ * different handles are independent.  (An update also runs part of its work
+ * on a stream of the handle's own, forked from and joined back into the
+ * caller's stream, so later work on that stream still follows all of it.)
+ * Every call that returns a count or a host buffer synchronises with its
+ * stream before returning.
  *
  * Key layout (reference rpma.cuh:43-50): a 64-bit key is
  *     src << 42 | dst << 20 | t
