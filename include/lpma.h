@@ -93,7 +93,10 @@ typedef struct {
     uint64_t d2h_bytes;        /* device->host bytes the call copied (status blocks) */
     uint32_t sort_passes;      /* digit passes the batch sort ran: one per byte that varies over the batch,
                                   or, for the cooperative sort, one per 9-bit digit window */
-    uint32_t reserved1;
+    uint32_t levelup;          /* update_rpma's return value (rpma.cuh:1646-1653, 1662-1668): 1 when updates
+                                  reached the root level, i.e. the root window absorbed them (root_executed,
+                                  whether or not a level was added) or they overflowed it (overflow, whatever
+                                  the new height, a lower one after a rebuild included) */
 } LpmaStats;
 
 /* defaults that reproduce the reference: 32 / 0.42 / 1.0 / skip rule on */
@@ -275,6 +278,15 @@ typedef struct {
     uint32_t reserved;
     float us[6];
 } LpmaTuneEntry;
+/* Test setting of the cooperative batch sort's grid barrier on the current
+ * device, for tests of its give-up path: every barrier wait of that sort
+ * polls at most poll_limit times (0 restores the built-in limit of 2^22)
+ * and, with unreachable set, waits for an arrival count that never comes,
+ * so every wait gives up.  A sort whose wait gave up leaves the structure
+ * unchanged and its update returns LPMA_ERR_TIMEOUT; the handle stays
+ * usable.  Synchronous; no update may be in flight on the device. */
+LPMA_API lpma_status_t lpma_debug_sort_barrier(uint32_t poll_limit, int unreachable);
+
 LPMA_API lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEntry *out, size_t cap,
                                      size_t *n_out);
 LPMA_API lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier);

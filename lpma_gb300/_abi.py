@@ -28,7 +28,7 @@ EXPORTS = [
     "lpma_read_edgelist", "lpma_read_queries", "lpma_memory_bytes", "lpma_pool_create", "lpma_pool_submit",
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
-    "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve",
+    "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve", "lpma_debug_sort_barrier",
 ]
 SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
@@ -53,7 +53,7 @@ class LpmaStats(ctypes.Structure):
                 ("slots_rewritten", ctypes.c_uint64), ("slots_small", ctypes.c_uint64),
                 ("num_items", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("sort_passes", ctypes.c_uint32), ("reserved1", ctypes.c_uint32)]
+                ("sort_passes", ctypes.c_uint32), ("levelup", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -143,6 +143,7 @@ def load():
         "lpma_autotune": [U32, P, P, SZ, P],
         "lpma_tune_set": [U32, U32, U32],
         "lpma_tune_get": [U32, U32, P],
+        "lpma_debug_sort_barrier": [U32, I],
     }
     for name, args in sig.items():
         f = getattr(L, name)

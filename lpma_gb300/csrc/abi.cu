@@ -115,6 +115,10 @@ struct LpmaHandle {
     cudaStream_t cap_stream = nullptr;  // private stream for graph capture
     cudaEvent_t front_ev = nullptr;     // recorded after the front's status read-back
     cudaEvent_t front_ev_blk = nullptr; // the same, waited on without spinning (concurrent handles)
+    // recorded after the last work of each call that returns with work in
+    // flight, on the call's stream: lpma_destroy waits for it, not the device
+    cudaEvent_t done_ev = nullptr;
+    bool done_recorded = false;
     // the front's 4- and 32-segment executors run on side_stream, beside the
     // single-segment one: fork after the status read-back, join after them
     cudaStream_t side_stream = nullptr;
@@ -173,18 +177,62 @@ bool poison_this(const char *name) {
     return !only || !only[0] || strstr(name, only) != nullptr;
 }
 
+cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s);
+
+// Device buffers of handles and batchers come from the stream-ordered pool
+// (allocated on the calling thread's default stream, which is synchronised
+// before the buffer is used, so any stream may use it).  A buffer replaced
+// in mid-life is freed with dfree (cudaFree: it waits for the device, so no
+// kernel still reads it); a handle that is destroyed after waiting for its
+// own work frees its buffers with dfree_async, which does not wait for the
+// other handles' streams.
 template <typename T>
 cudaError_t dalloc_named(const char *name, T **p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
-    if (e == cudaSuccess && poison_this(name)) e = cudaMemset(*p, 0xA5, count * sizeof(T));
+    cudaError_t e = pool_alloc((void **)p, count * sizeof(T), cudaStreamPerThread);
+    if (e == cudaSuccess && poison_this(name)) e = cudaMemsetAsync(*p, 0xA5, count * sizeof(T), cudaStreamPerThread);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamPerThread);
     return e;
 }
 #define dalloc(p, n) dalloc_named(#p, p, n)
 template <typename T>
 void dfree(T *&p) {
     if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+template <typename T>
+void dfree_async(T *&p) {
+    if (p) cudaFreeAsync((void *)p, cudaStreamPerThread);
+    p = nullptr;
+}
+
+// Small page-locked host buffers (status mirrors, read-back words, the
+// batcher's tables) are kept on a free list when released instead of being
+// handed to cudaFreeHost, which waits for the whole device.
+std::mutex g_pinned_mu;
+std::vector<std::pair<size_t, void *>> g_pinned_free;
+
+template <typename T>
+cudaError_t pinned_alloc(T **p, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        for (size_t i = 0; i < g_pinned_free.size(); i++)
+            if (g_pinned_free[i].first == bytes) {
+                *p = (T *)g_pinned_free[i].second;
+                g_pinned_free[i] = g_pinned_free.back();
+                g_pinned_free.pop_back();
+                return cudaSuccess;
+            }
+    }
+    return cudaMallocHost((void **)p, bytes);
+}
+template <typename T>
+void pinned_release(T *&p, size_t bytes) {
+    if (p) {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        g_pinned_free.emplace_back(bytes, (void *)p);
+    }
     p = nullptr;
 }
 
@@ -700,6 +748,11 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     return LPMA_OK;
 }
 
+// The handle's last work is on stream s: lpma_destroy waits for this event.
+void mark_done(LpmaHandle *h, cudaStream_t s) {
+    if (h->done_ev && cudaEventRecord(h->done_ev, s) == cudaSuccess) h->done_recorded = true;
+}
+
 lpma_status_t wait_front(LpmaHandle *h, cudaStream_t) {
     CK(blocking_waits(h) ? event_wait(h->front_ev_blk) : cudaEventSynchronize(h->front_ev));
     CK(cudaGetLastError());
@@ -751,6 +804,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
         r = exec_plan(h, h->u, (uint32_t)n, thres, thres_active, s, &st, small_done);
         if (r == LPMA_OK && root) {
             st.root_executed = 1;
+            st.levelup = 1;  // update_rpma returns true once the root absorbed (rpma.cuh:1646-1653)
             if (min_height((uint64_t)live_after) + 1 > h->H) {  // eager level-up
                 r = level_up(h, s);
                 st.eager_levelup = 1;
@@ -758,6 +812,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
         }
     } else if (n_u > 0) {
         st.overflow = 1;
+        st.levelup = 1;  // and after any overflow, whatever the new height (rpma.cuh:1662-1668)
         const uint32_t hh = min_height((uint64_t)live_after);
         if (hh == h->H + 1) {
             st.levelup_path = 1;
@@ -819,6 +874,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
     st.h2d_bytes = h->h2d;
     st.d2h_bytes = h->d2h;
     if (out) *out = st;
+    mark_done(h, s);
     return LPMA_OK;
 }
 
@@ -969,11 +1025,22 @@ namespace {
 // maximal windows, then the sort's tile launch and merge rounds
 constexpr int FOREST_TABLES = 6 + (int)FOREST_MERGE_ROUNDS_MAX;
 
-void batcher_free(LpmaBatcher *b) {
-    dfree(b->dF), dfree(b->dB), dfree(b->dJ), dfree(b->dS), dfree(b->dE), dfree(b->dX);
-    for (void *p : {(void *)b->hF, (void *)b->hB, (void *)b->hJ, (void *)b->hS, (void *)b->hE, (void *)b->hX})
-        if (p) cudaFreeHost(p);
-    b->hF = nullptr, b->hB = nullptr, b->hJ = nullptr, b->hS = nullptr, b->hE = nullptr, b->hX = nullptr;
+// final: the batcher's work is known to be done, so the device buffers go
+// back to the pool without a device-wide synchronisation
+void batcher_free(LpmaBatcher *b, bool final = false) {
+    if (final) {
+        dfree_async(b->dF), dfree_async(b->dB), dfree_async(b->dJ), dfree_async(b->dS), dfree_async(b->dE),
+            dfree_async(b->dX);
+    } else {
+        dfree(b->dF), dfree(b->dB), dfree(b->dJ), dfree(b->dS), dfree(b->dE), dfree(b->dX);
+    }
+    const size_t c = b->cap_g;
+    pinned_release(b->hF, c * sizeof(ForestGraph));
+    pinned_release(b->hB, FOREST_TABLES * (c + 1) * sizeof(uint32_t));
+    pinned_release(b->hJ, c * sizeof(ForestSortJob));
+    pinned_release(b->hS, c * sizeof(DevStatus));
+    pinned_release(b->hE, c * sizeof(ForestExec));
+    pinned_release(b->hX, 3 * (c + 1) * sizeof(uint32_t));
     b->cap_g = 0;
 }
 
@@ -985,14 +1052,14 @@ lpma_status_t batcher_reserve(LpmaBatcher *b, size_t G) {
     CK(dalloc(&b->dB, FOREST_TABLES * (c + 1)));
     CK(dalloc(&b->dJ, c));
     CK(dalloc(&b->dS, c));
-    CK(cudaMallocHost(&b->hF, c * sizeof(ForestGraph)));
-    CK(cudaMallocHost(&b->hB, FOREST_TABLES * (c + 1) * sizeof(uint32_t)));
-    CK(cudaMallocHost(&b->hJ, c * sizeof(ForestSortJob)));
-    CK(cudaMallocHost(&b->hS, c * sizeof(DevStatus)));
+    CK(pinned_alloc(&b->hF, c * sizeof(ForestGraph)));
+    CK(pinned_alloc(&b->hB, FOREST_TABLES * (c + 1) * sizeof(uint32_t)));
+    CK(pinned_alloc(&b->hJ, c * sizeof(ForestSortJob)));
+    CK(pinned_alloc(&b->hS, c * sizeof(DevStatus)));
     CK(dalloc(&b->dE, c));
     CK(dalloc(&b->dX, 3 * (c + 1)));
-    CK(cudaMallocHost(&b->hE, c * sizeof(ForestExec)));
-    CK(cudaMallocHost(&b->hX, 3 * (c + 1) * sizeof(uint32_t)));
+    CK(pinned_alloc(&b->hE, c * sizeof(ForestExec)));
+    CK(pinned_alloc(&b->hX, 3 * (c + 1) * sizeof(uint32_t)));
     b->cap_g = c;
     return LPMA_OK;
 }
@@ -1014,7 +1081,13 @@ lpma_status_t lpma_config_default(LpmaConfig *cfg) {
 
 lpma_status_t lpma_destroy(LpmaHandle *h) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
-    cudaDeviceSynchronize();
+    // wait for this handle's own work only: its last call's stream (the
+    // event recorded after that call's last launch) and its private streams;
+    // then every buffer goes back to the stream-ordered pool without a
+    // device-wide synchronisation, so other handles' streams keep running
+    if (h->done_recorded) cudaEventSynchronize(h->done_ev);
+    for (cudaStream_t st : {h->side_stream, h->cap_stream, h->copy_stream})
+        if (st) cudaStreamSynchronize(st);
     for (FrontGraph &f : h->graphs) {
         cudaGraphExecDestroy(f.exec);
         cudaGraphDestroy(f.graph);
@@ -1026,24 +1099,27 @@ lpma_status_t lpma_destroy(LpmaHandle *h) {
     if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->front_ev) cudaEventDestroy(h->front_ev);
     if (h->front_ev_blk) cudaEventDestroy(h->front_ev_blk);
-    free_cap(h->c, nullptr, true);
-    dfree(h->sent), dfree(h->dst);
-    if (h->hst) cudaFreeHost(h->hst);
-    if (h->hinit) cudaFreeHost(h->hinit);
-    if (h->arena) cudaFree(h->arena);  // the batch scratch (synchronises)
+    free_cap(h->c, cudaStreamPerThread);
+    dfree_async(h->sent), dfree_async(h->dst);
+    pinned_release(h->hst, sizeof(DevStatus));
+    pinned_release(h->hinit, sizeof(DevStatus));
+    if (h->arena) cudaFreeAsync(h->arena, cudaStreamPerThread);  // the batch scratch
     h->arena = nullptr;
-    dfree(h->sort.hist), dfree(h->sort.counters);
-    dfree(h->jobs_d);
+    dfree_async(h->sort.hist), dfree_async(h->sort.counters), dfree_async(h->sort_err);
+    dfree_async(h->jobs_d);
     for (int b = 0; b < 2; b++) {
-        dfree(h->stage_ins[b]), dfree(h->stage_del[b]), dfree(h->stage_vals[b]);
+        dfree_async(h->stage_ins[b]), dfree_async(h->stage_del[b]), dfree_async(h->stage_vals[b]);
         if (h->stage_free[b]) cudaEventDestroy(h->stage_free[b]);
     }
     if (h->copy_done) cudaEventDestroy(h->copy_done);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
-    dfree(h->row_offset), dfree(h->col_index), dfree(h->view_vals), dfree(h->exp_keys), dfree(h->exp_vals);
-    dfree(h->q_cnt), dfree(h->q_tmp), dfree(h->bfs_a), dfree(h->bfs_b), dfree(h->bfs_cnt);
-    dfree(h->pr_deg), dfree(h->pr_contrib), dfree(h->pr_acc), dfree(h->pr_dangling);
-    if (h->pin_word) cudaFreeHost(h->pin_word);
+    dfree_async(h->row_offset), dfree_async(h->col_index), dfree_async(h->view_vals), dfree_async(h->exp_keys),
+        dfree_async(h->exp_vals);
+    dfree_async(h->q_cnt), dfree_async(h->q_tmp), dfree_async(h->bfs_a), dfree_async(h->bfs_b),
+        dfree_async(h->bfs_cnt);
+    dfree_async(h->pr_deg), dfree_async(h->pr_contrib), dfree_async(h->pr_acc), dfree_async(h->pr_dangling);
+    if (h->done_ev) cudaEventDestroy(h->done_ev);
+    pinned_release(h->pin_word, 2 * sizeof(uint32_t));
     delete h;
     return LPMA_OK;
 }
@@ -1068,8 +1144,8 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         lpma_destroy(h);
         return r;
     };
-    if (cudaMalloc(&h->dst, sizeof(DevStatus)) || cudaMallocHost(&h->hst, sizeof(DevStatus)) ||
-        cudaMallocHost(&h->hinit, sizeof(DevStatus)) || dalloc(&h->sent, num_vertices) ||
+    if (dalloc(&h->dst, 1) || pinned_alloc(&h->hst, sizeof(DevStatus)) ||
+        pinned_alloc(&h->hinit, sizeof(DevStatus)) || dalloc(&h->sent, num_vertices) ||
         dalloc(&h->sort.hist, 8 * 256) || dalloc(&h->sort.counters, 16) || dalloc(&h->sort_err, 1))
         return fail(LPMA_ERR_OUT_OF_MEMORY);
     // batches up to coop_sort_max_keys() sort in one cooperative launch,
@@ -1089,7 +1165,8 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) ||
         cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) ||
         cudaEventCreateWithFlags(&h->front_ev, cudaEventDisableTiming) ||
-        cudaEventCreateWithFlags(&h->front_ev_blk, cudaEventDisableTiming | cudaEventBlockingSync) || sort_prepare())
+        cudaEventCreateWithFlags(&h->front_ev_blk, cudaEventDisableTiming | cudaEventBlockingSync) ||
+        cudaEventCreateWithFlags(&h->done_ev, cudaEventDisableTiming) || sort_prepare())
         return fail(LPMA_ERR_CUDA);
     if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), s) || cudaMemsetAsync(h->c.keys, 0xFF, 32 * 8, s) ||
         cudaMemsetAsync(h->c.vals, 0, 32, s) ||
@@ -1102,8 +1179,8 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
     launch_sentinels(num_vertices, sk, sv, s);
     lpma_status_t r = do_update(h, sk, sv, num_vertices, nullptr, 0, 0, s, nullptr, true);
     cudaStreamSynchronize(s);
-    cudaFree(sk);
-    cudaFree(sv);
+    dfree_async(sk);
+    dfree_async(sv);
     if (r != LPMA_OK) return fail(r);
     h->min_t = 0xFFFFF;
     *out = h;
@@ -1203,6 +1280,7 @@ lpma_status_t lpma_csr_view(LpmaHandle *h, const uint32_t **row_offset, const ui
     if (!h->view_valid) {
         CKS(fill_view(h, s, true, false));
         h->view_valid = true;
+        mark_done(h, s);
     }
     *row_offset = h->row_offset;
     *col_index = h->col_index;
@@ -1285,7 +1363,7 @@ lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const 
     if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!h->pin_word) CK(cudaMallocHost(&h->pin_word, 2 * sizeof(uint32_t)));
+    if (!h->pin_word) CK(pinned_alloc(&h->pin_word, 2 * sizeof(uint32_t)));
     if (n > h->q_cap) {
         dfree(h->q_cnt), dfree(h->q_tmp);
         h->q_cap = 0;
@@ -1308,6 +1386,7 @@ lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const 
     if (*total > cap) return LPMA_ERR_BUFFER_TOO_SMALL;
     launch_nbr_fill(d_srcs, d_windows, (uint32_t)n, g, h->c.cnt, h->sent, h->V, d_offsets, d_nbrs, d_vals, s);
     CK(cudaGetLastError());
+    mark_done(h, s);
     return LPMA_OK;
 }
 
@@ -1319,6 +1398,7 @@ lpma_status_t lpma_edge_query(LpmaHandle *h, const uint64_t *d_keys, size_t n, u
     launch_edge_query(d_keys, (uint32_t)n, window, Geo{h->c.keys, h->c.vals, h->H}, h->c.cnt, h->c.fl, h->sent, h->V,
                       d_counts, (cudaStream_t)stream);
     CK(cudaGetLastError());
+    mark_done(h, (cudaStream_t)stream);
     return LPMA_OK;
 }
 
@@ -1327,7 +1407,7 @@ lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_source
     if (!h || !d_dist || (n_sources && !d_sources) || n_sources >= (1u << 31)) return LPMA_ERR_INVALID_ARGUMENT;
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!h->pin_word) CK(cudaMallocHost(&h->pin_word, 2 * sizeof(uint32_t)));
+    if (!h->pin_word) CK(pinned_alloc(&h->pin_word, 2 * sizeof(uint32_t)));
     if (!h->bfs_a) {
         CK(dalloc(&h->bfs_a, h->V));
         CK(dalloc(&h->bfs_b, h->V));
@@ -1375,6 +1455,7 @@ lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, do
     for (uint32_t it = 0; it < iterations; it++)
         launch_pr_iteration(g, h->c.cnt, h->pr_deg, h->V, alpha, d_rank, h->pr_contrib, h->pr_acc, h->pr_dangling, s);
     CK(cudaGetLastError());
+    mark_done(h, s);
     return LPMA_OK;
 }
 
@@ -1431,9 +1512,15 @@ lpma_status_t lpma_batcher_create(LpmaBatcher **out) {
 
 lpma_status_t lpma_batcher_destroy(LpmaBatcher *b) {
     if (!b) return LPMA_ERR_INVALID_ARGUMENT;
-    cudaDeviceSynchronize();
+    // wait for the batcher's own work: the shared executors of its last call
+    // (the done event), its side stream and its worker threads' streams
+    if (b->pending && b->done) cudaEventSynchronize(b->done);
+    if (b->side) cudaStreamSynchronize(b->side);
+    if (b->workers)
+        for (cudaStream_t x : b->workers->st)
+            if (x) cudaStreamSynchronize(x);
     delete b->workers;
-    batcher_free(b);
+    batcher_free(b, true);
     if (b->done) cudaEventDestroy(b->done);
     if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->join_ev) cudaEventDestroy(b->join_ev);
@@ -1728,6 +1815,11 @@ lpma_status_t lpma_gen_rmat(uint64_t seed, uint32_t scale, uint32_t edge_factor,
     dfree(tmp), dfree(p0), dfree(p1), dfree(flags), dfree(pos), dfree(total), dfree(stmp), dfree(err);
     dfree(ss.status), dfree(ss.hist), dfree(ss.counters);
     return r;
+}
+
+lpma_status_t lpma_debug_sort_barrier(uint32_t poll_limit, int unreachable) {
+    CK(set_barrier_debug(poll_limit, unreachable ? 1u : 0u));
+    return LPMA_OK;
 }
 
 lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier) {

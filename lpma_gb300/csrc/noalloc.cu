@@ -12,6 +12,7 @@
 
 #include "kernels.cuh"
 #include "lpma.h"
+#include "per_device.h"
 #include "prims.cuh"
 
 using namespace lpma;
@@ -40,9 +41,7 @@ static_assert(USED_BYTES <= (size_t)LPMA_SHUFFLE_STATIC_SCRATCH_BYTES, "scratch 
 // The scratch: one array per device, shared by every call in the process.
 static __device__ __align__(256) unsigned char g_shuffle_scratch[LPMA_SHUFFLE_STATIC_SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_setup_mu;
-unsigned char *g_scratch_ptr[MAX_DEVICES];  // device address of the array, per device
+PerDevice<unsigned char *> g_scratch_ptr;  // device address of the array, per device
 
 // One-time set-up for the current device: the array's device address (the
 // host must pass this address to kernels, not the symbol) and the sort
@@ -50,16 +49,17 @@ unsigned char *g_scratch_ptr[MAX_DEVICES];  // device address of the array, per 
 lpma_status_t scratch_for_current_device(unsigned char **out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return LPMA_ERR_CUDA;
-    if (dev < 0 || dev >= MAX_DEVICES) return LPMA_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        unsigned char *ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_shuffle_scratch);
-        if (e != cudaSuccess || ptr == nullptr) return LPMA_ERR_CUDA;
-        if (sort_prepare() != cudaSuccess) return LPMA_ERR_CUDA;
-        g_scratch_ptr[dev] = ptr;
-    }
-    *out = g_scratch_ptr[dev];
+    unsigned char *const *p = nullptr;
+    const int r = g_scratch_ptr.get(
+        dev,
+        [](int, unsigned char *&ptr) -> int {
+            const cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_shuffle_scratch);
+            if (e != cudaSuccess || ptr == nullptr) return (int)LPMA_ERR_CUDA;
+            return sort_prepare() != cudaSuccess ? (int)LPMA_ERR_CUDA : 0;
+        },
+        &p, (int)LPMA_ERR_INVALID_ARGUMENT);
+    if (r) return (lpma_status_t)r;
+    *out = *p;
     return LPMA_OK;
 }
 
@@ -68,8 +68,9 @@ lpma_status_t scratch_for_current_device(unsigned char **out) {
 extern "C" {
 
 lpma_status_t lpma_shuffle_static(uint64_t seed, uint64_t *d_keys, size_t n, lpma_stream_t stream) {
-    if (n > MAXN) return LPMA_ERR_SCRATCH_LIMIT;
+    // a null pointer is reported before the size, whatever the size
     if (!d_keys && n) return LPMA_ERR_INVALID_ARGUMENT;
+    if (n > MAXN) return LPMA_ERR_SCRATCH_LIMIT;
     unsigned char *base = nullptr;
     const lpma_status_t r = scratch_for_current_device(&base);
     if (r != LPMA_OK) return r;

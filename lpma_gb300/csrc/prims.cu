@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "lpma_common.cuh"
+#include "per_device.h"
 #include "prims.cuh"
 
 namespace lpma {
@@ -383,6 +384,14 @@ __global__ void __launch_bounds__(SORT_TPB) k_downsweep(uint64_t *k0, V *v0, uin
 
 constexpr uint32_t BAR_SPIN_LIMIT = 1u << 22;
 
+// Test setting of the grid barrier (lpma_debug_sort_barrier): a poll limit
+// in place of BAR_SPIN_LIMIT (0: the default) and, when unreachable is set,
+// a target that no arrival count reaches, so that every wait runs out and
+// takes the give-up path.  Read by the waiting thread at run time, so
+// captured update fronts follow it too.
+__device__ uint32_t g_bar_poll_limit = 0;
+__device__ uint32_t g_bar_unreachable = 0;
+
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -400,9 +409,11 @@ __device__ __forceinline__ void grid_arrive(uint32_t *bar) {
 
 __device__ __forceinline__ void grid_wait(uint32_t *bar, uint32_t target, uint32_t *err) {
     if (threadIdx.x == 0) {
+        const uint32_t lim = g_bar_poll_limit ? g_bar_poll_limit : BAR_SPIN_LIMIT;
+        if (g_bar_unreachable) target = 0xFFFFFFFFu;
         uint32_t it = 0;
         while (ld_acquire_gpu(bar) < target) {
-            if (++it > BAR_SPIN_LIMIT) {
+            if (++it > lim) {
                 if (err) atomicOr(err, ERR_TIMEOUT);
                 break;
             }
@@ -1064,9 +1075,21 @@ cudaError_t scan_u8_to_u32(const uint8_t *in, uint32_t *out, uint32_t n, uint32_
     return scan_impl<uint8_t>(in, out, n, total, tmp, st);
 }
 
-// resident CTAs of k_coop_sort<u16/u32/u64, 8-bit digits> and of
-// k_coop_sort<u16, 9-bit digits>, set by sort_prepare
-uint32_t g_coop_max_ctas[4];
+// Per device: resident CTAs of k_coop_sort<u16/u32/u64, 8-bit digits> and
+// of k_coop_sort<u16, 9-bit digits>, measured by sort_prepare with the
+// device current (the shared-memory opt-ins it sets are per device too).
+struct CoopCtas {
+    uint32_t n[4];
+};
+PerDevice<CoopCtas> g_sort_setup;
+
+// the current device's figure for one slot; 0 before sort_prepare ran on it
+static uint32_t coop_max_ctas(int slot) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    const CoopCtas *c = g_sort_setup.peek(dev);
+    return c ? c->n[slot] : 0u;
+}
 
 template <typename V>
 constexpr int coop_slot(bool wide) {
@@ -1080,7 +1103,7 @@ template <typename V>
 static bool coop_geometry(uint32_t n, const SortScratch &s, uint32_t *tile_len_out, uint32_t *G_out,
                           bool wide = false) {
     if (wide && sizeof(V) != 2) return false;
-    const uint32_t mc = g_coop_max_ctas[coop_slot<V>(wide)];
+    const uint32_t mc = coop_max_ctas(coop_slot<V>(wide));
     const uint32_t maxG = mc < 512u ? mc : 512u;
     const uint32_t tile_len = maxG ? std::max<uint32_t>(COOP_MIN_TILE, (n + maxG - 1) / maxG) : 0u;
     const uint32_t G = tile_len ? (n + tile_len - 1) / tile_len : 0u;
@@ -1251,17 +1274,16 @@ cudaError_t forest_sort(const ForestSortJob *d_jobs, uint32_t G, const uint32_t 
 }
 
 uint32_t coop_sort_max_keys() {
-    const uint32_t g = g_coop_max_ctas[0] < 512u ? g_coop_max_ctas[0] : 512u;
+    const uint32_t mc = coop_max_ctas(0);
+    const uint32_t g = mc < 512u ? mc : 512u;
     return g * (uint32_t)COOP_TILE;
 }
 
-// Shared-memory opt-ins of the sort kernels, set once outside any stream
-// capture.
-cudaError_t sort_prepare() {
-    static std::mutex mu;
-    static bool done = false;
-    std::lock_guard<std::mutex> lk(mu);
-    if (done) return cudaSuccess;
+// Shared-memory opt-ins of the sort kernels and the cooperative sort's
+// occupancy, set once per device (with that device current) outside any
+// stream capture.  cudaFuncSetAttribute applies to the current device only,
+// so a process that uses several devices runs this on each.
+static cudaError_t sort_setup_device(int dev, CoopCtas &out) {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_small_sort<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(SmallSmem<uint16_t>))))
@@ -1283,9 +1305,8 @@ cudaError_t sort_prepare() {
                                   (int)sizeof(BlockSortSmem))))
         return e;
     {
-        int dev = 0, sms = 0, per[4] = {0, 0, 0, 0};
-        if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
-            return e;
+        int sms = 0, per[4] = {0, 0, 0, 0};
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
         if ((e = cudaFuncSetAttribute(k_coop_sort<uint16_t, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(CoopSmem<uint16_t, 256>))) ||
             (e = cudaFuncSetAttribute(k_coop_sort<uint32_t, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1304,10 +1325,23 @@ cudaError_t sort_prepare() {
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], k_coop_sort<uint16_t, WIDE_DIGIT_BITS>,
                                                                SORT_TPB, sizeof(CoopSmem<uint16_t, 512>))))
             return e;
-        for (int i = 0; i < 4; i++) g_coop_max_ctas[i] = (uint32_t)(per[i] * sms);
+        for (int i = 0; i < 4; i++) out.n[i] = (uint32_t)(per[i] * sms);
     }
-    done = true;
     return cudaSuccess;
+}
+
+cudaError_t set_barrier_debug(uint32_t poll_limit, uint32_t unreachable) {
+    cudaError_t e = cudaMemcpyToSymbol(g_bar_poll_limit, &poll_limit, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_bar_unreachable, &unreachable, sizeof(uint32_t));
+    return e;
+}
+
+cudaError_t sort_prepare() {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    return (cudaError_t)g_sort_setup.get(
+        dev, [](int d, CoopCtas &v) { return (int)sort_setup_device(d, v); }, nullptr, (int)cudaErrorInvalidDevice);
 }
 
 template <typename V>

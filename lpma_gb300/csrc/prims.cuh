@@ -160,6 +160,10 @@ constexpr size_t sort_status_words_wide(uint32_t n) {
 // One-time kernel attribute setup (outside stream capture).
 cudaError_t sort_prepare();
 
+// Test setting of the cooperative sort's grid barrier on the current device
+// (poll_limit 0: the default limit; unreachable: every wait gives up).
+cudaError_t set_barrier_debug(uint32_t poll_limit, uint32_t unreachable);
+
 // Tile-merge sort of 16-bit-payload pairs: batches of TM_TILE_MAX + 1 ..
 // TM_MAX pairs on their own, and the batch of each graph of a batched
 // update (lpma_update_batch, any size up to FOREST_SORT_MAX).  The batch is

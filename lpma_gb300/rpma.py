@@ -252,7 +252,9 @@ def init_csr_rpma(row_num, config=None, stream=None):
 
 
 def update_rpma(rpma, keys, values=None, thres=0, del_keys=None):
-    return rpma.update(ins=keys, ins_vals=values, dels=del_keys, thres=thres)
+    """update_rpma (rpma.cuh:1549-1718): returns the reference's bool, true
+    when the updates reached the root level (absorbed there or overflowed)."""
+    return bool(rpma.update(ins=keys, ins_vals=values, dels=del_keys, thres=thres)["levelup"])
 
 
 def to_csr_rpma(rpma):

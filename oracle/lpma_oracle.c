@@ -350,6 +350,7 @@ static void run_level_loop(OPma *p, Pending *P, uint32_t thres, int use_skip, in
         P->n = o;
         /* eager level-up when the root absorbed everything, rpma.cuh:1646-1653 */
         if (eager && level == H + 1 && P->n == 0) {
+            if (st) st->levelup = 1;
             uint64_t c = count_live(p, thres);
             uint32_t h = min_height(c) + 1;
             if (h > p->H) {
@@ -542,6 +543,7 @@ static int update_impl(OPma *p, const uint64_t *ins, const uint8_t *ins_vals, si
     if (P.n > 0) {
         /* overflow, rpma.cuh:1662-1712 */
         st->overflow = 1;
+        st->levelup = 1;
         uint64_t c = count_live(p, thres);
         for (size_t q = 0; q < P.n; q++) c += (P.u[q].kind == K_INS);
         uint32_t h = min_height(c);

@@ -39,6 +39,8 @@ typedef struct {
     uint32_t rebuilt;           /* full rebuild happened (resize to new height) */
     uint32_t levelup_path;      /* overflow handled by adding one level + second loop */
     uint32_t fill_empty;        /* fill_empty_segs redistributed the array */
+    uint32_t levelup;           /* update_rpma's return value: the level H+1 loop step absorbed the
+                                   remaining updates (rpma.cuh:1646-1653) or updates overflowed (:1662-1668) */
     uint64_t win_count[32];     /* executed windows per level (reference order) */
     uint64_t win_slots[32];     /* slots covered by executed windows per level */
 } OPmaStats;

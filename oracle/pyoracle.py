@@ -40,11 +40,12 @@ class OPmaStats(ctypes.Structure):
         ("root_executed", ctypes.c_uint32), ("eager_levelup", ctypes.c_uint32),
         ("overflow", ctypes.c_uint32), ("rebuilt", ctypes.c_uint32),
         ("levelup_path", ctypes.c_uint32), ("fill_empty", ctypes.c_uint32),
+        ("levelup", ctypes.c_uint32),
         ("win_count", ctypes.c_uint64 * 32), ("win_slots", ctypes.c_uint64 * 32),
     ]
 
     def as_dict(self):
-        d = {f: getattr(self, f) for f, _ in self._fields_[:12]}
+        d = {f: getattr(self, f) for f, _ in self._fields_[:13]}
         d["win_count"] = list(self.win_count)
         d["win_slots"] = list(self.win_slots)
         return d

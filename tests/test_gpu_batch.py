@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 # every stat but sort_passes, which counts the passes of the sort that ran
 # (the shared tile-merge sort here, possibly the cooperative one for the twin)
 STAT_KEYS = ("height_before", "height_after", "n_ins_applied", "n_upserts", "n_del_applied", "n_noop",
-             "root_executed", "eager_levelup", "overflow", "rebuilt", "levelup_path", "fill_empty",
+             "root_executed", "eager_levelup", "overflow", "rebuilt", "levelup_path", "fill_empty", "levelup",
              "windows_single", "windows_small", "windows_big", "slots_rewritten", "slots_small", "num_items")
 
 

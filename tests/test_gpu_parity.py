@@ -124,12 +124,20 @@ def test_bulk_then_heavy_deletes_halving(engine, oracle):
     g.update(ins=_dev(e))
     o.update(ins=e)
     heights = [o.height]
+    lowered = 0
     for i in range(0, int(e.size * 0.95), 4096):
-        g.update(dels=_dev(e[i:i + 4096]))
-        o.update(dels=e[i:i + 4096])
+        sg = g.update(dels=_dev(e[i:i + 4096]))
+        so = o.update(dels=e[i:i + 4096])
         assert_same(g, o, "del %d" % i)
+        # update_rpma's return value: true after any overflow, also when the
+        # rebuild it triggers lowers the height
+        for key in ("levelup", "overflow", "rebuilt", "root_executed"):
+            assert sg[key] == so[key], "del %d: %s %d vs %d" % (i, key, sg[key], so[key])
+        if sg["height_after"] < sg["height_before"]:
+            assert sg["rebuilt"] and sg["levelup"], sg
+            lowered += 1
         heights.append(o.height)
-    assert heights[-1] < heights[0]
+    assert heights[-1] < heights[0] and lowered > 0
     assert_csr(g, o)
 
 
@@ -258,13 +266,14 @@ def test_scale18_stream(engine, oracle, batch):
         o.update(dels=e[a:(a + b) // 2])
         assert_same(g, o, "del %d" % i)
         for s in (s1, s2):
+            assert s["levelup"] == int(bool(s["root_executed"] or s["overflow"])), s
             for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path", "fill_empty"):
                 if s[k]:
                     events.add(k)
     assert_csr(g, o)
 
 
-PATH_FLAGS = ("overflow", "levelup_path", "rebuilt", "eager_levelup", "root_executed", "fill_empty")
+PATH_FLAGS = ("overflow", "levelup_path", "rebuilt", "eager_levelup", "root_executed", "fill_empty", "levelup")
 
 
 @pytest.mark.parametrize("V,frac,dfrac,path", [

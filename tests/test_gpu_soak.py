@@ -17,7 +17,7 @@ from test_gpu_parity import _dev, _dev8, assert_csr, assert_same
 
 pytestmark = pytest.mark.gpu
 
-PATH_FLAGS = ("overflow", "levelup_path", "rebuilt", "eager_levelup", "root_executed", "fill_empty")
+PATH_FLAGS = ("overflow", "levelup_path", "rebuilt", "eager_levelup", "root_executed", "fill_empty", "levelup")
 
 
 def _live(o):

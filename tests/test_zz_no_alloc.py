@@ -64,3 +64,39 @@ def test_static_shuffle_trivial_sizes():
     _abi.check(L.lpma_shuffle_static(4, None, 0, None), "n=0")
     torch.cuda.synchronize()
     assert torch.equal(one, before)
+
+
+def test_static_shuffle_null_keys_rejected_before_size():
+    _abi, L = _lib()
+    for n in (5, _abi.SHUFFLE_STATIC_MAX_KEYS + 1):
+        st = L.lpma_shuffle_static(4, None, n, None)
+        assert _abi.STATUS_NAMES[st] == "LPMA_ERR_INVALID_ARGUMENT", (n, st)
+
+
+def test_static_shuffle_on_a_caller_stream_holds_device_memory_constant():
+    """Two back-to-back calls on the caller's own (non-default) stream, with
+    only that stream synchronised: both results equal lpma_shuffle's, and the
+    device's free memory is the same after the warm calls as before them (a
+    scratch buffer taken from cudaMalloc or a stream-ordered pool would leave
+    it lower)."""
+    import torch
+    _abi, L = _lib()
+    n = 50000
+    a, b = _keys(n, 11), _keys(n, 12)
+    wa, wb = a.clone(), b.clone()
+    _abi.check(L.lpma_shuffle(5, ctypes.c_void_p(wa.data_ptr()), n, None), "lpma_shuffle")
+    _abi.check(L.lpma_shuffle(6, ctypes.c_void_p(wb.data_ptr()), n, None), "lpma_shuffle")
+    torch.cuda.synchronize()
+    ga, gb = a.clone(), b.clone()
+    warm = a.clone()
+    _abi.check(L.lpma_shuffle_static(5, ctypes.c_void_p(warm.data_ptr()), n, None), "warm-up")
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    torch.cuda.synchronize()  # the inputs above are ready before the stream reads them
+    free_before = torch.cuda.mem_get_info()[0]
+    _abi.check(L.lpma_shuffle_static(5, ctypes.c_void_p(ga.data_ptr()), n, sp), "first")
+    _abi.check(L.lpma_shuffle_static(6, ctypes.c_void_p(gb.data_ptr()), n, sp), "second")
+    s.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert torch.equal(ga, wa) and torch.equal(gb, wb)
+    assert free_after == free_before, (free_before, free_after)
