@@ -21,9 +21,12 @@
  * compaction (gpma.cuh:228 predicate).  For insert-only batches with
  * distinct keys this is exactly the reference.
  *
- * Parity status: "parity unpinned" for the physical layout (the reference
- * does not build under CUDA 13).  Pinned by the reference's known-answer
- * checks held in tests/golden.
+ * Parity status: the steps that have a host-compilable counterpart in the
+ * reference (index macros, density, skip rule, resize height, locate,
+ * redistribution) are pinned to that code, compiled from the reference by
+ * oracle/ref_host.py; the whole-batch layout is "partially unpinned" (the
+ * reference's update loop does not build under CUDA 13) and is pinned by the
+ * reference's result checks and a second restatement (tests/golden).
  */
 #include "lpma_oracle.h"
 
@@ -728,6 +731,32 @@ void opma_shuffle(uint64_t seed, uint64_t *keys, uint64_t n) {
     radix_sort_u64(h, keys, n);
     free(h);
 }
+
+/* ------------------------------------------------------------------ */
+/* test hooks: single steps of the oracle, for the comparison with the   */
+/* reference's own functions compiled for the host (oracle/ref_host.py)  */
+/* ------------------------------------------------------------------ */
+int opma_locate_keys(const OPma *p, const uint64_t *keys, size_t n, uint32_t *out) {
+    for (size_t i = 0; i < n; i++) out[i] = (uint32_t)locate(p, keys[i]);
+    return 0;
+}
+
+int opma_redistribute_window(uint32_t H, uint32_t V, uint64_t node, uint64_t width, const uint64_t *mk,
+                             const uint8_t *mv, uint64_t m, uint64_t *keys, uint8_t *vals, uint32_t *sent) {
+    OPma t;
+    memset(&t, 0, sizeof(t));
+    t.H = H;
+    t.V = V;
+    t.keys = keys;
+    t.vals = vals;
+    t.sent = sent;
+    if (m > width || node + width > nslots_of(H) + 32) return -1;
+    redistribute(&t, mk, mv, m, node, width);
+    return 0;
+}
+
+/* resize_rpma's height for `count` items, plus one when the root absorbed */
+uint32_t opma_resize_height(uint64_t count, int reach_root) { return min_height(count) + (reach_root ? 1u : 0u); }
 
 /* ------------------------------------------------------------------ */
 /* CPU baseline: sorted-merge CSR rebuild per batch (test_cusparse.cu:51-78

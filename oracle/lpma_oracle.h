@@ -5,14 +5,18 @@
  * check and the CPU-baseline leg of bench.py load it to compute the expected
  * layout and results.  The product (lpma_gb300) never links or calls it.
  *
- * Parity status: the reference (pkumod/LPMA) cannot be compiled with CUDA 13
- * (device-side cudaDeviceSynchronize / CDP1 and the removed __shfl_down), so
- * no reference binary exists to pin this restatement against.  It is pinned
- * instead by the reference's own known-answer checks for this path
- * (sorted key set, per-row adjacency with the sentinel closing each row, the
- * index algebra, the density table and the redistribution formula), which
- * tests/golden holds as fixtures.  The physical-layout parity of the
- * restatement itself is "parity unpinned".
+ * Parity status: the reference (pkumod/LPMA) does not compile with CUDA 13
+ * as a whole (device-side cudaDeviceSynchronize / CDP1 and the removed
+ * __shfl_down).  Its integer functions on the update path do compile for
+ * the host (oracle/ref_host.py): the index macros, fls / lls, the density
+ * table, the skip state machine, the resize height rule, the locate descent
+ * and the even redistribution.  Each of these steps of this restatement is
+ * pinned to that compiled reference code, live (tests/test_oracle_reference.py)
+ * and through fixtures it generated (tests/golden).  The whole-batch control
+ * flow (level loop, window choice, merge, resize paths) is pinned only by the
+ * reference's own result checks (sorted key set, per-row adjacency closed by
+ * the sentinel) and by a second restatement in Python: for whole layouts the
+ * parity is "partially unpinned".
  */
 #ifndef LPMA_ORACLE_H
 #define LPMA_ORACLE_H
@@ -83,6 +87,18 @@ void opma_skip_table(uint32_t height, uint8_t *out, int n);
 /* segment count of one destination segment under even redistribution
  * (rpma.cuh:677-679): item i -> segment floor(f*i/m) */
 void opma_redistribute_counts(uint64_t f, uint64_t m, uint32_t *counts);
+
+/* ---- test hooks: single steps of the restatement, compared with the
+ * reference's own functions compiled for the host (oracle/ref_host.py) ----
+ * opma_locate_keys: the stop segment of each key (linear slot of its first
+ * lane), locate_leaf_kernel rpma.cuh:253-315.  opma_redistribute_window:
+ * m sorted items spread over [node, node + width) of a heap layout of
+ * height H, sentinel slots into sent (redispatch_kernel rpma.cuh:953-983).
+ * opma_resize_height: resize_rpma's height rule (rpma.cuh:1340-1352). */
+int opma_locate_keys(const OPma *p, const uint64_t *keys, size_t n, uint32_t *out);
+int opma_redistribute_window(uint32_t H, uint32_t V, uint64_t node, uint64_t width, const uint64_t *mk,
+                             const uint8_t *mv, uint64_t m, uint64_t *keys, uint8_t *vals, uint32_t *sent);
+uint32_t opma_resize_height(uint64_t count, int reach_root);
 
 /* ---- synthetic workload generators (identical integer arithmetic to the
  * device generator in lpma_gb300/csrc/gen.cu) ---- */

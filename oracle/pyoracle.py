@@ -4,9 +4,12 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
 and by the CPU-baseline leg of ``bench.py``.  The product package never
 imports this module.
 
-Parity status of the restatement: layout "parity unpinned" (the reference
-does not build under CUDA 13); pinned by the reference's known-answer checks
-held in tests/golden.
+Parity status of the restatement: its single steps (index macros, density,
+skip rule, resize height, locate, redistribution) are pinned to the
+reference's own code compiled for the host (oracle/ref_host.py); whole-batch
+layouts are "partially unpinned" (the reference's update loop does not build
+under CUDA 13), pinned by the reference's result checks and a second
+restatement (tests/golden).
 """
 import ctypes
 import os
@@ -77,6 +80,9 @@ def lib():
             "opma_density_table": (None, [P, P, I]),
             "opma_skip_table": (None, [U32, P, I]),
             "opma_redistribute_counts": (None, [U64, U64, P]),
+            "opma_locate_keys": (I, [P, P, SZ, P]),
+            "opma_redistribute_window": (I, [U32, U32, U64, U64, P, P, U64, P, P, P]),
+            "opma_resize_height": (U32, [U64, I]),
             "opma_mix64": (U64, [U64]),
             "opma_rmat_raw": (None, [U64, U32, U64, U32, U32, U32, P]),
             "opma_dedup": (U64, [P, U64]),
@@ -159,6 +165,13 @@ class OracleLpma:
         got = lib().opma_export_sorted(self.h, _ptr(k), _ptr(v), n)
         assert got == n
         return k, v
+
+    def locate(self, keys):
+        """Stop segment of each key (linear slot index of its first lane)."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        out = np.zeros(keys.size, np.uint32)
+        assert lib().opma_locate_keys(self.h, _ptr(keys), keys.size, _ptr(out)) == 0
+        return out
 
     def csr(self):
         n = self.num_items()
@@ -330,3 +343,13 @@ def pagerank(keys, V, alpha, iterations):
         acc = np.bincount(dst, weights=contrib[src], minlength=V)
         rank = (1 - alpha) / V + alpha * (acc + dangling / V)
     return rank
+
+
+def redistribute_window(H, V, node, width, items, item_vals, keys, vals, sent):
+    """The oracle's even redistribution of sorted items over one window of
+    a heap layout (keys / vals / sent are updated in place)."""
+    items = np.ascontiguousarray(items, dtype=np.uint64)
+    iv = np.ascontiguousarray(item_vals, dtype=np.uint8)
+    rc = lib().opma_redistribute_window(H, V, node, width, _ptr(items), _ptr(iv), items.size, _ptr(keys), _ptr(vals),
+                                        _ptr(sent))
+    assert rc == 0

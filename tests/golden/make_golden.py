@@ -1,19 +1,11 @@
-"""Generate the golden fixtures of tests/golden from the reference's own text.
+"""Generate the layout-stream fixture of tests/golden from a second restatement.
 
-Run from the repository root with the reference checked out at
-/root/reference (read only; only the index-algebra self-check reads it):
+Run from the repository root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--reference <reference checkout>]
 
 What it writes (JSON, committed):
 
-* index_algebra.json -- GET_IDX / GET_LANE / GET_LINEAR_IDX (rpma.cuh:98-134)
-  over every slot of trees of height 0..6, evaluated with the reference's
-  32-bit unsigned arithmetic.
-* tables.json -- the density table of recalculate_density (rpma.cuh:137-168,
-  lower = trunc(0.42 * 32 * 2^i), upper = 32 * 2^i), the skip state machine of
-  update_rpma (rpma.cuh:1609-1619) for heights 0..24, and the even
-  redistribution counts of rpma.cuh:677-679 for a grid of (segments, items).
 * small_streams.json -- layouts produced by a pure-Python restatement of the
   reference's insert path (init_csr_rpma + update_rpma, rpma.cuh:1301-1823),
   written slot for slot from the reference with its per-level arrays, for
@@ -21,9 +13,14 @@ What it writes (JSON, committed):
   a SHA-256 of the layout (keys and values of every slot, level arrays laid
   end to end) and, for the last snapshot of a stream, the full layout.
 
-The C oracle (oracle/lpma_oracle.c) must reproduce every value here; the
-restatement below is independent of it (different language, the reference's
-own per-level data structure and locate/rebalance code paths).
+The whole update loop of the reference does not compile here, so these
+layouts are "parity unpinned": they pin the C oracle (oracle/lpma_oracle.c)
+to a second, independent restatement (different language, the reference's
+own per-level data structure and locate/rebalance code paths).  The
+restatement's index macros, density table and skip rule are first checked
+against index_algebra.json and tables.json, which the reference's own code
+produced (tests/golden/make_ref_golden.py).  With --reference, the macro
+definitions are also looked up in the reference header.
 """
 import hashlib
 import json
@@ -393,9 +390,11 @@ def streams_fixture():
     return out
 
 
-def check_macros_against_reference_text():
+def check_macros_against_reference_text(reference_dir):
     """The restated macros are those of the reference header, verbatim in form."""
-    path = "/root/reference/rpma.cuh"
+    if not reference_dir:
+        return
+    path = os.path.join(reference_dir, "rpma.cuh")
     if not os.path.exists(path):
         return
     src = open(path).read()
@@ -403,30 +402,29 @@ def check_macros_against_reference_text():
         assert re.search(r"#define\s+%s\(" % name, src), name
 
 
-def main():
-    check_macros_against_reference_text()
-    alg = []
-    for H in range(0, 7):
-        n = 32 * ((2 << H) - 1)
-        rows = []
-        for L in range(n):
-            i = GET_IDX(L, H)
-            ln = GET_LANE(L, i, H)
-            rows.append([L, i, ln, GET_LINEAR_IDX(i, ln, H) + (ln % 32)])
-        alg.append({"height": H, "rows": rows})
-    with open(os.path.join(HERE, "index_algebra.json"), "w") as f:
-        json.dump(alg, f, separators=(",", ":"))
+def main(argv):
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=os.environ.get("LPMA_REFERENCE_DIR"),
+                    help="checkout of the reference, for the macro self-check (optional)")
+    args = ap.parse_args(argv)
+    check_macros_against_reference_text(args.reference)
+    # cross-check of this restatement against the fixtures that the
+    # reference's own code produced (tests/golden/make_ref_golden.py)
+    with open(os.path.join(HERE, "index_algebra.json")) as f:
+        for block in json.load(f)["blocks"]:
+            H = block["height"]
+            for lin, idx, lane, back in block["rows"]:
+                assert GET_IDX(lin, H) == idx and GET_LANE(lin, idx, H) == lane
+    with open(os.path.join(HERE, "tables.json")) as f:
+        t = json.load(f)
     lower, upper = density_tables(26)
-    tables = {"lower": lower, "upper": upper, "skip": {str(H): skip_table(H) for H in range(0, 25)},
-              "fls": {str(x): fls(x) for x in [0, 1, 2, 3, 31, 32, 33, 1023, 1024, 1025, 1 << 20]},
-              "redistribute": [{"f": f, "m": m, "counts": redistribute_counts(f, m)}
-                               for f in (1, 2, 3, 4, 7, 32, 63) for m in (1, 5, 13, 31, 32, 40, 100) if m <= 32 * f]}
-    with open(os.path.join(HERE, "tables.json"), "w") as f:
-        json.dump(tables, f, separators=(",", ":"))
+    assert lower == t["lower"] and upper == t["upper"]
+    assert all(skip_table(int(H)) == v for H, v in t["skip"].items())
     with open(os.path.join(HERE, "small_streams.json"), "w") as f:
         json.dump(streams_fixture(), f, separators=(",", ":"))
-    print("golden fixtures written to", HERE)
+    print("small_streams.json written to", HERE)
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv[1:]))
