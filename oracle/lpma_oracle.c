@@ -758,6 +758,430 @@ int opma_redistribute_window(uint32_t H, uint32_t V, uint64_t node, uint64_t wid
 /* resize_rpma's height for `count` items, plus one when the root absorbed */
 uint32_t opma_resize_height(uint64_t count, int reach_root) { return min_height(count) + (reach_root ? 1u : 0u); }
 
+/* ================================================================== */
+/* GPMA (gpma.cuh): one flat packed memory array                        */
+/* ================================================================== */
+/* Keys src << 32 | dst; the sentinel of row v is v << 32 | 0xFFFFFFFF
+ * (col_idx_none, gpma.cuh:826-834); two KEY_MAX guards (init_gpma,
+ * gpma.cuh:818-823) stay at the end.  size = segment_length << tree_height,
+ * a power of two.  A delete is an update with value VALUE_NONE: it
+ * tombstones a present key in place and never enters the level loop
+ * (handle_del_mod, gpma.cuh:162-175). */
+#define G_KEY_MAX 0xFFFFFFFFFFFFFFFEull
+#define G_COL_NONE 0xFFFFFFFFull
+#define G_SIGNIFICANT 5000000u
+
+struct OGpma {
+    uint32_t V;
+    uint64_t size;
+    uint32_t seg, h;
+    uint64_t *keys;
+    uint8_t *vals;
+    uint32_t *row; /* row_offset: row_offset[v + 1] = slot of v's sentinel */
+    double dlow;   /* density_lower_thres_root (gpma.cuh:52) */
+    uint32_t lower[40], upper[40];
+};
+
+static uint32_t g_fls(uint32_t x) { return x ? 32u - (uint32_t)__builtin_clz(x) : 0u; }
+
+/* recalculate_density, gpma.cuh:102-131 */
+static void g_density(OGpma *g) {
+    uint32_t len = g->seg;
+    for (uint32_t i = 0; i <= g->h && i < 40; i++) {
+        g->lower[i] = (uint32_t)(g->dlow * (double)len);
+        g->upper[i] = len;
+        len <<= 1;
+    }
+}
+
+/* the size rule of resize_gpma, gpma.cuh:706-711 */
+static void g_size_rule(uint64_t merge, uint64_t *size, uint32_t *seg, uint32_t *h) {
+    uint64_t t = 4;
+    while ((double)t < (double)merge) t <<= 1;
+    *size = t;
+    *seg = 1u << (g_fls(g_fls((uint32_t)t)) - 1);
+    *h = g_fls((uint32_t)(t / *seg)) - 1;
+}
+
+static inline int g_kept(uint64_t k, uint8_t v) { return k != KEY_NONE && v != VAL_TOMB; }
+static inline int g_is_sentinel(uint64_t k) { return (k & G_COL_NONE) == G_COL_NONE && k != KEY_NONE; }
+
+/* redispatch_kernel, gpma.cuh:428-452: item i of m to segment f*i/m, lane
+ * (f*i % m)/f of the window [node, node + width); the callers leave every
+ * other key of the window empty (block_compact_kernel + the first-m clear
+ * of block_redispatch_kernel, or memset_kernel) */
+static void g_spread(OGpma *g, const uint64_t *k, const uint8_t *v, uint64_t m, uint64_t node, uint64_t width) {
+    const uint64_t frac = width / g->seg;
+    for (uint64_t i = 0; i < width; i++) g->keys[node + i] = KEY_NONE;
+    for (uint64_t i = 0; i < m; i++) {
+        const uint64_t si = frac * i / m, lane = frac * i % m / frac;
+        const uint64_t p = node + si * g->seg + lane;
+        g->keys[p] = k[i];
+        g->vals[p] = v[i];
+        if (g_is_sentinel(k[i])) {
+            const uint64_t row = k[i] >> 32;
+            if (row < g->V) g->row[row + 1] = (uint32_t)p;
+        }
+    }
+}
+
+/* locate_leaf_kernel, gpma.cuh:177-200: binary search over the first slot
+ * of the segments */
+static uint64_t g_locate(const OGpma *g, uint64_t key) {
+    uint64_t prefix = 0, bit = ((uint64_t)g->seg << g->h) >> 1;
+    while (g->seg <= bit) {
+        if (g->keys[prefix | bit] <= key) prefix |= bit;
+        bit >>= 1;
+    }
+    return prefix;
+}
+
+typedef struct {
+    uint64_t key;
+    uint64_t idx;
+    uint8_t val;
+} GItem;
+
+static int cmp_gitem(const void *a, const void *b) {
+    const GItem *x = (const GItem *)a, *y = (const GItem *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+/* the window's kept items followed by its inserts, sorted stably by key
+ * (the block radix sort of block_redispatch_kernel / cub_sort_key_value) */
+static uint64_t g_merge_sorted(GItem *buf, uint64_t n, uint64_t *k, uint8_t *v) {
+    qsort(buf, n, sizeof(GItem), cmp_gitem);
+    for (uint64_t i = 0; i < n; i++) k[i] = buf[i].key, v[i] = buf[i].val;
+    return n;
+}
+
+/* resize_gpma, gpma.cuh:694-718: compact the whole array in order, choose
+ * the size for compacted + pending, reallocate (copying) */
+static int g_resize(OGpma *g, uint64_t pending) {
+    uint64_t c = 0;
+    for (uint64_t i = 0; i < g->size; i++)
+        if (g_kept(g->keys[i], g->vals[i])) {
+            g->keys[c] = g->keys[i];
+            g->vals[c] = g->vals[i];
+            c++;
+        }
+    uint64_t ns;
+    uint32_t seg, h;
+    g_size_rule(c + pending, &ns, &seg, &h);
+    uint64_t *k = (uint64_t *)malloc(ns * sizeof(uint64_t));
+    uint8_t *v = (uint8_t *)calloc(ns, 1);
+    if (!k || !v) return -1;
+    for (uint64_t i = 0; i < ns; i++) k[i] = i < c ? g->keys[i] : KEY_NONE;
+    for (uint64_t i = 0; i < c && i < ns; i++) v[i] = g->vals[i];
+    free(g->keys);
+    free(g->vals);
+    g->keys = k;
+    g->vals = v;
+    g->size = ns;
+    g->seg = seg;
+    g->h = h;
+    g_density(g);
+    return 0;
+}
+
+/* every kept item plus the pending inserts, sorted and spread over the whole
+ * array: the root rebalance after resize_gpma (gpma.cuh:801-813) and
+ * significant_insert (gpma.cuh:720-744; its scratch is value-initialised,
+ * so there every empty slot holds key 0 -- here empty slots hold KEY_NONE,
+ * as after every other rebalance) */
+static int g_spread_all(OGpma *g, const Upd *u, size_t n) {
+    if (g_resize(g, n)) return -1;
+    uint64_t c = 0;
+    while (c < g->size && g->keys[c] != KEY_NONE) c++;
+    GItem *buf = (GItem *)malloc((c + n + 1) * sizeof(GItem));
+    uint64_t *mk = (uint64_t *)malloc((c + n + 1) * sizeof(uint64_t));
+    uint8_t *mv = (uint8_t *)malloc(c + n + 1);
+    if (!buf || !mk || !mv) return -1;
+    for (uint64_t i = 0; i < c; i++) buf[i] = (GItem){g->keys[i], i, g->vals[i]};
+    for (size_t q = 0; q < n; q++) buf[c + q] = (GItem){u[q].key, c + q, u[q].val};
+    uint64_t m = g_merge_sorted(buf, c + n, mk, mv);
+    if (m < g->lower[g->h] || m > g->upper[g->h]) return -4; /* the root check after a resize always passes */
+    g_spread(g, mk, mv, m, 0, g->size);
+    free(buf);
+    free(mk);
+    free(mv);
+    return 0;
+}
+
+static int g_build_from(OGpma *g, const uint64_t *k, const uint8_t *v, uint64_t n) {
+    Upd *u = (Upd *)calloc(n + 1, sizeof(Upd));
+    if (!u) return -1;
+    for (uint64_t i = 0; i < n; i++) u[i].key = k[i], u[i].val = v[i];
+    int rc = g_spread_all(g, u, n);
+    free(u);
+    return rc;
+}
+
+/* init_csr_gpma (gpma.cuh:836-847): the V sentinels (value 1) and init_gpma's
+ * two KEY_MAX guards (value 1).  init_gpma leaves segment_length 32 over a
+ * 4-slot array, so the reference's first update reads and writes past it
+ * (gpma.cuh:185-187, 229-231); here the first state is the one that
+ * update's resize path gives: everything spread over the smallest power of
+ * two >= V + 2. */
+OGpma *ogpma_create(uint32_t V, double density_lower) {
+    if (V == 0 || V >= 0xFFFFFFFFu) return NULL;
+    OGpma *g = (OGpma *)calloc(1, sizeof(OGpma));
+    if (!g) return NULL;
+    g->V = V;
+    g->dlow = density_lower;
+    g->row = (uint32_t *)calloc((size_t)V + 1, sizeof(uint32_t));
+    g->size = 4;
+    g->keys = (uint64_t *)malloc(4 * sizeof(uint64_t));
+    g->vals = (uint8_t *)calloc(4, 1);
+    if (!g->row || !g->keys || !g->vals) return NULL;
+    for (int i = 0; i < 4; i++) g->keys[i] = KEY_NONE;
+    g->seg = 2;
+    g->h = 1;
+    uint64_t *k = (uint64_t *)malloc(((size_t)V + 2) * sizeof(uint64_t));
+    uint8_t *v = (uint8_t *)malloc((size_t)V + 2);
+    for (uint32_t i = 0; i < V; i++) k[i] = ((uint64_t)i << 32) | G_COL_NONE, v[i] = 1;
+    k[V] = k[V + 1] = G_KEY_MAX;
+    v[V] = v[V + 1] = 1;
+    int rc = g_build_from(g, k, v, (uint64_t)V + 2);
+    free(k);
+    free(v);
+    if (rc) return NULL;
+    return g;
+}
+
+void ogpma_destroy(OGpma *g) {
+    if (!g) return;
+    free(g->keys);
+    free(g->vals);
+    free(g->row);
+    free(g);
+}
+
+/* update_gpma (gpma.cuh:747-816) for a batch of inserts (values ins_vals or
+ * 1) and deletes (updates with VALUE_NONE).  Extension, as for the leveled
+ * array: the batch is resolved to a set first (an insert and a delete of one
+ * key apply delete-first, the last insert of a key gives its value); the
+ * reference applies repeated keys of one batch from concurrent threads. */
+int ogpma_update(OGpma *g, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins, const uint64_t *del,
+                 size_t n_del, OPmaStats *st) {
+    OPmaStats dummy;
+    if (!st) st = &dummy;
+    memset(st, 0, sizeof(*st));
+    st->height_before = g->h;
+    size_t n = n_ins + n_del;
+    for (size_t i = 0; i < n_ins; i++) {
+        if ((ins[i] >> 32) >= g->V || (ins[i] & G_COL_NONE) >= g->V) return -2;
+        if (ins_vals && ins_vals[i] == VAL_TOMB) return -2;
+    }
+    for (size_t i = 0; i < n_del; i++)
+        if ((del[i] >> 32) >= g->V || (del[i] & G_COL_NONE) >= g->V) return -2;
+    if (n == 0) {
+        st->height_after = g->h;
+        return 0;
+    }
+    Ent *e = (Ent *)malloc(n * sizeof(Ent));
+    Upd *u = (Upd *)malloc(n * sizeof(Upd));
+    if (!e || !u) return -1;
+    for (size_t i = 0; i < n_ins; i++) e[i] = (Ent){ins[i], (uint32_t)i, K_INS, ins_vals ? ins_vals[i] : (uint8_t)1};
+    for (size_t i = 0; i < n_del; i++) e[n_ins + i] = (Ent){del[i], (uint32_t)(n_ins + i), K_DEL, 0};
+    qsort(e, n, sizeof(Ent), cmp_ent);
+    size_t np = 0;
+    for (size_t i = 0; i < n;) {
+        size_t j = i;
+        while (j < n && e[j].key == e[i].key) j++;
+        const Ent *rep = &e[i];
+        if (e[i].kind == K_INS) {
+            size_t q = i;
+            while (q + 1 < j && e[q + 1].kind == K_INS) q++;
+            rep = &e[q];
+        }
+        st->n_noop += (uint32_t)(j - i - 1);
+        /* locate + handle_del_mod: the first equal key of the segment */
+        const uint64_t node = g_locate(g, rep->key);
+        int64_t hit = -1;
+        for (uint32_t l = 0; l < g->seg; l++)
+            if (g->keys[node + l] == rep->key) {
+                hit = (int64_t)(node + l);
+                break;
+            }
+        if (rep->kind == K_INS) {
+            if (hit >= 0) {
+                if (g->vals[hit] == VAL_TOMB)
+                    st->n_ins_applied++; /* a tombstoned key comes back in place */
+                else
+                    st->n_upserts++;
+                g->vals[hit] = rep->val;
+            } else {
+                u[np] = (Upd){rep->key, node, rep->val, K_INS, 0};
+                np++;
+                st->n_ins_applied++;
+            }
+        } else {
+            if (hit >= 0 && g->vals[hit] != VAL_TOMB) {
+                g->vals[hit] = VAL_TOMB;
+                st->n_del_applied++;
+            } else {
+                st->n_noop++;
+            }
+        }
+        i = j;
+    }
+    free(e);
+    int rc = 0;
+    if (np >= G_SIGNIFICANT) {
+        /* significant_insert, gpma.cuh:771-776 */
+        st->rebuilt = 1;
+        st->levelup = 1;
+        rc = g_spread_all(g, u, np);
+        np = 0;
+    }
+    GItem *buf = (GItem *)malloc((g->size + np + 1) * sizeof(GItem));
+    uint64_t *mk = (uint64_t *)malloc((g->size + np + 1) * sizeof(uint64_t));
+    uint8_t *mv = (uint8_t *)malloc(g->size + np + 1);
+    if (!buf || !mk || !mv) return -1;
+    /* the level loop, gpma.cuh:779-797 */
+    for (uint32_t level = 0; level <= g->h && np > 0 && rc == 0; level++) {
+        const uint64_t width = (uint64_t)g->seg << level;
+        const uint32_t lower = g->lower[level], upper = g->upper[level];
+        for (size_t i = 0; i < np;) {
+            size_t j = i;
+            const uint64_t node = u[i].node;
+            while (j < np && u[j].node == node) j++;
+            /* compaction: in place for windows of up to 1024 slots
+             * (block_compact_kernel, whatever the check decides), into
+             * scratch above (compact_kernel) */
+            uint64_t c = 0;
+            for (uint64_t q = 0; q < width; q++)
+                if (g_kept(g->keys[node + q], g->vals[node + q])) {
+                    buf[c] = (GItem){g->keys[node + q], c, g->vals[node + q]};
+                    c++;
+                }
+            if (width <= 1024) {
+                for (uint64_t q = 0; q < width; q++) g->keys[node + q] = KEY_NONE;
+                for (uint64_t q = 0; q < c; q++) g->keys[node + q] = buf[q].key, g->vals[node + q] = buf[q].val;
+            }
+            const uint64_t m = c + (j - i);
+            if (lower <= m && m <= upper) {
+                for (size_t q = i; q < j; q++) {
+                    buf[c + (q - i)] = (GItem){u[q].key, c + (q - i), u[q].val};
+                    u[q].applied = 1;
+                }
+                g_merge_sorted(buf, m, mk, mv);
+                g_spread(g, mk, mv, m, node, width);
+                if (level < 32) {
+                    st->win_count[level]++;
+                    st->win_slots[level] += width;
+                }
+                if (level == g->h) st->root_executed = 1;
+            }
+            i = j;
+        }
+        size_t o = 0;
+        for (size_t q = 0; q < np; q++)
+            if (!u[q].applied) {
+                u[o] = u[q];
+                u[o].node &= ~width;
+                o++;
+            }
+        np = o;
+    }
+    free(buf);
+    free(mk);
+    free(mv);
+    if (np > 0 && rc == 0) {
+        /* the root could not take them: resize_gpma + root rebalance,
+         * gpma.cuh:800-813 */
+        st->overflow = 1;
+        st->rebuilt = 1;
+        st->root_executed = 1;
+        st->levelup = 1;
+        rc = g_spread_all(g, u, np);
+    }
+    free(u);
+    st->height_after = g->h;
+    return rc;
+}
+
+uint64_t ogpma_size(const OGpma *g, uint32_t *seg, uint32_t *h) {
+    if (seg) *seg = g->seg;
+    if (h) *h = g->h;
+    return g->size;
+}
+
+/* the flat array (empty slots: key ~0, value 0) and row_offset */
+int ogpma_layout(const OGpma *g, uint64_t *keys, uint8_t *vals, size_t cap, uint32_t *row_offset) {
+    if (cap < g->size) return -1;
+    for (uint64_t i = 0; i < g->size; i++) {
+        keys[i] = g->keys[i];
+        vals[i] = g->keys[i] == KEY_NONE ? 0 : g->vals[i];
+    }
+    if (row_offset) memcpy(row_offset, g->row, ((size_t)g->V + 1) * sizeof(uint32_t));
+    return 0;
+}
+
+/* live keys (tombstones and the two guards left out), sorted */
+int64_t ogpma_export_sorted(const OGpma *g, uint64_t *keys, uint8_t *vals, size_t cap) {
+    int64_t o = 0;
+    for (uint64_t i = 0; i < g->size; i++)
+        if (g_kept(g->keys[i], g->vals[i]) && g->keys[i] != G_KEY_MAX) {
+            if ((size_t)o >= cap) return -1;
+            keys[o] = g->keys[i];
+            if (vals) vals[o] = g->vals[i];
+            o++;
+        }
+    return o;
+}
+
+/* test hooks for the comparison with the reference's compiled functions */
+void ogpma_size_rule(uint64_t merge, uint64_t *size, uint32_t *seg, uint32_t *h) { g_size_rule(merge, size, seg, h); }
+void ogpma_density(uint32_t seg, uint32_t h, double dlow, uint32_t *lower, uint32_t *upper) {
+    OGpma t;
+    memset(&t, 0, sizeof(t));
+    t.seg = seg;
+    t.h = h;
+    t.dlow = dlow;
+    g_density(&t);
+    for (uint32_t i = 0; i <= h && i < 40; i++) lower[i] = t.lower[i], upper[i] = t.upper[i];
+}
+/* locate + handle_del_mod alone, literally, for n updates in order (value
+ * VALUE_NONE: delete): leaf[i] = the located slot, or 0xFFFFFFFF when the
+ * update was applied in place or is a delete (gpma.cuh:162-200) */
+int ogpma_resolve_only(OGpma *g, const uint64_t *keys, const uint8_t *vals, size_t n, uint32_t *leaf) {
+    for (size_t i = 0; i < n; i++) {
+        uint64_t node = g_locate(g, keys[i]);
+        uint32_t lf = vals[i] == VAL_TOMB ? 0xFFFFFFFFu : (uint32_t)node;
+        for (uint32_t l = 0; l < g->seg; l++)
+            if (g->keys[node + l] == keys[i]) {
+                g->vals[node + l] = vals[i];
+                lf = 0xFFFFFFFFu;
+                break;
+            }
+        leaf[i] = lf;
+    }
+    return 0;
+}
+
+/* g_spread over [node, node + width) of a caller's flat array */
+int ogpma_spread_window(uint32_t V, uint32_t seg, uint64_t node, uint64_t width, const uint64_t *mk, const uint8_t *mv,
+                        uint64_t m, uint64_t *keys, uint8_t *vals, uint32_t *row_offset) {
+    OGpma t;
+    memset(&t, 0, sizeof(t));
+    t.V = V;
+    t.seg = seg;
+    t.keys = keys;
+    t.vals = vals;
+    t.row = row_offset;
+    if (m > width) return -1;
+    g_spread(&t, mk, mv, m, node, width);
+    return 0;
+}
+
+int ogpma_locate_keys(const OGpma *g, const uint64_t *keys, size_t n, uint32_t *out) {
+    for (size_t i = 0; i < n; i++) out[i] = (uint32_t)g_locate(g, keys[i]);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* CPU baseline: sorted-merge CSR rebuild per batch (test_cusparse.cu:51-78
  * sort-then-coo2csr method, test_algos.cu:197-203 host CSR build)        */

@@ -100,6 +100,26 @@ int opma_redistribute_window(uint32_t H, uint32_t V, uint64_t node, uint64_t wid
                              const uint8_t *mv, uint64_t m, uint64_t *keys, uint8_t *vals, uint32_t *sent);
 uint32_t opma_resize_height(uint64_t count, int reach_root);
 
+/* ---- GPMA (gpma.cuh): the flat packed memory array ----
+ * Keys src << 32 | dst, sentinel v << 32 | 0xFFFFFFFF, two KEY_MAX guards.
+ * ogpma_create: init_csr_gpma (gpma.cuh:836-847); ogpma_update: update_gpma
+ * (gpma.cuh:747-816) with deletes as VALUE_NONE updates; density_lower is
+ * density_lower_thres_root (0.15, gpma.cuh:52). */
+typedef struct OGpma OGpma;
+OGpma *ogpma_create(uint32_t num_vertices, double density_lower);
+void ogpma_destroy(OGpma *g);
+int ogpma_update(OGpma *g, const uint64_t *ins, const uint8_t *ins_vals, size_t n_ins, const uint64_t *del,
+                 size_t n_del, OPmaStats *st);
+uint64_t ogpma_size(const OGpma *g, uint32_t *seg, uint32_t *height);
+int ogpma_layout(const OGpma *g, uint64_t *keys, uint8_t *vals, size_t cap, uint32_t *row_offset);
+int64_t ogpma_export_sorted(const OGpma *g, uint64_t *keys, uint8_t *vals, size_t cap);
+void ogpma_size_rule(uint64_t merge, uint64_t *size, uint32_t *seg, uint32_t *height);
+void ogpma_density(uint32_t seg, uint32_t height, double density_lower, uint32_t *lower, uint32_t *upper);
+int ogpma_locate_keys(const OGpma *g, const uint64_t *keys, size_t n, uint32_t *out);
+int ogpma_resolve_only(OGpma *g, const uint64_t *keys, const uint8_t *vals, size_t n, uint32_t *leaf);
+int ogpma_spread_window(uint32_t V, uint32_t seg, uint64_t node, uint64_t width, const uint64_t *mk, const uint8_t *mv,
+                        uint64_t m, uint64_t *keys, uint8_t *vals, uint32_t *row_offset);
+
 /* ---- synthetic workload generators (identical integer arithmetic to the
  * device generator in lpma_gb300/csrc/gen.cu) ---- */
 uint64_t opma_mix64(uint64_t z);

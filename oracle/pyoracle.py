@@ -83,6 +83,17 @@ def lib():
             "opma_locate_keys": (I, [P, P, SZ, P]),
             "opma_redistribute_window": (I, [U32, U32, U64, U64, P, P, U64, P, P, P]),
             "opma_resize_height": (U32, [U64, I]),
+            "ogpma_create": (P, [U32, ctypes.c_double]),
+            "ogpma_destroy": (None, [P]),
+            "ogpma_update": (I, [P, P, P, SZ, P, SZ, P]),
+            "ogpma_size": (U64, [P, P, P]),
+            "ogpma_layout": (I, [P, P, P, SZ, P]),
+            "ogpma_export_sorted": (ctypes.c_int64, [P, P, P, SZ]),
+            "ogpma_size_rule": (None, [U64, P, P, P]),
+            "ogpma_density": (None, [U32, U32, ctypes.c_double, P, P]),
+            "ogpma_locate_keys": (I, [P, P, SZ, P]),
+            "ogpma_resolve_only": (I, [P, P, P, SZ, P]),
+            "ogpma_spread_window": (I, [U32, U32, U64, U64, P, P, U64, P, P, P]),
             "opma_mix64": (U64, [U64]),
             "opma_rmat_raw": (None, [U64, U32, U64, U32, U32, U32, P]),
             "opma_dedup": (U64, [P, U64]),
@@ -181,6 +192,77 @@ class OracleLpma:
         got = lib().opma_csr(self.h, _ptr(ro), _ptr(ci), _ptr(vals), n)
         assert got == n
         return ro, ci, vals
+
+
+GPMA_KEY_MAX = 0xFFFFFFFFFFFFFFFE
+GPMA_DENSITY_LOWER = 0.15
+
+
+def gpma_sentinel_key(v):
+    return (int(v) << 32) | 0xFFFFFFFF
+
+
+class OracleGpma:
+    """update_gpma (gpma.cuh:747-816) restated on the CPU: one flat array,
+    keys src << 32 | dst, deletes tombstone in place."""
+
+    def __init__(self, num_vertices, density_lower=GPMA_DENSITY_LOWER):
+        self.V = int(num_vertices)
+        self.h = lib().ogpma_create(self.V, float(density_lower))
+        if not self.h:
+            raise RuntimeError("ogpma_create failed (num_vertices=%d)" % self.V)
+
+    def close(self):
+        if self.h:
+            lib().ogpma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def update(self, ins=None, ins_vals=None, dels=None):
+        ins = np.ascontiguousarray(ins if ins is not None else np.zeros(0, np.uint64), dtype=np.uint64)
+        dels = np.ascontiguousarray(dels if dels is not None else np.zeros(0, np.uint64), dtype=np.uint64)
+        iv = None if ins_vals is None else np.ascontiguousarray(ins_vals, dtype=np.uint8)
+        st = OPmaStats()
+        rc = lib().ogpma_update(self.h, _ptr(ins), _ptr(iv), ins.size, _ptr(dels), dels.size, ctypes.byref(st))
+        if rc != 0:
+            raise ValueError("ogpma_update failed rc=%d" % rc)
+        return st.as_dict()
+
+    def geometry(self):
+        seg, hh = ctypes.c_uint32(), ctypes.c_uint32()
+        size = lib().ogpma_size(self.h, ctypes.byref(seg), ctypes.byref(hh))
+        return size, seg.value, hh.value
+
+    def layout(self):
+        """(keys, values, row_offset) of the flat array; empty slots key ~0, value 0."""
+        size, _, _ = self.geometry()
+        k = np.empty(size, np.uint64)
+        v = np.empty(size, np.uint8)
+        ro = np.empty(self.V + 1, np.uint32)
+        assert lib().ogpma_layout(self.h, _ptr(k), _ptr(v), size, _ptr(ro)) == 0
+        return k, v, ro
+
+    def export_sorted(self):
+        size, _, _ = self.geometry()
+        k = np.empty(size, np.uint64)
+        v = np.empty(size, np.uint8)
+        n = lib().ogpma_export_sorted(self.h, _ptr(k), _ptr(v), size)
+        return k[:n].copy(), v[:n].copy()
+
+    def locate(self, keys):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        out = np.zeros(keys.size, np.uint32)
+        assert lib().ogpma_locate_keys(self.h, _ptr(keys), keys.size, _ptr(out)) == 0
+        return out
+
+    def resolve_only(self, keys, vals):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        vals = np.ascontiguousarray(vals, dtype=np.uint8)
+        out = np.zeros(keys.size, np.uint32)
+        assert lib().ogpma_resolve_only(self.h, _ptr(keys), _ptr(vals), keys.size, _ptr(out)) == 0
+        return out
 
 
 class CsrBaseline:
@@ -352,4 +434,24 @@ def redistribute_window(H, V, node, width, items, item_vals, keys, vals, sent):
     iv = np.ascontiguousarray(item_vals, dtype=np.uint8)
     rc = lib().opma_redistribute_window(H, V, node, width, _ptr(items), _ptr(iv), items.size, _ptr(keys), _ptr(vals),
                                         _ptr(sent))
+    assert rc == 0
+
+
+def gpma_size_rule(merge):
+    size, seg, h = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+    lib().ogpma_size_rule(merge, ctypes.byref(size), ctypes.byref(seg), ctypes.byref(h))
+    return size.value, seg.value, h.value
+
+
+def gpma_density(seg, h, dlow=GPMA_DENSITY_LOWER):
+    lo, up = np.zeros(h + 1, np.uint32), np.zeros(h + 1, np.uint32)
+    lib().ogpma_density(seg, h, float(dlow), _ptr(lo), _ptr(up))
+    return lo, up
+
+
+def gpma_spread_window(V, seg, node, width, items, item_vals, keys, vals, row_offset):
+    items = np.ascontiguousarray(items, dtype=np.uint64)
+    iv = np.ascontiguousarray(item_vals, dtype=np.uint8)
+    rc = lib().ogpma_spread_window(V, seg, node, width, _ptr(items), _ptr(iv), items.size, _ptr(keys), _ptr(vals),
+                                   _ptr(row_offset))
     assert rc == 0

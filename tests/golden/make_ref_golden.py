@@ -13,8 +13,10 @@ them and writes what they return:
 * ref_vectors.json -- the resize height rule (rpma.cuh:1340-1352) on a grid,
   locate_leaf_kernel (rpma.cuh:253-315) over the layouts of seeded streams
   (the queries and the stop segment the reference finds), redispatch_kernel
-  slot placements, and GPMA's size rule (gpma.cuh:706-711) and density table
-  (gpma.cuh:102-131).
+  slot placements, GPMA's size rule (gpma.cuh:706-711) and density table
+  (gpma.cuh:102-131), and GPMA's locate_leaf_kernel with handle_del_mod
+  (gpma.cuh:162-200: stop slot and in-place value changes) over the layouts
+  of seeded GPMA streams.
 
 Each file records the SHA-256 of the generated translation units it came
 from.  Run from the repository root, with the reference where
@@ -55,6 +57,31 @@ def stream_states(spec):
         o.update(ins=e[(j - 1) * b:j * b])
         if j % 2 == 0:
             o.update(dels=e[(j - 2) * b:(j - 2) * b + b // 3])
+        if j in spec["steps"]:
+            yield j, o, e
+
+
+# GPMA streams (keys src << 32 | dst): step j inserts e[(j-1)*batch : j*batch]
+# and, on even steps, deletes the first half of the batch two steps before
+GPMA_STREAMS = [
+    {"seed": 3, "scale": 5, "ef": 4, "batch": 11, "steps": [1, 3, 6]},
+    {"seed": 5, "scale": 9, "ef": 8, "batch": 700, "steps": [2, 4, 5]},
+]
+
+
+def gpma_keys(e):
+    return ((e >> np.uint64(42)) << np.uint64(32)) | ((e >> np.uint64(20)) & np.uint64(0x3FFFFF))
+
+
+def gpma_stream_states(spec):
+    V = 1 << spec["scale"]
+    e = gpma_keys(O.shuffle(O.rmat_edges(spec["seed"], spec["scale"], spec["ef"]), spec["seed"] + 1))
+    o = O.OracleGpma(V)
+    b = spec["batch"]
+    for j in range(1, max(spec["steps"]) + 1):
+        o.update(ins=e[(j - 1) * b:j * b])
+        if j % 2 == 0:
+            o.update(dels=e[(j - 2) * b:(j - 2) * b + b // 2])
         if j in spec["steps"]:
             yield j, o, e
 
@@ -164,6 +191,23 @@ def main():
         spread.append({"height": H, "node": node, "width": width, "items": [str(int(x)) for x in items],
                        "vals": vals.tolist(), "slots": slots, "sentinels": sent})
 
+    gpma_locate = []
+    for spec in GPMA_STREAMS:
+        for j, o, e in gpma_stream_states(spec):
+            keys, vals, _ = o.layout()
+            size, seg, h = o.geometry()
+            qrng = np.random.default_rng(1000 * spec["seed"] + j)
+            q = np.unique(np.concatenate([e[qrng.integers(0, e.size, 150)],
+                                          qrng.integers(0, 1 << 40, 30, dtype=np.uint64)]))
+            qv = qrng.integers(1, 255, q.size).astype(np.uint8)
+            qv[qrng.random(q.size) < 0.3] = 0xFF
+            leaf, v2 = R.gpma_locate(keys, vals, seg, h, q, qv)
+            occ = keys != np.uint64(0xFFFFFFFFFFFFFFFF)
+            gpma_locate.append({"stream": {x: spec[x] for x in ("seed", "scale", "ef", "batch")}, "step": j,
+                                "geometry": [size, seg, h], "queries": [str(int(x)) for x in q],
+                                "qvals": qv.tolist(), "leaf": leaf.tolist(),
+                                "vals_after": [int(x) for x in v2[occ]]})
+
     gpma_size = [[m] + list(R.gpma_size(m)) for m in list(range(0, 70)) + [100, 127, 128, 129, 1000, 4096, 4097,
                                                                             100000, 5_000_000, 33_554_433]]
     gpma_density = []
@@ -172,7 +216,8 @@ def main():
         gpma_density.append({"segment_length": seg, "height": h, "lower": lo_.tolist(), "upper": up_.tolist()})
     with open(os.path.join(out, "ref_vectors.json"), "w") as f:
         json.dump({"provenance": prov, "resize_height": resize, "locate": locate, "redistribute": spread,
-                   "gpma_size": gpma_size, "gpma_density": gpma_density}, f, separators=(",", ":"))
+                   "gpma_size": gpma_size, "gpma_density": gpma_density, "gpma_locate": gpma_locate}, f,
+                  separators=(",", ":"))
     print("wrote index_algebra.json, tables.json, ref_vectors.json from units %s" % digest[:16])
 
 

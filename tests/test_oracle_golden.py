@@ -156,6 +156,38 @@ def test_redistribution_vectors(oracle):
             assert sent[row] == 32 * ((1 << idx) - 1) + lane
 
 
+def test_gpma_size_and_density_vectors(oracle):
+    v = load("ref_vectors.json")
+    for m, size, seg, h in v["gpma_size"]:
+        assert oracle.gpma_size_rule(m) == (size, seg, h), m
+    for t in v["gpma_density"]:
+        lo, up = oracle.gpma_density(t["segment_length"], t["height"])
+        assert lo.tolist() == t["lower"] and up.tolist() == t["upper"]
+
+
+def test_gpma_locate_vectors(oracle):
+    """GPMA's locate_leaf_kernel + handle_del_mod, as the reference's code
+    ran it on layouts of seeded streams; the oracle replays each stream."""
+    for c in load("ref_vectors.json")["gpma_locate"]:
+        spec = c["stream"]
+        V = 1 << spec["scale"]
+        e = oracle.shuffle(oracle.rmat_edges(spec["seed"], spec["scale"], spec["ef"]), spec["seed"] + 1)
+        e = ((e >> np.uint64(42)) << np.uint64(32)) | ((e >> np.uint64(20)) & np.uint64(0x3FFFFF))
+        o = oracle.OracleGpma(V)
+        b = spec["batch"]
+        for j in range(1, c["step"] + 1):
+            o.update(ins=e[(j - 1) * b:j * b])
+            if j % 2 == 0:
+                o.update(dels=e[(j - 2) * b:(j - 2) * b + b // 2])
+        assert list(o.geometry()) == c["geometry"]
+        keys, _, _ = o.layout()
+        q = np.array([int(x) for x in c["queries"]], np.uint64)
+        leaf = o.resolve_only(q, np.array(c["qvals"], np.uint8))
+        assert leaf.tolist() == c["leaf"], (spec, c["step"])
+        _, vals, _ = o.layout()
+        assert vals[keys != np.uint64(0xFFFFFFFFFFFFFFFF)].tolist() == c["vals_after"]
+
+
 def _digest(keys, vals):
     h = hashlib.sha256()
     h.update(keys.astype("<u8").tobytes())

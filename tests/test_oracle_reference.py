@@ -158,3 +158,96 @@ def _phys(L, H):
     s1 = (L >> 5) + 1
     t = (s1 & -s1).bit_length() - 1
     return 32 * ((1 << (H - t)) - 1) + 32 * (s1 >> (t + 1)) + (L & 31)
+
+
+# ---------------------------------------------------------------- GPMA (gpma.cuh)
+def _gpma_keys(e):
+    """src << 32 | dst form of leveled keys src << 42 | dst << 20."""
+    return ((e >> np.uint64(42)) << np.uint64(32)) | ((e >> np.uint64(20)) & np.uint64(0x3FFFFF))
+
+
+def test_gpma_size_rule_and_density(ref, oracle):
+    for m in list(range(0, 300)) + [1000, 4095, 4096, 4097, 65537, 1 << 20, 5_000_000, 33_554_432, 33_554_433]:
+        assert ref.gpma_size(m) == oracle.gpma_size_rule(m), m
+    for seg, h in [(2, 1), (4, 2), (4, 4), (8, 7), (8, 11), (16, 12), (16, 21), (32, 25)]:
+        lo, up = ref.gpma_density(seg, h)
+        olo, oup = oracle.gpma_density(seg, h)
+        assert np.array_equal(lo, olo) and np.array_equal(up, oup), (seg, h)
+
+
+def _gpma_states(oracle):
+    """GPMA oracles along seeded streams with tombstones: (oracle, edges, ops)
+    where replaying ops on a new oracle gives the same state."""
+    for seed, scale, ef, batch in [(3, 5, 4, 11), (5, 8, 8, 300), (7, 11, 8, 2500)]:
+        V = 1 << scale
+        e = _gpma_keys(oracle.shuffle(oracle.rmat_edges(seed, scale, ef), seed + 1))
+        rng = np.random.default_rng(seed)
+        a = oracle.OracleGpma(V)
+        ops = []
+        yield a, e, list(ops)
+        pos = 0
+        while pos < e.size:
+            ops.append(("ins", e[pos:pos + batch]))
+            pos += batch
+            if rng.random() < 0.6:
+                ops.append(("del", rng.choice(e[:pos], size=min(pos, batch // 2 + 1), replace=False)))
+            for kind, keys in ops[-2:] if ops[-1][0] == "del" else ops[-1:]:
+                a.update(ins=keys) if kind == "ins" else a.update(dels=keys)
+            yield a, e, list(ops)
+
+
+def _replay(oracle, V, ops):
+    b = oracle.OracleGpma(V)
+    for kind, keys in ops:
+        b.update(ins=keys) if kind == "ins" else b.update(dels=keys)
+    return b
+
+
+def test_gpma_locate_and_handle_del_mod(ref, oracle):
+    """locate_leaf_kernel with handle_del_mod (gpma.cuh:162-200): the stop
+    segment of every update, and what it does in place (upsert, tombstone,
+    a tombstoned key brought back), on the oracle's layouts."""
+    rng = np.random.default_rng(8)
+    n_cases = 0
+    for a, e, ops in _gpma_states(oracle):
+        keys, vals, _ = a.layout()
+        size, seg, h = a.geometry()
+        q = np.unique(np.concatenate([e[rng.integers(0, e.size, 200)], rng.integers(0, 1 << 40, 50, dtype=np.uint64)]))
+        qv = rng.integers(1, 255, q.size).astype(np.uint8)
+        qv[rng.random(q.size) < 0.3] = 0xFF  # deletes
+        leaf_ref, vals_ref = ref.gpma_locate(keys, vals, seg, h, q, qv)
+        b = _replay(oracle, a.V, ops)
+        assert np.array_equal(b.layout()[0], keys)
+        leaf_o = b.resolve_only(q, qv)
+        assert np.array_equal(leaf_ref, leaf_o), (seg, h, len(ops))
+        _, vals_o, _ = b.layout()
+        occupied = keys != np.uint64(0xFFFFFFFFFFFFFFFF)
+        assert np.array_equal(vals_ref[occupied], vals_o[occupied])
+        n_cases += 1
+    assert n_cases > 10
+
+
+def test_gpma_redistribution(ref, oracle):
+    rng = np.random.default_rng(9)
+    V = 256
+    for _ in range(300):
+        size = 1 << int(rng.integers(2, 12))
+        _, seg, h = oracle.gpma_size_rule(size)
+        level = int(rng.integers(0, h + 1))
+        width = seg << level
+        node = int(rng.integers(0, size // width)) * width
+        m = int(rng.integers(0, width + 1))
+        items = np.unique((rng.integers(0, V, m).astype(np.uint64) << np.uint64(32)) |
+                          rng.integers(0, V, m).astype(np.uint64))
+        sel = rng.random(items.size) < 0.2
+        items[sel] |= np.uint64(0xFFFFFFFF)
+        items = np.unique(items)
+        iv = rng.integers(1, 250, items.size).astype(np.uint8)
+        keys = np.sort(rng.integers(0, 1 << 62, size, dtype=np.uint64))
+        vals = rng.integers(0, 256, size).astype(np.uint8)
+        keys[node:node + width] = np.uint64(0xFFFFFFFFFFFFFFFF)  # the callers clear the window first
+        ro = np.zeros(V + 1, np.uint32)
+        rk, rv, rro = ref.gpma_redispatch(keys, vals, node, width, seg, items, iv, ro)
+        ok, ov, oro = keys.copy(), vals.copy(), ro.copy()
+        oracle.gpma_spread_window(V, seg, node, width, items, iv, ok, ov, oro)
+        assert np.array_equal(rk, ok) and np.array_equal(rv, ov) and np.array_equal(rro, oro), (size, seg, level)
