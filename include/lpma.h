@@ -59,7 +59,10 @@ enum { LPMA_KEY_PACKED = 0, LPMA_KEY_PAIR32 = 1 };
  * ordinary launches instead of the one cooperative launch, because two
  * cooperative grids that each hold part of the GPU could wait on each
  * other. */
-enum { LPMA_FLAG_CONCURRENT = 1 };
+/* LPMA_FLAG_GPMA: the handle stores the flat packed memory array of the
+ * reference's gpma.cuh instead of the leveled tree of rpma.cuh (see
+ * lpma_config_gpma). */
+enum { LPMA_FLAG_CONCURRENT = 1, LPMA_FLAG_GPMA = 2 };
 enum { LPMA_MAX_HEIGHT = 24 };
 
 typedef struct {
@@ -101,6 +104,43 @@ typedef struct {
 
 /* defaults that reproduce the reference: 32 / 0.42 / 1.0 / skip rule on */
 LPMA_API lpma_status_t lpma_config_default(LpmaConfig *cfg);
+
+/* ---- GPMA mode (gpma.cuh) ----
+ * A handle created with lpma_config_gpma's configuration (flags =
+ * LPMA_FLAG_GPMA) holds the reference's flat GPMA instead of the leveled
+ * array: one array of size slots (a power of two) cut into segments of
+ * 2^(fls(fls(size)) - 1) slots, density bounds trunc(density_lower_root *
+ * len) and len per level (0.15 / 1.0, gpma.cuh:52-55), a copying resize to
+ * the smallest power of two that holds the items (resize_gpma,
+ * gpma.cuh:694-718) and a whole-array respread for batches of 5,000,000 new
+ * keys or more (significant_insert, gpma.cuh:720-744).  Keys are
+ * src << 32 | dst with src, dst < num_vertices <= 0xFFFFFFFE; the sentinel
+ * of vertex v is v << 32 | 0xFFFFFFFF (value 1) and two guards of key
+ * 0xFFFFFFFFFFFFFFFE (value 1) stay at the end (init_csr_gpma / init_gpma,
+ * gpma.cuh:818-847).  lpma_update inserts (values default 1) and deletes
+ * (handle_del_mod, gpma.cuh:162-175: a present key is tombstoned in place,
+ * value 0xFF, and leaves at the next rebalance of its window; inserting a
+ * tombstoned key brings it back in place); thres must be 0.  The first
+ * state after lpma_create is the one update_gpma's resize path gives for
+ * the sentinels and guards (the reference's first update reads past its
+ * 4-slot initial array).  lpma_export_sorted returns the live keys
+ * (sentinels included, guards and tombstones left out), lpma_export_layout
+ * the flat array with sentinel_slots[v] = row_offset[v + 1], lpma_info the
+ * tree height.  The CSR view, the read paths, lpma_set_flags and the
+ * batched update return LPMA_ERR_INVALID_ARGUMENT for these handles. */
+LPMA_API lpma_status_t lpma_config_gpma(LpmaConfig *cfg);
+
+/* The GPMA view analytics read (gpma.cuh:341-344, 471-474): device
+ * pointers, valid until the next update, to row_offset (num_vertices + 1
+ * entries; row_offset[0] = 0 and row_offset[v + 1] is the slot of v's
+ * sentinel, so row v's keys lie in slots row_offset[v] .. row_offset[v + 1]
+ * skipping empty slots, value-0xFF tombstones and, for v > 0, the slot
+ * row_offset[v] itself), the key and value arrays (*size slots), and the
+ * segment length and height.  LPMA_ERR_INVALID_ARGUMENT for a leveled
+ * handle. */
+LPMA_API lpma_status_t lpma_gpma_view(LpmaHandle *h, const uint32_t **row_offset, const uint64_t **keys,
+                                      const uint8_t **values, uint64_t *size, uint32_t *segment_length,
+                                      uint32_t *height);
 
 /* Replaces init_csr_rpma(RPMA&, SIZE_TYPE row_num) (rpma.cuh:1808-1824):
  * empty height-0 array, then the num_vertices sentinel keys inserted through

@@ -9,9 +9,9 @@ from . import _abi
 _abi.load()
 
 from .rpma import (Batcher, Lpma, LpmaError, default_config, destroy_rpma, gen_rmat_device, get_data_rpma,  # noqa: E402
-                   init_csr_rpma, kernel_launches, pack_key, profile_enable, profile_report, sentinel_key,
+                   gpma_config, gpma_key, init_csr_rpma, kernel_launches, pack_key, profile_enable, profile_report, sentinel_key,
                    shuffle_device, to_csr_rpma, update_rpma)
 
-__all__ = ["Lpma", "Batcher", "LpmaError", "default_config", "init_csr_rpma", "update_rpma", "to_csr_rpma", "get_data_rpma",
+__all__ = ["Lpma", "Batcher", "LpmaError", "default_config", "gpma_config", "gpma_key", "init_csr_rpma", "update_rpma", "to_csr_rpma", "get_data_rpma",
            "destroy_rpma", "pack_key", "sentinel_key", "gen_rmat_device", "shuffle_device", "kernel_launches",
            "profile_enable", "profile_report"]

@@ -29,6 +29,7 @@ EXPORTS = [
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
     "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve", "lpma_debug_sort_barrier",
+    "lpma_config_gpma", "lpma_gpma_view",
 ]
 SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
@@ -144,6 +145,8 @@ def load():
         "lpma_tune_set": [U32, U32, U32],
         "lpma_tune_get": [U32, U32, P],
         "lpma_debug_sort_barrier": [U32, I],
+        "lpma_config_gpma": [P],
+        "lpma_gpma_view": [P, P, P, P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -13,8 +13,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "_lpma.so")
-SOURCES = ["prims.cu", "update.cu", "view.cu", "query.cu", "abi.cu", "noalloc.cu", "loader.cu", "pool.cu"]
-HEADERS = ["lpma_common.cuh", "prims.cuh", "kernels.cuh", "per_device.h"]
+SOURCES = ["prims.cu", "update.cu", "view.cu", "query.cu", "abi.cu", "noalloc.cu", "loader.cu", "pool.cu", "gpma.cu"]
+HEADERS = ["lpma_common.cuh", "prims.cuh", "kernels.cuh", "per_device.h", "gpma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -27,6 +27,7 @@
 #include <thread>
 #include <vector>
 
+#include "gpma.cuh"
 #include "kernels.cuh"
 #include "lpma.h"
 #include "prims.cuh"
@@ -119,6 +120,9 @@ struct LpmaHandle {
     // flight, on the call's stream: lpma_destroy waits for it, not the device
     cudaEvent_t done_ev = nullptr;
     bool done_recorded = false;
+    // LPMA_FLAG_GPMA: the flat array of gpma.cuh (gpma.cu) instead of the
+    // leveled tree; the leveled fields above stay unused
+    GpmaState *gp = nullptr;
     // the front's 4- and 32-segment executors run on side_stream, beside the
     // single-segment one: fork after the status read-back, join after them
     cudaStream_t side_stream = nullptr;
@@ -176,8 +180,6 @@ bool poison_this(const char *name) {
     const char *only = getenv("LPMA_POISON_ONLY");
     return !only || !only[0] || strstr(name, only) != nullptr;
 }
-
-cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s);
 
 // Device buffers of handles and batchers come from the stream-ordered pool
 // (allocated on the calling thread's default stream, which is synchronised
@@ -270,10 +272,14 @@ cudaMemPool_t batch_pool() {
     return pools[dev];
 }
 
-cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s) {
+}  // namespace
+
+cudaError_t lpma::pool_alloc(void **p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool = batch_pool();
     return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMallocAsync(p, bytes, s);
 }
+
+namespace {
 
 // Releases the capacity's arena in stream order (s = nullptr: at once, with
 // a device synchronisation).
@@ -1079,8 +1085,31 @@ lpma_status_t lpma_config_default(LpmaConfig *cfg) {
     return LPMA_OK;
 }
 
+lpma_status_t lpma_config_gpma(LpmaConfig *cfg) {
+    if (!cfg) return LPMA_ERR_INVALID_ARGUMENT;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->segment_length = 0;  // 2^(fls(fls(size)) - 1), from the size
+    cfg->key_format = LPMA_KEY_PAIR32;
+    cfg->flags = LPMA_FLAG_GPMA;
+    cfg->density_lower_root = 0.15;  // gpma.cuh:52
+    cfg->density_upper_root = 1.0;
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_gpma_view(LpmaHandle *h, const uint32_t **row_offset, const uint64_t **keys, const uint8_t **values,
+                             uint64_t *size, uint32_t *segment_length, uint32_t *height) {
+    if (!h || !h->gp) return LPMA_ERR_INVALID_ARGUMENT;
+    gpma_view(h->gp, row_offset, keys, values);
+    return gpma_geometry(h->gp, size, segment_length, height, nullptr);
+}
+
 lpma_status_t lpma_destroy(LpmaHandle *h) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        gpma_destroy(h->gp);
+        delete h;
+        return LPMA_OK;
+    }
     // wait for this handle's own work only: its last call's stream (the
     // event recorded after that call's last launch) and its private streams;
     // then every buffer goes back to the stream-ordered pool without a
@@ -1132,6 +1161,24 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
         c = *cfg;
     else
         lpma_config_default(&c);
+    if (c.flags & LPMA_FLAG_GPMA) {
+        // the flat array of gpma.cuh: keys src << 32 | dst, vertex ids below
+        // 2^32 - 1 (the sentinel's column is all ones), segment length from
+        // the size, no expiry, no concurrent mode
+        if ((c.flags & ~(uint32_t)LPMA_FLAG_GPMA) || !(c.density_lower_root >= 0.0 && c.density_lower_root <= 1.0) ||
+            c.density_upper_root != 1.0 || num_vertices == 0 || num_vertices > 0xFFFFFFFEu)
+            return LPMA_ERR_INVALID_ARGUMENT;
+        LpmaHandle *h = new LpmaHandle();
+        h->cfg = c;
+        h->V = num_vertices;
+        const lpma_status_t r = gpma_create(num_vertices, c.density_lower_root, (cudaStream_t)stream, &h->gp);
+        if (r != LPMA_OK) {
+            delete h;
+            return r;
+        }
+        *out = h;
+        return LPMA_OK;
+    }
     if (c.segment_length != 32 || c.key_format > 1 || !(c.density_lower_root >= 0.0 && c.density_lower_root <= 1.0) ||
         c.density_upper_root != 1.0)
         return LPMA_ERR_INVALID_ARGUMENT;
@@ -1189,12 +1236,17 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
 
 lpma_status_t lpma_build(LpmaHandle *h, const uint64_t *d_keys, const uint8_t *d_vals, size_t n, lpma_stream_t stream) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return gpma_update(h->gp, d_keys, d_vals, n, nullptr, 0, (cudaStream_t)stream, nullptr);
     return do_update(h, d_keys, d_vals, n, nullptr, 0, 0, (cudaStream_t)stream, nullptr, false);
 }
 
 lpma_status_t lpma_update(LpmaHandle *h, const uint64_t *d_ins, const uint8_t *d_ins_vals, size_t n_ins,
                           const uint64_t *d_del, size_t n_del, uint32_t thres, lpma_stream_t stream, LpmaStats *stats) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        if (thres) return LPMA_ERR_INVALID_ARGUMENT;  // GPMA keys carry no timestamp
+        return gpma_update(h->gp, d_ins, d_ins_vals, n_ins, d_del, n_del, (cudaStream_t)stream, stats);
+    }
     return do_update(h, d_ins, d_ins_vals, n_ins, d_del, n_del, thres, (cudaStream_t)stream, stats, false);
 }
 
@@ -1203,6 +1255,25 @@ lpma_status_t lpma_update_host(LpmaHandle *h, const uint64_t *h_ins, const uint8
                                LpmaStats *stats) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
     if ((n_ins && !h_ins) || (n_del && !h_del)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        if (thres) return LPMA_ERR_INVALID_ARGUMENT;
+        cudaStream_t s = (cudaStream_t)stream;
+        uint64_t *di = nullptr, *dd = nullptr;
+        uint8_t *dv = nullptr;
+        if (pool_alloc((void **)&di, n_ins * 8 + 8, s) || pool_alloc((void **)&dd, n_del * 8 + 8, s) ||
+            pool_alloc((void **)&dv, n_ins + 8, s))
+            return LPMA_ERR_OUT_OF_MEMORY;
+        lpma_status_t r = LPMA_OK;
+        if ((n_ins && cudaMemcpyAsync(di, h_ins, n_ins * 8, cudaMemcpyHostToDevice, s)) ||
+            (n_ins && h_ins_vals && cudaMemcpyAsync(dv, h_ins_vals, n_ins, cudaMemcpyHostToDevice, s)) ||
+            (n_del && cudaMemcpyAsync(dd, h_del, n_del * 8, cudaMemcpyHostToDevice, s)))
+            r = LPMA_ERR_CUDA;
+        if (r == LPMA_OK) r = gpma_update(h->gp, di, h_ins_vals ? dv : nullptr, n_ins, dd, n_del, s, stats);
+        cudaFreeAsync(di, s), cudaFreeAsync(dd, s), cudaFreeAsync(dv, s);
+        if (stats) stats->h2d_bytes = n_ins * 8 + (h_ins_vals ? n_ins : 0) + n_del * 8;
+        cudaStreamSynchronize(s);
+        return r;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     if (h->sticky != LPMA_OK) return h->sticky;
     if (!h->copy_stream) {
@@ -1275,6 +1346,7 @@ static lpma_status_t fill_view(LpmaHandle *h, cudaStream_t s, bool csr, bool exp
 lpma_status_t lpma_csr_view(LpmaHandle *h, const uint32_t **row_offset, const uint32_t **col_index,
                             const uint8_t **values, size_t *nnz, lpma_stream_t stream) {
     if (!h || !row_offset || !col_index || !nnz) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
     if (!h->view_valid) {
@@ -1292,6 +1364,7 @@ lpma_status_t lpma_csr_view(LpmaHandle *h, const uint32_t **row_offset, const ui
 lpma_status_t lpma_to_csr(LpmaHandle *h, uint32_t *row_offset, uint32_t *col_index, uint8_t *values, size_t cap,
                           size_t *nnz, lpma_stream_t stream) {
     if (!h || !nnz) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     const uint32_t *ro, *ci;
     const uint8_t *va;
     size_t n;
@@ -1311,6 +1384,13 @@ lpma_status_t lpma_to_csr(LpmaHandle *h, uint32_t *row_offset, uint32_t *col_ind
 lpma_status_t lpma_export_sorted(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_vals, size_t cap, size_t *n,
                                  lpma_stream_t stream) {
     if (!h || !n) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        uint64_t items = 0;
+        gpma_geometry(h->gp, nullptr, nullptr, nullptr, &items);
+        *n = items;
+        if (!h_keys) return LPMA_OK;
+        return gpma_export_sorted(h->gp, h_keys, h_vals, cap, n, (cudaStream_t)stream);
+    }
     if (h->sticky != LPMA_OK) return h->sticky;
     *n = h->total;
     if (!h_keys) return LPMA_OK;
@@ -1327,6 +1407,19 @@ lpma_status_t lpma_export_layout(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_val
                                  uint32_t *sentinel_slots, size_t cap_vertices, uint32_t *height,
                                  lpma_stream_t stream) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        // the flat array; sentinel_slots[v] = row_offset[v + 1], the slot of v's sentinel
+        uint64_t size = 0;
+        uint32_t hh = 0;
+        gpma_geometry(h->gp, &size, nullptr, &hh, nullptr);
+        if (height) *height = hh;
+        if (sentinel_slots && cap_vertices < h->V) return LPMA_ERR_BUFFER_TOO_SMALL;
+        std::vector<uint32_t> ro(sentinel_slots ? (size_t)h->V + 1 : 0);
+        const lpma_status_t r = gpma_export_layout(h->gp, h_keys, h_vals, h_keys ? cap_slots : size,
+                                                   sentinel_slots ? ro.data() : nullptr, ro.size(), (cudaStream_t)stream);
+        if (r == LPMA_OK && sentinel_slots) std::memcpy(sentinel_slots, ro.data() + 1, 4ull * h->V);
+        return r;
+    }
     if (h->sticky != LPMA_OK) return h->sticky;
     if (height) *height = h->H;
     const uint64_t ns = nslots_of(h->H);
@@ -1349,6 +1442,10 @@ lpma_status_t lpma_export_layout(LpmaHandle *h, uint64_t *h_keys, uint8_t *h_val
 
 lpma_status_t lpma_info(const LpmaHandle *h, uint32_t *height, uint64_t *num_items, uint32_t *num_vertices) {
     if (!h) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        if (num_vertices) *num_vertices = h->V;
+        return gpma_geometry(h->gp, nullptr, nullptr, height, num_items);
+    }
     if (height) *height = h->H;
     if (num_items) *num_items = h->total;
     if (num_vertices) *num_vertices = h->V;
@@ -1360,6 +1457,7 @@ lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const 
                                    lpma_stream_t stream) {
     if (!h || !total || (n && (!d_srcs || !d_windows)) || !d_offsets || (d_nbrs && !d_vals))
         return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     if (n >= (1u << 30)) return LPMA_ERR_INVALID_ARGUMENT;
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1393,6 +1491,7 @@ lpma_status_t lpma_query_neighbors(LpmaHandle *h, const uint32_t *d_srcs, const 
 lpma_status_t lpma_edge_query(LpmaHandle *h, const uint64_t *d_keys, size_t n, uint32_t window, uint32_t *d_counts,
                               lpma_stream_t stream) {
     if (!h || (n && (!d_keys || !d_counts)) || n >= (1u << 31)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     if (h->sticky != LPMA_OK) return h->sticky;
     if (!n) return LPMA_OK;
     launch_edge_query(d_keys, (uint32_t)n, window, Geo{h->c.keys, h->c.vals, h->H}, h->c.cnt, h->c.fl, h->sent, h->V,
@@ -1405,6 +1504,7 @@ lpma_status_t lpma_edge_query(LpmaHandle *h, const uint64_t *d_keys, size_t n, u
 lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_sources, uint32_t max_depth, int32_t *d_dist,
                        uint32_t *levels, uint64_t *reached, lpma_stream_t stream) {
     if (!h || !d_dist || (n_sources && !d_sources) || n_sources >= (1u << 31)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
     if (!h->pin_word) CK(pinned_alloc(&h->pin_word, 2 * sizeof(uint32_t)));
@@ -1439,6 +1539,7 @@ lpma_status_t lpma_bfs(LpmaHandle *h, const uint32_t *d_sources, size_t n_source
 
 lpma_status_t lpma_pagerank(LpmaHandle *h, double alpha, uint32_t iterations, double *d_rank, lpma_stream_t stream) {
     if (!h || !d_rank || !(alpha >= 0.0 && alpha <= 1.0)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // not offered for the flat GPMA layout
     if (h->sticky != LPMA_OK) return h->sticky;
     cudaStream_t s = (cudaStream_t)stream;
     if (!h->pr_deg) {
@@ -1467,6 +1568,7 @@ lpma_status_t lpma_error_detail(const LpmaHandle *h, uint32_t *site) {
 
 lpma_status_t lpma_set_flags(LpmaHandle *h, uint32_t flags) {
     if (!h || (flags & ~(uint32_t)LPMA_FLAG_CONCURRENT)) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) return LPMA_ERR_INVALID_ARGUMENT;  // the layout is fixed at creation
     h->cfg.flags = flags;
     h->sort.bar = (flags & LPMA_FLAG_CONCURRENT) ? nullptr : h->sort.counters;
     return LPMA_OK;  // cached fronts are keyed by the sort mode
@@ -1491,6 +1593,10 @@ lpma_status_t lpma_memory_reserve(uint64_t bytes, lpma_stream_t stream) {
 
 lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes) {
     if (!h || !bytes) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->gp) {
+        *bytes = gpma_memory_bytes(h->gp);
+        return LPMA_OK;
+    }
     uint64_t b = 0;
     if (h->c.Hc || h->c.keys) {
         const uint64_t ns = nslots_of(h->c.Hc), nseg = nseg_of(h->c.Hc);
@@ -1542,7 +1648,7 @@ lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *graphs, const
         LpmaHandle *h = graphs[i];
         const LpmaBatch &it = items[i];
         sts[i] = LpmaStats{};
-        if (!h || (it.n_ins && !it.ins) || (it.n_del && !it.del)) {
+        if (!h || h->gp || (it.n_ins && !it.ins) || (it.n_del && !it.del)) {  // leveled graphs only
             res[i] = LPMA_ERR_INVALID_ARGUMENT;
             continue;
         }

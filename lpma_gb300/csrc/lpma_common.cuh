@@ -107,6 +107,10 @@ struct Window {
 struct Tables {
     uint32_t lower[32];  // trunc(0.42 * 32 * 2^i), rpma.cuh:164
     uint32_t allowed;    // bit l: windows of level l may execute
+    // the flat (GPMA) layout: slots per segment and segment count (0: the
+    // leveled tree's 32 and 2^(H+1) - 1)
+    uint32_t seg_len;
+    unsigned long long nseg;
 };
 
 __device__ inline uint32_t lanemask_lt() {

@@ -639,7 +639,8 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
     bool own = false;
     if (lead) {
         const uint32_t hi0 = lb_fwd(u.seg, x, nu, (uint64_t)s + 1);
-        const uint64_t nseg = nseg_of(H);
+        const uint64_t nseg = tb.nseg ? tb.nseg : nseg_of(H);
+        const uint64_t seg_len = tb.seg_len ? tb.seg_len : 32u;
         hi = hi0;
         for (uint32_t l = 0; l <= H + 1; l++) {
             if (!((tb.allowed >> l) & 1u)) continue;
@@ -656,7 +657,7 @@ __device__ __forceinline__ void k_plan_body(const UpdList u, uint32_t n_cap, con
                 live = (int64_t)P[b] - (int64_t)P[a];
             const int64_t net = 2 * ((int64_t)u.ip[hi] - (int64_t)u.ip[lo]) - (int64_t)(hi - lo);
             const int64_t m = live + net;
-            if (m >= (int64_t)tb.lower[l] && m <= (int64_t)(32 * (b - a))) {
+            if (m >= (int64_t)tb.lower[l] && m <= (int64_t)(seg_len * (b - a))) {
                 e = l;
                 wa = a;
                 wf = b - a;

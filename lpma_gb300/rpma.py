@@ -38,6 +38,21 @@ def default_config(**kw):
     return cfg
 
 
+def gpma_config(**kw):
+    """The configuration of a GPMA-mode handle (gpma.cuh's flat array): flags
+    LPMA_FLAG_GPMA, density 0.15 / 1.0, keys src << 32 | dst."""
+    cfg = LpmaConfig()
+    check(_abi.load().lpma_config_gpma(ctypes.byref(cfg)), "lpma_config_gpma")
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def gpma_key(src, dst):
+    """src << 32 | dst, the GPMA key layout (gpma.cuh)."""
+    return (int(src) << 32) | int(dst)
+
+
 _torch = None
 
 
@@ -98,6 +113,7 @@ class Lpma:
         check(self._L.lpma_create(ctypes.byref(cfg), self.num_vertices, _stream_ptr(stream), ctypes.byref(h)),
               "lpma_create")
         self._h = h
+        self.gpma = bool(cfg.flags & 2)
 
     # -------------------------------------------------------------- updates
     def build(self, keys, values=None):
@@ -166,10 +182,20 @@ class Lpma:
                                          _stream_ptr(self.stream)), "lpma_export_sorted")
         return k[:got.value], v[:got.value]
 
+    def gpma_view(self):
+        """GPMA handles: device pointers (row_offset, keys, values) and the
+        geometry (size, segment_length, height)."""
+        ro, k, v = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        size, seg, h = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(self._L.lpma_gpma_view(self._h, ctypes.byref(ro), ctypes.byref(k), ctypes.byref(v), ctypes.byref(size),
+                                     ctypes.byref(seg), ctypes.byref(h)), "lpma_gpma_view")
+        return (ro.value, k.value, v.value), (size.value, seg.value, h.value)
+
     def layout(self):
-        """(keys, values, sentinel_slots, height) of the physical heap-order layout."""
+        """(keys, values, sentinel_slots, height) of the physical layout: the
+        heap-order level arrays, or for a GPMA handle the flat array."""
         H = self.height
-        ns = 32 * ((2 << H) - 1)
+        ns = self.gpma_view()[1][0] if self.gpma else 32 * ((2 << H) - 1)
         k = np.empty(ns, np.uint64)
         v = np.empty(ns, np.uint8)
         sent = np.empty(self.num_vertices, np.uint32)
