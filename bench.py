@@ -33,13 +33,13 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "updated edges/s vs batch size on 1 GB300 (bit-exact); served p50/p99 batch latency"
-WORKLOAD = "rmat-s21-ef16 stream, 50% bulk, alternating insert/delete batches"
+WORKLOAD = "rmat-s%d-ef%d stream, 50%% bulk, alternating insert/delete batches"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=1 << 20)
@@ -90,15 +90,61 @@ def peaks():
         return 6800.0, "fallback"
 
 
-class Clocks:
-    """nvidia-smi samples during the timed region."""
+class _Nvml:
+    """Read-only NVML queries through the driver's libnvidia-ml (ctypes):
+    the SM clock, its maximum and the active clock-event (throttle)
+    reasons.  Nothing is set."""
 
-    def __init__(self, index=0):
+    SM = 1
+    REASONS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+               "hw_power_brake_slowdown": 0x80}
+
+    def __init__(self, pci_bus_id=None, index=0):
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        rc = 1
+        if pci_bus_id:
+            rc = self.lib.nvmlDeviceGetHandleByPciBusId_v2(pci_bus_id.encode(), ctypes.byref(self.h))
+        if rc != 0:
+            rc = self.lib.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h))
+        if rc != 0:
+            raise OSError("no NVML handle")
+        mx = ctypes.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, self.SM, ctypes.byref(mx))
+        self.max_mhz = mx.value
+
+    def sample(self):
+        c, r = ctypes.c_uint(), ctypes.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, ctypes.byref(c))
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        fn(self.h, ctypes.byref(r))
+        return c.value, r.value
+
+
+class Clocks:
+    """SM clock and throttle reasons sampled during the timed region: NVML
+    every 2 ms (the region of a 200-step run lasts about 65 ms), else
+    nvidia-smi every 100 ms."""
+
+    def __init__(self, index=0, pci_bus_id=None):
         self.samples = []
         self.index = index
+        self.pci = pci_bus_id
         self.proc = None
+        self.nvml = None
+        self.stop = False
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.pci, self.index)
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
+        except Exception:
+            self.nvml = None
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -112,6 +158,14 @@ class Clocks:
             self.proc = None
         return self
 
+    def _poll(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        while not self.stop:
+            mhz, rs = self.nvml.sample()
+            self.samples.append([str(mhz), str(self.nvml.max_mhz), ""] +
+                                ["Active" if rs & _Nvml.REASONS[n] else "Not Active" for n in names])
+            time.sleep(0.002)
+
     def _read(self):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
@@ -119,6 +173,9 @@ class Clocks:
                 self.samples.append(parts)
 
     def __exit__(self, *a):
+        self.stop = True
+        if self.nvml:
+            self.t.join(timeout=1)
         if self.proc:
             self.proc.terminate()
             try:
@@ -134,7 +191,7 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = [n for i, n in enumerate(names) if any(s[3 + i].lower() == "active" for s in self.samples)]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
 class Stream:
@@ -179,6 +236,78 @@ def build_workload(args, device, seed):
     return e, S, ins_seq, del_seq
 
 
+MIX = 0x9E3779B97F4A7C15
+M64 = (1 << 64) - 1
+
+
+def key_checksum_dev(t):
+    """(sum k, sum (k * MIX) ^ (k >> 31)) mod 2^64 of an int64 device tensor
+    of keys below 2^63 (two's-complement sums wrap)."""
+    import torch
+    a = int(t.sum()) & M64
+    b = int(torch.bitwise_xor(t * (MIX - (1 << 64)), t >> 31).sum()) & M64
+    return a, b
+
+
+def key_checksum_host(k):
+    k = np.asarray(k, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        a = int(k.sum(dtype=np.uint64))
+        b = int(((k * np.uint64(MIX)) ^ (k >> np.uint64(31))).sum(dtype=np.uint64))
+    return a, b
+
+
+class SetCheck:
+    """Size-independent checks of the stored set, outside the timed region:
+    every batch of the stream inserts only new keys and deletes only stored
+    ones, so each call must report exactly B applied updates; the stored set
+    (export_sorted, sentinels included) must be strictly sorted, of the
+    expected size, and its two checksums must equal the bulk's plus the
+    inserted batches' minus the deleted batches' (computed on the device
+    from the batches); the CSR view must hold one sentinel-closed row per
+    vertex."""
+
+    def __init__(self, S, V):
+        import torch
+        sent = (torch.arange(V, dtype=torch.int64, device=S.device) << 42) + 0x000003FFFFEFFFFF
+        a1, b1 = key_checksum_dev(S)
+        a2, b2 = key_checksum_dev(sent)
+        self.sum = [(a1 + a2) & M64, (b1 + b2) & M64]
+        self.count = int(S.numel()) + V
+        self.V = V
+        self.batches = 0
+        self.stat_errors = 0
+        self.points = []
+
+    def batch(self, kind, x, st, B):
+        a, b = key_checksum_dev(x)
+        sign = 1 if kind == "ins" else -1
+        self.sum = [(self.sum[0] + sign * a) & M64, (self.sum[1] + sign * b) & M64]
+        self.count += sign * int(x.numel())
+        want = (B, 0) if kind == "ins" else (0, B)
+        if (st["n_ins_applied"], st["n_del_applied"]) != want:
+            self.stat_errors += 1
+        self.batches += 1
+
+    def point(self, g, where):
+        k, _ = g.export_sorted()
+        ok_count = k.size == self.count
+        ok_sorted = bool(k.size < 2 or (k[1:] > k[:-1]).all())
+        ok_sum = list(key_checksum_host(k)) == self.sum
+        ro, ci, _ = g.to_csr()
+        ends = ro[1:].astype(np.int64) - 1
+        ok_csr = bool(ro[0] == 0 and (np.diff(ro.astype(np.int64)) >= 1).all() and ro[-1] == k.size and
+                      (ci[ends] == np.arange(self.V, dtype=np.uint32)).all())
+        self.points.append({"after": where, "keys": int(k.size), "count": ok_count, "sorted": ok_sorted,
+                            "checksums": ok_sum, "csr": ok_csr})
+
+    def summary(self):
+        ok = self.stat_errors == 0 and all(p["count"] and p["sorted"] and p["checksums"] and p["csr"]
+                                           for p in self.points)
+        return {"ok": ok, "batches": self.batches, "batches_with_wrong_counts": self.stat_errors,
+                "points": self.points}
+
+
 def gpu_arm(args, rank, world):
     import torch
     import lpma_gb300 as L
@@ -193,77 +322,97 @@ def gpu_arm(args, rank, world):
     e, S, ins_seq, del_seq = build_workload(args, device, replica_seed(args.seed, rank))
     g = L.Lpma(V)
     g.build(S)
+    check = SetCheck(S, V)
     st = Stream(ins_seq, del_seq)
     kinds = ["ins", "del"]
     stream = torch.cuda.current_stream()
 
-    def run(B, steps):
-        for i in range(steps):
-            batch = st.next(kinds[i % 2], B)
-            g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+    def step(kind, B):
+        batch = st.next(kind, B)
+        s_ = g.update(ins=batch) if kind == "ins" else g.update(dels=batch)
+        return batch, s_
 
     # per-batch-size sweep (1K, 10K, 100K): same stream, 20 steps each
     sweep = {}
+    peak, _ = peaks()
     for B in [int(x) for x in args.sweep.split(",") if x]:
-        run(B, 2)
+        for i in range(2):
+            x, s_ = step(kinds[i % 2], B)
+            check.batch(kinds[i % 2], x, s_, B)
         torch.cuda.synchronize()
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweep_steps + 1)]
+        sw_stats, sw_batches = [], []
         evs[0].record(stream)
         for i in range(args.sweep_steps):
-            batch = st.next(kinds[i % 2], B)
-            g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+            x, s_ = step(kinds[i % 2], B)
+            sw_stats.append(s_)
+            sw_batches.append((kinds[i % 2], x))
             evs[i + 1].record(stream)
         torch.cuda.synchronize()
+        for (k_, x), s_ in zip(sw_batches, sw_stats):
+            check.batch(k_, x, s_, B)
         lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.sweep_steps)]
         tot = sum(lat) / 1e3
+        alg = sum(16 * B + 18 * s_["slots_rewritten"] for s_ in sw_stats)
         sweep[str(B)] = {"edges_per_s": B * args.sweep_steps / tot, "p50_ms": float(np.percentile(lat, 50)),
-                         "p99_ms": float(np.percentile(lat, 99))}
+                         "p99_ms": float(np.percentile(lat, 99)), "hbm_GBps": alg / tot / 1e9,
+                         "hbm_frac": alg / tot / 1e9 / peak}
 
     # main: W warmup + K timed steps at B
     B = args.batch
-    clk = Clocks(device.index).__enter__()
-    time.sleep(0.3)
     for i in range(args.warmup):
-        batch = st.next(kinds[i % 2], B)
-        g.update(ins=batch) if i % 2 == 0 else g.update(dels=batch)
+        x, s_ = step(kinds[i % 2], B)
+        check.batch(kinds[i % 2], x, s_, B)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    props = torch.cuda.get_device_properties(device)
+    pci = None
+    if all(hasattr(props, a) for a in ("pci_domain_id", "pci_bus_id", "pci_device_id")):
+        pci = "%08X:%02X:%02X.0" % (props.pci_domain_id, props.pci_bus_id, props.pci_device_id)
+    clk = Clocks(device.index, pci).__enter__()
+    if not clk.nvml:
+        time.sleep(0.3)  # nvidia-smi needs a moment before its first sample
     launches0 = L.kernel_launches()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    stats = []
-    if True:
-        t0 = time.perf_counter()
-        evs[0].record(stream)
-        for i in range(args.steps):
-            batch = st.next(kinds[(args.warmup + i) % 2], B)
-            s = g.update(ins=batch) if (args.warmup + i) % 2 == 0 else g.update(dels=batch)
-            stats.append(s)
-            evs[i + 1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    time.sleep(0.25)
+    stats, batches = [], []
+    t0 = time.perf_counter()
+    evs[0].record(stream)
+    for i in range(args.steps):
+        k_ = kinds[(args.warmup + i) % 2]
+        x, s_ = step(k_, B)
+        stats.append(s_)
+        batches.append((k_, x))
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
     clk.__exit__()
     if world > 1:
         torch.distributed.barrier()
     launches = L.kernel_launches() - launches0
     lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     t = max_over_ranks(evs[0].elapsed_time(evs[-1]) / 1e3, device)
+    # the check of the timed steps, after the timed region
+    for (k_, x), s_ in zip(batches, stats):
+        check.batch(k_, x, s_, B)
+    del batches
+    check.point(g, "timed steps")
 
     # roofline: per-kernel CUDA events over K more steps of the same stream
     L.profile_enable(True)
     pstats = []
     prof_steps = min(args.steps, 10)
     for i in range(prof_steps):
-        k = (args.warmup + args.steps + i) % 2
-        batch = st.next(kinds[k], B)
-        pstats.append(g.update(ins=batch) if k == 0 else g.update(dels=batch))
+        k_ = kinds[(args.warmup + args.steps + i) % 2]
+        x, s_ = step(k_, B)
+        pstats.append(s_)
+        check.batch(k_, x, s_, B)
     torch.cuda.synchronize()
     prof = L.profile_report()
     L.profile_enable(False)
 
     # end to end through the host entry point: pinned host batch -> lpma_update_host
-    e2e_steps = min(args.steps, 20)  # the default K; capped so that the edge stream lasts
+    e2e_steps = min(args.steps, 50)
     e2e_warm = 2  # untimed: the host entry allocates its staging buffers on first use
     host_batches = []
     for i in range(e2e_warm + e2e_steps):
@@ -271,26 +420,28 @@ def gpu_arm(args, rank, world):
         b = st.next(kinds[k], B)
         hb = torch.empty(B, dtype=torch.int64, pin_memory=True)
         hb.copy_(b)
-        host_batches.append((k, hb.numpy().view(np.uint64)))
-    for k, hb in host_batches[:e2e_warm]:
-        g.update(ins=hb) if k == 0 else g.update(dels=hb)
-    host_batches = host_batches[e2e_warm:]
+        host_batches.append((k, hb.numpy().view(np.uint64), b))
+    warm_stats = [g.update(ins=hb) if k == 0 else g.update(dels=hb) for k, hb, _ in host_batches[:e2e_warm]]
     torch.cuda.synchronize()
     e2e_stats = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     t_e0 = time.perf_counter()
-    for k, hb in host_batches:
+    for k, hb, _ in host_batches[e2e_warm:]:
         e2e_stats.append(g.update(ins=hb) if k == 0 else g.update(dels=hb))
     ev1.record(stream)
     torch.cuda.synchronize()
     t_e2e = max(ev0.elapsed_time(ev1) / 1e3, time.perf_counter() - t_e0)
-    h2d = sum(s["h2d_bytes"] for s in e2e_stats) / len(e2e_stats)
-    d2h = sum(s["d2h_bytes"] for s in e2e_stats) / len(e2e_stats)
+    h2d = sum(s_["h2d_bytes"] for s_ in e2e_stats) / len(e2e_stats)
+    d2h = sum(s_["d2h_bytes"] for s_ in e2e_stats) / len(e2e_stats)
+    for (k, _, b), s_ in zip(host_batches, warm_stats + e2e_stats):
+        check.batch(kinds[k], b, s_, B)
+    check.point(g, "end-to-end steps")
     info = g.info()
     res = {"t": t, "lat": lat, "wall": wall, "launches": launches, "clocks": clk.summary(), "stats": stats,
            "pstats": pstats, "prof": prof, "sweep": sweep, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
-           "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"], "sort_tiers": tiers}
+           "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"], "sort_tiers": tiers,
+           "check": check.summary()}
     host_edges = None
     if rank == 0 and not args.no_cpu_baseline:
         host_edges = (e.cpu().numpy().view(np.uint64), int(S.shape[0]))
@@ -748,14 +899,16 @@ def main():
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["t"] * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded device R-MAT)",
-        "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.ef, "batch": B,
-                   "edges": res["n_edges"], "bulk": res["n_edges"] // 2, "height": res["height"],
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "PMA working set > 129 MB L2, no flush", "timing": "CUDA events on the update stream"},
+        "config": config_of(args, res["n_edges"], world),
+        "tree_height": res["height"],
+        "l2": "PMA working set (0.3-0.6 GB) > 129 MB L2: no flush between steps",
+        "timing": "CUDA events on the update stream",
         "batch_latency_ms": {"p50": float(np.percentile(res["lat"], 50)), "p99": float(np.percentile(res["lat"], 99))},
         "per_batch_size": dict(res["sweep"], **{str(B): {
             "edges_per_s": B * args.steps / res["t"], "p50_ms": float(np.percentile(res["lat"], 50)),
-            "p99_ms": float(np.percentile(res["lat"], 99))}}),
+            "p99_ms": float(np.percentile(res["lat"], 99)),
+            "hbm_GBps": sum(16 * B + 18 * x["slots_rewritten"] for x in res["stats"]) / res["t"] / 1e9,
+            "hbm_frac": sum(16 * B + 18 * x["slots_rewritten"] for x in res["stats"]) / res["t"] / 1e9 / peak}}),
         "roofline": roofline(res, B, peak, peak_kind),
         "rebalance_roofline": rebalance_roofline(res, peak, peak_kind),
         "e2e": {"value": B * res["e2e_steps"] * world / res["t_e2e"], "unit": "edges/s", "h2d_bytes_per_step": res["h2d"],
@@ -763,6 +916,7 @@ def main():
         "gpu_launches": res["launches"],
         "sort_tiers": res["sort_tiers"],
         "clocks": res["clocks"],
+        "check": res["check"],
     }
     s = res["stats"]
     out["events"] = {k: sum(x[k] for x in s) for k in ("root_executed", "eager_levelup", "rebuilt", "levelup_path",
@@ -775,29 +929,37 @@ def main():
     if rank == 0 and host_edges is not None:
         threads = os.cpu_count() or 1
         cb = cpu_baseline(host_edges, B, args.cpu_steps, threads)
+        cb1 = cpu_baseline(host_edges, B, 2, 1)
         out["cpu_baseline"] = {"value": cb["value"], "unit": "edges/s", "cores": threads, "kind": "port",
+                               "load_s": cb["load_s"], "value_1_thread": cb1["value"], "load_s_1_thread": cb1["load_s"],
                                "sample": "%d alternating insert/delete batches of %d edges on the scale-%d stream "
-                                         "(sorted-merge CSR rebuild per batch, oracle/lpma_oracle.c)"
+                                         "(sorted-merge CSR rebuild per batch, oracle/lpma_oracle.c), after the "
+                                         "bulk load of the stored half (load_s); one-thread figure over 2 batches"
                                          % (args.cpu_steps, B, args.scale)}
+    if not res["check"]["ok"]:
+        print("bench: the stored set failed its check: %s" % json.dumps(res["check"]), file=sys.stderr)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
+def config_of(args, n_edges, world):
+    """The workload's configuration, identical in both arms."""
+    return {"workload": WORKLOAD % (args.scale, args.ef), "scale": args.scale, "edge_factor": args.ef, "batch": args.batch, "edges": n_edges,
+            "bulk": n_edges // 2, "parallelism": "replicas" if world > 1 else "single"}
+
+
 def reference_arm(args, rank, world):
-    """The reference's CPU path for this workload on the host cores (rank 0 only)."""
+    """The reference's CPU path for this workload on the host cores (rank 0
+    only), over the same edge stream as the GPU arm, generated here by the
+    CPU restatement of the device generator (the two are tested equal bit
+    for bit)."""
     if rank != 0:
         return
-    import torch
-    import lpma_gb300 as L  # only to generate the identical edge stream on the device
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    n_raw = (1 << args.scale) * args.ef
-    raw = torch.empty(n_raw, dtype=torch.int64, device="cuda")
-    n = L.gen_rmat_device(args.seed, args.scale, args.ef, raw)
-    e = raw[:n]
-    L.shuffle_device(args.seed + 1000, e)
-    edges = e.cpu().numpy().view(np.uint64)
+    from oracle import pyoracle as O
+    edges = O.shuffle(O.rmat_edges(replica_seed(args.seed, 0), args.scale, args.ef), replica_seed(args.seed, 0) + 1000)
+    n = int(edges.size)
     threads = os.cpu_count() or 1
     B = args.batch
     steps = args.steps
@@ -805,12 +967,12 @@ def reference_arm(args, rank, world):
     out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "edges/s", "n_gpus": world,
            "steps": steps, "warmup": args.warmup, "ms_per_step": sum(cb["lat"]) * 1e3 / steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-           "data": "synthetic (seeded R-MAT)",
-           "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.ef, "batch": B, "edges": n},
+           "data": "synthetic (seeded R-MAT)", "config": config_of(args, n, world),
            "cpu_baseline": {"value": cb["value"], "unit": "edges/s", "cores": threads, "kind": "port",
+                            "load_s": cb["load_s"],
                             "sample": "%d alternating insert/delete batches of %d edges (sorted-merge CSR rebuild "
-                                      "per batch; the reference GPU build does not compile under CUDA 13)"
-                                      % (steps, B)},
+                                      "per batch, after the bulk load of the stored half; the reference GPU build "
+                                      "does not compile under CUDA 13)" % (steps, B)},
            "e2e": {"value": cb["value"], "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

@@ -28,3 +28,44 @@ def test_cpu_baseline_batches_wrap():
     e = O.shuffle(O.rmat_edges(3, 10, 8), 4)
     r = bench.cpu_baseline((e, e.size // 2), 3000, 12, 2)  # 12 batches of 3000 > the 8K-edge stream
     assert len(r["lat"]) == 12 and r["value"] > 0
+
+
+class _OracleAsEngine:
+    """The oracle behind the two calls the bench's check makes."""
+
+    def __init__(self, o):
+        self.o = o
+
+    def export_sorted(self):
+        return self.o.export_sorted()
+
+    def to_csr(self):
+        return self.o.csr()
+
+
+def test_set_check_follows_the_stream_and_catches_a_wrong_set():
+    import torch
+    import bench
+    from oracle import pyoracle as O
+    V = 1 << 10
+    e = O.shuffle(O.rmat_edges(5, 10, 8), 6)
+    half = e.size // 2
+    S = torch.from_numpy(e[:half].view(np.int64))
+    o = O.OracleLpma(V)
+    o.update(ins=e[:half])
+    chk = bench.SetCheck(S, V)
+    B = 500
+    st = bench.Stream(torch.from_numpy(np.concatenate([e[half:], e[:half]]).view(np.int64)),
+                      torch.from_numpy(np.concatenate([e[:half], e[half:]]).view(np.int64)))
+    for i in range(6):
+        kind = "ins" if i % 2 == 0 else "del"
+        x = st.next(kind, B)
+        s = o.update(ins=x.numpy().view(np.uint64)) if kind == "ins" else o.update(dels=x.numpy().view(np.uint64))
+        chk.batch(kind, x, s, B)
+    chk.point(_OracleAsEngine(o), "six batches")
+    assert chk.summary()["ok"], chk.summary()
+    # a key the stream never deleted goes missing: count and checksums catch it
+    o.update(dels=e[half - 1:half])
+    chk.point(_OracleAsEngine(o), "one key lost")
+    p = chk.summary()["points"][-1]
+    assert not chk.summary()["ok"] and not p["count"] and not p["checksums"]
