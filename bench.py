@@ -779,10 +779,15 @@ def served_arm(args):
                     # latency = queueing (arrival to a worker taking it) + service
                     wait = [(q.t_start_ns - min(q.t_submit_ns, q.arrival_ns)) / 1e6 for q, _ in sel]
                     serv = [(q.t_end_ns - q.t_start_ns) / 1e6 for q, _ in sel]
+                    call = [(q.t_call_ns - q.t_start_ns) / 1e6 for q, _ in sel]
+                    dev = [q.device_ms for q, _ in sel]
                     stat[kind] = {"n": len(lat), "p50_ms": float(np.percentile(lat, 50)),
                                   "p99_ms": float(np.percentile(lat, 99)), "errors": bad,
                                   "queue_p99_ms": float(np.percentile(wait, 99)),
-                                  "service_p99_ms": float(np.percentile(serv, 99))}
+                                  "service_p99_ms": float(np.percentile(serv, 99)),
+                                  "call_p99_ms": float(np.percentile(call, 99)),
+                                  "device_p99_ms": float(np.percentile(dev, 99)),
+                                  "pool_growths": sum(1 for q, _ in sel if q.pool_growth_bytes)}
             # the slowest requests of the run: when each arrived, how long it
             # queued, how long it ran, its graph and size
             order = sorted(range(len(reqs)), key=lambda i: reqs[i][1].arrival_ns - reqs[i][1].t_end_ns)[:5]
@@ -794,7 +799,10 @@ def served_arm(args):
             order = sorted(range(len(reqs)), key=lambda i: reqs[i][1].t_start_ns - reqs[i][1].t_end_ns)[:5]
             stat["longest_service"] = [
                 {"kind": reqs[i][0], "at_ms": round((reqs[i][1].arrival_ns - t0_ns) / 1e6, 2),
-                 "service_ms": round((reqs[i][1].t_end_ns - reqs[i][1].t_start_ns) / 1e6, 3), "graph": plan[i][1],
+                 "service_ms": round((reqs[i][1].t_end_ns - reqs[i][1].t_start_ns) / 1e6, 3),
+                 "call_ms": round((reqs[i][1].t_call_ns - reqs[i][1].t_start_ns) / 1e6, 3),
+                 "device_ms": round(reqs[i][1].device_ms, 3),
+                 "pool_growth_mb": round(reqs[i][1].pool_growth_bytes / 2 ** 20, 1), "graph": plan[i][1],
                  "edges": reqs[i][2], "height": [reqs[i][1].stats.height_before, reqs[i][1].stats.height_after],
                  "rebuilt": reqs[i][1].stats.rebuilt} for i in order]
             stat["resident_gb"] = sum(rpma.memory_bytes(G["g"]) for G in gs.graphs) / 1e9

@@ -382,8 +382,17 @@ typedef struct {
     uint64_t reached;           /* BFS: vertices reached; neighbours: total */
     LpmaStats stats;            /* update */
     uint64_t t_submit_ns, t_start_ns, t_end_ns;
+    /* where a request's service time went: t_call_ns is when the library
+     * call returned (its host part, launches and host waits inside the call
+     * included); device_ms the interval between two events recorded on the
+     * worker's stream before and after the request's work (GPU time plus
+     * any gap while the host had not yet launched); pool_growth_bytes how
+     * much the update memory pool's reserved memory grew meanwhile (new
+     * device memory mapped during the request) */
+    uint64_t t_call_ns;
+    uint64_t pool_growth_bytes;
+    float device_ms;
     volatile uint32_t done;
-    uint32_t reserved;
 } LpmaRequest;
 
 LPMA_API lpma_status_t lpma_pool_create(uint32_t n_workers, uint64_t hbm_budget_bytes, LpmaPool **out);

@@ -74,7 +74,8 @@ class LpmaRequest(ctypes.Structure):
                 ("status", ctypes.c_int), ("levels", ctypes.c_uint32), ("reached", ctypes.c_uint64),
                 ("stats", LpmaStats),
                 ("t_submit_ns", ctypes.c_uint64), ("t_start_ns", ctypes.c_uint64), ("t_end_ns", ctypes.c_uint64),
-                ("done", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("t_call_ns", ctypes.c_uint64), ("pool_growth_bytes", ctypes.c_uint64), ("device_ms", ctypes.c_float),
+                ("done", ctypes.c_uint32)]
 
 
 class LpmaBatch(ctypes.Structure):

@@ -274,6 +274,13 @@ cudaMemPool_t batch_pool() {
 
 }  // namespace
 
+uint64_t lpma::pool_reserved_bytes() {
+    cudaMemPool_t pool = batch_pool();
+    uint64_t v = 0;
+    if (pool) cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &v);
+    return v;
+}
+
 cudaError_t lpma::pool_alloc(void **p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool = batch_pool();
     return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMallocAsync(p, bytes, s);

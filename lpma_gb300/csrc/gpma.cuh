@@ -17,6 +17,8 @@ struct GpmaState;
 
 // stream-ordered allocation from the engine's memory pool (abi.cu)
 cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s);
+// reserved bytes of the current device's update memory pool
+uint64_t pool_reserved_bytes();
 
 lpma_status_t gpma_create(uint32_t num_vertices, double density_lower, cudaStream_t s, GpmaState **out);
 void gpma_destroy(GpmaState *g);

@@ -20,9 +20,9 @@
 
 #include <cuda_runtime.h>
 
-#include "prims.cuh"
-
+#include "gpma.cuh"
 #include "lpma.h"
+#include "prims.cuh"
 
 namespace {
 
@@ -103,11 +103,16 @@ struct LpmaPool {
         cudaSetDevice(device);
         cudaStream_t s = nullptr;
         cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
         for (;;) {
             uint64_t est = 0;
             LpmaRequest *r = take(est);
             if (!r) break;
             r->t_start_ns = now_ns();
+            const uint64_t pool0 = lpma::pool_reserved_bytes();
+            cudaEventRecord(ev0, s);
             lpma_status_t st = LPMA_ERR_INVALID_ARGUMENT;
             const lpma_stream_t ls = (lpma_stream_t)s;
             switch (r->kind) {
@@ -132,12 +137,20 @@ struct LpmaPool {
                     st = lpma_edge_query(r->graph, r->keys0, r->n0, r->thres, r->out_u32, ls);
                     break;
             }
+            r->t_call_ns = now_ns();
+            cudaEventRecord(ev1, s);
             const cudaError_t ce = lpma::host_wait(s, true);
             if (st == LPMA_OK && ce != cudaSuccess) st = LPMA_ERR_CUDA;
             r->status = st;
             r->t_end_ns = now_ns();
+            float ms = 0.f;
+            r->device_ms = cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess ? ms : -1.f;
+            const uint64_t pool1 = lpma::pool_reserved_bytes();
+            r->pool_growth_bytes = pool1 > pool0 ? pool1 - pool0 : 0;
             finish(r, est);
         }
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
         cudaStreamDestroy(s);
     }
 };
