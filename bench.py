@@ -81,6 +81,31 @@ def replica_seed(seed, rank):
     return seed + 7919 * rank
 
 
+def l2_copy_gbs(device):
+    """Copy bandwidth with both buffers resident in the 129 MB L2 (two 32 MB
+    tensors copied back and forth, read + write bytes over CUDA-event time,
+    best of 5): the bound of kernels whose passes run out of L2."""
+    import torch
+    a = torch.empty(4 << 20, dtype=torch.int64, device=device)
+    b = torch.empty_like(a)
+    a.fill_(1)
+    for _ in range(20):
+        b.copy_(a)
+        a.copy_(b)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+            a.copy_(b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 100 * 2 * a.numel() * 8 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -441,7 +466,7 @@ def gpu_arm(args, rank, world):
     res = {"t": t, "lat": lat, "wall": wall, "launches": launches, "clocks": clk.summary(), "stats": stats,
            "pstats": pstats, "prof": prof, "sweep": sweep, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
            "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"], "sort_tiers": tiers,
-           "check": check.summary()}
+           "check": check.summary(), "l2_gbs": l2_copy_gbs(device)}
     host_edges = None
     if rank == 0 and not args.no_cpu_baseline:
         host_edges = (e.cpu().numpy().view(np.uint64), int(S.shape[0]))
@@ -449,11 +474,16 @@ def gpu_arm(args, rank, world):
     return res, host_edges
 
 
-def roofline(res, B, peak, peak_kind):
+def roofline(res, B, peak, peak_kind, name=None):
+    """The dominant kernel's (or `name`'s) algorithmic bytes per launch over
+    its average launch time, against the measured HBM and L2 bandwidths."""
     prof = res["prof"]
     if not prof:
         return None
-    name = max(prof, key=lambda k: prof[k][1])
+    if name is None:
+        name = max(prof, key=lambda k: prof[k][1])
+    if name not in prof:
+        return None
     cnt, ms = prof[name]
     pst = res["pstats"]
     # algorithmic bytes per launch of the dominant kernel
@@ -490,8 +520,11 @@ def roofline(res, B, peak, peak_kind):
             p = line.split()
             if len(p) >= 3 and p[0] == name:
                 traffic = float(p[1]) * (units / float(p[2]) if float(p[2]) else 1.0)
+    l2 = res.get("l2_gbs")
     return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "l2_peak": l2, "l2_frac": (achieved / l2) if l2 else None,
+            "l2_peak_kind": "measured in this run (L2-resident copy, 2 x 32 MB)",
             "bytes_per_launch": alg, "per_unit_bytes": per_unit, "unit_desc": unit_name,
             "launches": cnt, "avg_launch_us": avg_s * 1e6,
             "kernel_share": {k: round(v[1] / sum(x[1] for x in prof.values()), 4) for k, v in prof.items()},
@@ -918,6 +951,8 @@ def main():
             "hbm_GBps": sum(16 * B + 18 * x["slots_rewritten"] for x in res["stats"]) / res["t"] / 1e9,
             "hbm_frac": sum(16 * B + 18 * x["slots_rewritten"] for x in res["stats"]) / res["t"] / 1e9 / peak}}),
         "roofline": roofline(res, B, peak, peak_kind),
+        # the batch sort runs out of L2: its figure against both bounds
+        "sort_roofline": roofline(res, B, peak, peak_kind, "sort_coop"),
         "rebalance_roofline": rebalance_roofline(res, peak, peak_kind),
         "e2e": {"value": B * res["e2e_steps"] * world / res["t_e2e"], "unit": "edges/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"], "entry": "lpma_update_host (pinned host batch)"},
