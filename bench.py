@@ -533,7 +533,7 @@ def roofline(res, B, peak, peak_kind, name=None):
 
 REBALANCE_CLASSES = (
     ("single", ("exec_single",)),
-    ("small", ("exec_small4", "exec_small32")),
+    ("small", ("exec_small", "exec_small4", "exec_small32")),
     ("big", ("exec_gather", "exec_spread", "seg_counts", "seg_q", "scan")),
 )
 
@@ -966,6 +966,7 @@ def main():
                                                        "fill_empty")}
     out["slots_rewritten_per_step"] = sum(x["slots_rewritten"] for x in s) / len(s)
     out["single_windows_per_step"] = sum(x["windows_single"] for x in s) / len(s)
+    out["multi_windows_per_step"] = sum(x["windows_small"] - x["windows_single"] for x in s) / len(s)
     alg = 16 * B + 18 * out["slots_rewritten_per_step"]
     out["batch_hbm"] = {"alg_bytes_per_step": alg, "achieved_GBps": alg / (res["t"] / args.steps) / 1e9,
                         "frac": alg / (res["t"] / args.steps) / 1e9 / peak}

@@ -480,9 +480,9 @@ lpma_status_t exec_plan(LpmaHandle *h, const UpdList &u, uint32_t n_list, uint32
                    n_big = h->hst->n_big;
     Geo g{h->c.keys, h->c.vals, h->H};
     if (!small_done) {
-        launch_exec_small(h->wsingle, n_single, 0, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-        launch_exec_small(h->wsmall4, n_small4, 1, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
-        launch_exec_small(h->wsmall, n_small, 2, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        launch_exec_single(h->wsingle, n_single, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres, h->dst, s);
+        launch_exec_multi(h->wsmall4, n_small4, h->wsmall, n_small, g, h->c.cnt, h->c.fl, h->sent, h->V, u, thres,
+                          h->dst, s);
     }
     st->windows_single += n_single;
     st->windows_small += n_single + n_small4 + n_small;
@@ -610,7 +610,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     // round trip: the executors read their counts on the device and do
     // nothing when the plan overflowed, so they run while the host decides
     // what else the call needs.  The read-back and the 4- and 32-segment
-    // executors run on a second stream (a parallel branch of the captured
+    // executors (one launch) run on a second stream (a parallel branch of the captured
     // graph): the single-segment executor follows the planner directly, as
     // its programmatic dependent, and the windows of the three are
     // disjoint.  The join makes everything after them on s wait for all.
@@ -629,12 +629,10 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     CK(cudaStreamIsCapturing(s, &cs));
     CK(cudaEventRecordWithFlags(blocking_waits(h) ? h->front_ev_blk : h->front_ev, side,
                                 cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
-    launch_exec_small(h->wsmall4, (uint32_t)n, 1, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
-                      true);
-    launch_exec_small(h->wsmall, (uint32_t)n, 2, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, side,
-                      true);
+    launch_exec_multi(h->wsmall4, (uint32_t)n, h->wsmall, (uint32_t)n, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u,
+                      thres, h->dst, side, true);
     if (fork) CK(cudaEventRecord(h->join_ev, side));
-    launch_exec_small(h->wsingle, (uint32_t)n, 0, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
+    launch_exec_single(h->wsingle, (uint32_t)n, ge, h->c.cnt, h->c.fl, h->sent, h->V, h->u, thres, h->dst, s, true);
     if (fork) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     return LPMA_OK;
 }

@@ -76,14 +76,17 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
                  uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
                  uint8_t *pend, DevStatus *st, cudaStream_t s);
 
-// in-place executors for windows of <= 32 segments: kind 0 the
-// single-segment list (DevStatus::n_single), 1 windows of 2..4 segments
-// (n_small4), 2 windows of 5..32 segments (n_small).  guarded: launched
-// before the host has read the plan (n_cap an upper bound), the executor
+// in-place executors for windows of <= 32 segments: the single-segment
+// list (DevStatus::n_single), and in one launch the windows of 2..4
+// segments (n_small4) and of 5..32 segments (n_small).  guarded: launched
+// before the host has read the plan (the caps an upper bound), the executor
 // does nothing when the plan overflowed or the batch was rejected.
-void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s,
-                       bool guarded = false);
+void launch_exec_single(const Window *w, uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+                        uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s,
+                        bool guarded = false);
+void launch_exec_multi(const Window *w4, uint32_t cap4, const Window *w32, uint32_t cap32, Geo g, uint8_t *cnt,
+                       ulonglong2 *fl, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
+                       cudaStream_t s, bool guarded = false);
 
 // per-segment counts for the tile grain: qi/qd from the update list
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,

@@ -76,9 +76,18 @@ cudaError_t event_wait(cudaEvent_t ev) {
     return cudaEventSynchronize(ev);
 }
 
+// one thread spins for `cycles` SM clocks (bounded by construction)
+__global__ void k_prof_delay(long long cycles) {
+    if (threadIdx.x) return;
+    const long long t0 = clock64();
+    while (clock64() - t0 < cycles) {
+    }
+}
+
 ProfScope::ProfScope(const char *name, cudaStream_t st) : idx(-1), s(st) {
     if (!g_prof_on) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
+    k_prof_delay<<<1, 32, 0, s>>>(60000);  // about 30 us at 2 GHz
     ProfRec r{name, pool_event(), pool_event()};
     cudaEventRecord(r.a, s);
     g_prof.push_back(r);

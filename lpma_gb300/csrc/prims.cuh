@@ -284,6 +284,12 @@ cudaError_t host_wait(cudaStream_t s, bool blocking);
 // then sleep until it completes.
 cudaError_t event_wait(cudaEvent_t ev);
 
+// In-library profiler: the kernels launched inside a scope are timed with
+// a CUDA event pair on its stream.  Profiled calls launch kernel by kernel
+// (no graph), so before the first event the scope puts a short bounded
+// delay kernel on the stream: the host enqueues the timed launch while the
+// GPU is still busy, and the pair measures device time, not the host's
+// launch latency.
 struct ProfScope {
     ProfScope(const char *name, cudaStream_t s);
     ~ProfScope();

@@ -793,141 +793,193 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
 }
 
 // ------------------------------------------------------------------ multi-segment windows
-// A unit of G groups of 8 lanes rewrites one window of 2..G segments in
-// shared memory: group g loads segment a+g (16-byte loads, 4 slots a lane),
-// the unit scans the per-segment item counts, every group places its kept
-// slots and inserts at their window ranks, then group g writes destination
-// segment g.  G = 4 makes a unit of one warp (windows of 2..4 segments),
-// G = 32 a unit of the whole CTA (5..32 segments).  In place: the unit reads
-// every slot of its window before it writes any.
-constexpr int EM_TPB = 256;
-
-template <int G>
-struct MultiSmem {
-    uint64_t outk[32 / G][32 * G];
-    uint8_t outv[32 / G][32 * G];
-    uint64_t kk[32][32];
-    uint32_t q[32];
-    uint32_t base[32];
-};
-
-template <int G>
-__device__ inline void unit_sync() {
-    if (G == 32)
-        __syncthreads();
-    else
-        __syncwarp();
+// Both classes merge a window the same way: the window's inserts are staged
+// in shared memory at their insert rank (the update list is in key order),
+// the kept keys of the whole window are compacted in slot order, each
+// insert finds its merged rank (insert index + kept keys below it, a binary
+// search) and marks it in a bitmask, and every output slot takes its key by
+// a popcount of the marks below its rank: a marked rank holds the insert of
+// that index, any other the kept key of index rank - marks below.  This is
+// the merge of the per-segment runs the reference performs
+// (block_rebalancing_kernel, rpma.cuh:765-847); destination segment d then
+// receives ranks [first_rank(d), first_rank(d + 1)) of the even spread.  In
+// place: a window's slots are all read before any is written, and windows
+// are disjoint.
+//
+// Windows of 2..4 segments (most of them) take one group of 8 lanes each, so
+// a warp merges 4 windows at once: lane gl of the group loads slots
+// 4gl..4gl+3 of every segment of its window together (16-byte loads), and
+// the window record after the next is already loaded.  The kept keys fill
+// the group's 128-entry row of shared memory from the front and the inserts
+// from the back (together they are the window's m <= 128 items).
+// Windows of 5..32 segments take the whole CTA: group g loads segment a+g.
+// kept_slot with the timestamp test compiled in only for calls that pass an
+// expiry threshold (TH); without one every stored key with a live value is
+// kept
+template <bool TH>
+__device__ __forceinline__ bool kept_t(uint64_t key, uint8_t val, uint32_t thres) {
+    return TH ? kept_slot(key, val, thres) : (key != KEY_NONE && val != VAL_TOMB);
 }
 
-template <int G>
-__device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
-                                                       uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                                                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
-                                                       DevStatus *st, uint32_t bid_, uint32_t nblk_) {
-    __shared__ MultiSmem<G> S;
-    constexpr int UNITS = 32 / G;
+// first_rank for windows of <= 32 segments (k <= 32, m <= 1024): the
+// product fits 32 bits, and a 32-bit division is far cheaper than the
+// 64-bit one
+__device__ __forceinline__ uint32_t first_rank32(uint32_t k, uint32_t m, uint32_t f) { return (k * m + f - 1) / f; }
+
+constexpr int EM_TPB = 256;
+constexpr int EM_GROUPS = EM_TPB / 8;
+constexpr uint32_t EM_SLOTS = 1024;
+
+struct Multi4Smem {  // 2..4-segment windows, one row per group
+    uint64_t k[EM_GROUPS][128];
+    uint8_t v[EM_GROUPS][128];
+    uint32_t im[EM_GROUPS][4];
+};
+struct MultiWarpSmem {  // a window per warp: 4 warps with rows of 1024, or 8 of 128
+    uint64_t k[4 * 1024];
+    uint8_t v[4 * 1024];
+    uint32_t im[4 * 32];   // insert marks by merged rank
+    uint32_t imc[4 * 32];  // marks in the words before
+};
+constexpr size_t EM_SMEM = sizeof(Multi4Smem) > sizeof(MultiWarpSmem) ? sizeof(Multi4Smem) : sizeof(MultiWarpSmem);
+
+template <bool TH>
+__device__ __forceinline__ void k_exec_multi4_body(Multi4Smem &S, const Window *__restrict__ wins,
+                                                   const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
+                                                   uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
+                                                   const UpdList u, uint32_t thres, DevStatus *st, uint32_t bid_,
+                                                   uint32_t nblk_) {
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
-    const int unit = grp / G, ug = grp % G;
+    uint64_t *K = S.k[grp];
+    uint8_t *KV = S.v[grp];
+    uint32_t *IM = S.im[grp];
     const uint32_t nwin = min(*n_win, n_cap);
-    for (uint32_t wi = bid_ * UNITS + unit; wi < nwin; wi += nblk_ * UNITS) {
-        const Window W = wins[wi];
-        const bool active = (uint32_t)ug < W.f;
-        const uint32_t s = W.a + ug;
-        uint64_t k[4] = {KEY_NONE, KEY_NONE, KEY_NONE, KEY_NONE};
-        uint8_t v[4] = {0, 0, 0, 0};
-        uint32_t kmask = 0, us = W.hi, ue = W.hi;
-        uint64_t j = 0;
-        if (active) {
-            j = heap_of_linear(s, g.H);
-            const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
-            const ulonglong2 a = kp[0], b = kp[1];
-            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
-            k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+    const uint32_t stride = nblk_ * EM_GROUPS;
+    uint32_t wi = bid_ * EM_GROUPS + grp;
+    Window Wn{};
+    if (wi < nwin) Wn = wins[wi];
+    for (; __any_sync(0xffffffffu, wi < nwin); wi += stride) {
+        const bool active = wi < nwin;
+        const Window W = Wn;
+        if (wi + stride < nwin) Wn = wins[wi + stride];
+        const uint32_t f = active ? min(W.f, 4u) : 0u;
+        // segment rounds: as many as the warp's largest window needs
+        const uint32_t fmax = __reduce_max_sync(0xffffffffu, f);
+        // every segment's slots and the update bounds load together
+        uint64_t k[4][4];
+        uint32_t v4[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                v[q] = (uint8_t)(v4 >> (8 * q));
-                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
-            }
-            us = lb_seg(u.seg, W.lo, W.hi, s);
-            ue = lb_seg(u.seg, us, W.hi, s + 1);
-        }
-        const uint32_t nl = __popc(kmask);
-        uint32_t incl = nl;
-#pragma unroll
-        for (int o = 1; o < 8; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 8);
-            if (gl >= o) incl += y;
-        }
-        const uint32_t kbase = incl - nl;
-        const uint32_t nk = __shfl_sync(0xffffffffu, incl, 7, 8);
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if ((kmask >> q) & 1u) S.kk[grp][kbase + __popc(kmask & ((1u << q) - 1))] = k[q];
-        const uint32_t ip0 = u.ip[us];
-        const uint32_t nins = u.ip[ue] - ip0;
-        if (gl == 0) S.q[grp] = active ? nk + nins : 0;
-        unit_sync<G>();
-        if (gl == 0) {
-            uint32_t b = 0;
-            for (int t = 0; t < ug; t++) b += S.q[unit * G + t];
-            S.base[grp] = b;
-        }
-        unit_sync<G>();
-        const uint32_t base = S.base[grp];
-        uint64_t *outk = S.outk[unit];
-        uint8_t *outv = S.outv[unit];
-        // kept slots: rank = kept before + inserts of the segment below the key
-        // (a segment with deletes only needs no search: its deletes are
-        // tombstones already)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if ((kmask >> q) & 1u) {
-                const uint32_t below = nins ? u.ip[lb_key(u.key, us, ue, k[q])] - ip0 : 0;
-                const uint32_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
-                if (r < 32 * G) {
-                    outk[r] = k[q];
-                    outv[r] = v[q];
-                }
+        for (int r = 0; r < 4; r++) {
+            k[r][0] = k[r][1] = k[r][2] = k[r][3] = KEY_NONE;
+            v4[r] = 0;
+            if ((uint32_t)r < f) {
+                const uint64_t j = heap_of_linear(W.a + r, g.H);
+                const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+                const ulonglong2 a = kp[0], b = kp[1];
+                k[r][0] = a.x, k[r][1] = a.y, k[r][2] = b.x, k[r][3] = b.y;
+                v4[r] = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
             }
         }
-        // inserts: rank = inserts before + kept keys below
-        for (uint32_t x = us + gl; nins && x < ue; x += 8) {
-            if (u.kind[x] != KIND_INS) continue;
+        const uint32_t ip0 = active ? u.ip[W.lo] : 0u;
+        const uint32_t nins = active ? u.ip[W.hi] - ip0 : 0u;
+        // inserts from the back of the row, rank r at 127 - r
+        for (uint32_t x = W.lo + gl; active && nins && x < W.hi; x += 8) {
+            const uint8_t kd = u.kind[x];
+            const uint32_t r = u.ip[x] - ip0;
             const uint64_t y = u.key[x];
+            const uint8_t yv = u.val[x];
+            if (kd == KIND_INS && r < 128) {
+                K[127 - r] = y;
+                KV[127 - r] = yv;
+            }
+        }
+        // kept keys from the front, in slot order
+        uint32_t nk = 0;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if ((uint32_t)r >= fmax) break;
+            uint32_t kmask = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if ((uint32_t)r < f && kept_t<TH>(k[r][q], (uint8_t)(v4[r] >> (8 * q)), thres)) kmask |= 1u << q;
+            const uint32_t nl = __popc(kmask);
+            uint32_t incl = nl;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, 8);
+                if (gl >= o) incl += y;
+            }
+            const uint32_t base = nk + incl - nl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if ((kmask >> q) & 1u) {
+                    const uint32_t c = base + __popc(kmask & ((1u << q) - 1));
+                    if (c < 128) {
+                        K[c] = k[r][q];
+                        KV[c] = (uint8_t)(v4[r] >> (8 * q));
+                    }
+                }
+            nk += __shfl_sync(0xffffffffu, incl, 7, 8);
+        }
+        if (gl < 4) IM[gl] = 0;
+        __syncwarp();
+        const uint32_t m = nk + nins;
+        const bool ok = active && m == W.m && m <= 32u * W.f && W.f <= 4u && W.f >= 1u;
+        // inserts: merged rank = insert index + kept keys below, marked
+        for (uint32_t i = gl; ok && i < nins; i += 8) {
+            const uint64_t y = K[127 - i];
             uint32_t L = 0, R = nk;
             while (L < R) {
                 const uint32_t mid = (L + R) >> 1;
-                if (S.kk[grp][mid] < y)
+                if (K[mid] < y)
                     L = mid + 1;
                 else
                     R = mid;
             }
-            const uint32_t r = base + (u.ip[x] - ip0) + L;
-            if (r < 32 * G) {
-                outk[r] = y;
-                outv[r] = u.val[x];
-            }
+            const uint32_t r = i + L;
+            if (r < 128) atomicOr(&IM[r >> 5], 1u << (r & 31));
         }
-        unit_sync<G>();
-        const uint32_t total = S.base[unit * G + W.f - 1] + S.q[unit * G + W.f - 1];
-        if (total != W.m || W.m > 32u * W.f) {
-            if (ug == 0 && gl == 0) {
-                atomicOr(&st->sticky, ERR_INTERNAL);
-                atomicCAS(&st->sticky_site, 0u, 1u);
-            }
-        } else if (active) {
-            // destination segment ug of the even spread
-            const uint64_t f0 = first_rank(ug, W.m, W.f), f1 = first_rank(ug + 1, W.m, W.f);
-            const uint32_t cnk = (uint32_t)(f1 - f0);
+        __syncwarp();
+        if (active && !ok && gl == 0) {
+            atomicOr(&st->sticky, ERR_INTERNAL);
+            atomicCAS(&st->sticky_site, 0u, 1u);
+        }
+        const uint32_t w0 = IM[0], w1 = IM[1], w2 = IM[2], w3 = IM[3];
+        const uint32_t c1 = __popc(w0), c2 = c1 + __popc(w1), c3 = c2 + __popc(w2);
+        // row position of merged rank rk: an insert from the back, a kept key
+        // from the front
+        auto row_of = [&](uint32_t rk) -> uint32_t {
+            const uint32_t wd = rk >> 5, bit = 1u << (rk & 31);
+            const uint32_t w = wd == 0 ? w0 : wd == 1 ? w1 : wd == 2 ? w2 : w3;
+            const uint32_t below = (wd == 0 ? 0u : wd == 1 ? c1 : wd == 2 ? c2 : c3) + __popc(w & (bit - 1));
+            return ((w & bit) ? 127 - below : rk - below) & 127;
+        };
+        uint32_t f1 = 0;  // first rank of the segment after
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if ((uint32_t)r >= fmax) break;
+            if (!ok || (uint32_t)r >= f) continue;
+            const uint32_t f0 = f1;
+            f1 = first_rank32(r + 1, m, f);
+            const uint32_t cnk = f1 - f0;
+            const uint64_t j = heap_of_linear(W.a + r, g.H);
             uint64_t o[4];
-            uint32_t ov = 0;
+            uint32_t ovw = 0;
+            // the marks of this lane's 4 ranks rb..rb+3, and the marks below rb
+            const uint32_t rb = f0 + 4 * gl, wd = (rb >> 5) & 3, sh = rb & 31;
+            const uint32_t wa = wd == 0 ? w0 : wd == 1 ? w1 : wd == 2 ? w2 : w3;
+            const uint32_t wb = wd == 0 ? w1 : wd == 1 ? w2 : wd == 2 ? w3 : 0u;
+            const uint32_t bits = (wa >> sh) | (sh ? wb << (32 - sh) : 0u);
+            const uint32_t below0 = (wd == 0 ? 0u : wd == 1 ? c1 : wd == 2 ? c2 : c3) + __popc(wa & ((1u << sh) - 1));
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const uint32_t slot = 4 * gl + q;
                 o[q] = KEY_NONE;
                 if (slot < cnk) {
-                    o[q] = outk[f0 + slot];
-                    ov |= (uint32_t)outv[f0 + slot] << (8 * q);
+                    const uint32_t below = below0 + __popc(bits & ((1u << q) - 1));
+                    const uint32_t at = (((bits >> q) & 1u) ? 127 - below : rb + q - below) & 127;
+                    o[q] = K[at];
+                    ovw |= (uint32_t)KV[at] << (8 * q);
                     if (is_sentinel(o[q])) {
                         const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
                         if (row < V) sent[row] = (uint32_t)(32 * j + slot);
@@ -937,27 +989,227 @@ __device__ __forceinline__ void k_exec_multi_body(const Window *__restrict__ win
             ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(g.keys + 32 * j + 4 * gl);
             kp[0] = make_ulonglong2(o[0], o[1]);
             kp[1] = make_ulonglong2(o[2], o[3]);
-            *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ov;
+            *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ovw;
             if (gl == 0) {
-                cnt[s] = (uint8_t)cnk;
-                fl[j] = cnk ? make_ulonglong2(outk[f0], outk[f1 - 1]) : make_ulonglong2(KEY_NONE, KEY_NONE);
+                cnt[W.a + r] = (uint8_t)cnk;
+                fl[j] = cnk ? make_ulonglong2(o[0], K[row_of(f1 - 1)]) : make_ulonglong2(KEY_NONE, KEY_NONE);
             }
         }
-        unit_sync<G>();
+        __syncwarp();
     }
+}
+
+// A window of up to ROW / 32 segments on one warp: its 4 groups take 4
+// segments a round (group q: segment 4r + q), so a window of <= 4 segments
+// is one round; the next round's slots load while a round compacts.  The
+// row holds the kept keys from the front and the inserts from the back.
+template <uint32_t ROW, bool TH>
+__device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV, uint32_t *IM, uint32_t *IMC,
+                                                       const Window *__restrict__ wins,
+                                                       const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
+                                                       uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
+                                                       const UpdList u, uint32_t thres, DevStatus *st, uint32_t wid,
+                                                       uint32_t nwarps) {
+    constexpr uint32_t WORDS = ROW / 32, MAXF = ROW / 32;
+    const int lane = threadIdx.x & 31, gl = lane & 7, gq = lane >> 3;
+    const uint32_t nwin = min(*n_win, n_cap);
+    for (uint32_t wi = wid; wi < nwin; wi += nwarps) {  // uniform over the warp
+        const Window W = wins[wi];
+        const uint32_t f = min(W.f, MAXF);
+        const uint32_t rounds = (f + 3) / 4;
+        auto load = [&](uint32_t r, uint64_t (&k)[4], uint32_t &v4) {
+            const uint32_t sg = 4 * r + gq;
+            k[0] = k[1] = k[2] = k[3] = KEY_NONE;
+            v4 = 0;
+            if (sg < f) {
+                const uint64_t j = heap_of_linear(W.a + sg, g.H);
+                const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+                const ulonglong2 a = kp[0], b = kp[1];
+                k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+                v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
+            }
+        };
+        uint64_t kn[4];
+        uint32_t vn;
+        load(0, kn, vn);
+        const uint32_t ip0 = u.ip[W.lo];
+        const uint32_t nins = u.ip[W.hi] - ip0;
+        // inserts from the back of the row, rank r at ROW - 1 - r
+        for (uint32_t x = W.lo + lane; nins && x < W.hi; x += 32) {
+            const uint8_t kd = u.kind[x];
+            const uint32_t r = u.ip[x] - ip0;
+            const uint64_t y = u.key[x];
+            const uint8_t yv = u.val[x];
+            if (kd == KIND_INS && r < ROW) {
+                K[ROW - 1 - r] = y;
+                KV[ROW - 1 - r] = yv;
+            }
+        }
+        // kept keys from the front, in slot order (lane order within a round)
+        uint32_t nk = 0;
+        for (uint32_t r = 0; r < rounds; r++) {
+            uint64_t k[4] = {kn[0], kn[1], kn[2], kn[3]};
+            const uint32_t v4 = vn;
+            if (r + 1 < rounds) load(r + 1, kn, vn);
+            uint32_t kmask = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (kept_t<TH>(k[q], (uint8_t)(v4 >> (8 * q)), thres)) kmask |= 1u << q;
+            const uint32_t nl = __popc(kmask);
+            uint32_t incl = nl;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const uint32_t base = nk + incl - nl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if ((kmask >> q) & 1u) {
+                    const uint32_t c = base + __popc(kmask & ((1u << q) - 1));
+                    if (c < ROW) {
+                        K[c] = k[q];
+                        KV[c] = (uint8_t)(v4 >> (8 * q));
+                    }
+                }
+            nk += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if ((uint32_t)lane < WORDS) IM[lane] = 0;
+        __syncwarp();
+        const uint32_t m = nk + nins;
+        const bool ok = m == W.m && m <= 32u * W.f && W.f <= MAXF;
+        // inserts: merged rank = insert index + kept keys below, marked
+        for (uint32_t i = lane; ok && i < nins; i += 32) {
+            const uint64_t y = K[ROW - 1 - i];
+            uint32_t L = 0, R = nk;
+            while (L < R) {
+                const uint32_t mid = (L + R) >> 1;
+                if (K[mid] < y)
+                    L = mid + 1;
+                else
+                    R = mid;
+            }
+            const uint32_t r = i + L;
+            if (r < ROW) atomicOr(&IM[r >> 5], 1u << (r & 31));
+        }
+        __syncwarp();
+        {
+            const uint32_t c = (uint32_t)lane < WORDS ? __popc(IM[lane]) : 0u;
+            uint32_t x = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if ((uint32_t)lane < WORDS) IMC[lane] = x - c;
+        }
+        __syncwarp();
+        if (!ok) {
+            if (lane == 0) {
+                atomicOr(&st->sticky, ERR_INTERNAL);
+                atomicCAS(&st->sticky_site, 0u, 1u);
+            }
+        } else {
+            auto row_of = [&](uint32_t rk) -> uint32_t {
+                const uint32_t w = IM[rk >> 5], bit = 1u << (rk & 31);
+                const uint32_t below = IMC[rk >> 5] + __popc(w & (bit - 1));
+                return ((w & bit) ? ROW - 1 - below : rk - below) & (ROW - 1);
+            };
+            for (uint32_t r = 0; r < rounds; r++) {
+                const uint32_t sg = 4 * r + gq;
+                if (sg >= f) continue;
+                const uint32_t f0 = first_rank32(sg, m, f), f1 = first_rank32(sg + 1, m, f);
+                const uint32_t cnk = f1 - f0;
+                const uint64_t j = heap_of_linear(W.a + sg, g.H);
+                uint64_t o[4];
+                uint32_t ovw = 0;
+                const uint32_t rb = f0 + 4 * gl, wd = (rb >> 5) & (WORDS - 1), sh = rb & 31;
+                const uint32_t wa = IM[wd], wb = wd + 1 < WORDS ? IM[wd + 1] : 0u;
+                const uint32_t bits = (wa >> sh) | (sh ? wb << (32 - sh) : 0u);
+                const uint32_t below0 = IMC[wd] + __popc(wa & ((1u << sh) - 1));
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint32_t slot = 4 * gl + q;
+                    o[q] = KEY_NONE;
+                    if (slot < cnk) {
+                        const uint32_t below = below0 + __popc(bits & ((1u << q) - 1));
+                        const uint32_t at = (((bits >> q) & 1u) ? ROW - 1 - below : rb + q - below) & (ROW - 1);
+                        o[q] = K[at];
+                        ovw |= (uint32_t)KV[at] << (8 * q);
+                        if (is_sentinel(o[q])) {
+                            const uint32_t row = (uint32_t)(o[q] >> SRC_SHIFT);
+                            if (row < V) sent[row] = (uint32_t)(32 * j + slot);
+                        }
+                    }
+                }
+                ulonglong2 *kp = reinterpret_cast<ulonglong2 *>(g.keys + 32 * j + 4 * gl);
+                kp[0] = make_ulonglong2(o[0], o[1]);
+                kp[1] = make_ulonglong2(o[2], o[3]);
+                *reinterpret_cast<uint32_t *>(g.vals + 32 * j + 4 * gl) = ovw;
+                if (gl == 0) {
+                    cnt[W.a + sg] = (uint8_t)cnk;
+                    fl[j] = cnk ? make_ulonglong2(o[0], K[row_of(f1 - 1)]) : make_ulonglong2(KEY_NONE, KEY_NONE);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// The 2..4-segment list: one window per 8-lane group (4 per warp) when the
+// list holds more windows than the grid has warps, else one per warp (a
+// single round, the shorter chain when few windows run).
+template <bool TH>
+__device__ __forceinline__ void exec_multi4(unsigned char *smem, const Window *__restrict__ w4,
+                                            const uint32_t *__restrict__ n4, uint32_t cap4, Geo g, uint8_t *cnt,
+                                            ulonglong2 *fl, uint32_t *sent, uint32_t V, const UpdList u,
+                                            uint32_t thres, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+    const uint32_t warps = nblk_ * (EM_TPB / 32);
+    if (min(*n4, cap4) > warps) {
+        k_exec_multi4_body<TH>(*reinterpret_cast<Multi4Smem *>(smem), w4, n4, cap4, g, cnt, fl, sent, V, u, thres, st,
+                           bid_, nblk_);
+    } else {
+        MultiWarpSmem &S = *reinterpret_cast<MultiWarpSmem *>(smem);
+        const uint32_t w = threadIdx.x >> 5;
+        k_exec_multi_warp_body<128, TH>(S.k + 128 * w, S.v + 128 * w, S.im + 4 * w, S.imc + 4 * w, w4, n4, cap4, g, cnt,
+                                    fl, sent, V, u, thres, st, bid_ * (EM_TPB / 32) + w, warps);
+    }
+}
+
+// The 5..32-segment list: one window per warp, 4 warps a block (rows of
+// 1024 entries).
+template <bool TH>
+__device__ __forceinline__ void exec_multi32(unsigned char *smem, const Window *__restrict__ w32,
+                                             const uint32_t *__restrict__ n32, uint32_t cap32, Geo g, uint8_t *cnt,
+                                             ulonglong2 *fl, uint32_t *sent, uint32_t V, const UpdList u,
+                                             uint32_t thres, DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+    const uint32_t w = threadIdx.x >> 5;
+    if (w >= 4) return;
+    MultiWarpSmem &S = *reinterpret_cast<MultiWarpSmem *>(smem);
+    k_exec_multi_warp_body<1024, TH>(S.k + 1024 * w, S.v + 1024 * w, S.im + 32 * w, S.imc + 32 * w, w32, n32, cap32, g,
+                                 cnt, fl, sent, V, u, thres, st, bid_ * 4 + w, nblk_ * 4);
 }
 
 // a plan that overflowed or a rejected batch: the guarded executors skip
 __device__ __forceinline__ bool plan_void(const DevStatus *st) { return (st->ovf | st->error) != 0; }
 
-template <int G>
-__global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
-                                                       uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                                                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres,
-                                                       DevStatus *st, int guarded) {
+// Both multi-segment classes in one launch: the first gridDim.x - nb4
+// blocks run the 5..32-segment windows one CTA each, the last nb4 blocks
+// the 2..4-segment windows one 8-lane group each.
+template <bool TH>
+__global__ void __launch_bounds__(EM_TPB, 4) k_exec_multi(const Window *__restrict__ w4, const uint32_t *__restrict__ n4,
+                                                       uint32_t cap4, uint32_t nb4, const Window *__restrict__ w32,
+                                                       const uint32_t *__restrict__ n32, uint32_t cap32, Geo g,
+                                                       uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
+                                                       const UpdList u, uint32_t thres, DevStatus *st, int guarded) {
+    __shared__ __align__(16) unsigned char smem[EM_SMEM];
     griddep_wait();
     if (guarded && plan_void(st)) return;
-    k_exec_multi_body<G>(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
+    const uint32_t nb32 = gridDim.x - nb4;
+    if (blockIdx.x < nb32)
+        exec_multi32<TH>(smem, w32, n32, cap32, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, nb32);
+    else
+        exec_multi4<TH>(smem, w4, n4, cap4, g, cnt, fl, sent, V, u, thres, st, blockIdx.x - nb32, nb4);
 }
 
 // ------------------------------------------------------------------ single-segment windows
@@ -974,6 +1226,7 @@ __global__ void __launch_bounds__(EM_TPB) k_exec_multi(const Window *__restrict_
 constexpr int ES_TPB = 256;
 constexpr int ES_GROUPS = ES_TPB / 8;
 
+template <bool TH>
 __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wins,
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
@@ -1022,7 +1275,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if (active && kept_slot(k[q], (uint8_t)(v4 >> (8 * q)), thres)) kmask |= 1u << q;
+            if (active && kept_t<TH>(k[q], (uint8_t)(v4 >> (8 * q)), thres)) kmask |= 1u << q;
         // exclusive prefix of kept counts across the group
         const uint32_t nl = __popc(kmask);
         uint32_t incl = nl;
@@ -1123,6 +1376,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
     }
 }
 
+template <bool TH>
 __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restrict__ wins,
                                                         const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                         uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
@@ -1130,7 +1384,7 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_exec_single(const Window *__restr
                                                         int guarded) {
     griddep_wait();
     if (guarded && plan_void(st)) return;
-    k_exec_single_body(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
+    k_exec_single_body<TH>(wins, n_win, n_cap, g, cnt, fl, sent, V, u, thres, st, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ tile grain
@@ -1437,24 +1691,23 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
     note_launch(2);
 }
 
-void launch_exec_small(const Window *w, uint32_t n_cap, int kind, Geo g, uint8_t *cnt, ulonglong2 *fl,
-                       uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s,
-                       bool guarded) {
+void launch_exec_single(const Window *w, uint32_t n_cap, Geo g, uint8_t *cnt, ulonglong2 *fl, uint32_t *sent,
+                        uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s, bool guarded) {
     if (!n_cap) return;
-    const int gd = guarded ? 1 : 0;
-    if (kind == 0) {
-        ProfScope ps_("exec_single", s);
-        launch_pdl(k_exec_single, dim3(grid_for(n_cap, ES_GROUPS, 152 * 8)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap,
-                   g, cnt, fl, sent, V, u, thres, st, gd);
-    } else if (kind == 1) {
-        ProfScope ps_("exec_small4", s);
-        launch_pdl(k_exec_multi<4>, dim3(grid_for(n_cap, 8, 152 * 8)), dim3(EM_TPB), 0, s, w, &st->n_small4, n_cap, g,
-                   cnt, fl, sent, V, u, thres, st, gd);
-    } else {
-        ProfScope ps_("exec_small32", s);
-        launch_pdl(k_exec_multi<32>, dim3(grid_for(n_cap, 1, 152 * 8)), dim3(EM_TPB), 0, s, w, &st->n_small, n_cap, g,
-                   cnt, fl, sent, V, u, thres, st, gd);
-    }
+    ProfScope ps_("exec_single", s);
+    launch_pdl(thres ? k_exec_single<true> : k_exec_single<false>, dim3(grid_for(n_cap, ES_GROUPS, 152 * 8)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap, g,
+               cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
+    note_launch();
+}
+
+void launch_exec_multi(const Window *w4, uint32_t cap4, const Window *w32, uint32_t cap32, Geo g, uint8_t *cnt,
+                       ulonglong2 *fl, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
+                       cudaStream_t s, bool guarded) {
+    const uint32_t nb4 = cap4 ? grid_for(cap4, EM_GROUPS, 152 * 8) : 0, nb32 = cap32 ? grid_for(cap32, 4, 152 * 8) : 0;
+    if (!nb4 && !nb32) return;
+    ProfScope ps_("exec_small", s);
+    launch_pdl(thres ? k_exec_multi<true> : k_exec_multi<false>, dim3(nb4 + nb32), dim3(EM_TPB), 0, s, w4, &st->n_small4, cap4, nb4, w32, &st->n_small,
+               cap32, g, cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
     note_launch();
 }
 
@@ -1656,18 +1909,23 @@ __global__ void __launch_bounds__(ES_TPB, 4) k_forest_exec_single(const ForestEx
                                                                    const uint32_t *boff, uint32_t G) {
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestExec &e = E[g];
-    k_exec_single_body(e.w[0], &e.st->n_single, e.n[0], e.g, e.cnt, e.fl, e.sent, e.V, e.u, 0, e.st,
+    k_exec_single_body<false>(e.w[0], &e.st->n_single, e.n[0], e.g, e.cnt, e.fl, e.sent, e.V, e.u, 0, e.st,
                        blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 template <int GS>
-__global__ void __launch_bounds__(EM_TPB) k_forest_exec_multi(const ForestExec *__restrict__ E, const uint32_t *boff,
-                                                              uint32_t G) {
+__global__ void __launch_bounds__(EM_TPB, 4) k_forest_exec_multi(const ForestExec *__restrict__ E, const uint32_t *boff,
+                                                                 uint32_t G) {
     constexpr int K = GS == 4 ? 1 : 2;
+    __shared__ __align__(16) unsigned char smem[EM_SMEM];
     const uint32_t g = forest_job_of(boff, G, blockIdx.x);
     const ForestExec &e = E[g];
-    k_exec_multi_body<GS>(e.w[K], K == 1 ? &e.st->n_small4 : &e.st->n_small, e.n[K], e.g, e.cnt, e.fl, e.sent, e.V,
-                          e.u, 0, e.st, blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+    if (GS == 4)
+        exec_multi4<false>(smem, e.w[K], &e.st->n_small4, e.n[K], e.g, e.cnt, e.fl, e.sent, e.V, e.u, 0, e.st,
+                    blockIdx.x - boff[g], boff[g + 1] - boff[g]);
+    else
+        exec_multi32<false>(smem, e.w[K], &e.st->n_small, e.n[K], e.g, e.cnt, e.fl, e.sent, e.V, e.u, 0, e.st,
+                     blockIdx.x - boff[g], boff[g + 1] - boff[g]);
 }
 
 __global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restrict__ F, DevStatus *out) {
@@ -1680,7 +1938,7 @@ __global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restr
 
 uint32_t exec_ctas(int kind, uint32_t n) {
     if (!n) return 0;
-    return grid_for(n, kind == 0 ? ES_GROUPS : (kind == 1 ? 8 : 1), 152 * 8);
+    return grid_for(n, kind == 0 ? ES_GROUPS : (kind == 1 ? EM_GROUPS : 4), 152 * 8);
 }
 
 void launch_forest_exec(int kind, const ForestExec *E, const uint32_t *boff, uint32_t G, uint32_t nblocks,
