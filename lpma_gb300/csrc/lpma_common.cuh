@@ -95,8 +95,9 @@ struct DevStatus {
     uint32_t sticky_site;  // which internal check set ERR_INTERNAL (first one)
 };
 
-// A rebalance window chosen by the planner (maximal executed window).
-struct Window {
+// A rebalance window chosen by the planner (maximal executed window); 8-byte
+// aligned so that a record loads as three 64-bit words.
+struct __align__(8) Window {
     uint32_t a;      // first linear segment
     uint32_t f;      // segments (clipped)
     uint32_t m;      // items after the update

@@ -1342,13 +1342,15 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         if (ok) {
             uint64_t o[4];
             uint32_t ov = 0;
+            // marks of this lane's slots 4gl..4gl+3 and the marks below them
+            const uint32_t bits = imask >> (4 * gl), below0 = __popc(imask & ((1u << (4 * gl)) - 1));
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const uint32_t slot = 4 * gl + q;
                 o[q] = KEY_NONE;
                 if (slot < m) {
-                    const uint32_t below = __popc(imask & ((1u << slot) - 1));
-                    if ((imask >> slot) & 1u) {
+                    const uint32_t below = below0 + __popc(bits & ((1u << q) - 1));
+                    if ((bits >> q) & 1u) {
                         o[q] = ik[grp][below];
                         ov |= (uint32_t)iv[grp][below] << (8 * q);
                     } else {
@@ -1695,7 +1697,9 @@ void launch_exec_single(const Window *w, uint32_t n_cap, Geo g, uint8_t *cnt, ul
                         uint32_t V, const UpdList u, uint32_t thres, DevStatus *st, cudaStream_t s, bool guarded) {
     if (!n_cap) return;
     ProfScope ps_("exec_single", s);
-    launch_pdl(thres ? k_exec_single<true> : k_exec_single<false>, dim3(grid_for(n_cap, ES_GROUPS, 152 * 8)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap, g,
+    // one wave of resident blocks (4 a SM at 64 registers), each looping over
+    // its windows: a second, partial wave would leave SMs idle at the end
+    launch_pdl(thres ? k_exec_single<true> : k_exec_single<false>, dim3(grid_for(n_cap, ES_GROUPS, 152 * 4)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap, g,
                cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
     note_launch();
 }
