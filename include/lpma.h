@@ -298,8 +298,9 @@ LPMA_API lpma_status_t lpma_update_batch(LpmaBatcher *b, LpmaHandle *const *grap
 
 /* ---- autotuner: the batch-sort algorithm per batch-size bucket ----
  * The update front sorts each batch with one of five algorithms ("tiers"):
- * 1 one CTA through shared memory (<= 2048 keys), 2 one 1024-thread CTA
- * with keys in registers (<= 8192), 3 register-sorted tiles plus
+ * 1 one CTA through shared memory (<= 2048 keys), 2 tiles of 2048 keys
+ * sorted by all-pairs rank over many CTAs, then placed by binary searches
+ * across the tiles (<= 16384), 3 register-sorted tiles plus
  * merge-path rounds (<= 2^24), 4 one cooperative launch for all digit
  * passes (handles without LPMA_FLAG_CONCURRENT), 5 three launches per digit
  * pass.  All give the same order.  lpma_autotune times every usable tier on

@@ -826,10 +826,91 @@ __device__ __forceinline__ void block_sort_inreg(uint64_t *keys, uint16_t *vals,
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_SORT_TPB, 1) k_block_sort(uint64_t *keys, uint16_t *vals, uint32_t n,
-                                                                   SortMask mask) {
+// The block tier: n <= RANK2_MAX pairs sorted by ranks, in two launches.
+// Phase 1 sorts tiles of RANK_TILE pairs by all-pairs rank: the stable
+// position of key i in its tile is the number of the tile's keys below it
+// plus its equal keys earlier in the input.  Each CTA stages its tile in
+// shared memory and ranks RANK_KEYS of its keys, RANK_SPLIT threads a key
+// over interleaved slices of the tile, so a batch of 1024 keys spreads over
+// 32 SMs (about 900 instructions a thread) where one CTA's digit passes
+// serialise on one SM.  The ranked tiles land in (k1, v1).  Phase 2 puts
+// every pair at its final position in (k0, v0): its place in its tile plus,
+// for each other tile, the keys that precede it there (keys <= it in earlier
+// tiles, < it in later ones: equal keys keep their input order), by binary
+// searches over the whole batch staged in shared memory.  A single tile is
+// copied back instead.
+constexpr uint32_t RANK_TILE = 2048, RANK2_MAX = 8 * RANK_TILE, RANK_TPB = 256, RANK_SPLIT = 8,
+                   RANK_KEYS = RANK_TPB / RANK_SPLIT, RANK_CPT = RANK_TILE / RANK_KEYS;
+
+__global__ void __launch_bounds__(RANK_TPB) k_rank_tiles(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ v0,
+                                                         uint64_t *__restrict__ k1, uint16_t *__restrict__ v1,
+                                                         uint32_t n) {
+    __shared__ uint64_t sk[RANK_TILE];
     griddep_wait();
-    block_sort_inreg(keys, vals, n, active_bytes(mask));
+    const uint32_t tile = blockIdx.x / RANK_CPT, part_blk = blockIdx.x % RANK_CPT;
+    const uint32_t off = tile * RANK_TILE;
+    if (off >= n) return;
+    const uint32_t len = min(RANK_TILE, n - off);
+    for (uint32_t i = threadIdx.x; i < len; i += RANK_TPB) sk[i] = k0[off + i];
+    __syncthreads();
+    const uint32_t i = part_blk * RANK_KEYS + threadIdx.x / RANK_SPLIT, part = threadIdx.x % RANK_SPLIT;
+    const uint64_t ki = i < len ? sk[i] : 0ull;
+    uint32_t rank = 0;
+    if (i < len)
+        for (uint32_t j = part; j < len; j += RANK_SPLIT) {
+            const uint64_t kj = sk[j];
+            rank += (kj < ki || (kj == ki && j < i)) ? 1u : 0u;
+        }
+#pragma unroll
+    for (uint32_t o = RANK_SPLIT / 2; o; o >>= 1) rank += __shfl_down_sync(0xffffffffu, rank, o, RANK_SPLIT);
+    if (part == 0 && i < len) {
+        k1[off + rank] = ki;
+        v1[off + rank] = v0[off + i];
+    }
+}
+
+// phase 2 of a one-tile batch: the sorted tile goes home
+__global__ void __launch_bounds__(1024) k_rank_back(uint64_t *__restrict__ k0, uint16_t *__restrict__ v0,
+                                                    const uint64_t *__restrict__ k1, const uint16_t *__restrict__ v1,
+                                                    uint32_t n) {
+    griddep_wait();
+    for (uint32_t i = threadIdx.x; i < n && n <= RANK_TILE; i += 1024) {
+        k0[i] = k1[i];
+        v0[i] = v1[i];
+    }
+}
+
+// phase 2 of a batch of several tiles (n * 8 bytes of dynamic shared memory)
+__global__ void __launch_bounds__(RANK_TPB) k_rank_merge(uint64_t *__restrict__ k0, uint16_t *__restrict__ v0,
+                                                         const uint64_t *__restrict__ k1,
+                                                         const uint16_t *__restrict__ v1, uint32_t n) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t *sk = reinterpret_cast<uint64_t *>(smem_raw);
+    griddep_wait();
+    if (n > RANK2_MAX) return;
+    for (uint32_t i = threadIdx.x; i < n; i += RANK_TPB) sk[i] = k1[i];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * RANK_TPB + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t key = sk[i];
+    const uint32_t t = i / RANK_TILE, ntiles = (n + RANK_TILE - 1) / RANK_TILE;
+    uint32_t rank = i - t * RANK_TILE;
+    for (uint32_t u = 0; u < ntiles; u++) {
+        if (u == t) continue;
+        const uint32_t a = u * RANK_TILE, len = min(RANK_TILE, n - a);
+        uint32_t L = 0, R = len;  // keys of tile u that precede `key`
+        while (L < R) {
+            const uint32_t mid = (L + R) >> 1;
+            const uint64_t x = sk[a + mid];
+            if (u < t ? x <= key : x < key)
+                L = mid + 1;
+            else
+                R = mid;
+        }
+        rank += L;
+    }
+    k0[rank] = key;
+    v0[rank] = v1[i];
 }
 
 // ---------------------------------------------------------------- tile-merge sort
@@ -1128,7 +1209,7 @@ static bool tier_ok(SortTier t, uint32_t n, const SortScratch &s) {
     uint32_t tl, G;
     switch (t) {
         case TIER_SMALL: return n <= (uint32_t)SORT_TILE;
-        case TIER_BLOCK: return sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX;
+        case TIER_BLOCK: return sizeof(V) == 2 && n <= RANK2_MAX;
         case TIER_TILE_MERGE: return sizeof(V) == 2 && n <= (1u << 24);
         case TIER_COOP: return coop_geometry<V>(n, s, &tl, &G);
         case TIER_MULTIPASS:
@@ -1141,8 +1222,8 @@ static bool tier_ok(SortTier t, uint32_t n, const SortScratch &s) {
 // the measured cutovers of this build (used until a tuning run says otherwise)
 template <typename V>
 static SortTier tier_default(uint32_t n, const SortScratch &s) {
+    if (sizeof(V) == 2 && n <= RANK2_MAX) return TIER_BLOCK;
     if (sizeof(V) == 2 && n > TM_TILE_MAX && n <= TM_MAX) return TIER_TILE_MERGE;
-    if (sizeof(V) == 2 && n <= (uint32_t)BLOCK_SORT_MAX) return TIER_BLOCK;
     if (tier_ok<V>(TIER_COOP, n, s)) return TIER_COOP;
     if (n <= (uint32_t)SORT_TILE) return TIER_SMALL;
     // without a cooperative launch (concurrent handles) the merge rounds beat
@@ -1181,10 +1262,18 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         return cudaGetLastError();
     }
     if (tier == TIER_BLOCK) {
+        if (sizeof(V) != 2 || n > RANK2_MAX) return cudaErrorInvalidValue;
         ProfScope ps("sort_block", st);
-        launch_pdl(k_block_sort, dim3(1), dim3(BLOCK_SORT_TPB), sizeof(BlockSortSmem), st, k0,
-                   reinterpret_cast<uint16_t *>(v0), n, mask);
-        note_launch();
+        uint16_t *p0 = reinterpret_cast<uint16_t *>(v0), *p1 = reinterpret_cast<uint16_t *>(v1);
+        const uint32_t ntiles = (n + RANK_TILE - 1) / RANK_TILE;
+        launch_pdl(k_rank_tiles, dim3((ntiles - 1) * RANK_CPT + (n - (ntiles - 1) * RANK_TILE + RANK_KEYS - 1) / RANK_KEYS),
+                   dim3(RANK_TPB), 0, st, k0, p0, k1, p1, n);
+        if (ntiles == 1)
+            launch_pdl(k_rank_back, dim3(1), dim3(1024), 0, st, k0, p0, k1, p1, n);
+        else
+            launch_pdl(k_rank_merge, dim3((n + RANK_TPB - 1) / RANK_TPB), dim3(RANK_TPB), (size_t)n * 8, st, k0, p0, k1,
+                       p1, n);
+        note_launch(2);
         return cudaGetLastError();
     }
     // the 9-bit digit plan belongs to the cooperative sort alone: the
@@ -1306,8 +1395,8 @@ static cudaError_t sort_setup_device(int dev, CoopCtas &out) {
     if ((e = cudaFuncSetAttribute(k_downsweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(PassSmem<uint64_t>))))
         return e;
-    if ((e = cudaFuncSetAttribute(k_block_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(BlockSortSmem))) ||
+    if ((e = cudaFuncSetAttribute(k_rank_merge, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(RANK2_MAX * sizeof(uint64_t)))) ||
         (e = cudaFuncSetAttribute(k_forest_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(BlockSortSmem))) ||
         (e = cudaFuncSetAttribute(k_tm_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,

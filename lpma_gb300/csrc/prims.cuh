@@ -46,7 +46,7 @@ struct SortMask {
 enum SortTier : uint32_t {
     TIER_AUTO = 0,        // the tuned choice, else the default cutovers
     TIER_SMALL = 1,       // one CTA through shared memory, <= 2048 keys, in place
-    TIER_BLOCK = 2,       // one 1024-thread CTA, keys in registers, <= 8192 keys, in place
+    TIER_BLOCK = 2,       // ranks: tiles of 2048 by all-pairs rank, then merged by binary searches, <= 16384 keys, in place
     TIER_TILE_MERGE = 3,  // register-sorted tiles + merge-path rounds, <= 2^24 keys, in place
     TIER_COOP = 4,        // one cooperative launch, all digit passes, ping-pong
     TIER_MULTIPASS = 5,   // three launches per digit pass, ping-pong
@@ -80,8 +80,9 @@ __device__ inline uint32_t active_bytes(SortMask m) {
     return r & m.host_mask;
 }
 
-// One CTA of BLOCK_SORT_TPB threads sorts a batch of up to BLOCK_SORT_MAX
-// (key, u16 payload) pairs in shared memory, in place.
+// One CTA of BLOCK_SORT_TPB threads sorts up to BLOCK_SORT_MAX (key, u16
+// payload) pairs in shared memory, in place: the tiles of the tile-merge
+// sort and of a batched update's sort.
 constexpr int BLOCK_SORT_TPB = 1024, BLOCK_SORT_IPT = 8;
 constexpr int BLOCK_SORT_MAX = BLOCK_SORT_TPB * BLOCK_SORT_IPT;  // 8192
 

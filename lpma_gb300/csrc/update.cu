@@ -13,6 +13,8 @@
 // first level at which a segment's updates are absorbed is a pure function
 // of per-segment counts, and the final layout is that of the maximal
 // executed windows alone (each re-spreads its whole content), executed once.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -84,17 +86,6 @@ __device__ inline uint32_t lb_key(const uint64_t *key, uint32_t lo, uint32_t hi,
     while (lo < hi) {
         uint32_t mid = (lo + hi) >> 1;
         if (key[mid] < k)
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
-__device__ inline uint32_t lb_seg(const uint32_t *seg, uint32_t lo, uint32_t hi, uint32_t s) {
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (seg[mid] < s)
             lo = mid + 1;
         else
             hi = mid;
@@ -828,7 +819,6 @@ __device__ __forceinline__ uint32_t first_rank32(uint32_t k, uint32_t m, uint32_
 
 constexpr int EM_TPB = 256;
 constexpr int EM_GROUPS = EM_TPB / 8;
-constexpr uint32_t EM_SLOTS = 1024;
 
 struct Multi4Smem {  // 2..4-segment windows, one row per group
     uint64_t k[EM_GROUPS][128];
@@ -1629,7 +1619,9 @@ void launch_pack(const uint64_t *ins, const uint8_t *ins_vals, uint32_t n_ins, c
                  DevStatus *st, uint32_t *bitmap, uint32_t bitmap_words, const ulonglong2 *fl, const uint8_t *cnt,
                  uint64_t pf_segs, uint32_t *sup, uint32_t sup_words, uint32_t *sort_bar, cudaStream_t s) {
     ProfScope ps_("pack", s);
-    k_pack<<<grid_for(n_ins + n_del, TPB), TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
+    // enough blocks for the planner bitmap's clear too (16 words a thread)
+    const uint32_t nb = std::max(grid_for(n_ins + n_del, TPB), grid_for(bitmap_words, TPB * 16, 152 * 4));
+    k_pack<<<nb, TPB, 0, s>>>(ins, ins_vals, n_ins, del, n_del, V, thres, key_format, internal,
                                                         keys_out, pay_out, st, bitmap, bitmap_words, fl, cnt, pf_segs,
                                                         sup, sup_words, sort_bar);
     note_launch();
