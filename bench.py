@@ -426,7 +426,8 @@ def gpu_arm(args, rank, world):
     # roofline: per-kernel CUDA events over K more steps of the same stream
     L.profile_enable(True)
     pstats = []
-    prof_steps = min(args.steps, 10)
+    # 30 steps: long enough to take in a root window (one about every 25 batches)
+    prof_steps = min(args.steps, 30)
     for i in range(prof_steps):
         k_ = kinds[(args.warmup + args.steps + i) % 2]
         x, s_ = step(k_, B)

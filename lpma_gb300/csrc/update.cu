@@ -812,6 +812,16 @@ __device__ __forceinline__ bool kept_t(uint64_t key, uint8_t val, uint32_t thres
     return TH ? kept_slot(key, val, thres) : (key != KEY_NONE && val != VAL_TOMB);
 }
 
+// first_rank(k, m, f) with a reciprocal inv = floor((2^64 - 1) / f): the
+// high half of n * inv is floor(n / f) or one less (n = k * m + f - 1 <
+// 2^58 here), so one check replaces a 64-bit division
+__device__ __forceinline__ uint64_t first_rank_recip(uint64_t k, uint64_t m, uint64_t f, uint64_t inv) {
+    const uint64_t n = k * m + f - 1;
+    uint64_t q = __umul64hi(n, inv);
+    if ((q + 1) * f <= n) q++;
+    return q;
+}
+
 // first_rank for windows of <= 32 segments (k <= 32, m <= 1024): the
 // product fits 32 bits, and a 32-bit division is far cheaper than the
 // 64-bit one
@@ -1426,7 +1436,9 @@ __device__ inline uint32_t find_job(const TileJob *jobs, uint32_t njobs, uint32_
 }
 
 constexpr int GT_TPB = 256;  // 32 groups of 8 lanes: one 32-segment tile per CTA
+constexpr uint32_t GT_LOCAL = 8;  // updates of a segment the group merges in registers
 
+template <bool TH>
 __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ jobs, uint32_t njobs, uint32_t ntiles,
                                                    Geo src, const uint32_t *__restrict__ PQ,
                                                    const uint32_t *__restrict__ US, const UpdList u, uint32_t thres,
@@ -1450,7 +1462,7 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 v[q] = (uint8_t)(v4 >> (8 * q));
-                if (kept_slot(k[q], v[q], thres)) kmask |= 1u << q;
+                if (kept_t<TH>(k[q], v[q], thres)) kmask |= 1u << q;
             }
             us = US[s];
             ue = US[s + 1];
@@ -1464,14 +1476,54 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
             if (gl >= o) incl += y;
         }
         const uint32_t kbase = incl - nl;
-        const uint32_t ip0 = active ? u.ip[us] : 0;
+        const uint32_t nupd = ue - us;
+        // a segment with few updates (nearly all of them in a root window)
+        // merges them in registers: lane gl holds update us + gl
+        const bool local = active && nupd <= GT_LOCAL;
+        uint64_t y = KEY_NONE;
+        uint32_t yip = 0;
+        uint8_t yv = 0;
+        bool yins = false;
+        if (local && (uint32_t)gl < nupd) {
+            const uint32_t x = us + gl;
+            yins = u.kind[x] == KIND_INS;
+            y = u.key[x];
+            yip = u.ip[x];
+            yv = u.val[x];
+        }
+        // ip of the segment's first update (every lane takes part in the shuffle)
+        const uint32_t ip0 = __shfl_sync(0xffffffffu, yip, lane & ~7);
+        uint32_t below[4] = {0, 0, 0, 0};
+        uint32_t my_kept_below = 0;  // for this lane's insert: kept slots of the segment below it
+        // as many rounds as the warp's busiest local segment has updates
+        const uint32_t tmax = __reduce_max_sync(0xffffffffu, local ? nupd : 0u);
+        if (tmax) {
+            for (uint32_t t = 0; t < tmax; t++) {
+                const uint64_t yt = __shfl_sync(0xffffffffu, y, (lane & ~7) + t);
+                const bool it = __shfl_sync(0xffffffffu, (int)yins, (lane & ~7) + t) != 0;
+                // the kept keys above insert t count it below them
+#pragma unroll
+                for (int q = 0; q < 4; q++) below[q] += (it && yt < k[q]) ? 1u : 0u;
+                // kept slots below insert t, summed over the group
+                uint32_t c = 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) c += (((kmask >> q) & 1u) && k[q] < yt) ? 1u : 0u;
+                c += __shfl_xor_sync(0xffffffffu, c, 1, 8);
+                c += __shfl_xor_sync(0xffffffffu, c, 2, 8);
+                c += __shfl_xor_sync(0xffffffffu, c, 4, 8);
+                if ((uint32_t)gl == t) my_kept_below = c;
+            }
+        }
         // kept slots: rank = kept before + inserts of this segment below the key
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if ((kmask >> q) & 1u) {
-                uint32_t below = 0;
-                if (ue > us) below = u.ip[lb_key(u.key, us, ue, k[q])] - ip0;
-                const uint64_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + below;
+                uint32_t bl;
+                if (local)
+                    bl = below[q];
+                else
+                    bl = ue > us ? u.ip[lb_key(u.key, us, ue, k[q])] - u.ip[us] : 0u;
+                const uint64_t r = base + kbase + __popc(kmask & ((1u << q) - 1)) + bl;
                 if (r < m_cap) {
                     Mk[r] = k[q];
                     Mv[r] = v[q];
@@ -1481,12 +1533,24 @@ __global__ void __launch_bounds__(GT_TPB) k_gather(const TileJob *__restrict__ j
                 }
             }
         }
+        // this lane's insert of a local segment: inserts before it + kept below
+        if (local && yins) {
+            const uint64_t r = base + (yip - ip0) + my_kept_below;
+            if (r < m_cap) {
+                Mk[r] = y;
+                Mv[r] = yv;
+            } else {
+                atomicOr(&st->sticky, ERR_INTERNAL);
+                atomicCAS(&st->sticky_site, 0u, 4u);
+            }
+        }
         __syncwarp();
     }
 }
 
-// The inserts of big windows, one thread each (a segment may carry millions
-// of them when a bulk load lands in a near-empty tree): rank = segment base
+// The inserts of big windows in segments with more than GT_LOCAL updates,
+// one thread each (a segment may carry millions of them when a bulk load
+// lands in a near-empty tree): rank = segment base
 // + inserts of the segment before it + kept slots of the segment below it.
 // Slots below it that are not kept are the tombstones of the segment's
 // deletes before it in the sorted update list, plus expired keys.
@@ -1509,8 +1573,9 @@ __global__ void __launch_bounds__(TPB) k_gather_ins(const TileJob *__restrict__ 
                 R = mid - 1;
         }
         if (s < jobs[L].sa || s >= jobs[L].sa + jobs[L].sf) continue;  // a small window took it
-        const uint64_t y = u.key[x];
         const uint32_t us = US[s];
+        if (US[s + 1] - us <= GT_LOCAL) continue;  // k_gather merged this segment's updates
+        const uint64_t y = u.key[x];
         const uint32_t ri = u.ip[x] - u.ip[us];
         const uint32_t tomb_below = (x - us) - ri;
         const uint64_t *sk = src.keys + 32 * heap_of_linear(s, src.H);
@@ -1544,6 +1609,7 @@ __global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ j
     const int lane = threadIdx.x & 31, gl = lane & 7, grp = threadIdx.x >> 3;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const TileJob J = jobs[find_job(jobs, njobs, tile, true)];
+        const uint64_t inv = ~0ull / J.df;  // the same for every thread of the tile
         const uint64_t k = 32ull * (tile - J.dtile0) + grp;
         if (k >= J.df) continue;
         const uint64_t mb = PQ[J.sa];
@@ -1554,7 +1620,7 @@ __global__ void __launch_bounds__(GT_TPB) k_spread(const TileJob *__restrict__ j
         if (mb + J.m > m_cap) continue;  // reported above; never read past M
         const uint64_t ds = J.da + k;
         const uint64_t j = heap_of_linear(ds, dst.H);
-        const uint64_t f0 = first_rank(k, J.m, J.df), f1 = first_rank(k + 1, J.m, J.df);
+        const uint64_t f0 = first_rank_recip(k, J.m, J.df, inv), f1 = first_rank_recip(k + 1, J.m, J.df, inv);
         const uint32_t nk = (uint32_t)(f1 - f0);
         uint64_t o[4];
         uint32_t ov = 0;
@@ -1729,8 +1795,8 @@ void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint3
     if (!njobs) return;
     {
         ProfScope ps_("exec_gather", s);
-        k_gather<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv,
-                                                                 m_cap, st);
+        (thres ? k_gather<true> : k_gather<false>)<<<grid_for(stiles, 1, 152 * 8), GT_TPB, 0, s>>>(
+            jobs, njobs, stiles, src, PQ, US, u, thres, Mk, Mv, m_cap, st);
         if (n_upd)
             k_gather_ins<<<grid_for(n_upd, TPB), TPB, 0, s>>>(jobs, njobs, src, PQ, US, u, st, n_upd, thres, Mk, Mv,
                                                               m_cap);
