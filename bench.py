@@ -426,13 +426,18 @@ def gpu_arm(args, rank, world):
     # roofline: per-kernel CUDA events over K more steps of the same stream
     L.profile_enable(True)
     pstats = []
-    # 30 steps: long enough to take in a root window (one about every 25 batches)
-    prof_steps = min(args.steps, 30)
-    for i in range(prof_steps):
-        k_ = kinds[(args.warmup + args.steps + i) % 2]
+    # at least 30 steps, then on until a root window (about one every 25
+    # batches, not strictly periodic) is among them, 60 at most: the big
+    # windows' class is measured too
+    prof_steps = 0
+    while prof_steps < min(args.steps, 60):
+        k_ = kinds[(args.warmup + args.steps + prof_steps) % 2]
         x, s_ = step(k_, B)
         pstats.append(s_)
         check.batch(k_, x, s_, B)
+        prof_steps += 1
+        if prof_steps >= min(args.steps, 30) and any(p["slots_rewritten"] > p["slots_small"] for p in pstats):
+            break
     torch.cuda.synchronize()
     prof = L.profile_report()
     L.profile_enable(False)
