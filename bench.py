@@ -426,11 +426,11 @@ def gpu_arm(args, rank, world):
     # roofline: per-kernel CUDA events over K more steps of the same stream
     L.profile_enable(True)
     pstats = []
-    # at least 30 steps, then on until a root window (about one every 25
-    # batches, not strictly periodic) is among them, 60 at most: the big
-    # windows' class is measured too
+    # at least 30 steps, then on until a root window (one every 25 to 70
+    # batches on this stream, not periodic) is among them, 150 at most: the
+    # big windows' class is measured too
     prof_steps = 0
-    while prof_steps < min(args.steps, 60):
+    while prof_steps < min(args.steps, 150):
         k_ = kinds[(args.warmup + args.steps + prof_steps) % 2]
         x, s_ = step(k_, B)
         pstats.append(s_)
