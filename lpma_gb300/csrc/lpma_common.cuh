@@ -50,6 +50,13 @@ __host__ __device__ inline uint64_t heap_of_linear(uint64_t s, uint32_t H) {
     return ((1ull << level) - 1) + (s1 >> (t + 1));
 }
 
+// heap_of_linear in 32-bit arithmetic, for segment indexes below 2^31 (every
+// tree here: at most 2^(LPMA_MAX_HEIGHT + 1) segments)
+__device__ __forceinline__ uint32_t heap_of_linear32(uint32_t s, uint32_t H) {
+    const uint32_t s1 = s + 1, t = (uint32_t)__ffs((int)s1) - 1;
+    return ((1u << (H - t)) - 1) + (s1 >> (t + 1));
+}
+
 // linear segment of heap index j at level `level` of a tree of height H
 __host__ __device__ inline uint64_t linear_of_heap(uint64_t j, uint32_t level, uint32_t H) {
     uint64_t pos = j - ((1ull << level) - 1);

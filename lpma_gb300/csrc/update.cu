@@ -873,7 +873,7 @@ __device__ __forceinline__ void k_exec_multi4_body(Multi4Smem &S, const Window *
             k[r][0] = k[r][1] = k[r][2] = k[r][3] = KEY_NONE;
             v4[r] = 0;
             if ((uint32_t)r < f) {
-                const uint64_t j = heap_of_linear(W.a + r, g.H);
+                const uint64_t j = heap_of_linear32(W.a + r, g.H);
                 const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
                 const ulonglong2 a = kp[0], b = kp[1];
                 k[r][0] = a.x, k[r][1] = a.y, k[r][2] = b.x, k[r][3] = b.y;
@@ -962,7 +962,7 @@ __device__ __forceinline__ void k_exec_multi4_body(Multi4Smem &S, const Window *
             const uint32_t f0 = f1;
             f1 = first_rank32(r + 1, m, f);
             const uint32_t cnk = f1 - f0;
-            const uint64_t j = heap_of_linear(W.a + r, g.H);
+            const uint64_t j = heap_of_linear32(W.a + r, g.H);
             uint64_t o[4];
             uint32_t ovw = 0;
             // the marks of this lane's 4 ranks rb..rb+3, and the marks below rb
@@ -1022,7 +1022,7 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
             k[0] = k[1] = k[2] = k[3] = KEY_NONE;
             v4 = 0;
             if (sg < f) {
-                const uint64_t j = heap_of_linear(W.a + sg, g.H);
+                const uint64_t j = heap_of_linear32(W.a + sg, g.H);
                 const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * j + 4 * gl);
                 const ulonglong2 a = kp[0], b = kp[1];
                 k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
@@ -1120,7 +1120,7 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
                 if (sg >= f) continue;
                 const uint32_t f0 = first_rank32(sg, m, f), f1 = first_rank32(sg + 1, m, f);
                 const uint32_t cnk = f1 - f0;
-                const uint64_t j = heap_of_linear(W.a + sg, g.H);
+                const uint64_t j = heap_of_linear32(W.a + sg, g.H);
                 uint64_t o[4];
                 uint32_t ovw = 0;
                 const uint32_t rb = f0 + 4 * gl, wd = (rb >> 5) & (WORDS - 1), sh = rb & 31;
@@ -1248,7 +1248,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
     uint32_t nv4 = 0, nip0 = 0, nip1 = 0;
     if (wi < nwin) {
         Wn = wins[wi];
-        jn = heap_of_linear(Wn.a, g.H);
+        jn = heap_of_linear32(Wn.a, g.H);
         const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
         na = kp[0], nb = kp[1];
         nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
@@ -1263,7 +1263,7 @@ __device__ __forceinline__ void k_exec_single_body(const Window *__restrict__ wi
         const uint32_t v4 = nv4, ip0c = nip0, ip1c = nip1;
         if (wi + stride < nwin) {
             Wn = Wnn;
-            jn = heap_of_linear(Wn.a, g.H);
+            jn = heap_of_linear32(Wn.a, g.H);
             const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(g.keys + 32 * jn + 4 * gl);
             na = kp[0], nb = kp[1];
             nv4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * jn + 4 * gl);
