@@ -800,10 +800,13 @@ __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ can
 // Windows of 2..4 segments (most of them) take one group of 8 lanes each, so
 // a warp merges 4 windows at once: lane gl of the group loads slots
 // 4gl..4gl+3 of every segment of its window together (16-byte loads), and
-// the window record after the next is already loaded.  The kept keys fill
+// the next window's record loads while this one merges.  The kept keys fill
 // the group's 128-entry row of shared memory from the front and the inserts
-// from the back (together they are the window's m <= 128 items).
-// Windows of 5..32 segments take the whole CTA: group g loads segment a+g.
+// from the back (together they are the window's m <= 128 items).  When the
+// list holds no more windows than the grid has warps, each window takes a
+// warp instead (one round, a shorter chain).  Windows of 5..32 segments take
+// one warp each with a 1024-entry row, 4 segments a round.
+
 // kept_slot with the timestamp test compiled in only for calls that pass an
 // expiry threshold (TH); without one every stored key with a live value is
 // kept
@@ -1757,8 +1760,8 @@ void launch_exec_single(const Window *w, uint32_t n_cap, Geo g, uint8_t *cnt, ul
     ProfScope ps_("exec_single", s);
     // one wave of resident blocks (4 a SM at 64 registers), each looping over
     // its windows: a second, partial wave would leave SMs idle at the end
-    launch_pdl(thres ? k_exec_single<true> : k_exec_single<false>, dim3(grid_for(n_cap, ES_GROUPS, 152 * 4)), dim3(ES_TPB), 0, s, w, &st->n_single, n_cap, g,
-               cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
+    launch_pdl(thres ? k_exec_single<true> : k_exec_single<false>, dim3(grid_for(n_cap, ES_GROUPS, 152 * 4)),
+               dim3(ES_TPB), 0, s, w, &st->n_single, n_cap, g, cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
     note_launch();
 }
 
@@ -1768,8 +1771,9 @@ void launch_exec_multi(const Window *w4, uint32_t cap4, const Window *w32, uint3
     const uint32_t nb4 = cap4 ? grid_for(cap4, EM_GROUPS, 152 * 8) : 0, nb32 = cap32 ? grid_for(cap32, 4, 152 * 8) : 0;
     if (!nb4 && !nb32) return;
     ProfScope ps_("exec_small", s);
-    launch_pdl(thres ? k_exec_multi<true> : k_exec_multi<false>, dim3(nb4 + nb32), dim3(EM_TPB), 0, s, w4, &st->n_small4, cap4, nb4, w32, &st->n_small,
-               cap32, g, cnt, fl, sent, V, u, thres, st, guarded ? 1 : 0);
+    launch_pdl(thres ? k_exec_multi<true> : k_exec_multi<false>, dim3(nb4 + nb32), dim3(EM_TPB), 0, s, w4,
+               &st->n_small4, cap4, nb4, w32, &st->n_small, cap32, g, cnt, fl, sent, V, u, thres, st,
+               guarded ? 1 : 0);
     note_launch();
 }
 
