@@ -345,6 +345,26 @@ def gpu_arm(args, rank, world):
         from lpma_gb300 import rpma
         tiers = {str(r["keys"]): r["tier"] for r in rpma.autotune(max(args.batch, 1 << 11)) if not r["concurrent"]}
     e, S, ins_seq, del_seq = build_workload(args, device, replica_seed(args.seed, rank))
+    grain = None
+    if not args.no_autotune:
+        # executor cut-overs for this batch size, timed on a scratch copy of
+        # the graph that first runs 20 batches of the stream (the windows of
+        # a fill cycle), with the stream's next insert batch (absent keys);
+        # the timed handle is not touched
+        from lpma_gb300 import rpma
+        scratch = L.Lpma(V)
+        scratch.build(S)
+        sst = Stream(ins_seq, del_seq)
+        for i in range(20):
+            kind = ("ins", "del")[i % 2]
+            x = sst.next(kind, args.batch)
+            scratch.update(ins=x) if kind == "ins" else scratch.update(dels=x)
+        try:
+            timed = rpma.autotune_grain(scratch, sst.next("ins", args.batch), reps=3)
+        except L.LpmaError as ex:  # a small graph: the stream's next batch holds stored keys
+            timed = str(ex)
+        scratch.close()
+        grain = {"timed": timed, "chosen": rpma.grain_get(int(args.batch - 1).bit_length())}
     g = L.Lpma(V)
     g.build(S)
     check = SetCheck(S, V)
@@ -472,7 +492,7 @@ def gpu_arm(args, rank, world):
     res = {"t": t, "lat": lat, "wall": wall, "launches": launches, "clocks": clk.summary(), "stats": stats,
            "pstats": pstats, "prof": prof, "sweep": sweep, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
            "n_edges": int(e.shape[0]), "height": info["height"], "items": info["num_items"], "sort_tiers": tiers,
-           "check": check.summary(), "l2_gbs": l2_copy_gbs(device)}
+           "check": check.summary(), "l2_gbs": l2_copy_gbs(device), "grain": grain}
     host_edges = None
     if rank == 0 and not args.no_cpu_baseline:
         host_edges = (e.cpu().numpy().view(np.uint64), int(S.shape[0]))
@@ -964,6 +984,7 @@ def main():
                 "d2h_bytes_per_step": res["d2h"], "entry": "lpma_update_host (pinned host batch)"},
         "gpu_launches": res["launches"],
         "sort_tiers": res["sort_tiers"],
+        "grain": res["grain"],
         "clocks": res["clocks"],
         "check": res["check"],
     }

@@ -333,6 +333,40 @@ LPMA_API lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, Lp
 LPMA_API lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier);
 LPMA_API lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, uint32_t *tier);
 
+/* ---- executor grain cut-overs per batch-size bucket ----
+ * After planning, every maximal window goes to one of four executors by its
+ * segment count: 1 segment, up to max_segs_group (8-lane-group executor,
+ * 1..4, default 4), up to max_segs_shared (shared-memory executor,
+ * max_segs_group..32, default 32), larger (the tile grain: gather and
+ * spread through the alternate array).  The reference fixes its cut-over
+ * at 1024 slots (rebalance_batch, rpma.cuh:1214-1256).  No setting changes
+ * the layout an update produces, only its speed.  Entry log2_keys serves
+ * batches of 2^(log2_keys-1)+1 .. 2^log2_keys keys, process-wide;
+ * lpma_grain_set(b, 0, 0) restores the defaults, lpma_grain_get reports the
+ * values in effect. */
+typedef struct {
+    uint32_t max_segs_group;
+    uint32_t max_segs_shared;
+    float us_median; /* one insert plus one delete of the batch, CUDA events on the stream */
+    uint32_t reserved;
+} LpmaGrainTime;
+LPMA_API lpma_status_t lpma_grain_set(uint32_t log2_keys, uint32_t max_segs_group, uint32_t max_segs_shared);
+LPMA_API lpma_status_t lpma_grain_get(uint32_t log2_keys, uint32_t *max_segs_group, uint32_t *max_segs_shared);
+/* Times six grain settings ({4, 2} x {32, 16, 8}) on the caller's own leveled
+ * handle: rounds of lpma_update inserting the n device keys and lpma_update
+ * deleting them again, the settings taking turns (one warm-up round each,
+ * then `reps` timed), and keeps the fastest in the entry of n's bucket when
+ * it is at least 3% faster than the defaults (else the defaults).  The
+ * settings only differ where the handle's windows do: tune on a handle in
+ * the state the updates will meet.  The keys must be absent
+ * from the handle: a batch holding a stored key is refused
+ * (LPMA_ERR_INVALID_ARGUMENT) before anything changes.  Afterwards the
+ * handle stores the same set (its layout is another valid one of it).
+ * Writes one LpmaGrainTime per setting timed to out (up to cap) and their
+ * count to *n_out.  Blocks the calling thread; not for GPMA handles. */
+LPMA_API lpma_status_t lpma_autotune_grain(LpmaHandle *h, const uint64_t *d_keys, size_t n, uint32_t reps,
+                                           lpma_stream_t stream, LpmaGrainTime *out, size_t cap, size_t *n_out);
+
 /* Device bytes the handle holds (structure, scratch, views). */
 LPMA_API lpma_status_t lpma_memory_bytes(const LpmaHandle *h, uint64_t *bytes);
 

@@ -29,7 +29,7 @@ EXPORTS = [
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
     "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve", "lpma_debug_sort_barrier",
-    "lpma_config_gpma", "lpma_gpma_view",
+    "lpma_config_gpma", "lpma_gpma_view", "lpma_grain_set", "lpma_grain_get", "lpma_autotune_grain",
 ]
 SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
 REQ_UPDATE, REQ_NEIGHBORS, REQ_BFS, REQ_EDGE_QUERY = 0, 1, 2, 3
@@ -89,6 +89,11 @@ class LpmaTuneEntry(ctypes.Structure):
                 ("reserved", ctypes.c_uint32), ("us", ctypes.c_float * 6)]
 
 
+class LpmaGrainTime(ctypes.Structure):
+    _fields_ = [("max_segs_group", ctypes.c_uint32), ("max_segs_shared", ctypes.c_uint32),
+                ("us_median", ctypes.c_float), ("reserved", ctypes.c_uint32)]
+
+
 class LpmaError(RuntimeError):
     def __init__(self, status, where=""):
         self.status = status
@@ -145,6 +150,9 @@ def load():
         "lpma_autotune": [U32, P, P, SZ, P],
         "lpma_tune_set": [U32, U32, U32],
         "lpma_tune_get": [U32, U32, P],
+        "lpma_grain_set": [U32, U32, U32],
+        "lpma_grain_get": [U32, P, P],
+        "lpma_autotune_grain": [P, P, SZ, U32, P, P, SZ, P],
         "lpma_debug_sort_barrier": [U32, I],
         "lpma_config_gpma": [P],
         "lpma_gpma_view": [P, P, P, P, P, P, P],

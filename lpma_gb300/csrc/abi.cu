@@ -288,6 +288,24 @@ cudaError_t lpma::pool_alloc(void **p, size_t bytes, cudaStream_t s) {
 
 namespace {
 
+// Executor grain cut-overs per batch-size bucket (entry b: batches of
+// 2^(b-1)+1 .. 2^b keys): cut_group | cut_shared << 8, 0 for the defaults
+// (4 and 32 segments).  Process-wide, like the sort tier table.
+std::atomic<uint32_t> g_grain[33];
+
+uint32_t grain_bucket(size_t n) {
+    const uint32_t b = n <= 1 ? 0u : 64u - (uint32_t)__builtin_clzll((unsigned long long)(n - 1));
+    return b > 32 ? 32u : b;
+}
+
+uint32_t grain_word(size_t n) { return g_grain[grain_bucket(n)].load(std::memory_order_relaxed); }
+
+void set_grain(Tables &tb, size_t n) {
+    const uint32_t w = grain_word(n);
+    tb.cut_group = w & 0xFFu;
+    tb.cut_shared = (w >> 8) & 0xFFu;
+}
+
 // Releases the capacity's arena in stream order (s = nullptr: at once, with
 // a device synchronisation).
 void free_cap(Cap &c, cudaStream_t s, bool now = false) {
@@ -602,6 +620,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
                    h->u, h->dst, s);
     // plan the first loop
     Tables tb = make_tables(h, h->H, true);
+    set_grain(tb, n);
     // the status reset cleared the plan counters and k_pack the bitmap
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
                  thres_active ? &h->dst->live_total : &h->dst->total_items, true));
@@ -661,7 +680,8 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
         const uint64_t key[12] = {n_ins, n_del, h->H, thres,
                                   (uint64_t)thres_active | ((uint64_t)(ins_vals != nullptr) << 1) |
                                       ((uint64_t)(h->sort.bar != nullptr) << 2) |
-                                      ((uint64_t)sort_tier_for_update((uint32_t)n, h->sort) << 3),
+                                      ((uint64_t)sort_tier_for_update((uint32_t)n, h->sort) << 3) |
+                                      ((uint64_t)grain_word(n) << 16),
                                   (uint64_t)h->c.keys, (uint64_t)h->c.vals, (uint64_t)h->c.cnt, (uint64_t)h->c.fl,
                                   (uint64_t)h->bk0, (uint64_t)h->c.cnt_live, (uint64_t)h->c.bitmap};
         if (h->graph_gen != h->buf_gen) {
@@ -843,6 +863,7 @@ lpma_status_t finish_update(LpmaHandle *h, lpma_status_t rs, size_t n, uint32_t 
                     launch_live_counts(h->c.keys, h->H, thres, h->c.cnt_live, h->dst, s);
                 }
                 Tables tb2 = make_tables(h, h->H, false);
+                set_grain(tb2, n);
                 r = run_plan(h, h->u2, n2, thres_active, (uint64_t)live_mid, tb2, s);
                 if (r == LPMA_OK) r = sync_status(h, s);
                 if (r == LPMA_OK && h->hst->ovf) {
@@ -1943,6 +1964,99 @@ lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, uint32_t *t
     if (log2_keys > 32 || !tier) return LPMA_ERR_INVALID_ARGUMENT;
     *tier = (uint32_t)sort_tier_get(log2_keys, concurrent ? 1 : 0);
     return LPMA_OK;
+}
+
+lpma_status_t lpma_grain_set(uint32_t log2_keys, uint32_t max_segs_group, uint32_t max_segs_shared) {
+    if (log2_keys > 32) return LPMA_ERR_INVALID_ARGUMENT;
+    if (max_segs_group == 0 && max_segs_shared == 0) {
+        g_grain[log2_keys].store(0, std::memory_order_relaxed);
+        return LPMA_OK;
+    }
+    if (max_segs_group < 1 || max_segs_group > CUT_GROUP_MAX || max_segs_shared < max_segs_group ||
+        max_segs_shared > SMALL_WIN_SEGS)
+        return LPMA_ERR_INVALID_ARGUMENT;
+    g_grain[log2_keys].store(max_segs_group | (max_segs_shared << 8), std::memory_order_relaxed);
+    return LPMA_OK;
+}
+
+lpma_status_t lpma_grain_get(uint32_t log2_keys, uint32_t *max_segs_group, uint32_t *max_segs_shared) {
+    if (log2_keys > 32 || !max_segs_group || !max_segs_shared) return LPMA_ERR_INVALID_ARGUMENT;
+    const uint32_t w = g_grain[log2_keys].load(std::memory_order_relaxed);
+    *max_segs_group = (w & 0xFFu) ? (w & 0xFFu) : CUT_GROUP_DEFAULT;
+    *max_segs_shared = ((w >> 8) & 0xFFu) ? ((w >> 8) & 0xFFu) : SMALL_WIN_SEGS;
+    return LPMA_OK;
+}
+
+// Times the update of the caller's own handle under each candidate grain
+// setting: the batch of absent keys inserted and deleted again (the stored
+// set is the same afterwards; the layout is a valid one of it), and keeps
+// the fastest for the batch's bucket.  Keys already stored are refused
+// before anything changes.
+lpma_status_t lpma_autotune_grain(LpmaHandle *h, const uint64_t *d_keys, size_t n, uint32_t reps,
+                                  lpma_stream_t stream, LpmaGrainTime *out, size_t cap, size_t *n_out) {
+    if (!h || h->gp || !d_keys || !n || n > 0xFFFFFFFFu || !reps || reps > 1000) return LPMA_ERR_INVALID_ARGUMENT;
+    if (h->sticky != LPMA_OK) return h->sticky;
+    cudaStream_t s = (cudaStream_t)stream;
+    {
+        uint32_t *cnt_d = nullptr;
+        CK(dalloc(&cnt_d, 1));
+        uint32_t present = 0;
+        cudaError_t e = cudaMemsetAsync(cnt_d, 0, 4, s);
+        if (!e) {
+            Geo g{h->c.keys, h->c.vals, h->H};
+            launch_count_present(d_keys, (uint32_t)n, h->cfg.key_format, g, h->c.fl, cnt_d, s);
+            e = cudaGetLastError();
+        }
+        if (!e) e = cudaMemcpyAsync(&present, cnt_d, 4, cudaMemcpyDeviceToHost, s);
+        if (!e) e = cudaStreamSynchronize(s);
+        dfree(cnt_d);
+        if (e) return LPMA_ERR_CUDA;
+        if (present) return LPMA_ERR_INVALID_ARGUMENT;
+    }
+    static const uint32_t cand[6][2] = {{4, 32}, {2, 32}, {4, 16}, {2, 16}, {4, 8}, {2, 8}};
+    const uint32_t b = grain_bucket(n);
+    const uint32_t saved = g_grain[b].load(std::memory_order_relaxed);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) || cudaEventCreate(&e1)) {
+        if (e0) cudaEventDestroy(e0);
+        return LPMA_ERR_CUDA;
+    }
+    lpma_status_t r = LPMA_OK;
+    // the settings take turns round by round (round 0 warms each up and
+    // captures its front), so that a drift of the handle or the clocks
+    // spreads over all of them
+    std::vector<float> t[6];
+    for (uint32_t rep = 0; rep <= reps && r == LPMA_OK; rep++) {
+        for (int c = 0; c < 6 && r == LPMA_OK; c++) {
+            g_grain[b].store(cand[c][0] | (cand[c][1] << 8), std::memory_order_relaxed);
+            LpmaStats st{};
+            if (cudaEventRecord(e0, s)) r = LPMA_ERR_CUDA;
+            if (r == LPMA_OK) r = lpma_update(h, d_keys, nullptr, n, nullptr, 0, 0, stream, &st);
+            if (r == LPMA_OK) r = lpma_update(h, nullptr, nullptr, 0, d_keys, n, 0, stream, &st);
+            if (r == LPMA_OK && (cudaEventRecord(e1, s) || cudaEventSynchronize(e1))) r = LPMA_ERR_CUDA;
+            float ms = 0.f;
+            if (r == LPMA_OK && rep > 0 && !cudaEventElapsedTime(&ms, e0, e1)) t[c].push_back(ms * 1000.f);
+        }
+    }
+    // a setting replaces the defaults (the first candidate) only when it is
+    // at least 3% faster: the difference between settings is often within
+    // the noise of a few rounds
+    float med[6] = {0, 0, 0, 0, 0, 0};
+    size_t nout = 0;
+    int best = 0;
+    for (int c = 0; c < 6 && r == LPMA_OK; c++) {
+        std::sort(t[c].begin(), t[c].end());
+        med[c] = t[c].empty() ? 0.f : t[c][t[c].size() / 2];
+        if (out && nout < cap) out[nout] = LpmaGrainTime{cand[c][0], cand[c][1], med[c], 0u};
+        nout++;
+        if (med[c] > 0.f && med[c] < med[best]) best = c;
+    }
+    const uint32_t best_w = (best == 0 || med[best] > 0.97f * med[0]) ? 0u : (cand[best][0] | (cand[best][1] << 8));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_grain[b].store(r == LPMA_OK ? best_w : saved, std::memory_order_relaxed);
+    if (n_out) *n_out = nout;
+    return r;
 }
 
 // Times every usable sort tier on seeded batches of 2^b keys (the update

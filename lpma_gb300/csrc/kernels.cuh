@@ -88,6 +88,11 @@ void launch_exec_multi(const Window *w4, uint32_t cap4, const Window *w32, uint3
                        ulonglong2 *fl, uint32_t *sent, uint32_t V, const UpdList u, uint32_t thres, DevStatus *st,
                        cudaStream_t s, bool guarded = false);
 
+// adds to *count how many of the n keys (key_format as lpma_update's) the
+// tree stores, live or tombstoned; read only
+void launch_count_present(const uint64_t *keys, uint32_t n, uint32_t key_format, Geo g, const ulonglong2 *fl,
+                          uint32_t *count, cudaStream_t s);
+
 // per-segment counts for the tile grain: qi/qd from the update list
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
                               cudaStream_t s);

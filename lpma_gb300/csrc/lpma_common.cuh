@@ -119,7 +119,12 @@ struct Tables {
     // leveled tree's 32 and 2^(H+1) - 1)
     uint32_t seg_len;
     unsigned long long nseg;
+    // executor grain cut-overs (0: the defaults): windows of up to cut_group
+    // segments go to the 8-lane-group executor, up to cut_shared to the
+    // shared-memory one, larger ones to the tile grain
+    uint32_t cut_group, cut_shared;
 };
+constexpr uint32_t CUT_GROUP_DEFAULT = 4, CUT_GROUP_MAX = 4;
 
 __device__ inline uint32_t lanemask_lt() {
     uint32_t r;

@@ -462,6 +462,28 @@ __device__ inline uint64_t block_excl_scan_u64(uint64_t x, uint64_t *wsum) {
     return r;
 }
 
+// How many of n keys the tree stores (live or tombstoned): the locate
+// descent and the membership search of k_resolve_locate, read only.
+__global__ void __launch_bounds__(TPB) k_count_present(const uint64_t *__restrict__ keys, uint32_t n,
+                                                       uint32_t key_format, Geo g, const ulonglong2 *__restrict__ fl,
+                                                       uint32_t *count) {
+    uint32_t c = 0;
+    for (uint32_t i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
+        uint64_t key = keys[i];
+        if (key_format == 1) key = ((key >> 32) << SRC_SHIFT) | ((key & 0xFFFFFFFFull) << DST_SHIFT);
+        uint32_t lvl;
+        const uint64_t j = descend(key, nullptr, 0, fl, g.H, &lvl);
+        const uint64_t *sk = g.keys + 32 * j;
+        uint32_t pos = 0;
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1)
+            if (sk[pos + step - 1] < key) pos += step;
+        c += (pos < 32 && sk[pos] == key) ? 1u : 0u;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
 __device__ __forceinline__ void k_compact_body(const uint64_t *__restrict__ k0, const uint16_t *__restrict__ p0,
                                                  const uint64_t *__restrict__ k1, const uint16_t *__restrict__ p1,
                                                  SortMask mask, const uint8_t *__restrict__ kind,
@@ -704,7 +726,9 @@ __global__ void __launch_bounds__(TPB) k_plan(const UpdList u, uint32_t n_cap, c
 __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
                                                   Window *small, Window *big, const UpdList u, uint8_t *pend,
-                                                  DevStatus *st, uint32_t bid_, uint32_t nblk_) {
+                                                  DevStatus *st, uint32_t bid_, uint32_t nblk_,
+                                                  uint32_t cut_group = CUT_GROUP_DEFAULT,
+                                                  uint32_t cut_shared = SMALL_WIN_SEGS) {
     // updates of segments that no window absorbed stay pending (overflow):
     // each update copies the mark its run's first update (the planner's
     // leader) wrote.  The marks are read only on the overflow paths.
@@ -719,12 +743,13 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
     __shared__ uint32_t base_s[4];
     __shared__ unsigned long long sl[2][TPB / 32];
     const uint32_t c = bid_ * TPB + threadIdx.x;
-    // classes: 0 single segment, 1 two to four, 2 five to 32, 3 larger, 4 none
+    // classes: 0 single segment, 1 two to cut_group (4), 2 up to cut_shared (32),
+    // 3 larger, 4 none
     uint32_t cls = 4;
     Window w{};
     if (c < st->n_cand && c < n_cap) {
         w = cand[c];
-        cls = w.f == 1 ? 0 : (w.f <= 4 ? 1 : (w.f <= SMALL_WIN_SEGS ? 2 : 3));
+        cls = w.f == 1 ? 0 : (w.f <= cut_group ? 1 : (w.f <= cut_shared ? 2 : 3));
         // inside a larger executed window?  The ancestor words are loaded
         // without an early exit so that the loads are in flight together.
         uint32_t hit = 0;
@@ -778,9 +803,10 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
 __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
                                                   Window *small, Window *big, const UpdList u, uint8_t *pend,
-                                                  DevStatus *st) {
+                                                  DevStatus *st, uint32_t cut_group, uint32_t cut_shared) {
     griddep_wait();
-    k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st, blockIdx.x, gridDim.x);
+    k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st, blockIdx.x, gridDim.x, cut_group,
+                    cut_shared);
 }
 
 // ------------------------------------------------------------------ multi-segment windows
@@ -1750,7 +1776,8 @@ void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint
     if (!nb) return;
     launch_pdl(k_plan, dim3(nb), dim3(TPB), 0, s, u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap,
                cand, pend, st);
-    launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st);
+    launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st,
+               tb.cut_group ? tb.cut_group : CUT_GROUP_DEFAULT, tb.cut_shared ? tb.cut_shared : SMALL_WIN_SEGS);
     note_launch(2);
 }
 
@@ -1774,6 +1801,13 @@ void launch_exec_multi(const Window *w4, uint32_t cap4, const Window *w32, uint3
     launch_pdl(thres ? k_exec_multi<true> : k_exec_multi<false>, dim3(nb4 + nb32), dim3(EM_TPB), 0, s, w4,
                &st->n_small4, cap4, nb4, w32, &st->n_small, cap32, g, cnt, fl, sent, V, u, thres, st,
                guarded ? 1 : 0);
+    note_launch();
+}
+
+void launch_count_present(const uint64_t *keys, uint32_t n, uint32_t key_format, Geo g, const ulonglong2 *fl,
+                          uint32_t *count, cudaStream_t s) {
+    if (!n) return;
+    k_count_present<<<grid_for(n, TPB, 152 * 8), TPB, 0, s>>>(keys, n, key_format, g, fl, count);
     note_launch();
 }
 

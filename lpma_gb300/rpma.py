@@ -449,6 +449,31 @@ def tune_set(log2_keys, tier, concurrent=False):
     check(_abi.load().lpma_tune_set(int(log2_keys), 1 if concurrent else 0, int(tier or 0)), "lpma_tune_set")
 
 
+def grain_set(log2_keys, max_segs_group=0, max_segs_shared=0):
+    """Executor cut-overs of one batch-size bucket (0, 0: the defaults 4 and 32)."""
+    check(_abi.load().lpma_grain_set(int(log2_keys), int(max_segs_group), int(max_segs_shared)), "lpma_grain_set")
+
+
+def grain_get(log2_keys):
+    g, sh = ctypes.c_uint32(), ctypes.c_uint32()
+    check(_abi.load().lpma_grain_get(int(log2_keys), ctypes.byref(g), ctypes.byref(sh)), "lpma_grain_get")
+    return g.value, sh.value
+
+
+def autotune_grain(g, keys, reps=3):
+    """lpma_autotune_grain on handle g with a device batch of absent keys;
+    returns one dict per setting timed (the fastest is kept for the batch's
+    bucket)."""
+    cap = 8
+    out = (_abi.LpmaGrainTime * cap)()
+    n = ctypes.c_size_t()
+    p, nk = _dev(keys, "uint64")
+    check(_abi.load().lpma_autotune_grain(g._h, p, nk, int(reps), _stream_ptr(g.stream), out, cap, ctypes.byref(n)),
+          "lpma_autotune_grain")
+    return [{"max_segs_group": e.max_segs_group, "max_segs_shared": e.max_segs_shared,
+             "us": round(e.us_median, 1)} for e in out[:n.value]]
+
+
 def memory_bytes(g):
     b = ctypes.c_uint64()
     check(_abi.load().lpma_memory_bytes(g._h, ctypes.byref(b)), "lpma_memory_bytes")
