@@ -341,9 +341,10 @@ LPMA_API lpma_status_t lpma_tune_get(uint32_t log2_keys, uint32_t concurrent, ui
  * spread through the alternate array).  The reference fixes its cut-over
  * at 1024 slots (rebalance_batch, rpma.cuh:1214-1256).  No setting changes
  * the layout an update produces, only its speed.  Entry log2_keys serves
- * batches of 2^(log2_keys-1)+1 .. 2^log2_keys keys, process-wide;
- * lpma_grain_set(b, 0, 0) restores the defaults, lpma_grain_get reports the
- * values in effect. */
+ * batches of 2^(log2_keys-1)+1 .. 2^log2_keys keys, process-wide, for
+ * lpma_update and lpma_update_host on leveled handles (lpma_update_batch
+ * and GPMA handles keep the defaults); lpma_grain_set(b, 0, 0) restores the
+ * defaults, lpma_grain_get reports the values in effect. */
 typedef struct {
     uint32_t max_segs_group;
     uint32_t max_segs_shared;
