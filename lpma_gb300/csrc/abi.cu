@@ -47,11 +47,12 @@ struct Cap {
     uint32_t Hc = 0;
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     uint8_t *vals = nullptr, *vals_alt = nullptr;
-    uint8_t *cnt = nullptr, *cnt_alt = nullptr, *cnt_live = nullptr, *srcc = nullptr;
+    uint8_t *cnt = nullptr, *cnt_alt = nullptr, *cnt_live = nullptr;
     ulonglong2 *fl = nullptr;
-    uint32_t *segP = nullptr, *q = nullptr, *qn = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
+    uint32_t *segP = nullptr, *PQ = nullptr, *US = nullptr, *qi = nullptr, *qd = nullptr;
     uint32_t *bitmap = nullptr;
     uint32_t *scan_tmp = nullptr;
+    uint64_t *ts_tmp = nullptr;  // block totals of the big windows' prefix scan
     void *arena = nullptr;  // one stream-ordered allocation holding all of the above
 };
 
@@ -330,11 +331,12 @@ cudaError_t alloc_cap(Cap &c, uint32_t Hc, cudaStream_t s) {
         off += (count * sizeof(**p) + 255) & ~size_t(255);
     };
     part(&c.keys, ns), part(&c.keys_alt, ns), part(&c.vals, ns), part(&c.vals_alt, ns);
-    part(&c.cnt, nseg + 64), part(&c.cnt_alt, nseg + 64), part(&c.cnt_live, nseg + 64), part(&c.srcc, nseg + 64);
+    part(&c.cnt, nseg + 64), part(&c.cnt_alt, nseg + 64), part(&c.cnt_live, nseg + 64);
     part(&c.fl, nseg);
-    part(&c.segP, nseg + 2), part(&c.q, nseg + 2), part(&c.qn, nseg + 2), part(&c.PQ, nseg + 2);
+    part(&c.segP, nseg + 2), part(&c.PQ, nseg + 2);
     part(&c.US, nseg + 2), part(&c.qi, nseg + 2), part(&c.qd, nseg + 2);
     part(&c.bitmap, bitmap_words(Hc)), part(&c.scan_tmp, scan_tmp_words((uint32_t)nseg + 2) + 64);
+    part(&c.ts_tmp, tile_prefix_tmp_words(nseg));
     cudaError_t e = pool_alloc(&c.arena, off, s);
     if (e != cudaSuccess) {
         c = Cap{};
@@ -481,10 +483,8 @@ lpma_status_t tile_prep(LpmaHandle *h, const UpdList &u, uint32_t n_list, bool t
     CK(cudaMemsetAsync(h->c.qi, 0, (nseg + 2) * 4, s));
     CK(cudaMemsetAsync(h->c.qd, 0, (nseg + 2) * 4, s));
     launch_seg_update_counts(u, n_list, h->c.qi, h->c.qd, h->dst, s);
-    launch_seg_q(h->c.cnt, thres_active ? h->c.cnt_live : nullptr, h->c.qi, h->c.qd, nseg, h->c.q, h->c.qn, h->c.srcc,
-                 s);
-    CK(scan_u32(h->c.q, h->c.PQ, (uint32_t)nseg, h->c.PQ + nseg, h->c.scan_tmp, s));
-    CK(scan_u32(h->c.qn, h->c.US, (uint32_t)nseg, h->c.US + nseg, h->c.scan_tmp, s));
+    launch_tile_prefix(h->c.cnt, thres_active ? h->c.cnt_live : nullptr, h->c.qi, h->c.qd, nseg, h->c.PQ, h->c.US,
+                       h->c.ts_tmp, s);
     CK(cudaGetLastError());
     return LPMA_OK;
 }

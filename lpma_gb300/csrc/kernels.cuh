@@ -96,9 +96,11 @@ void launch_count_present(const uint64_t *keys, uint32_t n, uint32_t key_format,
 // per-segment counts for the tile grain: qi/qd from the update list
 void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uint32_t *qd, const DevStatus *st,
                               cudaStream_t s);
-// q[s] = kept(s) + ins(s), qn[s] = ins(s) + del(s), srcc[s] = cnt[s]
-void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
-                  uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s);
+// PQ / US: exclusive prefixes over the segments of q = kept + ins - del and
+// qn = ins + del, the totals at [nseg]; tmp holds ceil(nseg / 2048) words
+void launch_tile_prefix(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd,
+                        uint64_t nseg, uint32_t *PQ, uint32_t *US, uint64_t *tmp, cudaStream_t s);
+inline size_t tile_prefix_tmp_words(uint64_t nseg) { return (size_t)((nseg + 2047) / 2048) + 1; }
 
 struct TileJob {      // one window of more than 32 segments, or a rebuild
     uint32_t sa, sf;  // source linear segment range

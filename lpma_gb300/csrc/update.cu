@@ -1432,15 +1432,107 @@ __global__ void __launch_bounds__(TPB) k_seg_update_counts(const UpdList u, uint
     qd[s] = (hi0 - x) - ins;
 }
 
-__global__ void __launch_bounds__(TPB) k_seg_q(const uint8_t *__restrict__ cnt, const uint8_t *__restrict__ cnt_live,
-                                               const uint32_t *__restrict__ qi, const uint32_t *__restrict__ qd,
-                                               uint64_t nseg, uint32_t *q, uint32_t *qn, uint8_t *srcc) {
-    for (uint64_t s = blockIdx.x * (uint64_t)TPB + threadIdx.x; s < nseg; s += gridDim.x * (uint64_t)TPB) {
-        const uint32_t c = cnt[s];
-        const uint32_t cl = cnt_live ? cnt_live[s] : c;
-        q[s] = cl - qd[s] + qi[s];
-        qn[s] = qi[s] + qd[s];
-        srcc[s] = (uint8_t)c;
+// The big windows' prefixes: for every segment s, q = live(s) - deletes(s)
+// + inserts(s) (its items after the update) and qn = inserts(s) +
+// deletes(s) (its updates), and their exclusive prefixes PQ (the window
+// rank base of its items) and US (its first update), PQ[nseg] and
+// US[nseg] the totals.  The pairs are computed where they are read and
+// scanned packed in one u64 (each sum stays below 2^32): a reduce, a top
+// and a down pass.
+constexpr uint32_t TS_IPT = 8, TS_TILE = TPB * TS_IPT;
+
+__device__ __forceinline__ uint64_t seg_pair(const uint8_t *__restrict__ cnt, const uint8_t *__restrict__ cnt_live,
+                                             const uint32_t *__restrict__ qi, const uint32_t *__restrict__ qd,
+                                             uint64_t s) {
+    const uint32_t c = cnt_live ? cnt_live[s] : cnt[s];
+    const uint32_t i = qi[s], d = qd[s];
+    return (uint64_t)(c - d + i) | ((uint64_t)(i + d) << 32);
+}
+
+__global__ void __launch_bounds__(TPB) k_ts_reduce(const uint8_t *__restrict__ cnt, const uint8_t *__restrict__ cnt_live,
+                                                   const uint32_t *__restrict__ qi, const uint32_t *__restrict__ qd,
+                                                   uint64_t nseg, uint64_t *tmp) {
+    __shared__ uint64_t wsum[TPB / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * TS_TILE;
+    uint64_t v = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < TS_IPT; i++) {
+        const uint64_t p = base + (uint64_t)i * TPB + threadIdx.x;
+        if (p < nseg) v += seg_pair(cnt, cnt_live, qi, qd, p);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (int w = 0; w < TPB / 32; w++) t += wsum[w];
+        tmp[blockIdx.x] = t;
+    }
+}
+
+// one CTA: the block totals to exclusive offsets, and the two totals
+__global__ void __launch_bounds__(1024) k_ts_top(uint64_t *tmp, uint32_t nb, uint32_t *pq_total, uint32_t *us_total) {
+    __shared__ uint64_t ws[32];
+    __shared__ uint64_t carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+        const uint32_t i = b0 + threadIdx.x;
+        const uint64_t x = i < nb ? tmp[i] : 0;
+        uint64_t v = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) ws[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            uint64_t t = ws[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            ws[lane] = t;
+        }
+        __syncthreads();
+        if (i < nb) tmp[i] = carry + (w ? ws[w - 1] : 0) + v - x;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += ws[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *pq_total = (uint32_t)carry;
+        *us_total = (uint32_t)(carry >> 32);
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_ts_down(const uint8_t *__restrict__ cnt, const uint8_t *__restrict__ cnt_live,
+                                                 const uint32_t *__restrict__ qi, const uint32_t *__restrict__ qd,
+                                                 uint64_t nseg, const uint64_t *__restrict__ tmp, uint32_t *PQ,
+                                                 uint32_t *US) {
+    __shared__ uint64_t wsum[TPB / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * TS_TILE + (uint64_t)threadIdx.x * TS_IPT;
+    uint64_t x[TS_IPT];
+    uint64_t v = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < TS_IPT; i++) {
+        const uint64_t p = base + i;
+        x[i] = p < nseg ? seg_pair(cnt, cnt_live, qi, qd, p) : 0;
+        v += x[i];
+    }
+    uint64_t off = block_excl_scan_u64(v, wsum) + tmp[blockIdx.x];
+#pragma unroll
+    for (uint32_t i = 0; i < TS_IPT; i++) {
+        const uint64_t p = base + i;
+        if (p < nseg) {
+            PQ[p] = (uint32_t)off;
+            US[p] = (uint32_t)(off >> 32);
+        }
+        off += x[i];
     }
 }
 
@@ -1819,11 +1911,19 @@ void launch_seg_update_counts(const UpdList u, uint32_t n_cap, uint32_t *qi, uin
     note_launch();
 }
 
-void launch_seg_q(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd, uint64_t nseg,
-                  uint32_t *q, uint32_t *qn, uint8_t *srcc, cudaStream_t s) {
-    ProfScope ps_("seg_q", s);
-    k_seg_q<<<grid_for(nseg, TPB), TPB, 0, s>>>(cnt, cnt_live, qi, qd, nseg, q, qn, srcc);
-    note_launch();
+void launch_tile_prefix(const uint8_t *cnt, const uint8_t *cnt_live, const uint32_t *qi, const uint32_t *qd,
+                        uint64_t nseg, uint32_t *PQ, uint32_t *US, uint64_t *tmp, cudaStream_t s) {
+    ProfScope ps_("scan", s);
+    const uint32_t nb = (uint32_t)((nseg + TS_TILE - 1) / TS_TILE);
+    if (!nb) {
+        k_ts_top<<<1, 1024, 0, s>>>(tmp, 0, PQ + nseg, US + nseg);
+        note_launch();
+        return;
+    }
+    k_ts_reduce<<<nb, TPB, 0, s>>>(cnt, cnt_live, qi, qd, nseg, tmp);
+    k_ts_top<<<1, 1024, 0, s>>>(tmp, nb, PQ + nseg, US + nseg);
+    k_ts_down<<<nb, TPB, 0, s>>>(cnt, cnt_live, qi, qd, nseg, tmp, PQ, US);
+    note_launch(3);
 }
 
 void launch_exec_big(const TileJob *jobs, uint32_t njobs, uint32_t stiles, uint32_t dtiles, Geo src,
