@@ -22,8 +22,12 @@ namespace lpma {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int TOPL = 10;               // tree levels staged in shared memory by locate
-constexpr int TOPN = (1 << TOPL) - 1;  // 1023 heap entries = 16 KB of (first, last)
+// tree levels staged in shared memory by every CTA of the locate: 9 levels
+// (511 heap entries = 8 KB of (first, last)) measured faster than 10 or 11
+// (the staging of each persistent CTA costs more than a descent level) and
+// than 8
+constexpr int TOPL = 9;
+constexpr int TOPN = (1 << TOPL) - 1;
 constexpr int LSUM = 8;
 constexpr uint32_t SUP_CHUNKS = 64;     // chunks (of TPB keys) per group total of the locate                // windows up to 2^8 segments sum counts directly
 
