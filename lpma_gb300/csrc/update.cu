@@ -28,8 +28,8 @@ constexpr int TPB = 256;
 // than 8
 constexpr int TOPL = 9;
 constexpr int TOPN = (1 << TOPL) - 1;
-constexpr int LSUM = 8;
-constexpr uint32_t SUP_CHUNKS = 64;     // chunks (of TPB keys) per group total of the locate                // windows up to 2^8 segments sum counts directly
+constexpr int LSUM = 8;                // windows up to 2^8 segments sum counts directly
+constexpr uint32_t SUP_CHUNKS = 64;     // chunks (of TPB keys) per group total of the locate
 
 __device__ inline uint32_t warp_sum(uint32_t v) {
 #pragma unroll
