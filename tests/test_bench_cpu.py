@@ -69,3 +69,23 @@ def test_set_check_follows_the_stream_and_catches_a_wrong_set():
     chk.point(_OracleAsEngine(o), "one key lost")
     p = chk.summary()["points"][-1]
     assert not chk.summary()["ok"] and not p["count"] and not p["checksums"]
+
+
+def test_rebalance_roofline_classes_and_big_fallback():
+    """18 bytes per rewritten slot over each class's kernel time; with no big
+    window among the profiled steps the big class comes from the profiled
+    scratch batches, and the line names that source."""
+    import bench
+    st = {"windows_single": 1000, "slots_small": 32 * 1000 + 640, "slots_rewritten": 32 * 1000 + 640}
+    res = {"prof": {"exec_single": (2, 0.02), "exec_small": (2, 0.004)}, "pstats": [st, st]}
+    rb = bench.rebalance_roofline(res, 1000.0, "test")
+    assert rb["single"]["bytes_per_step"] == 18 * 32000 and rb["small"]["bytes_per_step"] == 18 * 640
+    assert abs(rb["single"]["ms_per_step"] - 0.01) < 1e-12 and rb["big"]["frac"] == 0.0
+    assert "source" not in rb["big"]
+    big = {"windows_single": 10, "slots_small": 320, "slots_rewritten": 320 + (1 << 20)}
+    res["big_alt"] = {"prof": {"exec_gather": (1, 0.2), "exec_spread": (1, 0.1)}, "pstats": [st, big],
+                      "source": "scratch"}
+    rb = bench.rebalance_roofline(res, 1000.0, "test")
+    assert rb["big"]["source"] == "scratch"
+    want = 18 * (big["slots_rewritten"] - big["slots_small"]) / 2
+    assert rb["big"]["bytes_per_step"] == want and abs(rb["big"]["ms_per_step"] - 0.15) < 1e-12
