@@ -52,11 +52,11 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the batch-sort autotuner (lpma_autotune) before the stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served", "skew"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "multigraph", "served", "skew", "gpma"],
                     help="stream: the single-graph update stream (the headline line); multigraph: 256 graphs, one "
                          "batch each per round, pooled vs one plain call per graph; served: Poisson arrivals over "
                          "64 resident graphs, pooled vs one request at a time; skew: hub-heavy mixed batches on "
-                         "2^20 vertices with 64M edges (resize stress)")
+                         "2^20 vertices with 64M edges (resize stress); gpma: the stream on a GPMA-mode handle")
     ap.add_argument("--graphs", type=int, default=256)
     ap.add_argument("--rounds", type=int, default=6)
     ap.add_argument("--workers", type=int, default=16)
@@ -975,12 +975,74 @@ def skew_arm(args):
     print(json.dumps(line))
 
 
+def gpma_arm(args):
+    """GPMA mode (LPMA_FLAG_GPMA: the flat packed memory array of gpma.cuh)
+    on the bench's stream: the same R-MAT graph, bulk half and alternating
+    insert / delete batches of B edges, keys src << 32 | dst; CUDA events
+    per batch on the update stream, inputs resident in HBM."""
+    import torch
+    import lpma_gb300 as L
+    device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    V = 1 << args.scale
+    e, S, ins_seq, del_seq = build_workload(args, device, args.seed)
+
+    def gk(x):
+        return ((x >> 42) << 32) | ((x >> 20) & 0x3FFFFF)
+
+    S, ins_seq, del_seq = gk(S), gk(ins_seq), gk(del_seq)
+    g = L.Lpma(V, config=L.gpma_config())
+    g.build(S)
+    st = Stream(ins_seq, del_seq)
+    kinds = ("ins", "del")
+    B = args.batch
+    for i in range(args.warmup):
+        x = st.next(kinds[i % 2], B)
+        g.update(ins=x) if i % 2 == 0 else g.update(dels=x)
+    steps = min(args.steps, 100)
+    stream = torch.cuda.current_stream()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    stats = []
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for i in range(steps):
+        k = (args.warmup + i) % 2
+        x = st.next(kinds[k], B)
+        stats.append(g.update(ins=x) if k == 0 else g.update(dels=x))
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    t = sum(lat) / 1e3
+    applied = sum(s_["n_ins_applied"] + s_["n_del_applied"] for s_ in stats)
+    # per-kernel device time over 10 more batches (kernels timed one at a time)
+    L.profile_enable(True)
+    for i in range(10):
+        k = (args.warmup + steps + i) % 2
+        x = st.next(kinds[k], B)
+        g.update(ins=x) if k == 0 else g.update(dels=x)
+    torch.cuda.synchronize()
+    prof = L.profile_report()
+    L.profile_enable(False)
+    (_, _, _), (size, seg, height) = g.gpma_view()
+    info = g.info()
+    g.close()
+    line = {"metric": "updated edges/s, GPMA mode (the flat array of gpma.cuh), 1M-edge batches",
+            "value": B * steps / t, "unit": "edges/s", "steps": steps, "warmup": args.warmup,
+            "config": dict(config_of(args, int(e.shape[0]), 1), workload="rmat-s%d-ef%d stream in GPMA mode, 50%% bulk, "
+                           "alternating insert/delete batches" % (args.scale, args.ef)),
+            "batch_p50_ms": float(np.percentile(lat, 50)), "batch_p99_ms": float(np.percentile(lat, 99)),
+            "applied_per_step": applied / steps, "resizes": sum(s_["rebuilt"] for s_ in stats),
+            "size_after": size, "segment_length": seg, "height": height, "items_after": info["num_items"],
+            "kernel_ms_per_step": {k: round(v[1] / 10, 4) for k, v in prof.items()},
+            "data": "synthetic (seeded device R-MAT)"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.workload != "stream":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        return {"multigraph": multigraph_arm, "served": served_arm, "skew": skew_arm}[args.workload](args)
+        return {"multigraph": multigraph_arm, "served": served_arm, "skew": skew_arm, "gpma": gpma_arm}[args.workload](args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restric
                                                         uint8_t *live, uint32_t seg, uint32_t seg_log, uint32_t h,
                                                         uint32_t *flag, uint32_t *seg_of, DevStatus *st) {
     const uint32_t i = blockIdx.x * GTPB + threadIdx.x;
-    const bool rejected = (st->error & ERR_KEY) != 0;
+    const bool rejected = (st->error & (ERR_KEY | ERR_TIMEOUT)) != 0;  // invalid key, or the sort gave up a wait
     uint32_t f = 0, back = 0, ups = 0, dels = 0, noop = 0;
     if (i < n && !rejected) {
         const uint64_t key = sk[i];
@@ -197,6 +197,58 @@ __device__ __forceinline__ uint32_t rank_in(const uint64_t *a, uint32_t n, uint6
             hi = mid;
     }
     return lo;
+}
+
+// ------------------------------------------------------------------ single-segment windows
+// Windows of one segment (at most 32 slots; most of the windows) take one
+// warp each, one slot a lane, on a persistent grid: the kept items' ranks by
+// ballot, each insert's merged rank by one ballot over the kept items and a
+// count of the inserts below every kept item, kept items before inserts on
+// equal keys as in k_gpma_exec_small; the segment is cleared and its items
+// placed at their ranks (the even spread over one segment packs them from
+// slot 0).  The warp reads every slot before it writes any.
+__global__ void __launch_bounds__(GTPB) k_gpma_exec_single(const Window *__restrict__ wins,
+                                                            const uint32_t *__restrict__ n_win, uint32_t n_cap,
+                                                            uint64_t *keys, uint8_t *vals, uint8_t *live,
+                                                            uint32_t *row_offset, uint32_t V, uint32_t seg, UpdList u,
+                                                            DevStatus *st) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (GTPB / 32);
+    const uint32_t nwin = min(*n_win, n_cap);
+    for (uint32_t wi = blockIdx.x * (GTPB / 32) + (threadIdx.x >> 5); wi < nwin; wi += warps) {  // uniform per warp
+        const Window w = wins[wi];
+        const uint32_t W = w.f * seg;
+        const uint64_t base = (uint64_t)w.a * seg;
+        const uint32_t k = w.hi - w.lo;  // the window's pending inserts, in key order
+        uint64_t key = KEY_NONE, b = KEY_NONE;
+        uint8_t val = VAL_TOMB, bv = 0;
+        if (lane < W && W <= 32) key = keys[base + lane], val = vals[base + lane];
+        if (lane < k && k <= 32) b = u.key[w.lo + lane], bv = u.val[w.lo + lane];
+        const bool kept = lane < W && g_kept(key, val);
+        const uint32_t kb = __ballot_sync(0xffffffffu, kept);
+        const uint32_t c = __popc(kb), kidx = __popc(kb & ((1u << lane) - 1));
+        const uint32_t m = c + k;
+        if (m != w.m || m > W || W > 32 || w.f != 1) {  // the plan's count and the slots disagree
+            if (lane == 0) {
+                atomicOr(&st->sticky, ERR_INTERNAL);
+                atomicCAS(&st->sticky_site, 0u, 7u);
+            }
+            continue;
+        }
+        uint32_t below = 0, kept_le = 0;  // inserts below this lane's kept item; kept items <= this lane's insert
+        for (uint32_t j = 0; j < k; j++) {
+            const uint64_t bj = __shfl_sync(0xffffffffu, b, j);
+            below += (kept && bj < key) ? 1u : 0u;
+            const uint32_t le = __popc(__ballot_sync(0xffffffffu, kept && key <= bj));
+            if (lane == j) kept_le = le;
+        }
+        __syncwarp();
+        if (lane < W) keys[base + lane] = KEY_NONE;
+        __syncwarp();
+        if (kept) put_item(keys, vals, row_offset, V, base + kidx + below, key, val);
+        if (lane < k) put_item(keys, vals, row_offset, V, base + lane + kept_le, b, bv);
+        if (lane == 0) live[w.a] = (uint8_t)m;
+    }
 }
 
 // ------------------------------------------------------------------ small windows
@@ -562,7 +614,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     uint64_t *k0 = nullptr, *k1 = nullptr;
     uint16_t *p0 = nullptr, *p1 = nullptr;
     uint32_t *flag = nullptr, *pos = nullptr, *seg_of = nullptr, *tmp = nullptr, *P = nullptr, *bitmap = nullptr;
-    uint32_t *sort_status = nullptr, *sort_hist = nullptr, *sort_cnt = nullptr;
+    uint32_t *sort_status = nullptr, *sort_hist = nullptr, *sort_cnt = nullptr, *sort_bar = nullptr;
     UpdList u{};
     uint8_t *pend = nullptr;
     Window *wl = nullptr;
@@ -574,6 +626,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     auto release = [&]() {
         sfree(k0, s), sfree(k1, s), sfree(p0, s), sfree(p1, s), sfree(flag, s), sfree(pos, s), sfree(seg_of, s);
         sfree(tmp, s), sfree(P, s), sfree(bitmap, s), sfree(sort_status, s), sfree(sort_hist, s), sfree(sort_cnt, s);
+        sfree(sort_bar, s);
         sfree(u.key, s), sfree(u.val, s), sfree(u.kind, s), sfree(u.seg, s), sfree(u.ip, s), sfree(pend, s), sfree(wl, s);
     };
 #define GCKR(x)                                                                               \
@@ -584,7 +637,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
             return e_ == cudaErrorMemoryAllocation ? LPMA_ERR_OUT_OF_MEMORY : LPMA_ERR_CUDA; \
         }                                                                                     \
     } while (0)
-    const size_t sw = sort_status_words(nn);
+    const size_t sw = sort_status_words_wide(nn);  // room for the cooperative sort's tile counts
     GCKR(salloc(&k0, n, s));
     GCKR(salloc(&k1, n, s));
     GCKR(salloc(&p0, n, s));
@@ -598,6 +651,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     GCKR(salloc(&sort_status, sw, s));
     GCKR(salloc(&sort_hist, 8 * 256, s));
     GCKR(salloc(&sort_cnt, 16, s));
+    GCKR(salloc(&sort_bar, 1, s));
     GCKR(salloc(&u.key, n, s));
     GCKR(salloc(&u.val, n, s));
     GCKR(salloc(&u.kind, n, s));
@@ -623,6 +677,10 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     ss.status_words = sw;
     ss.hist = sort_hist;
     ss.counters = sort_cnt;
+    // the cooperative sort (its barrier word cleared by the sort; a wait
+    // that gives up marks the status, and the resolve then changes nothing)
+    ss.bar = sort_bar;
+    ss.err = &g->dst->error;
     int which = 0;
     GCKR(sort_pairs<uint16_t>(k0, p0, k1, p1, nn, (vm << 32) | vm, ss, nullptr, s, &which));
     const uint64_t *sk = which ? k1 : k0;
@@ -644,6 +702,10 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     if (g->hst->error & ERR_KEY) {
         release();
         return LPMA_ERR_INVALID_KEY;
+    }
+    if (g->hst->error & ERR_TIMEOUT) {  // nothing changed
+        release();
+        return LPMA_ERR_TIMEOUT;
     }
     const uint32_t n_u = g->hst->n_u, back = g->hst->n_ins, dels = g->hst->n_del;
     st.n_ins_applied = n_u + back;
@@ -685,9 +747,16 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
             const uint32_t *dev_counts[3] = {&g->dst->n_single, &g->dst->n_small4, &g->dst->n_small};
             for (int c = 0; c < 3; c++) {
                 if (!counts[c]) continue;
-                ProfScope ps("gpma_exec_small", s);
-                k_gpma_exec_small<<<counts[c], GTPB, smem, s>>>(lists[c], dev_counts[c], g->keys, g->vals, g->live, g->row,
-                                                                 g->V, g->seg, u, g->dst);
+                const bool one = c == 0 && g->seg <= 32;  // single-segment windows: a warp each
+                ProfScope ps(one ? "gpma_exec_single" : "gpma_exec_small", s);
+                if (one) {
+                    const uint32_t nb = std::min<uint32_t>((counts[0] + GTPB / 32 - 1) / (GTPB / 32), 152 * 8);
+                    k_gpma_exec_single<<<nb, GTPB, 0, s>>>(lists[0], dev_counts[0], counts[0], g->keys, g->vals,
+                                                            g->live, g->row, g->V, g->seg, u, g->dst);
+                } else {
+                    k_gpma_exec_small<<<counts[c], GTPB, smem, s>>>(lists[c], dev_counts[c], g->keys, g->vals, g->live,
+                                                                     g->row, g->V, g->seg, u, g->dst);
+                }
                 note_launch();
             }
             GCKR(cudaGetLastError());
