@@ -403,14 +403,15 @@ def gpu_arm(args, rank, world):
         for i in range(2):
             x, s_ = step(kinds[i % 2], B)
             check.batch(kinds[i % 2], x, s_, B)
+        # the batches (views of the resident stream) are cut before the
+        # timed region: it holds the update calls and their events only
+        sw_batches = [(kinds[i % 2], st.next(kinds[i % 2], B)) for i in range(args.sweep_steps)]
         torch.cuda.synchronize()
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.sweep_steps + 1)]
-        sw_stats, sw_batches = [], []
+        sw_stats = []
         evs[0].record(stream)
-        for i in range(args.sweep_steps):
-            x, s_ = step(kinds[i % 2], B)
-            sw_stats.append(s_)
-            sw_batches.append((kinds[i % 2], x))
+        for i, (k_, x) in enumerate(sw_batches):
+            sw_stats.append(g.update(ins=x) if k_ == "ins" else g.update(dels=x))
             evs[i + 1].record(stream)
         torch.cuda.synchronize()
         for (k_, x), s_ in zip(sw_batches, sw_stats):
@@ -437,16 +438,15 @@ def gpu_arm(args, rank, world):
     clk = Clocks(device.index, pci).__enter__()
     if not clk.nvml:
         time.sleep(0.3)  # nvidia-smi needs a moment before its first sample
+    batches = [(kinds[(args.warmup + i) % 2], st.next(kinds[(args.warmup + i) % 2], B)) for i in range(args.steps)]
+    torch.cuda.synchronize()
     launches0 = L.kernel_launches()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    stats, batches = [], []
+    stats = []
     t0 = time.perf_counter()
     evs[0].record(stream)
-    for i in range(args.steps):
-        k_ = kinds[(args.warmup + i) % 2]
-        x, s_ = step(k_, B)
-        stats.append(s_)
-        batches.append((k_, x))
+    for i, (k_, x) in enumerate(batches):
+        stats.append(g.update(ins=x) if k_ == "ins" else g.update(dels=x))
         evs[i + 1].record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0

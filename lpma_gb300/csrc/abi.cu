@@ -81,6 +81,7 @@ struct LpmaHandle {
     uint32_t *sent = nullptr;
     DevStatus *dst = nullptr;
     DevStatus *hst = nullptr;   // pinned mirror
+    DevStatus *hst_dev = nullptr;  // its device address: the front's planner publishes the status there
     DevStatus *hinit = nullptr; // pinned reset template
     // batch scratch
     size_t bcap = 0;
@@ -412,6 +413,9 @@ lpma_status_t ensure_batch(LpmaHandle *h, size_t n, cudaStream_t s) {
 
 // a handle that shares the GPU with concurrent callers waits without spinning
 inline bool blocking_waits(const LpmaHandle *h) { return (h->cfg.flags & LPMA_FLAG_CONCURRENT) != 0; }
+// The front's status reaches the host through the planner's publish into
+// the pinned mirror (polled), unless the handle's waits must sleep.
+inline bool front_publishes(const LpmaHandle *h) { return h->hst_dev != nullptr && !blocking_waits(h); }
 
 lpma_status_t sync_status(LpmaHandle *h, cudaStream_t s) {
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
@@ -461,7 +465,7 @@ bool needs_prefix(const Tables &tb, uint32_t H) {
 // first plan), so no memset sits between the front's kernels
 lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thres_active, uint64_t total_live,
                        const Tables &tb, cudaStream_t s, const unsigned long long *total_live_dev = nullptr,
-                       bool fresh = false) {
+                       bool fresh = false, DevStatus *pub = nullptr) {
     const uint32_t H = h->H;
     const uint64_t nseg = nseg_of(H);
     if (!fresh) {
@@ -472,7 +476,7 @@ lpma_status_t run_plan(LpmaHandle *h, const UpdList &u, uint32_t n_cap, bool thr
     const bool useP = needs_prefix(tb, H);
     if (useP) CK(scan_u8_to_u32(cntp, h->c.segP, (uint32_t)nseg, h->c.segP + nseg, h->c.scan_tmp, s));
     launch_plan(u, n_cap, cntp, h->c.segP, useP ? 1 : 0, total_live, total_live_dev, H, tb, h->c.bitmap, h->cand,
-                h->wsingle, h->wsmall4, h->wsmall, h->wbig, h->pend, h->dst, s);
+                h->wsingle, h->wsmall4, h->wsmall, h->wbig, h->pend, h->dst, s, pub);
     CK(cudaGetLastError());
     return LPMA_OK;
 }
@@ -622,8 +626,9 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     Tables tb = make_tables(h, h->H, true);
     set_grain(tb, n);
     // the status reset cleared the plan counters and k_pack the bitmap
+    const bool pub = front_publishes(h);
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
-                 thres_active ? &h->dst->live_total : &h->dst->total_items, true));
+                 thres_active ? &h->dst->live_total : &h->dst->total_items, true, pub ? h->hst_dev : nullptr));
     // The status read-back (the host waits on the event after it) and the
     // first loop's single / 4 / 32-segment windows follow without a host
     // round trip: the executors read their counts on the device and do
@@ -642,7 +647,7 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
         CK(cudaEventRecord(h->fork_ev, s));
         CK(cudaStreamWaitEvent(side, h->fork_ev, 0));
     }
-    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, side));
+    if (!pub) CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, side));
     // an event record node when the front is being captured into a graph
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(s, &cs));
@@ -670,6 +675,9 @@ lpma_status_t run_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, cons
     const size_t n = n_ins + n_del;
     h->h2d += offsetof(DevStatus, sticky);
     h->d2h += sizeof(DevStatus);
+    // the planner of this front sets it again (no GPU write to the mirror
+    // is pending: the last front's was waited for)
+    if (front_publishes(h)) __atomic_store_n(&h->hst->published, 0u, __ATOMIC_RELEASE);
     // the stored-key count reaches the planner through the status reset copy,
     // so that it is not a kernel argument of a cached graph
     h->hinit->total_items = h->total;
@@ -784,8 +792,27 @@ void mark_done(LpmaHandle *h, cudaStream_t s) {
     if (h->done_ev && cudaEventRecord(h->done_ev, s) == cudaSuccess) h->done_recorded = true;
 }
 
+// Polls the mirror's `published` word (set by the planner's last CTA after
+// the status words).  The front's event completes after the planner too:
+// queried now and then, it ends the wait with the error of a failed kernel,
+// or, should the word not be seen once the planner has finished, the status
+// is copied back instead.
+cudaError_t wait_published(LpmaHandle *h) {
+    for (uint32_t spin = 1;; spin++) {
+        if (__atomic_load_n(&h->hst->published, __ATOMIC_ACQUIRE)) return cudaSuccess;
+        if (spin % 64) continue;
+        const cudaError_t q = cudaEventQuery(h->front_ev);
+        if (q == cudaErrorNotReady) continue;
+        if (q != cudaSuccess) return q;
+        if (__atomic_load_n(&h->hst->published, __ATOMIC_ACQUIRE)) return cudaSuccess;
+        const cudaError_t e = cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->side_stream);
+        return e ? e : cudaStreamSynchronize(h->side_stream);
+    }
+}
+
 lpma_status_t wait_front(LpmaHandle *h, cudaStream_t) {
-    CK(blocking_waits(h) ? event_wait(h->front_ev_blk) : cudaEventSynchronize(h->front_ev));
+    CK(front_publishes(h) ? wait_published(h)
+                          : blocking_waits(h) ? event_wait(h->front_ev_blk) : cudaEventSynchronize(h->front_ev));
     CK(cudaGetLastError());
     const uint32_t e = h->hst->error | h->hst->sticky;
     if (e & ERR_TIMEOUT) return LPMA_ERR_TIMEOUT;
@@ -1225,6 +1252,10 @@ lpma_status_t lpma_create(const LpmaConfig *cfg, uint32_t num_vertices, lpma_str
     // unless the handle shares the GPU with concurrent calls
     h->sort.bar = (c.flags & LPMA_FLAG_CONCURRENT) ? nullptr : h->sort.counters;
     h->sort.err = &h->dst->error;
+    if (cudaHostGetDevicePointer((void **)&h->hst_dev, h->hst, 0) != cudaSuccess) {
+        h->hst_dev = nullptr;  // the status then comes back by a copy
+        cudaGetLastError();
+    }
     std::memset(h->hinit, 0, sizeof(DevStatus));
     h->hinit->min_t_ins = 0xFFFFFFFFu;
     h->hinit->key_and = ~0ull;

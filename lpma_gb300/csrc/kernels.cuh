@@ -70,11 +70,13 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
                             uint32_t *blk_ins, DevStatus *st, cudaStream_t s);
 
 // count-only planner: per segment with updates, the first level whose
-// window passes the density test; maximal windows go to small/big lists
+// window passes the density test; maximal windows go to small/big lists.
+// pub: when set, the planner's last CTA writes the status block into this
+// pinned host mirror and then sets its `published` word.
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
                  uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
-                 uint8_t *pend, DevStatus *st, cudaStream_t s);
+                 uint8_t *pend, DevStatus *st, cudaStream_t s, DevStatus *pub = nullptr);
 
 // in-place executors for windows of <= 32 segments: the single-segment
 // list (DevStatus::n_single), and in one launch the windows of 2..4

@@ -96,10 +96,14 @@ struct DevStatus {
     unsigned long long cnt_total;    // sum of occupancy counts (recount)
     unsigned long long total_items;  // keys stored before the call (set by the host)
     uint32_t err_info[4];            // first offending input index, internal-check site
+    uint32_t plan_done;              // planner CTAs finished (the front's status publish)
     // Not reset per call (the reset copies the fields above only): the
     // executors set ERR_INTERNAL here after the call may have returned.
     uint32_t sticky;
     uint32_t sticky_site;  // which internal check set ERR_INTERNAL (first one)
+    // Meaningful in the host mirror only: set to 1 by the planner's last CTA
+    // after it wrote the words above into the mirror (k_plan_max, publish).
+    uint32_t published;
 };
 
 // A rebalance window chosen by the planner (maximal executed window); 8-byte

@@ -1266,14 +1266,15 @@ static cudaError_t sort_impl(uint64_t *k0, V *v0, uint64_t *k1, V *v1, uint32_t 
         ProfScope ps("sort_block", st);
         uint16_t *p0 = reinterpret_cast<uint16_t *>(v0), *p1 = reinterpret_cast<uint16_t *>(v1);
         const uint32_t ntiles = (n + RANK_TILE - 1) / RANK_TILE;
+        if (mask.pingpong == 2u && ntiles > 1) return cudaErrorInvalidValue;
         launch_pdl(k_rank_tiles, dim3((ntiles - 1) * RANK_CPT + (n - (ntiles - 1) * RANK_TILE + RANK_KEYS - 1) / RANK_KEYS),
                    dim3(RANK_TPB), 0, st, k0, p0, k1, p1, n);
-        if (ntiles == 1)
-            launch_pdl(k_rank_back, dim3(1), dim3(1024), 0, st, k0, p0, k1, p1, n);
-        else
+        if (ntiles > 1)
             launch_pdl(k_rank_merge, dim3((n + RANK_TPB - 1) / RANK_TPB), dim3(RANK_TPB), (size_t)n * 8, st, k0, p0, k1,
                        p1, n);
-        note_launch(2);
+        else if (mask.pingpong != 2u)  // the caller reads the tile where it is when pingpong is 2
+            launch_pdl(k_rank_back, dim3(1), dim3(1024), 0, st, k0, p0, k1, p1, n);
+        note_launch(ntiles > 1 || mask.pingpong != 2u ? 2 : 1);
         return cudaGetLastError();
     }
     // the 9-bit digit plan belongs to the cooperative sort alone: the
@@ -1467,7 +1468,8 @@ bool sort_tier_usable(SortTier t, uint32_t n, const SortScratch &s) { return tie
 SortMask update_sort_mask(const unsigned long long *andor, SortTier t, uint32_t n, const SortScratch &s) {
     uint32_t tl, G;
     const bool wide = t == TIER_COOP && coop_geometry<uint16_t>(n, s, &tl, &G, true);
-    return SortMask{andor, 0xFFu, sort_tier_in_place(t) ? 0u : 1u, wide ? 1u : 0u};
+    const uint32_t pp = t == TIER_BLOCK && n <= RANK_TILE ? 2u : sort_tier_in_place(t) ? 0u : 1u;
+    return SortMask{andor, 0xFFu, pp, wide ? 1u : 0u};
 }
 
 void sort_tier_set(uint32_t bucket, int concurrent, SortTier t) {

@@ -30,7 +30,9 @@ struct SortScratch {
 // of all keys) differ.
 // pingpong: the sort that produced the batch is a ping-pong one (one
 // buffer swap per digit pass), so its result is in the second buffer pair
-// when the number of digit passes is odd; 0: the result is in place.
+// when the number of digit passes is odd; 0: the result is in place; 2: the
+// result is in the second buffer pair (the rank sort of a single tile,
+// which then skips the copy back).
 // wide: the cooperative sort's 9-bit digits (set only with andor and
 // host_mask 0xFF): digit windows of up to 9 bits placed greedily over the
 // bits where the keys differ, instead of one pass per differing byte.
@@ -117,7 +119,7 @@ __device__ inline uint32_t sort_digit_passes(SortMask m) {
 
 // true when sort_pairs_dev<uint16_t> left its result in the second buffer pair
 __device__ inline bool sort_result_odd(SortMask m, uint32_t n) {
-    return n >= 2 && m.pingpong && (sort_digit_passes(m) & 1);
+    return n >= 2 && (m.pingpong == 2u || (m.pingpong == 1u && (sort_digit_passes(m) & 1)));
 }
 
 // Device-decided variant, sorted with `tier` (TIER_AUTO: the tuned or

@@ -804,13 +804,33 @@ __device__ __forceinline__ void k_plan_max_body(const Window *__restrict__ cand,
     }
 }
 
+// pub (optional): the handle's pinned host mirror of the status block.  The
+// last CTA to finish (a counter in the status block) copies the status words
+// there and then sets pub->published, so the host reads the front's verdict
+// as soon as the plan is complete, without a copy node and an event behind it.
 __global__ void __launch_bounds__(TPB) k_plan_max(const Window *__restrict__ cand, uint32_t n_cap, uint32_t H,
                                                   const uint32_t *__restrict__ bitmap, Window *single, Window *small4,
                                                   Window *small, Window *big, const UpdList u, uint8_t *pend,
-                                                  DevStatus *st, uint32_t cut_group, uint32_t cut_shared) {
+                                                  DevStatus *st, uint32_t cut_group, uint32_t cut_shared,
+                                                  DevStatus *pub) {
     griddep_wait();
     k_plan_max_body(cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st, blockIdx.x, gridDim.x, cut_group,
                     cut_shared);
+    if (pub == nullptr) return;  // uniform over the grid
+    __shared__ uint32_t last;
+    __threadfence();  // this CTA's status atomics before its count
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->plan_done, 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    constexpr uint32_t W = offsetof(DevStatus, published) / 4;  // every word up to the flag
+    const volatile uint32_t *src = reinterpret_cast<const volatile uint32_t *>(st);
+    volatile uint32_t *dst = reinterpret_cast<volatile uint32_t *>(pub);
+    for (uint32_t i = threadIdx.x; i < W; i += TPB) dst[i] = src[i];
+    __threadfence_system();  // the words before the flag, for the host
+    __syncthreads();
+    if (threadIdx.x == 0) dst[W] = 1u;
 }
 
 // ------------------------------------------------------------------ multi-segment windows
@@ -1866,14 +1886,14 @@ void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, U
 void launch_plan(const UpdList u, uint32_t n_cap, const uint8_t *cnt, const uint32_t *P, int use_P,
                  uint64_t total_live, const unsigned long long *total_live_dev, uint32_t H, const Tables &tb,
                  uint32_t *bitmap, Window *cand, Window *single, Window *small4, Window *small, Window *big,
-                 uint8_t *pend, DevStatus *st, cudaStream_t s) {
+                 uint8_t *pend, DevStatus *st, cudaStream_t s, DevStatus *pub) {
     ProfScope ps_("plan", s);
     const uint32_t nb = (n_cap + TPB - 1) / TPB;
     if (!nb) return;
     launch_pdl(k_plan, dim3(nb), dim3(TPB), 0, s, u, n_cap, cnt, P, use_P, total_live, total_live_dev, H, tb, bitmap,
                cand, pend, st);
     launch_pdl(k_plan_max, dim3(nb), dim3(TPB), 0, s, cand, n_cap, H, bitmap, single, small4, small, big, u, pend, st,
-               tb.cut_group ? tb.cut_group : CUT_GROUP_DEFAULT, tb.cut_shared ? tb.cut_shared : SMALL_WIN_SEGS);
+               tb.cut_group ? tb.cut_group : CUT_GROUP_DEFAULT, tb.cut_shared ? tb.cut_shared : SMALL_WIN_SEGS, pub);
     note_launch(2);
 }
 

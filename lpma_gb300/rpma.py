@@ -54,10 +54,11 @@ def gpma_key(src, dst):
 
 
 _torch = None
+_raw_stream = None
 
 
 def _stream_ptr(stream):
-    global _torch
+    global _torch, _raw_stream
     if stream is None:
         if _torch is None:
             try:
@@ -65,6 +66,15 @@ def _stream_ptr(stream):
                 _torch = torch if torch.cuda.is_available() else False
             except ImportError:
                 _torch = False
+            if _torch:
+                # the current stream's handle without building a Stream object
+                # (a few microseconds a call, which a 1K-edge update notices)
+                get_raw = getattr(_torch._C, "_cuda_getCurrentRawStream", None)
+                get_dev = getattr(_torch._C, "_cuda_getDevice", None)
+                if get_raw is not None and get_dev is not None:
+                    _raw_stream = lambda: get_raw(get_dev())  # noqa: E731
+        if _raw_stream is not None:
+            return _raw_stream()
         if _torch:
             return _torch.cuda.current_stream().cuda_stream
         return None
