@@ -629,17 +629,20 @@ lpma_status_t enqueue_front(LpmaHandle *h, cudaStream_t s, const uint64_t *ins, 
     const bool pub = front_publishes(h);
     CKS(run_plan(h, h->u, (uint32_t)n, thres_active, 0, tb, s,
                  thres_active ? &h->dst->live_total : &h->dst->total_items, true, pub ? h->hst_dev : nullptr));
-    // The status read-back (the host waits on the event after it) and the
-    // first loop's single / 4 / 32-segment windows follow without a host
-    // round trip: the executors read their counts on the device and do
-    // nothing when the plan overflowed, so they run while the host decides
-    // what else the call needs.  The read-back and the 4- and 32-segment
-    // executors (one launch) run on a second stream (a parallel branch of the captured
-    // graph): the single-segment executor follows the planner directly, as
-    // its programmatic dependent, and the windows of the three are
-    // disjoint.  The join makes everything after them on s wait for all.
-    // The in-library profiler times each kernel alone, so it keeps them on
-    // one stream.
+    // The status read-back and the first loop's single / 4 / 32-segment
+    // windows follow without a host round trip: the executors read their
+    // counts on the device and do nothing when the plan overflowed, so they
+    // run while the host decides what else the call needs.  The read-back is
+    // the planner's publish into the pinned mirror (the host polls its flag;
+    // the front's event, recorded after the planner, backs the poll), or,
+    // for a handle whose waits sleep, a copy with a blocking event after it.
+    // The copy, the event and the 4- and 32-segment executors (one launch)
+    // run on a second stream (a parallel branch of the captured graph): the
+    // single-segment executor follows the planner directly, as its
+    // programmatic dependent, and the windows of the three are disjoint.
+    // The join makes everything after them on s wait for all.  The
+    // in-library profiler times each kernel alone, so it keeps them on one
+    // stream.
     Geo ge{h->c.keys, h->c.vals, h->H};
     const bool fork = !prof_enabled();
     cudaStream_t side = fork ? h->side_stream : s;
