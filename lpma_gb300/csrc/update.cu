@@ -893,7 +893,44 @@ struct MultiWarpSmem {  // a window per warp: 4 warps with rows of 1024, or 8 of
     uint8_t v[4 * 1024];
     uint32_t im[4 * 32];   // insert marks by merged rank
     uint32_t imc[4 * 32];  // marks in the words before
+    uint64_t bar[4];       // the rows of 1024: one mbarrier per warp for the bulk copies
 };
+
+// Bulk copies (the TMA engine's untiled form) of global memory into shared
+// memory, completing on an mbarrier of the issuing CTA.  Both addresses
+// 16-byte aligned, sizes multiples of 16.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init1(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+// a bounded wait for the phase (each try suspends for at most a short,
+// hardware-defined time): false when it did not complete
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase) {
+    for (uint32_t it = 0; it < (1u << 20); it++)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+// generic-proxy accesses of shared memory before later bulk copies into it
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 constexpr size_t EM_SMEM = sizeof(Multi4Smem) > sizeof(MultiWarpSmem) ? sizeof(Multi4Smem) : sizeof(MultiWarpSmem);
 
 template <bool TH>
@@ -1054,22 +1091,46 @@ __device__ __forceinline__ void k_exec_multi4_body(Multi4Smem &S, const Window *
 
 // A window of up to ROW / 32 segments on one warp: its 4 groups take 4
 // segments a round (group q: segment 4r + q), so a window of <= 4 segments
-// is one round; the next round's slots load while a round compacts.  The
-// row holds the kept keys from the front and the inserts from the back.
+// is one round.  The row holds the kept keys from the front and the inserts
+// from the back.  Rows of 128 (windows of up to 4 segments): each lane
+// loads its slots, the next round's while a round compacts.  Rows of 1024
+// (5..32 segments): lane s first bulk-copies segment s's keys (256 B) and
+// values (32 B) into the row at 32 s, so all of the window's loads are in
+// flight at once (one mbarrier wait, bounded), and the kept keys are then
+// compacted in place (a kept key only moves down, past slots already read);
+// its inserts are written to the back of the row after the compaction.
 template <uint32_t ROW, bool TH>
 __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV, uint32_t *IM, uint32_t *IMC,
-                                                       const Window *__restrict__ wins,
+                                                       uint64_t *bar, const Window *__restrict__ wins,
                                                        const uint32_t *__restrict__ n_win, uint32_t n_cap, Geo g,
                                                        uint8_t *cnt, ulonglong2 *fl, uint32_t *sent, uint32_t V,
                                                        const UpdList u, uint32_t thres, DevStatus *st, uint32_t wid,
                                                        uint32_t nwarps) {
     constexpr uint32_t WORDS = ROW / 32, MAXF = ROW / 32;
+    constexpr bool STAGED = ROW == 1024;
     const int lane = threadIdx.x & 31, gl = lane & 7, gq = lane >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
+    uint32_t phase = 0;
+    if (STAGED) {
+        if (lane == 0) mbar_init1(bar);
+        __syncwarp();
+    }
     for (uint32_t wi = wid; wi < nwin; wi += nwarps) {  // uniform over the warp
         const Window W = wins[wi];
         const uint32_t f = min(W.f, MAXF);
         const uint32_t rounds = (f + 3) / 4;
+        if (STAGED) {
+            // the row's earlier reads and writes come before the copies into it
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_expect_tx(bar, f * 288u);
+            __syncwarp();
+            if ((uint32_t)lane < f) {
+                const uint64_t j = heap_of_linear32(W.a + lane, g.H);
+                bulk_to_smem(K + 32 * lane, g.keys + 32 * j, 256u, bar);
+                bulk_to_smem(KV + 32 * lane, g.vals + 32 * j, 32u, bar);
+            }
+        }
         auto load = [&](uint32_t r, uint64_t (&k)[4], uint32_t &v4) {
             const uint32_t sg = 4 * r + gq;
             k[0] = k[1] = k[2] = k[3] = KEY_NONE;
@@ -1082,28 +1143,62 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
                 v4 = *reinterpret_cast<const uint32_t *>(g.vals + 32 * j + 4 * gl);
             }
         };
-        uint64_t kn[4];
-        uint32_t vn;
-        load(0, kn, vn);
+        uint64_t kn[4] = {KEY_NONE, KEY_NONE, KEY_NONE, KEY_NONE};
+        uint32_t vn = 0;
+        if (!STAGED) load(0, kn, vn);
         const uint32_t ip0 = u.ip[W.lo];
         const uint32_t nins = u.ip[W.hi] - ip0;
-        // inserts from the back of the row, rank r at ROW - 1 - r
-        for (uint32_t x = W.lo + lane; nins && x < W.hi; x += 32) {
+        // inserts go to the back of the row, rank r at ROW - 1 - r; a staged
+        // row holds the slots until the compaction, so the window's first 32
+        // updates wait in registers meanwhile
+        uint64_t y0 = 0;
+        uint32_t r0 = ~0u, yv0 = 0;
+        for (uint32_t x = W.lo + lane; nins && x < (STAGED ? min(W.hi, W.lo + 32) : W.hi); x += 32) {
             const uint8_t kd = u.kind[x];
             const uint32_t r = u.ip[x] - ip0;
             const uint64_t y = u.key[x];
             const uint8_t yv = u.val[x];
-            if (kd == KIND_INS && r < ROW) {
+            if (STAGED) {
+                if (kd == KIND_INS) r0 = r, y0 = y, yv0 = yv;
+            } else if (kd == KIND_INS && r < ROW) {
                 K[ROW - 1 - r] = y;
                 KV[ROW - 1 - r] = yv;
+            }
+        }
+        if (STAGED) {
+            const uint32_t ph = phase;
+            phase ^= 1u;
+            if (!__all_sync(0xffffffffu, mbar_wait_bounded(bar, ph))) {
+                // the copies did not land in time: report, let them finish
+                // (bounded) before the row is left, and stop this warp
+                if (lane == 0) {
+                    atomicOr(&st->sticky, ERR_TIMEOUT);
+                    atomicCAS(&st->sticky_site, 0u, 9u);
+                }
+                mbar_wait_bounded(bar, ph);
+                return;
             }
         }
         // kept keys from the front, in slot order (lane order within a round)
         uint32_t nk = 0;
         for (uint32_t r = 0; r < rounds; r++) {
             uint64_t k[4] = {kn[0], kn[1], kn[2], kn[3]};
-            const uint32_t v4 = vn;
-            if (r + 1 < rounds) load(r + 1, kn, vn);
+            uint32_t v4 = vn;
+            if (STAGED) {
+                const uint32_t sg = 4 * r + gq;
+                if (sg < f) {
+                    const ulonglong2 *kp = reinterpret_cast<const ulonglong2 *>(K + 32 * sg + 4 * gl);
+                    const ulonglong2 a = kp[0], b = kp[1];
+                    k[0] = a.x, k[1] = a.y, k[2] = b.x, k[3] = b.y;
+                    v4 = *reinterpret_cast<const uint32_t *>(KV + 32 * sg + 4 * gl);
+                } else {
+                    k[0] = k[1] = k[2] = k[3] = KEY_NONE;
+                    v4 = 0;
+                }
+                __syncwarp();  // the round's slots are read before kept keys move down over them
+            } else if (r + 1 < rounds) {
+                load(r + 1, kn, vn);
+            }
             uint32_t kmask = 0;
 #pragma unroll
             for (int q = 0; q < 4; q++)
@@ -1126,6 +1221,20 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
                     }
                 }
             nk += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (STAGED) {
+            __syncwarp();  // the kept keys are in place: the back of the row is free
+            if (r0 < ROW) {
+                K[ROW - 1 - r0] = y0;
+                KV[ROW - 1 - r0] = (uint8_t)yv0;
+            }
+            for (uint32_t x = W.lo + 32 + lane; nins && x < W.hi; x += 32) {
+                const uint32_t r = u.ip[x] - ip0;
+                if (u.kind[x] == KIND_INS && r < ROW) {
+                    K[ROW - 1 - r] = u.key[x];
+                    KV[ROW - 1 - r] = u.val[x];
+                }
+            }
         }
         if ((uint32_t)lane < WORDS) IM[lane] = 0;
         __syncwarp();
@@ -1224,8 +1333,8 @@ __device__ __forceinline__ void exec_multi4(unsigned char *smem, const Window *_
     } else {
         MultiWarpSmem &S = *reinterpret_cast<MultiWarpSmem *>(smem);
         const uint32_t w = threadIdx.x >> 5;
-        k_exec_multi_warp_body<128, TH>(S.k + 128 * w, S.v + 128 * w, S.im + 4 * w, S.imc + 4 * w, w4, n4, cap4, g, cnt,
-                                    fl, sent, V, u, thres, st, bid_ * (EM_TPB / 32) + w, warps);
+        k_exec_multi_warp_body<128, TH>(S.k + 128 * w, S.v + 128 * w, S.im + 4 * w, S.imc + 4 * w, nullptr, w4, n4, cap4,
+                                        g, cnt, fl, sent, V, u, thres, st, bid_ * (EM_TPB / 32) + w, warps);
     }
 }
 
@@ -1239,8 +1348,8 @@ __device__ __forceinline__ void exec_multi32(unsigned char *smem, const Window *
     const uint32_t w = threadIdx.x >> 5;
     if (w >= 4) return;
     MultiWarpSmem &S = *reinterpret_cast<MultiWarpSmem *>(smem);
-    k_exec_multi_warp_body<1024, TH>(S.k + 1024 * w, S.v + 1024 * w, S.im + 32 * w, S.imc + 32 * w, w32, n32, cap32, g,
-                                 cnt, fl, sent, V, u, thres, st, bid_ * 4 + w, nblk_ * 4);
+    k_exec_multi_warp_body<1024, TH>(S.k + 1024 * w, S.v + 1024 * w, S.im + 32 * w, S.imc + 32 * w, S.bar + w, w32, n32,
+                                     cap32, g, cnt, fl, sent, V, u, thres, st, bid_ * 4 + w, nblk_ * 4);
 }
 
 // a plan that overflowed or a rejected batch: the guarded executors skip
