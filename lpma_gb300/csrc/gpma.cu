@@ -16,8 +16,9 @@
 // the pending inserts compacted into the update list, then the shared
 // count-only planner and maximal-window filter (k_plan / k_plan_max, with
 // the flat segment length and count) over per-segment live counts.  The
-// maximal windows run on flat executors: windows of up to 32 segments one
-// CTA each in shared memory, bigger ones as gather / clear / merge-spread.
+// maximal windows run on flat executors: single-segment windows one warp
+// each, windows of up to 32 segments one CTA each in shared memory, bigger
+// ones as gather / clear / merge-spread.
 // When the root cannot take the batch, or a batch brings 5,000,000 new keys
 // or more (significant_insert, gpma.cuh:720-744), the whole array is
 // rebuilt at the resize rule's size (a copying resize, gpma.cuh:694-718).
@@ -80,19 +81,40 @@ __global__ void __launch_bounds__(GTPB) k_gpma_pack(const uint64_t *__restrict__
 }
 
 // ------------------------------------------------------------------ resolve
-// One thread per sorted key.  Repeated keys collapse as in the leveled
-// path: the last insert of a key gives its value and an insert of a key
-// also deleted in the batch wins (delete first).  flag[i] = 1 for a pending
-// insert, seg_of[i] its located segment.  Counters: n_ins = tombstoned keys
-// brought back, n_upsert, n_del, n_noop.
+// One thread per sorted key, on a persistent grid.  Repeated keys collapse
+// as in the leveled path: the last insert of a key gives its value and an
+// insert of a key also deleted in the batch wins (delete first).  flag[i] =
+// 1 for a pending insert, seg_of[i] its located segment.  Counters: n_ins =
+// tombstoned keys brought back, n_upsert, n_del, n_noop.
+//
+// The locate is locate_leaf_kernel's binary search over the segments' first
+// slots (gpma.cuh:185-191): depth d probes slot prefix | (size >> (d + 1)).
+// Each CTA first stages the probe keys of the first GR_TOP depths in shared
+// memory in heap order (node k at depth d = floor(log2 k) probes slot
+// (k - 2^d) * (size >> d) + (size >> (d + 1))), so a key walks those depths
+// there and only the deeper ones in global memory.
+constexpr uint32_t GR_TOP = 10;
 __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restrict__ sk, const uint16_t *__restrict__ sp,
                                                         uint32_t n, const uint64_t *__restrict__ keys, uint8_t *vals,
                                                         uint8_t *live, uint32_t seg, uint32_t seg_log, uint32_t h,
                                                         uint32_t *flag, uint32_t *seg_of, DevStatus *st) {
-    const uint32_t i = blockIdx.x * GTPB + threadIdx.x;
+    __shared__ uint64_t sel[1u << GR_TOP];
     const bool rejected = (st->error & (ERR_KEY | ERR_TIMEOUT)) != 0;  // invalid key, or the sort gave up a wait
-    uint32_t f = 0, back = 0, ups = 0, dels = 0, noop = 0;
-    if (i < n && !rejected) {
+    const uint64_t size = (uint64_t)seg << h;
+    const uint32_t ts = h < GR_TOP ? h : GR_TOP;
+    if (!rejected)
+        for (uint32_t k = 1 + threadIdx.x; k < (1u << ts); k += GTPB) {
+            const uint32_t d = 31 - __clz(k);
+            sel[k] = keys[(uint64_t)(k - (1u << d)) * (size >> d) + (size >> (d + 1))];
+        }
+    __syncthreads();
+    uint32_t back = 0, ups = 0, dels = 0, noop = 0;
+    for (uint32_t i = blockIdx.x * GTPB + threadIdx.x; i < n; i += gridDim.x * GTPB) {
+        uint32_t f = 0;
+        if (rejected) {
+            flag[i] = 0;
+            continue;
+        }
         const uint64_t key = sk[i];
         const uint16_t p = sp[i];
         const bool is_del = (p >> 8) & 1;
@@ -102,9 +124,10 @@ __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restric
         else
             rep = (i + 1 == n || sk[i + 1] != key || ((sp[i + 1] >> 8) & 1));
         if (rep) {
-            // locate_leaf_kernel, gpma.cuh:185-191
-            uint64_t prefix = 0;
-            for (uint64_t bit = ((uint64_t)seg << h) >> 1; bit >= seg; bit >>= 1)
+            uint32_t node = 1;
+            for (uint32_t d = 0; d < ts; d++) node = 2 * node + (sel[node] <= key ? 1u : 0u);
+            uint64_t prefix = (uint64_t)(node - (1u << ts)) * (size >> ts);
+            for (uint64_t bit = (size >> ts) >> 1; bit >= seg; bit >>= 1)
                 if (keys[prefix | bit] <= key) prefix |= bit;
             // handle_del_mod: the first equal key of the segment
             int hit = -1;
@@ -120,9 +143,9 @@ __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restric
                     vals[prefix + hit] = (uint8_t)(p & 0xFF);
                     if (old == VAL_TOMB) {
                         cnt_add(live, s, +1);
-                        back = 1;
+                        back++;
                     } else {
-                        ups = 1;
+                        ups++;
                     }
                 } else {
                     f = 1;
@@ -131,15 +154,15 @@ __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restric
             } else if (hit >= 0 && vals[prefix + hit] != VAL_TOMB) {
                 vals[prefix + hit] = VAL_TOMB;
                 cnt_add(live, s, -1);
-                dels = 1;
+                dels++;
             } else {
-                noop = 1;
+                noop++;
             }
         } else {
-            noop = 1;
+            noop++;
         }
+        flag[i] = f;
     }
-    if (i < n) flag[i] = f;
     back = __reduce_add_sync(0xffffffffu, back);
     ups = __reduce_add_sync(0xffffffffu, ups);
     dels = __reduce_add_sync(0xffffffffu, dels);
@@ -687,7 +710,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     const uint16_t *sp = which ? p1 : p0;
     {
         ProfScope ps("gpma_resolve", s);
-        k_gpma_resolve<<<nblk(n), GTPB, 0, s>>>(sk, sp, nn, g->keys, g->vals, g->live, g->seg,
+        k_gpma_resolve<<<std::min<uint32_t>(nblk(n), 152 * 8), GTPB, 0, s>>>(sk, sp, nn, g->keys, g->vals, g->live, g->seg,
                                                   (uint32_t)__builtin_ctz(g->seg), g->h, flag, seg_of, g->dst);
         note_launch();
     }

@@ -1108,26 +1108,49 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *tmp, uint32_t nb, u
     if (threadIdx.x == 0 && total) *total = carry;
 }
 
+// Warp w of a block scans elements [tile + 256 w, tile + 256 w + 256) as 8
+// rows of 32 (lane l holds element 32 i + l of row i): each row is a shuffle
+// scan carried into the next, so every load and store instruction of a warp
+// covers consecutive elements (one 128-byte line of u32 output).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_TPB) k_scan_down(const T *__restrict__ in, uint32_t *out, uint32_t n,
                                                        const uint32_t *tmp, uint32_t *total_single) {
-    __shared__ uint32_t wsum[8];
-    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_IPT;
+    __shared__ uint32_t wsum[SCAN_TPB / 32];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)w * (32 * SCAN_IPT) + lane;
     uint32_t x[SCAN_IPT];
-    uint32_t s = 0;
 #pragma unroll
     for (int i = 0; i < SCAN_IPT; i++) {
-        uint64_t p = base + i;
-        x[i] = p < n ? (uint32_t)in[p] : 0;
-        s += x[i];
+        const uint64_t p = base + 32 * i;
+        x[i] = p < n ? (uint32_t)in[p] : 0u;
     }
-    uint32_t tot;
-    uint32_t off = block_excl_scan_256(s, wsum, &tot) + (tmp ? tmp[blockIdx.x] : 0);
+    uint32_t run = 0;  // the warp's elements before row i
 #pragma unroll
     for (int i = 0; i < SCAN_IPT; i++) {
-        uint64_t p = base + i;
-        if (p < n) out[p] = off;
-        off += x[i];
+        uint32_t v = x[i];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= (uint32_t)o) v += y;
+        }
+        const uint32_t row = __shfl_sync(0xffffffffu, v, 31);
+        x[i] = run + v - x[i];  // exclusive, within the warp
+        run += row;
+    }
+    if (lane == 0) wsum[w] = run;
+    __syncthreads();
+    uint32_t woff = 0, tot = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < SCAN_TPB / 32; k++) {
+        const uint32_t y = wsum[k];
+        woff += k < w ? y : 0u;
+        tot += y;
+    }
+    const uint32_t off = woff + (tmp ? tmp[blockIdx.x] : 0u);
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        const uint64_t p = base + 32 * i;
+        if (p < n) out[p] = off + x[i];
     }
     if (total_single && threadIdx.x == 0) *total_single = tot;
 }
