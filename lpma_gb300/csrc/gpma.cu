@@ -88,24 +88,27 @@ __global__ void __launch_bounds__(GTPB) k_gpma_pack(const uint64_t *__restrict__
 // tombstoned keys brought back, n_upsert, n_del, n_noop.
 //
 // The locate is locate_leaf_kernel's binary search over the segments' first
-// slots (gpma.cuh:185-191): depth d probes slot prefix | (size >> (d + 1)).
-// Each CTA first stages the probe keys of the first GR_TOP depths in shared
-// memory in heap order (node k at depth d = floor(log2 k) probes slot
-// (k - 2^d) * (size >> d) + (size >> (d + 1))), so a key walks those depths
-// there and only the deeper ones in global memory.
+// slots (gpma.cuh:185-191), run over the leaders table (lead[s] = the key in
+// segment s's first slot; 16 MB for 2M segments, so its deep levels are L2
+// reads, not random DRAM lines of the slot array): depth d probes segment
+// ps | (nseg >> (d + 1)).  Each CTA first stages the probes of the first
+// GR_TOP depths in shared memory in heap order (node k at depth d =
+// floor(log2 k) probes segment (k - 2^d) * (nseg >> d) + (nseg >> (d + 1))),
+// so a key walks those depths there and only the deeper ones in the table.
 constexpr uint32_t GR_TOP = 10;
 __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restrict__ sk, const uint16_t *__restrict__ sp,
                                                         uint32_t n, const uint64_t *__restrict__ keys, uint8_t *vals,
                                                         uint8_t *live, uint32_t seg, uint32_t seg_log, uint32_t h,
-                                                        uint32_t *flag, uint32_t *seg_of, DevStatus *st) {
+                                                        uint32_t *flag, uint32_t *seg_of, const uint64_t *__restrict__ lead,
+                                                        DevStatus *st) {
     __shared__ uint64_t sel[1u << GR_TOP];
     const bool rejected = (st->error & (ERR_KEY | ERR_TIMEOUT)) != 0;  // invalid key, or the sort gave up a wait
-    const uint64_t size = (uint64_t)seg << h;
+    const uint64_t nseg = 1ull << h;
     const uint32_t ts = h < GR_TOP ? h : GR_TOP;
     if (!rejected)
         for (uint32_t k = 1 + threadIdx.x; k < (1u << ts); k += GTPB) {
             const uint32_t d = 31 - __clz(k);
-            sel[k] = keys[(uint64_t)(k - (1u << d)) * (size >> d) + (size >> (d + 1))];
+            sel[k] = lead[(uint64_t)(k - (1u << d)) * (nseg >> d) + (nseg >> (d + 1))];
         }
     __syncthreads();
     uint32_t back = 0, ups = 0, dels = 0, noop = 0;
@@ -126,9 +129,10 @@ __global__ void __launch_bounds__(GTPB) k_gpma_resolve(const uint64_t *__restric
         if (rep) {
             uint32_t node = 1;
             for (uint32_t d = 0; d < ts; d++) node = 2 * node + (sel[node] <= key ? 1u : 0u);
-            uint64_t prefix = (uint64_t)(node - (1u << ts)) * (size >> ts);
-            for (uint64_t bit = (size >> ts) >> 1; bit >= seg; bit >>= 1)
-                if (keys[prefix | bit] <= key) prefix |= bit;
+            uint64_t ps = (uint64_t)(node - (1u << ts)) * (nseg >> ts);
+            for (uint64_t bit = (nseg >> ts) >> 1; bit; bit >>= 1)
+                if (lead[ps | bit] <= key) ps |= bit;
+            const uint64_t prefix = ps << seg_log;
             // handle_del_mod: the first equal key of the segment
             int hit = -1;
             for (uint32_t l = 0; l < seg; l++)
@@ -199,10 +203,14 @@ __device__ __forceinline__ uint64_t spread_slot(uint64_t r, uint64_t m, uint64_t
     return (fr / m) * seg + (fr % m) / f;
 }
 
-__device__ __forceinline__ void put_item(uint64_t *keys, uint8_t *vals, uint32_t *row_offset, uint32_t V, uint64_t slot,
-                                         uint64_t k, uint8_t v) {
+// lead (optional): the segment leaders (the first slot's key of every
+// segment), written here for the items that land in a first slot; the
+// executors that pass none write the leaders of their windows themselves
+__device__ __forceinline__ void put_item(uint64_t *keys, uint8_t *vals, uint32_t *row_offset, uint32_t V,
+                                         uint64_t *lead, uint32_t seg, uint64_t slot, uint64_t k, uint8_t v) {
     keys[slot] = k;
     vals[slot] = v;
+    if (lead && (slot & (seg - 1)) == 0) lead[slot >> (__ffs(seg) - 1)] = k;
     if (g_sentinel(k)) {
         const uint64_t row = k >> 32;
         if (row < V) row_offset[row + 1] = (uint32_t)slot;
@@ -230,11 +238,11 @@ __device__ __forceinline__ uint32_t rank_in(const uint64_t *a, uint32_t n, uint6
 // equal keys as in k_gpma_exec_small; the segment is cleared and its items
 // placed at their ranks (the even spread over one segment packs them from
 // slot 0).  The warp reads every slot before it writes any.
-__global__ void __launch_bounds__(GTPB) k_gpma_exec_single(const Window *__restrict__ wins,
+__global__ void __launch_bounds__(GTPB, 8) k_gpma_exec_single(const Window *__restrict__ wins,
                                                             const uint32_t *__restrict__ n_win, uint32_t n_cap,
                                                             uint64_t *keys, uint8_t *vals, uint8_t *live,
                                                             uint32_t *row_offset, uint32_t V, uint32_t seg, UpdList u,
-                                                            DevStatus *st) {
+                                                            uint64_t *lead, DevStatus *st) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (GTPB / 32);
     const uint32_t nwin = min(*n_win, n_cap);
@@ -266,10 +274,16 @@ __global__ void __launch_bounds__(GTPB) k_gpma_exec_single(const Window *__restr
             if (lane == j) kept_le = le;
         }
         __syncwarp();
+        // the segment's leader: written only when the first slot's key
+        // changes (an insert below the first key, or the first key gone)
+        const uint64_t old0 = __shfl_sync(0xffffffffu, key, 0);
         if (lane < W) keys[base + lane] = KEY_NONE;
         __syncwarp();
-        if (kept) put_item(keys, vals, row_offset, V, base + kidx + below, key, val);
-        if (lane < k) put_item(keys, vals, row_offset, V, base + lane + kept_le, b, bv);
+        if (kept) put_item(keys, vals, row_offset, V, nullptr, seg, base + kidx + below, key, val);
+        if (lane < k) put_item(keys, vals, row_offset, V, nullptr, seg, base + lane + kept_le, b, bv);
+        if (kept && kidx + below == 0 && key != old0) lead[w.a] = key;
+        if (lane < k && lane + kept_le == 0 && b != old0) lead[w.a] = b;
+        if (lane == 0 && m == 0 && old0 != KEY_NONE) lead[w.a] = KEY_NONE;
         if (lane == 0) live[w.a] = (uint8_t)m;
     }
 }
@@ -288,7 +302,7 @@ struct SmallSmem {
 __global__ void __launch_bounds__(GTPB) k_gpma_exec_small(const Window *__restrict__ wins, const uint32_t *__restrict__ n_win,
                                                            uint64_t *keys, uint8_t *vals, uint8_t *live,
                                                            uint32_t *row_offset, uint32_t V, uint32_t seg, UpdList u,
-                                                           DevStatus *st) {
+                                                           uint64_t *lead, DevStatus *st) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallSmem &S = *reinterpret_cast<SmallSmem *>(smem_raw);
     if (blockIdx.x >= *n_win) return;
@@ -361,9 +375,13 @@ __global__ void __launch_bounds__(GTPB) k_gpma_exec_small(const Window *__restri
     for (uint32_t x = tid; x < W; x += GTPB) keys[base + x] = KEY_NONE;
     __syncthreads();
     for (uint32_t r = tid; r < m; r += GTPB)
-        put_item(keys, vals, row_offset, V, base + spread_slot(r, m, w.f, seg), S.m[r], S.mv[r]);
-    for (uint32_t d = tid; d < w.f; d += GTPB)
-        live[w.a + d] = (uint8_t)(first_rank(d + 1, m, w.f) - first_rank(d, m, w.f));
+        put_item(keys, vals, row_offset, V, nullptr, seg, base + spread_slot(r, m, w.f, seg), S.m[r], S.mv[r]);
+    // segment d's first slot takes item first_rank(d), when it gets any
+    for (uint32_t d = tid; d < w.f; d += GTPB) {
+        const uint32_t r0 = (uint32_t)first_rank(d, m, w.f), r1 = (uint32_t)first_rank(d + 1, m, w.f);
+        live[w.a + d] = (uint8_t)(r1 - r0);
+        lead[w.a + d] = r1 > r0 ? S.m[r0] : KEY_NONE;
+    }
 }
 
 // ------------------------------------------------------------------ big windows and rebuilds
@@ -403,16 +421,16 @@ __global__ void __launch_bounds__(GTPB) k_gpma_merge_spread(const uint64_t *__re
                                                              uint32_t c, const uint64_t *__restrict__ Bk,
                                                              const uint8_t *__restrict__ Bv, uint32_t k, uint64_t base,
                                                              uint64_t f, uint32_t seg, uint64_t *keys, uint8_t *vals,
-                                                             uint32_t *row_offset, uint32_t V) {
+                                                             uint32_t *row_offset, uint32_t V, uint64_t *lead) {
     const uint64_t t = (uint64_t)blockIdx.x * GTPB + threadIdx.x;
     const uint64_t m = (uint64_t)c + k;
     if (t < c) {
         const uint64_t r = t + rank_in(Bk, k, Ak[t], true);
-        put_item(keys, vals, row_offset, V, base + spread_slot(r, m, f, seg), Ak[t], Av[t]);
+        put_item(keys, vals, row_offset, V, lead, seg, base + spread_slot(r, m, f, seg), Ak[t], Av[t]);
     } else if (t < m) {
         const uint32_t j = (uint32_t)(t - c);
         const uint64_t r = j + rank_in(Ak, c, Bk[j], false);
-        put_item(keys, vals, row_offset, V, base + spread_slot(r, m, f, seg), Bk[j], Bv[j]);
+        put_item(keys, vals, row_offset, V, lead, seg, base + spread_slot(r, m, f, seg), Bk[j], Bv[j]);
     }
 }
 
@@ -488,6 +506,7 @@ struct GpmaState {
     uint64_t *keys = nullptr;
     uint8_t *vals = nullptr;
     uint8_t *live = nullptr;  // per segment (padded to 16 bytes)
+    uint64_t *lead = nullptr; // per segment: the key in its first slot (the locate's search table)
     uint32_t *row = nullptr;  // V + 1
     DevStatus *dst = nullptr, *hst = nullptr;
     uint32_t sticky = 0;
@@ -509,7 +528,7 @@ uint64_t nseg_of_flat(const GpmaState *g) { return g->size / g->seg; }
 // significant_insert, and the first state).
 lpma_status_t rebuild(GpmaState *g, const uint64_t *Bk, const uint8_t *Bv, uint32_t k, cudaStream_t s) {
     uint64_t c = 0;
-    uint64_t *Ak = nullptr, *nk = nullptr;
+    uint64_t *Ak = nullptr, *nk = nullptr, *nld = nullptr;
     uint8_t *Av = nullptr, *nv = nullptr, *nl = nullptr;
     uint32_t *P = nullptr, *tmp = nullptr;
     const uint64_t nseg_old = g->keys ? nseg_of_flat(g) : 0;
@@ -533,6 +552,7 @@ lpma_status_t rebuild(GpmaState *g, const uint64_t *Bk, const uint8_t *Bv, uint3
     GCK(salloc(&nk, ns, s));
     GCK(salloc(&nv, ns, s));
     GCK(salloc(&nl, (nseg_new + 15) & ~15ull, s));
+    GCK(salloc(&nld, nseg_new, s));
     if (c) {
         k_gpma_gather<<<nblk(nseg_old * 32), GTPB, 0, s>>>(g->keys, g->vals, P, 0, nseg_old, g->seg, Ak, Av, c, g->dst);
         note_launch();
@@ -540,18 +560,19 @@ lpma_status_t rebuild(GpmaState *g, const uint64_t *Bk, const uint8_t *Bv, uint3
     GCK(cudaMemsetAsync(nk, 0xFF, ns * 8, s));
     GCK(cudaMemsetAsync(nv, 0, ns, s));
     GCK(cudaMemsetAsync(nl, 0, (nseg_new + 15) & ~15ull, s));
+    GCK(cudaMemsetAsync(nld, 0xFF, nseg_new * 8, s));
     {
         ProfScope ps("gpma_merge_spread", s);
         k_gpma_merge_spread<<<nblk(c + k), GTPB, 0, s>>>(Ak, Av, (uint32_t)c, Bk, Bv, k, 0, nseg_new, seg, nk, nv,
-                                                          g->row, g->V);
+                                                          g->row, g->V, nld);
         note_launch();
     }
     k_gpma_spread_counts<<<nblk(nseg_new), GTPB, 0, s>>>(nl, 0, nseg_new, c + k);
     note_launch();
     GCK(cudaGetLastError());
     sfree(Ak, s), sfree(Av, s), sfree(P, s), sfree(tmp, s);
-    sfree(g->keys, s), sfree(g->vals, s), sfree(g->live, s);
-    g->keys = nk, g->vals = nv, g->live = nl;
+    sfree(g->keys, s), sfree(g->vals, s), sfree(g->live, s), sfree(g->lead, s);
+    g->keys = nk, g->vals = nv, g->live = nl, g->lead = nld;
     g->size = ns, g->seg = seg, g->h = h;
     g->live_total = c + k;
     return LPMA_OK;
@@ -574,8 +595,9 @@ lpma_status_t exec_big(GpmaState *g, const Window &w, const uint32_t *P, const U
     ProfScope ps("gpma_exec_big", s);
     k_gpma_gather<<<nblk((uint64_t)w.f * 32), GTPB, 0, s>>>(g->keys, g->vals, P, w.a, w.f, g->seg, Ak, Av, c, g->dst);
     GCK(cudaMemsetAsync(g->keys + base, 0xFF, W * 8, s));
+    GCK(cudaMemsetAsync(g->lead + w.a, 0xFF, (uint64_t)w.f * 8, s));
     k_gpma_merge_spread<<<nblk((uint64_t)c + k), GTPB, 0, s>>>(Ak, Av, c, u.key + w.lo, u.val + w.lo, k, base, w.f,
-                                                                g->seg, g->keys, g->vals, g->row, g->V);
+                                                                g->seg, g->keys, g->vals, g->row, g->V, g->lead);
     k_gpma_spread_counts<<<nblk(w.f), GTPB, 0, s>>>(g->live, w.a, w.f, (uint64_t)c + k);
     note_launch(3);
     GCK(cudaGetLastError());
@@ -614,7 +636,7 @@ lpma_status_t gpma_create(uint32_t V, double density_lower, cudaStream_t s, Gpma
 void gpma_destroy(GpmaState *g) {
     if (!g) return;
     cudaStream_t s = cudaStreamPerThread;
-    sfree(g->keys, s), sfree(g->vals, s), sfree(g->live, s), sfree(g->row, s), sfree(g->dst, s);
+    sfree(g->keys, s), sfree(g->vals, s), sfree(g->live, s), sfree(g->lead, s), sfree(g->row, s), sfree(g->dst, s);
     if (g->hst) cudaFreeHost(g->hst);
     delete g;
 }
@@ -711,7 +733,7 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
     {
         ProfScope ps("gpma_resolve", s);
         k_gpma_resolve<<<std::min<uint32_t>(nblk(n), 152 * 8), GTPB, 0, s>>>(sk, sp, nn, g->keys, g->vals, g->live, g->seg,
-                                                  (uint32_t)__builtin_ctz(g->seg), g->h, flag, seg_of, g->dst);
+                                                  (uint32_t)__builtin_ctz(g->seg), g->h, flag, seg_of, g->lead, g->dst);
         note_launch();
     }
     GCKR(scan_u32(flag, pos, nn, &g->dst->n_u, tmp, s));
@@ -775,10 +797,10 @@ lpma_status_t gpma_update(GpmaState *g, const uint64_t *ins, const uint8_t *ins_
                 if (one) {
                     const uint32_t nb = std::min<uint32_t>((counts[0] + GTPB / 32 - 1) / (GTPB / 32), 152 * 8);
                     k_gpma_exec_single<<<nb, GTPB, 0, s>>>(lists[0], dev_counts[0], counts[0], g->keys, g->vals,
-                                                            g->live, g->row, g->V, g->seg, u, g->dst);
+                                                            g->live, g->row, g->V, g->seg, u, g->lead, g->dst);
                 } else {
                     k_gpma_exec_small<<<counts[c], GTPB, smem, s>>>(lists[c], dev_counts[c], g->keys, g->vals, g->live,
-                                                                     g->row, g->V, g->seg, u, g->dst);
+                                                                     g->row, g->V, g->seg, u, g->lead, g->dst);
                 }
                 note_launch();
             }
@@ -870,7 +892,7 @@ lpma_status_t gpma_export_sorted(GpmaState *g, uint64_t *h_keys, uint8_t *h_vals
 }
 
 uint64_t gpma_memory_bytes(const GpmaState *g) {
-    return g->size * 9ull + (g->size / std::max<uint32_t>(g->seg, 1)) + 4ull * (g->V + 1);
+    return g->size * 9ull + 9ull * (g->size / std::max<uint32_t>(g->seg, 1)) + 4ull * (g->V + 1);
 }
 
 }  // namespace lpma
