@@ -5,10 +5,11 @@
 //      into a no-op, so the structure does not change)
 //   2. radix sort, resolve + locate + membership, compaction
 //   3. count-only plan of the first level loop (skip rule on), the status
-//      block read back, then the windows of up to 32 segments executed
-//      (guarded on the device: nothing happens when the plan overflowed);
-//      steps 1-3 replay as one CUDA graph and the host waits for the
-//      read-back only (the one synchronisation of a call without overflow)
+//      block published by the planner's last CTA into the pinned host
+//      mirror, then the windows of up to 32 segments executed (guarded on
+//      the device: nothing happens when the plan overflowed); steps 1-3
+//      replay as one CUDA graph and the host waits for the published
+//      status only (the one synchronisation of a call without overflow)
 //   4. no overflow: execute the bigger maximal windows; if the root took
 //      updates, the eager level-up of rpma.cuh:1646-1653
 //      overflow (rpma.cuh:1662-1712): resize to h; h == H+1 executes the
@@ -116,7 +117,7 @@ struct LpmaHandle {
     bool view_valid = false;
     uint64_t h2d = 0, d2h = 0;  // bytes copied by the current call
     cudaStream_t cap_stream = nullptr;  // private stream for graph capture
-    cudaEvent_t front_ev = nullptr;     // recorded after the front's status read-back
+    cudaEvent_t front_ev = nullptr;     // recorded after the front's planner (and its status copy, if any)
     cudaEvent_t front_ev_blk = nullptr; // the same, waited on without spinning (concurrent handles)
     // recorded after the last work of each call that returns with work in
     // flight, on the call's stream: lpma_destroy waits for it, not the device
@@ -126,7 +127,7 @@ struct LpmaHandle {
     // leveled tree; the leveled fields above stay unused
     GpmaState *gp = nullptr;
     // the front's 4- and 32-segment executors run on side_stream, beside the
-    // single-segment one: fork after the status read-back, join after them
+    // single-segment one: fork after the planner, join after them
     cudaStream_t side_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::vector<FrontGraph> graphs;
