@@ -328,6 +328,15 @@ typedef struct {
  * usable.  Synchronous; no update may be in flight on the device. */
 LPMA_API lpma_status_t lpma_debug_sort_barrier(uint32_t poll_limit, int unreachable);
 
+/* Test setting of the executor of 5..32-segment windows on the current
+ * device, for tests of its give-up path: with give_up set, the bounded wait
+ * for a window's bulk copies into shared memory gives up at once; the warp
+ * then records LPMA_ERR_TIMEOUT in the handle's sticky error word, waits
+ * (bounded) for its copies in flight and stops, so the next call on that
+ * handle returns LPMA_ERR_TIMEOUT.  0 restores the normal wait.
+ * Synchronous; no update may be in flight on the device. */
+LPMA_API lpma_status_t lpma_debug_exec_wait(int give_up);
+
 LPMA_API lpma_status_t lpma_autotune(uint32_t max_keys, lpma_stream_t stream, LpmaTuneEntry *out, size_t cap,
                                      size_t *n_out);
 LPMA_API lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier);

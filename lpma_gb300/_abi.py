@@ -29,6 +29,7 @@ EXPORTS = [
     "lpma_pool_wait", "lpma_pool_drain", "lpma_pool_destroy", "lpma_set_flags", "lpma_error_detail", "lpma_pool_submit_many",
     "lpma_batcher_create", "lpma_batcher_destroy", "lpma_update_batch",
     "lpma_autotune", "lpma_tune_set", "lpma_tune_get", "lpma_memory_reserve", "lpma_debug_sort_barrier",
+    "lpma_debug_exec_wait",
     "lpma_config_gpma", "lpma_gpma_view", "lpma_grain_set", "lpma_grain_get", "lpma_autotune_grain",
 ]
 SORT_TIERS = {1: "small", 2: "block", 3: "tile_merge", 4: "cooperative", 5: "multi_pass"}
@@ -154,6 +155,7 @@ def load():
         "lpma_grain_get": [U32, P, P],
         "lpma_autotune_grain": [P, P, SZ, U32, P, P, SZ, P],
         "lpma_debug_sort_barrier": [U32, I],
+        "lpma_debug_exec_wait": [I],
         "lpma_config_gpma": [P],
         "lpma_gpma_view": [P, P, P, P, P, P, P],
     }

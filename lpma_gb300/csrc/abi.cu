@@ -1989,6 +1989,11 @@ lpma_status_t lpma_debug_sort_barrier(uint32_t poll_limit, int unreachable) {
     return LPMA_OK;
 }
 
+lpma_status_t lpma_debug_exec_wait(int give_up) {
+    CK(set_exec_wait_debug(give_up ? 1u : 0u));
+    return LPMA_OK;
+}
+
 lpma_status_t lpma_tune_set(uint32_t log2_keys, uint32_t concurrent, uint32_t tier) {
     if (log2_keys > 32 || tier >= TIER_COUNT) return LPMA_ERR_INVALID_ARGUMENT;
     sort_tier_set(log2_keys, concurrent ? 1 : 0, (SortTier)tier);

@@ -69,6 +69,10 @@ void launch_relocate(UpdList u, uint32_t n, Geo g, const ulonglong2 *fl, cudaStr
 void launch_compact_pending(const UpdList in, const uint8_t *pend, uint32_t n, UpdList out, uint32_t *blk_nn,
                             uint32_t *blk_ins, DevStatus *st, cudaStream_t s);
 
+// test setting of the 5..32-segment executor's bulk-copy wait (its first
+// wait per window gives up at once when give_up is set), current device
+cudaError_t set_exec_wait_debug(uint32_t give_up);
+
 // count-only planner: per segment with updates, the first level whose
 // window passes the density test; maximal windows go to small/big lists.
 // pub: when set, the planner's last CTA writes the status block into this

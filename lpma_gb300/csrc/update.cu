@@ -924,11 +924,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
 }
 // a bounded wait for the phase (each try suspends for at most a short,
 // hardware-defined time): false when it did not complete
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase) {
-    for (uint32_t it = 0; it < (1u << 20); it++)
+constexpr uint32_t MBAR_TRIES = 1u << 20;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t tries = MBAR_TRIES) {
+    for (uint32_t it = 0; it < tries; it++)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
+
+// Test setting of the 5..32-segment executor's bulk-copy wait
+// (lpma_debug_exec_wait): when set, a window's first wait makes no try and
+// so takes the give-up path; the wait that follows it, for the copies
+// still in flight, keeps the full limit.  Read at run time, so captured
+// update fronts follow it too.
+__device__ uint32_t g_exec_wait_give_up = 0;
 // generic-proxy accesses of shared memory before later bulk copies into it
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 constexpr size_t EM_SMEM = sizeof(Multi4Smem) > sizeof(MultiWarpSmem) ? sizeof(Multi4Smem) : sizeof(MultiWarpSmem);
@@ -1110,9 +1118,10 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
     constexpr bool STAGED = ROW == 1024;
     const int lane = threadIdx.x & 31, gl = lane & 7, gq = lane >> 3;
     const uint32_t nwin = min(*n_win, n_cap);
-    uint32_t phase = 0;
+    uint32_t phase = 0, tries = MBAR_TRIES;
     if (STAGED) {
         if (lane == 0) mbar_init1(bar);
+        if (*reinterpret_cast<volatile uint32_t *>(&g_exec_wait_give_up)) tries = 0;
         __syncwarp();
     }
     for (uint32_t wi = wid; wi < nwin; wi += nwarps) {  // uniform over the warp
@@ -1168,7 +1177,7 @@ __device__ __forceinline__ void k_exec_multi_warp_body(uint64_t *K, uint8_t *KV,
         if (STAGED) {
             const uint32_t ph = phase;
             phase ^= 1u;
-            if (!__all_sync(0xffffffffu, mbar_wait_bounded(bar, ph))) {
+            if (!__all_sync(0xffffffffu, mbar_wait_bounded(bar, ph, tries))) {
                 // the copies did not land in time: report, let them finish
                 // (bounded) before the row is left, and stop this warp
                 if (lane == 0) {
@@ -2268,6 +2277,10 @@ __global__ void __launch_bounds__(64) k_forest_status(const ForestGraph *__restr
 }
 
 }  // namespace
+
+cudaError_t set_exec_wait_debug(uint32_t give_up) {
+    return cudaMemcpyToSymbol(g_exec_wait_give_up, &give_up, sizeof(uint32_t));
+}
 
 uint32_t exec_ctas(int kind, uint32_t n) {
     if (!n) return 0;

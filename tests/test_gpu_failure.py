@@ -56,3 +56,39 @@ def test_sort_barrier_give_up_returns_timeout_and_keeps_handle(engine, oracle):
     assert_same(g, o, "after recovery")
     assert_csr(g, o)
     g.close()
+
+
+def test_executor_copy_wait_give_up_is_reported_on_the_next_call(engine, oracle):
+    """The bounded wait of the 5..32-segment executor for its bulk copies into
+    shared memory, made to give up (lpma_debug_exec_wait): the warp records
+    ERR_TIMEOUT in the handle's sticky word, waits (bounded) for its copies
+    in flight and stops.  The call that launched it returns normally (its
+    status was published before the executors ran); the next call on the
+    handle reports LPMA_ERR_TIMEOUT.  Nothing faults or hangs: the wait
+    that runs out is a bounded one, and the copies land before the warp
+    leaves."""
+    import torch
+    from lpma_gb300 import LpmaError, _abi
+    L = _abi.load()
+    V = 1 << 12
+    e = oracle.shuffle(oracle.rmat_edges(3, 12, 8), 4)
+    half = e.size // 2
+    g, o = engine.Lpma(V), oracle.OracleLpma(V)
+    g.update(ins=_dev(e[:half]))
+    o.update(ins=e[:half])
+    # 120 new edges of one low-degree source: one window of 15 segments
+    src = 4000
+    keys = np.array([(src << 42) | (d << 20) for d in range(100, 220)], dtype=np.uint64)
+    so = o.update(ins=keys)
+    assert so["win_slots"][4] == 480
+    _abi.check(L.lpma_debug_exec_wait(1), "lpma_debug_exec_wait")
+    try:
+        sg = g.update(ins=_dev(keys))
+        torch.cuda.synchronize()
+    finally:
+        L.lpma_debug_exec_wait(0)
+    assert sg["n_ins_applied"] == 120 and sg["windows_small"] - sg["windows_single"] == 1
+    with pytest.raises(LpmaError) as ei:
+        g.update(ins=_dev(keys[:1]))
+    assert ei.value.status == LPMA_ERR_TIMEOUT, ei.value
+    g.close()
